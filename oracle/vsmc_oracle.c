@@ -1,0 +1,1308 @@
+/* vsmc_oracle.c - CPU restatement of the vSMC particle-filter path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity oracle and the timed CPU baseline.
+ * The product library never links or loads this file.
+ *
+ * Paths in citations are inside the vSMC source tree.  Build flags keep
+ * a*b+c as two roundings (-ffp-contract=off), matching the x86 reference
+ * build, on every host. */
+#include "vsmc_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define VO_PI 3.14159265358979323846
+#define VO_PI_2 6.283185307179586476925286766559005768394
+#define VO_PI_2F 6.283185307179586476925286766559005768394f
+
+/* =====================================================================
+ * Philox4x32-10  (rng/philox.hpp:76-101 constants, 212-232 round,
+ * 162-188 key bump before rounds 2..10, 263-294 generator)
+ * ===================================================================== */
+void vo_philox4x32_block(
+    const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t s0 = ctr[0], s1 = ctr[1], s2 = ctr[2], s3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 1; r <= 10; ++r) {
+        if (r > 1) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t pa = (uint64_t)0xCD9E8D57u * s2;
+        const uint64_t pb = (uint64_t)0xD2511F53u * s0;
+        const uint32_t hi0 = (uint32_t)(pa >> 32) ^ k0;
+        const uint32_t lo1 = (uint32_t)pa;
+        const uint32_t hi2 = (uint32_t)(pb >> 32) ^ k1;
+        const uint32_t lo3 = (uint32_t)pb;
+        s0 = hi0 ^ s1;
+        s1 = lo1;
+        s2 = hi2 ^ s3;
+        s3 = lo3;
+    }
+    out[0] = s0;
+    out[1] = s1;
+    out[2] = s2;
+    out[3] = s3;
+}
+
+/* =====================================================================
+ * Threefry4x64-20  (rng/threefry.hpp:71-82 parity constant, 130-146
+ * rotations, 219-242 lane pairing, 279-298 key insertion every 4 rounds)
+ * ===================================================================== */
+static inline uint64_t vo_rotl64(uint64_t x, int r)
+{
+    return (x << r) | (x >> (64 - r));
+}
+
+void vo_threefry4x64_block(
+    const uint64_t ctr[4], const uint64_t key[4], uint64_t out[4])
+{
+    static const int R[8][2] = {{14, 16}, {52, 57}, {23, 40}, {5, 37},
+        {25, 33}, {46, 12}, {58, 22}, {32, 32}};
+    uint64_t par[5];
+    par[4] = 0x1BD11BDAA9FC1A22ull;
+    for (int i = 0; i != 4; ++i) {
+        par[i] = key[i];
+        par[4] ^= key[i];
+    }
+    uint64_t s[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    for (int i = 0; i != 4; ++i)
+        s[i] += par[i];
+    for (int n = 1; n <= 20; ++n) {
+        const int r = (n - 1) % 8;
+        if (n % 2) {
+            s[0] += s[1];
+            s[1] = vo_rotl64(s[1], R[r][0]) ^ s[0];
+            s[2] += s[3];
+            s[3] = vo_rotl64(s[3], R[r][1]) ^ s[2];
+        } else {
+            s[0] += s[3];
+            s[3] = vo_rotl64(s[3], R[r][0]) ^ s[0];
+            s[2] += s[1];
+            s[1] = vo_rotl64(s[1], R[r][1]) ^ s[2];
+        }
+        if (n % 4 == 0) {
+            const int inc = n / 4;
+            for (int i = 0; i != 4; ++i)
+                s[i] += par[(inc + i) % 5];
+            s[3] += (uint64_t)inc;
+        }
+    }
+    for (int i = 0; i != 4; ++i)
+        out[i] = s[i];
+}
+
+/* =====================================================================
+ * CounterEngine  (rng/counter.hpp:43-93 increment, 230-262 bulk counter
+ * blocks, 288-496 engine)
+ * ===================================================================== */
+#define VO_DEFINE_INCREMENT(T, name)                                          \
+    static inline void name##_inc(T *c)                                       \
+    {                                                                         \
+        for (int i = 0; i != 4; ++i)                                          \
+            if (++c[i] != 0)                                                  \
+                return;                                                       \
+    }                                                                         \
+    /* increment(ctr, nskip) (counter.hpp:78-89): note the carry into limb 1  \
+     * also fires when front + nskip == max exactly. */                      \
+    static inline void name##_inc_skip(T *c, T nskip, T maxv)                 \
+    {                                                                         \
+        if (c[0] < maxv - nskip) {                                            \
+            c[0] += nskip;                                                    \
+        } else {                                                              \
+            c[0] += nskip;                                                    \
+            for (int i = 1; i != 4; ++i)                                      \
+                if (++c[i] != 0)                                              \
+                    break;                                                    \
+        }                                                                     \
+    }                                                                         \
+    /* increment(ctr, n, ctr_block) (counter.hpp:230-262) */                 \
+    static void name##_inc_blocks(T *ctr, size_t n, T *blocks, T maxv)        \
+    {                                                                         \
+        if (n == 0)                                                           \
+            return;                                                           \
+        name##_inc(ctr);                                                      \
+        const uint64_t m = (uint64_t)maxv;                                    \
+        const uint64_t l = (uint64_t)ctr[0];                                  \
+        const uint64_t k = (uint64_t)n;                                       \
+        if (k < m && l < m - k) {                                             \
+            for (size_t i = 0; i != n; ++i) {                                 \
+                memcpy(blocks + 4 * i, ctr, 4 * sizeof(T));                   \
+                blocks[4 * i] += (T)i;                                        \
+            }                                                                 \
+        } else if (k < m) {                                                   \
+            for (size_t i = 0; i != n; ++i) {                                 \
+                memcpy(blocks + 4 * i, ctr, 4 * sizeof(T));                   \
+                name##_inc_skip(blocks + 4 * i, (T)i, maxv);                  \
+            }                                                                 \
+        } else {                                                              \
+            for (size_t i = 0; i != n; ++i) {                                 \
+                memcpy(blocks + 4 * i, ctr, 4 * sizeof(T));                   \
+                name##_inc(ctr);                                              \
+            }                                                                 \
+        }                                                                     \
+        memcpy(ctr, blocks + 4 * (n - 1), 4 * sizeof(T));                     \
+    }
+
+VO_DEFINE_INCREMENT(uint32_t, vo_c32)
+VO_DEFINE_INCREMENT(uint64_t, vo_c64)
+
+void vo_philox_init(vo_philox *e, const uint32_t key[2], const uint32_t ctr[4])
+{
+    e->key[0] = key[0];
+    e->key[1] = key[1];
+    memcpy(e->ctr, ctr, sizeof(e->ctr));
+    memset(e->buf, 0, sizeof(e->buf));
+    e->index = 4;
+}
+
+uint32_t vo_philox_next(vo_philox *e)
+{
+    if (e->index == 4) {
+        vo_c32_inc(e->ctr);
+        vo_philox4x32_block(e->ctr, e->key, e->buf);
+        e->index = 0;
+    }
+    return e->buf[e->index++];
+}
+
+/* CounterEngine::operator()(n, r) (counter.hpp:357-390): drain the buffer,
+ * then generator calls of 256 blocks, one call for the remaining whole
+ * blocks, then scalar draws for the last < 4 words. */
+void vo_philox_rand(vo_philox *e, size_t n, uint32_t *r)
+{
+    const size_t remain = 4 - e->index;
+    if (n < remain) {
+        memcpy(r, e->buf + e->index, n * sizeof(uint32_t));
+        e->index += (uint32_t)n;
+        return;
+    }
+    memcpy(r, e->buf + e->index, remain * sizeof(uint32_t));
+    r += remain;
+    n -= remain;
+    e->index = 4;
+    const size_t k = 256;
+    const size_t m = (n / 4) / k;
+    const size_t l = (n / 4) % k;
+    uint32_t *blocks = (uint32_t *)malloc(sizeof(uint32_t) * 4 * k);
+    for (size_t c = 0; c != m + 1; ++c) {
+        const size_t nb = c < m ? k : l;
+        vo_c32_inc_blocks(e->ctr, nb, blocks, 0xFFFFFFFFu);
+        for (size_t i = 0; i != nb; ++i)
+            vo_philox4x32_block(blocks + 4 * i, e->key, r + 4 * i);
+        r += 4 * nb;
+        n -= 4 * nb;
+    }
+    free(blocks);
+    for (size_t i = 0; i != n; ++i)
+        r[i] = vo_philox_next(e);
+}
+
+void vo_threefry_init(
+    vo_threefry *e, const uint64_t key[4], const uint64_t ctr[4])
+{
+    memcpy(e->key, key, sizeof(e->key));
+    memcpy(e->ctr, ctr, sizeof(e->ctr));
+    memset(e->buf, 0, sizeof(e->buf));
+    e->index = 4;
+}
+
+uint64_t vo_threefry_next(vo_threefry *e)
+{
+    if (e->index == 4) {
+        vo_c64_inc(e->ctr);
+        vo_threefry4x64_block(e->ctr, e->key, e->buf);
+        e->index = 0;
+    }
+    return e->buf[e->index++];
+}
+
+void vo_threefry_rand(vo_threefry *e, size_t n, uint64_t *r)
+{
+    const size_t remain = 4 - e->index;
+    if (n < remain) {
+        memcpy(r, e->buf + e->index, n * sizeof(uint64_t));
+        e->index += (uint32_t)n;
+        return;
+    }
+    memcpy(r, e->buf + e->index, remain * sizeof(uint64_t));
+    r += remain;
+    n -= remain;
+    e->index = 4;
+    const size_t k = 256;
+    const size_t m = (n / 4) / k;
+    const size_t l = (n / 4) % k;
+    uint64_t *blocks = (uint64_t *)malloc(sizeof(uint64_t) * 4 * k);
+    for (size_t c = 0; c != m + 1; ++c) {
+        const size_t nb = c < m ? k : l;
+        vo_c64_inc_blocks(e->ctr, nb, blocks, 0xFFFFFFFFFFFFFFFFull);
+        for (size_t i = 0; i != nb; ++i)
+            vo_threefry4x64_block(blocks + 4 * i, e->key, r + 4 * i);
+        r += 4 * nb;
+        n -= 4 * nb;
+    }
+    free(blocks);
+    for (size_t i = 0; i != n; ++i)
+        r[i] = vo_threefry_next(e);
+}
+
+void vo_philox4x32_words(const uint32_t key[2], const uint32_t ctr[4],
+    size_t n, uint32_t *out, int bulk)
+{
+    vo_philox e;
+    vo_philox_init(&e, key, ctr);
+    if (bulk) {
+        vo_philox_rand(&e, n, out);
+    } else {
+        for (size_t i = 0; i != n; ++i)
+            out[i] = vo_philox_next(&e);
+    }
+}
+
+void vo_threefry4x64_words(const uint64_t key[4], const uint64_t ctr[4],
+    size_t n, uint64_t *out, int bulk)
+{
+    vo_threefry e;
+    vo_threefry_init(&e, key, ctr);
+    if (bulk) {
+        vo_threefry_rand(&e, n, out);
+    } else {
+        for (size_t i = 0; i != n; ++i)
+            out[i] = vo_threefry_next(&e);
+    }
+}
+
+/* =====================================================================
+ * u01 conversions  (rng/u01.hpp:77-172).  W = integer bits, M = real
+ * mantissa bits; all scale factors are exact powers of two.
+ * ===================================================================== */
+#define VO_DEFINE_U01(UT, RT, W, M, name)                                     \
+    RT name(int lr, UT u)                                                     \
+    {                                                                         \
+        if (lr == 0) { /* [0,1]: U01LRImpl<Closed,Closed> */                 \
+            const int P = (W) - 1 < (M) ? (W) - 1 : (M);                      \
+            const int V = P + 1;                                              \
+            const int L = V < (W) ? 1 : 0;                                    \
+            const int R = V < (W) ? (W) - 1 - V : 0;                          \
+            const UT t = (UT)((UT)(u << L) >> (R + L));                       \
+            RT v;                                                             \
+            if (V < (W))                                                      \
+                v = (RT)(UT)((t & 1) + t);                                    \
+            else                                                              \
+                v = (RT)(t & 1) + (RT)t;                                      \
+            return v * (RT)ldexp(1.0, -(P + 1));                              \
+        }                                                                     \
+        if (lr == 1) { /* [0,1): Closed,Open */                              \
+            const int P = (W) < (M) ? (W) : (M);                              \
+            const int R = (W) - P;                                            \
+            return (RT)(u >> R) * (RT)ldexp(1.0, -P);                         \
+        }                                                                     \
+        if (lr == 2) { /* (0,1]: Open,Closed */                              \
+            const int P = (W) < (M) ? (W) : (M);                              \
+            const int R = (W) - P;                                            \
+            return (RT)(u >> R) * (RT)ldexp(1.0, -P) + (RT)ldexp(1.0, -P);    \
+        }                                                                     \
+        { /* (0,1): Open,Open */                                             \
+            const int P = (W) + 1 < (M) ? (W) + 1 : (M);                      \
+            const int R = (W) + 1 - P;                                        \
+            return (RT)(u >> R) * (RT)ldexp(1.0, -(P - 1)) +                  \
+                (RT)ldexp(1.0, -P);                                           \
+        }                                                                     \
+    }
+
+VO_DEFINE_U01(uint32_t, double, 32, 53, vo_u01_u32_f64)
+VO_DEFINE_U01(uint32_t, float, 32, 24, vo_u01_u32_f32)
+VO_DEFINE_U01(uint64_t, double, 64, 53, vo_u01_u64_f64)
+VO_DEFINE_U01(uint64_t, float, 64, 24, vo_u01_u64_f32)
+
+void vo_u01_u32_f64_n(int lr, size_t n, const uint32_t *u, double *r)
+{
+    for (size_t i = 0; i != n; ++i)
+        r[i] = vo_u01_u32_f64(lr, u[i]);
+}
+
+void vo_u01_u32_f32_n(int lr, size_t n, const uint32_t *u, float *r)
+{
+    for (size_t i = 0; i != n; ++i)
+        r[i] = vo_u01_u32_f32(lr, u[i]);
+}
+
+void vo_u01_u64_f64_n(int lr, size_t n, const uint64_t *u, double *r)
+{
+    for (size_t i = 0; i != n; ++i)
+        r[i] = vo_u01_u64_f64(lr, u[i]);
+}
+
+/* =====================================================================
+ * Engine-generic draws.  U01Distribution picks a 32-bit integer for a
+ * 32-bit engine and a 64-bit one otherwise (rng/u01_distribution.hpp:45-47,
+ * 67-72); batch draws take words through the bulk path in 1024-word calls
+ * (rng/u01_distribution.hpp:215-233).
+ * ===================================================================== */
+typedef struct {
+    int kind; /* 0 Philox4x32, 1 Threefry4x64 */
+    vo_philox p;
+    vo_threefry t;
+} vo_eng;
+
+static void vo_eng_init(vo_eng *e, int kind, const uint64_t key[4],
+    const uint64_t ctr[4])
+{
+    e->kind = kind;
+    if (kind == 0) {
+        uint32_t k[2] = {(uint32_t)key[0], (uint32_t)key[1]};
+        uint32_t c[4] = {(uint32_t)ctr[0], (uint32_t)ctr[1],
+            (uint32_t)ctr[2], (uint32_t)ctr[3]};
+        vo_philox_init(&e->p, k, c);
+    } else {
+        vo_threefry_init(&e->t, key, ctr);
+    }
+}
+
+static double vo_eng_u01d(vo_eng *e)
+{
+    if (e->kind == 0)
+        return vo_u01_u32_f64(1, vo_philox_next(&e->p));
+    return vo_u01_u64_f64(1, vo_threefry_next(&e->t));
+}
+
+static float vo_eng_u01f(vo_eng *e)
+{
+    if (e->kind == 0)
+        return vo_u01_u32_f32(1, vo_philox_next(&e->p));
+    return vo_u01_u64_f32(1, vo_threefry_next(&e->t));
+}
+
+/* one bulk call of n <= 1024 words turned into [0,1) reals */
+static void vo_eng_u01d_bulk(vo_eng *e, size_t n, double *r)
+{
+    if (e->kind == 0) {
+        uint32_t s[1024];
+        vo_philox_rand(&e->p, n, s);
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_u01_u32_f64(1, s[i]);
+    } else {
+        uint64_t s[1024];
+        vo_threefry_rand(&e->t, n, s);
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_u01_u64_f64(1, s[i]);
+    }
+}
+
+static void vo_eng_u01f_bulk(vo_eng *e, size_t n, float *r)
+{
+    if (e->kind == 0) {
+        uint32_t s[1024];
+        vo_philox_rand(&e->p, n, s);
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_u01_u32_f32(1, s[i]);
+    } else {
+        uint64_t s[1024];
+        vo_threefry_rand(&e->t, n, s);
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_u01_u64_f32(1, s[i]);
+    }
+}
+
+/* u01_distribution (rng/u01_distribution.hpp:215-233) */
+static void vo_u01_distribution_d(vo_eng *e, size_t n, double *r)
+{
+    const size_t k = 1024, m = n / k, l = n % k;
+    for (size_t i = 0; i != m; ++i, r += k)
+        vo_eng_u01d_bulk(e, k, r);
+    vo_eng_u01d_bulk(e, l, r);
+}
+
+static void vo_u01_distribution_f(vo_eng *e, size_t n, float *r)
+{
+    const size_t k = 1024, m = n / k, l = n % k;
+    for (size_t i = 0; i != m; ++i, r += k)
+        vo_eng_u01f_bulk(e, k, r);
+    vo_eng_u01f_bulk(e, l, r);
+}
+
+void vo_u01_dist_f64(int eng, const uint64_t key[4], const uint64_t ctr[4],
+    size_t n, double *r, int batch)
+{
+    vo_eng e;
+    vo_eng_init(&e, eng, key, ctr);
+    if (batch) {
+        vo_u01_distribution_d(&e, n, r);
+    } else {
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_eng_u01d(&e);
+    }
+}
+
+void vo_u01_dist_f32(int eng, const uint64_t key[4], const uint64_t ctr[4],
+    size_t n, float *r, int batch)
+{
+    vo_eng e;
+    vo_eng_init(&e, eng, key, ctr);
+    if (batch) {
+        vo_u01_distribution_f(&e, n, r);
+    } else {
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_eng_u01f(&e);
+    }
+}
+
+/* =====================================================================
+ * Normal  (rng/normal_distribution.hpp:199-216 scalar with cached sine
+ * value; 222-267 batch: per 1024-chunk the first half are radii, the second
+ * half angles, out[0..nu) = sine branch, out[nu..2nu) = cosine branch, and
+ * an odd total draws two extra scalar uniforms for the last element)
+ * ===================================================================== */
+typedef struct {
+    double mean, sd, v;
+    int saved;
+} vo_normal_d;
+
+static double vo_normal_d_draw(vo_normal_d *nd, vo_eng *e)
+{
+    double z;
+    if (nd->saved) {
+        z = nd->v;
+        nd->saved = 0;
+    } else {
+        const double u1 = sqrt(-2 * log(vo_eng_u01d(e)));
+        const double u2 = VO_PI_2 * vo_eng_u01d(e);
+        z = u1 * cos(u2);
+        nd->v = u1 * sin(u2);
+        nd->saved = 1;
+    }
+    return nd->mean + nd->sd * z;
+}
+
+typedef struct {
+    float mean, sd, v;
+    int saved;
+} vo_normal_f;
+
+static float vo_normal_f_draw(vo_normal_f *nd, vo_eng *e)
+{
+    float z;
+    if (nd->saved) {
+        z = nd->v;
+        nd->saved = 0;
+    } else {
+        const float u1 = sqrtf(-2 * logf(vo_eng_u01f(e)));
+        const float u2 = VO_PI_2F * vo_eng_u01f(e);
+        z = u1 * cosf(u2);
+        nd->v = u1 * sinf(u2);
+        nd->saved = 1;
+    }
+    return nd->mean + nd->sd * z;
+}
+
+static void vo_normal_impl_d(
+    vo_eng *e, size_t n, double *r, double mean, double sd)
+{
+    double s[512];
+    const size_t nu = n / 2;
+    double *u1 = r, *u2 = r + nu;
+    vo_u01_distribution_d(e, n, r);
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = log(u1[i]);
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = -2.0 * s[i];
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = sqrt(s[i]);
+    for (size_t i = 0; i != nu; ++i)
+        u2[i] = VO_PI_2 * u2[i];
+    for (size_t i = 0; i != nu; ++i) {
+        const double a = u2[i];
+        u1[i] = sin(a);
+        u2[i] = cos(a);
+    }
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = sd * s[i];
+    for (size_t i = 0; i != nu; ++i)
+        u1[i] = s[i] * u1[i] + mean;
+    for (size_t i = 0; i != nu; ++i)
+        u2[i] = s[i] * u2[i] + mean;
+}
+
+static void vo_normal_impl_f(vo_eng *e, size_t n, float *r, float mean, float sd)
+{
+    float s[512];
+    const size_t nu = n / 2;
+    float *u1 = r, *u2 = r + nu;
+    vo_u01_distribution_f(e, n, r);
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = logf(u1[i]);
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = -2.0f * s[i];
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = sqrtf(s[i]);
+    for (size_t i = 0; i != nu; ++i)
+        u2[i] = VO_PI_2F * u2[i];
+    for (size_t i = 0; i != nu; ++i) {
+        const float a = u2[i];
+        u1[i] = sinf(a);
+        u2[i] = cosf(a);
+    }
+    for (size_t i = 0; i != nu; ++i)
+        s[i] = sd * s[i];
+    for (size_t i = 0; i != nu; ++i)
+        u1[i] = s[i] * u1[i] + mean;
+    for (size_t i = 0; i != nu; ++i)
+        u2[i] = s[i] * u2[i] + mean;
+}
+
+void vo_normal_f64(int eng, const uint64_t key[4], const uint64_t ctr[4],
+    size_t n, double mean, double sd, double *r, int batch)
+{
+    vo_eng e;
+    vo_eng_init(&e, eng, key, ctr);
+    /* NormalDistribution::operator()(rng, n, r) uses scalar draws below 100
+     * (normal_distribution.hpp:122-131); callers here choose explicitly. */
+    if (!batch) {
+        vo_normal_d nd = {mean, sd, 0, 0};
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_normal_d_draw(&nd, &e);
+        return;
+    }
+    const size_t k = 1024, m = n / k, l = n % k;
+    for (size_t i = 0; i != m; ++i, r += k)
+        vo_normal_impl_d(&e, k, r, mean, sd);
+    vo_normal_impl_d(&e, l, r, mean, sd);
+    if (n % 2 != 0) {
+        const double u = vo_eng_u01d(&e);
+        const double v = vo_eng_u01d(&e);
+        r[l - 1] = mean + sd * sqrt(-2 * log(u)) * cos(VO_PI_2 * v);
+    }
+}
+
+void vo_normal_f32(int eng, const uint64_t key[4], const uint64_t ctr[4],
+    size_t n, float mean, float sd, float *r, int batch)
+{
+    vo_eng e;
+    vo_eng_init(&e, eng, key, ctr);
+    if (!batch) {
+        vo_normal_f nd = {mean, sd, 0, 0};
+        for (size_t i = 0; i != n; ++i)
+            r[i] = vo_normal_f_draw(&nd, &e);
+        return;
+    }
+    const size_t k = 1024, m = n / k, l = n % k;
+    for (size_t i = 0; i != m; ++i, r += k)
+        vo_normal_impl_f(&e, k, r, mean, sd);
+    vo_normal_impl_f(&e, l, r, mean, sd);
+    if (n % 2 != 0) {
+        const float u = vo_eng_u01f(&e);
+        const float v = vo_eng_u01f(&e);
+        r[l - 1] = mean + sd * sqrtf(-2 * logf(u)) * cosf(VO_PI_2F * v);
+    }
+}
+
+/* =====================================================================
+ * Gamma / chi-squared / Student-t, scalar forms
+ * (rng/gamma_distribution.hpp:57-91 constants, 132-216 generators;
+ * rng/chi_squared_distribution.hpp:64-78 = Gamma(n/2, 2);
+ * rng/student_t_distribution.hpp:78-91: normal first, then chi-squared)
+ * ===================================================================== */
+enum { VO_GAMMA_T, VO_GAMMA_W, VO_GAMMA_N, VO_GAMMA_E };
+
+typedef struct {
+    double alpha, beta, d, c;
+    int alg;
+} vo_gamma;
+
+static void vo_gamma_init(vo_gamma *g, double alpha, double beta)
+{
+    g->alpha = alpha;
+    g->beta = beta;
+    if (alpha < 0.6)
+        g->alg = VO_GAMMA_T;
+    else if (alpha < 1)
+        g->alg = VO_GAMMA_W;
+    else if (alpha > 1)
+        g->alg = VO_GAMMA_N;
+    else
+        g->alg = VO_GAMMA_E;
+    g->d = g->c = 0;
+    switch (g->alg) {
+        case VO_GAMMA_T:
+            g->d = 1 - alpha;
+            g->c = 1 / alpha;
+            break;
+        case VO_GAMMA_W:
+            g->d = pow(alpha, alpha / (1 - alpha)) * (1 - alpha);
+            g->c = 1 / alpha;
+            break;
+        case VO_GAMMA_N:
+            g->d = alpha - 1.0 / 3;
+            g->c = 1 / (3 * sqrt(g->d));
+            break;
+        default: break;
+    }
+}
+
+static double vo_gamma_draw(const vo_gamma *g, vo_eng *e)
+{
+    double r = 0;
+    switch (g->alg) {
+        case VO_GAMMA_T:
+            for (;;) {
+                double u = vo_eng_u01d(e);
+                double ee = -log(vo_eng_u01d(e));
+                if (u > g->d) {
+                    u = -log(g->c * (1 - u));
+                    ee += u;
+                    u = g->d + g->alpha * u;
+                }
+                const double x = exp(g->c * log(u));
+                if (fabs(x) < ee) {
+                    r = x;
+                    break;
+                }
+            }
+            break;
+        case VO_GAMMA_W: {
+            double u, ee, x;
+            do {
+                u = -log(vo_eng_u01d(e));
+                ee = -log(vo_eng_u01d(e));
+                x = exp(g->c * log(u));
+            } while (u + ee < g->d + x);
+            r = x;
+            break;
+        }
+        case VO_GAMMA_N: {
+            vo_normal_d rnorm = {0, 1, 0, 0};
+            for (;;) {
+                const double u = vo_eng_u01d(e);
+                double w, v;
+                do {
+                    w = vo_normal_d_draw(&rnorm, e);
+                    v = 1 + g->c * w;
+                } while (v <= 0);
+                v = v * v * v;
+                double ee = 1 - 0.0331 * (w * w) * (w * w);
+                if (u < ee) {
+                    r = g->d * v;
+                    break;
+                }
+                ee = w * w / 2 + g->d * (1 - v + log(v));
+                if (log(u) < ee) {
+                    r = g->d * v;
+                    break;
+                }
+            }
+            break;
+        }
+        default: r = -log(vo_eng_u01d(e)); break;
+    }
+    return g->beta * r;
+}
+
+void vo_student_t_f64(int eng, const uint64_t key[4], const uint64_t ctr[4],
+    size_t n, double df, double *r)
+{
+    vo_eng e;
+    vo_eng_init(&e, eng, key, ctr);
+    vo_normal_d nd = {0, 1, 0, 0};
+    vo_gamma g;
+    vo_gamma_init(&g, df / 2, 2);
+    for (size_t i = 0; i != n; ++i) {
+        const double z = vo_normal_d_draw(&nd, &e);
+        const double u = df / vo_gamma_draw(&g, &e);
+        r[i] = z * sqrt(u);
+    }
+}
+
+/* =====================================================================
+ * u01 sequences  (rng/u01_sequence.hpp:53-89 array forms; 131-259 lazy
+ * classes: only indices that are read consume engine words)
+ * ===================================================================== */
+void vo_u01_sorted(size_t N, const double *u01, double *u01seq)
+{
+    for (size_t i = 0; i != N; ++i)
+        u01seq[i] = log(u01[i]);
+    double lmax = 0;
+    for (size_t i = 0; i != N; ++i) {
+        lmax += u01seq[i] / (double)(N - i);
+        u01seq[i] = 1 - exp(lmax);
+    }
+}
+
+void vo_u01_stratified(size_t N, const double *u01, double *u01seq)
+{
+    const double delta = 1 / (double)N;
+    for (size_t i = 0; i != N; ++i)
+        u01seq[i] = u01[i] * delta + (double)i * delta;
+}
+
+void vo_u01_systematic(size_t N, double u01, double *u01seq)
+{
+    if (N == 0)
+        return;
+    const double delta = 1.0 / (double)N;
+    u01seq[0] = u01 * delta;
+    for (size_t i = 1; i != N; ++i)
+        u01seq[i] = u01seq[i - 1] + delta;
+}
+
+typedef struct {
+    int kind; /* 0 sorted, 1 stratified, 2 systematic, 3 array */
+    size_t N, n;
+    double u, lmax, delta, u0;
+    vo_philox *rng;
+    const double *arr;
+} vo_seq;
+
+static void vo_seq_init(vo_seq *s, int kind, size_t N, vo_philox *rng)
+{
+    s->kind = kind;
+    s->N = N;
+    s->n = N;
+    s->u = 0;
+    s->lmax = 0;
+    s->u0 = 0;
+    s->rng = rng;
+    s->arr = NULL;
+    s->delta = 1 / (double)N;
+    if (kind == 2)
+        s->u0 = vo_u01_u32_f64(1, vo_philox_next(rng)) * s->delta;
+}
+
+static double vo_seq_get(vo_seq *s, size_t n)
+{
+    if (s->kind == 3)
+        return s->arr[n];
+    if (n == s->n)
+        return s->u;
+    s->n = n;
+    if (s->kind == 0) {
+        s->lmax += log(vo_u01_u32_f64(1, vo_philox_next(s->rng))) /
+            (double)(s->N - n);
+        s->u = 1 - exp(s->lmax);
+    } else if (s->kind == 1) {
+        s->u = vo_u01_u32_f64(1, vo_philox_next(s->rng)) * s->delta +
+            (double)n * s->delta;
+    } else {
+        s->u = s->u0 + (double)n * s->delta;
+    }
+    return s->u;
+}
+
+void vo_u01_sequence(int kind, size_t N, const uint32_t key[2],
+    const uint32_t ctr[4], double *out, uint32_t next_words[4])
+{
+    vo_philox e;
+    vo_philox_init(&e, key, ctr);
+    vo_seq s;
+    vo_seq_init(&s, kind, N, &e);
+    for (size_t i = 0; i != N; ++i)
+        out[i] = vo_seq_get(&s, i);
+    for (int i = 0; i != 4; ++i)
+        next_words[i] = vo_philox_next(&e);
+}
+
+/* =====================================================================
+ * Resampling transforms  (resample/transform.hpp:43-71 u01 -> rep,
+ * 75-96 u01 -> index, 100-134 rep -> index, 138-150 index -> rep,
+ * 155-168 residual)
+ * ===================================================================== */
+static void vo_trans_u01_rep_seq(
+    size_t M, size_t N, const double *w, vo_seq *u01seq, int *rep)
+{
+    if (M == 0)
+        return;
+    if (M == 1) {
+        *rep = (int)N;
+        return;
+    }
+    memset(rep, 0, sizeof(int) * M);
+    if (N == 0)
+        return;
+    double accw = 0;
+    size_t j = 0;
+    for (size_t i = 0; i != M - 1; ++i) {
+        accw += w[i];
+        while (j != N && vo_seq_get(u01seq, j) <= accw) {
+            ++rep[i];
+            ++j;
+        }
+    }
+    rep[M - 1] = (int)(N - j);
+}
+
+void vo_resample_trans_u01_rep(
+    size_t M, size_t N, const double *w, const double *u01, int *rep)
+{
+    vo_seq s;
+    memset(&s, 0, sizeof(s));
+    s.kind = 3;
+    s.arr = u01;
+    vo_trans_u01_rep_seq(M, N, w, &s, rep);
+}
+
+void vo_resample_trans_u01_index(
+    size_t M, size_t N, const double *w, const double *u01, int *idx)
+{
+    if (M == 0 || N == 0)
+        return;
+    memset(idx, 0, sizeof(int) * N);
+    if (M == 1)
+        return;
+    double accw = 0;
+    size_t j = 0;
+    for (size_t i = 0; i != M - 1; ++i) {
+        accw += w[i];
+        while (j != N && u01[j] <= accw)
+            idx[j++] = (int)i;
+    }
+    while (j != N)
+        idx[j++] = (int)(M - 1);
+}
+
+void vo_resample_trans_rep_index(size_t M, size_t N, const int *rep, int *idx)
+{
+    if (M == 0 || N == 0)
+        return;
+    if (M != N) {
+        size_t dst = 0;
+        for (size_t src = 0; src != M; ++src)
+            for (int r = 0; r != rep[src]; ++r)
+                idx[dst++] = (int)src;
+        return;
+    }
+    int time = 0;
+    size_t src = 0;
+    for (size_t dst = 0; dst != N; ++dst) {
+        if (rep[dst] != 0) {
+            idx[dst] = (int)dst;
+        } else {
+            if (rep[src] < time + 2) {
+                time = 0;
+                do
+                    ++src;
+                while (rep[src] < 2);
+            }
+            idx[dst] = (int)src;
+            ++time;
+        }
+    }
+}
+
+void vo_resample_trans_index_rep(size_t M, size_t N, const int *idx, int *rep)
+{
+    if (M == 0 || N == 0)
+        return;
+    memset(rep, 0, sizeof(int) * M);
+    for (size_t i = 0; i != N; ++i)
+        ++rep[idx[i]];
+}
+
+size_t vo_resample_trans_residual(
+    size_t M, size_t N, const double *w, double *resid, int *integ)
+{
+    double integral = 0;
+    const double coeff = (double)N;
+    for (size_t i = 0; i != M; ++i) {
+        resid[i] = modf(coeff * w[i], &integral);
+        integ[i] = (int)integral;
+    }
+    double acc = 0;
+    for (size_t i = 0; i != M; ++i)
+        acc += resid[i];
+    const double inv = 1 / acc;
+    for (size_t i = 0; i != M; ++i)
+        resid[i] = inv * resid[i];
+    int R = 0;
+    for (size_t i = 0; i != M; ++i)
+        R += integ[i];
+    return N - (size_t)R;
+}
+
+/* scheme functors (resample/multinomial.hpp:46-52, stratified.hpp:46-52,
+ * systematic.hpp:46-52, residual*.hpp:46-57) */
+void vo_resample(int scheme, size_t M, size_t N, vo_philox *eng,
+    const double *w, int *rep)
+{
+    if (scheme <= 2) { /* Multinomial, Stratified, Systematic */
+        const int kind = scheme;
+        vo_seq s;
+        vo_seq_init(&s, kind, N, eng);
+        vo_trans_u01_rep_seq(M, N, w, &s, rep);
+        return;
+    }
+    int *integ = (int *)malloc(sizeof(int) * (M ? M : 1));
+    double *resid = (double *)malloc(sizeof(double) * (M ? M : 1));
+    const size_t R = vo_resample_trans_residual(M, N, w, resid, integ);
+    const int kind = scheme - 3; /* Residual, ResidualStratified, ResidualSystematic */
+    vo_seq s;
+    vo_seq_init(&s, kind, R, eng);
+    vo_trans_u01_rep_seq(M, R, resid, &s, rep);
+    for (size_t i = 0; i != M; ++i)
+        rep[i] = rep[i] + integ[i];
+    free(integ);
+    free(resid);
+}
+
+void vo_resample_words(int scheme, size_t M, size_t N, const uint32_t key[2],
+    const uint32_t ctr[4], const double *w, int *rep, uint32_t next_words[4])
+{
+    vo_philox e;
+    vo_philox_init(&e, key, ctr);
+    vo_resample(scheme, M, N, &e, w, rep);
+    for (int i = 0; i != 4; ++i)
+        next_words[i] = vo_philox_next(&e);
+}
+
+/* StateMatrix<ColMajor,Dim,T>::copy (core/state_matrix.hpp:357-364) */
+void vo_state_copy_f32(size_t N, const int *idx, float *state)
+{
+    for (size_t d = 0; d != 4; ++d)
+        for (size_t dst = 0; dst != N; ++dst)
+            state[d * N + dst] = state[d * N + (size_t)idx[dst]];
+}
+
+void vo_state_copy_f64(size_t N, const int *idx, double *state)
+{
+    for (size_t d = 0; d != 4; ++d)
+        for (size_t dst = 0; dst != N; ++dst)
+            state[d * N + dst] = state[d * N + (size_t)idx[dst]];
+}
+
+/* =====================================================================
+ * Weight  (core/weight.hpp:41-63 helpers, 99-103 set_equal, 145-149
+ * set_log, 168-173 add_log, 202-230 normalize: exp and a running sum in
+ * 1024-element chunks, scale by 1/sum, ESS = 1/dot(W, W))
+ * ===================================================================== */
+static double vo_weight_normalize(size_t N, double *w, int use_log)
+{
+    double accw = 0;
+    for (size_t i = 0; i != N; ++i) {
+        if (use_log)
+            w[i] = exp(w[i]);
+        accw = accw + w[i];
+    }
+    const double inv = 1 / accw;
+    for (size_t i = 0; i != N; ++i)
+        w[i] = inv * w[i];
+    double dot = 0;
+    for (size_t i = 0; i != N; ++i)
+        dot += w[i] * w[i];
+    return 1 / dot;
+}
+
+static double vo_weight_post_set_log(size_t N, double *w)
+{
+    double wmax = w[0];
+    for (size_t i = 1; i < N; ++i)
+        if (wmax < w[i])
+            wmax = w[i];
+    for (size_t i = 0; i != N; ++i)
+        w[i] -= wmax;
+    return vo_weight_normalize(N, w, 1);
+}
+
+static double vo_weight_set_equal(size_t N, double *W)
+{
+    const double v = 1.0 / (double)N;
+    for (size_t i = 0; i != N; ++i)
+        W[i] = v;
+    return vo_weight_normalize(N, W, 0);
+}
+
+double vo_weight_set_log(size_t N, const double *lw, double *W)
+{
+    memcpy(W, lw, sizeof(double) * N);
+    return vo_weight_post_set_log(N, W);
+}
+
+double vo_weight_add_log(size_t N, const double *W0, const double *l, double *W)
+{
+    memcpy(W, W0, sizeof(double) * N);
+    vo_weight_normalize(N, W, 0); /* Weight::set(W0) */
+    for (size_t i = 0; i != N; ++i)
+        W[i] = log(W[i]);
+    for (size_t i = 0; i != N; ++i)
+        W[i] = W[i] + l[i];
+    return vo_weight_post_set_log(N, W);
+}
+
+double vo_weight_set(size_t N, const double *w, double *W)
+{
+    memcpy(W, w, sizeof(double) * N);
+    return vo_weight_normalize(N, W, 0);
+}
+
+/* =====================================================================
+ * Particle filter: constant-velocity model, Student-t position
+ * observations, in the example/pf/include/pf.hpp:70-193 form, driven in
+ * the Sampler order (core/sampler.hpp:443-476, 735-785): weight, record
+ * ESS, resample if ESS < threshold * N (core/particle.hpp:170-197), then the
+ * weighted position mean (core/monitor.hpp:242-268, MonitorMCMC stage).
+ * The log-evidence increment log sum_i W_{t-1,i} exp(l_{t,i}) follows
+ * user_guide/tex/smc.tex:176-182.
+ * ===================================================================== */
+double vo_student_t_norm_const(double nu, double s)
+{
+    return lgamma(0.5 * (nu + 1)) - lgamma(0.5 * nu) - 0.5 * log(nu * VO_PI) -
+        log(s);
+}
+
+static inline void vo_particle_engine(
+    vo_philox *e, size_t t, uint32_t seed, size_t id)
+{
+    const uint32_t key[2] = {(uint32_t)t, seed};
+    const uint32_t ctr[4] = {0, (uint32_t)id, 0, 0};
+    vo_philox_init(e, key, ctr);
+}
+
+static inline void vo_pair_d(vo_philox *p, double sd, double *z1, double *z2)
+{
+    vo_eng e;
+    e.kind = 0;
+    e.p = *p;
+    vo_normal_d nd = {0, sd, 0, 0};
+    *z1 = vo_normal_d_draw(&nd, &e);
+    *z2 = vo_normal_d_draw(&nd, &e);
+    *p = e.p;
+}
+
+/* FP32 pair: Box-Muller with the (0,1] u01_oc radius uniform */
+static inline void vo_pair_f(vo_philox *p, float sd, float *z1, float *z2)
+{
+    const uint32_t w0 = vo_philox_next(p);
+    const uint32_t w1 = vo_philox_next(p);
+    const float u1 = vo_u01_u32_f32(2, w0);
+    const float u2 = vo_u01_u32_f32(1, w1);
+    const float r = sqrtf(-2 * logf(u1));
+    const float th = VO_PI_2F * u2;
+    *z1 = sd * (r * cosf(th));
+    *z2 = sd * (r * sinf(th));
+}
+
+#define VO_DEFINE_PF_KERNELS(T, SFX, PAIR, LOG1P, CAST)                       \
+    static inline T vo_ll_##SFX(const vo_model *m, const double obs[2], T x,  \
+        T y)                                                                  \
+    {                                                                         \
+        const T c2 = (T)(2 * vo_student_t_norm_const(m->nu, m->obs_scale));   \
+        const T inv_s = (T)(1 / m->obs_scale);                                \
+        const T inv_nu = (T)(1 / m->nu);                                      \
+        const T half_nu1 = (T)(0.5 * (m->nu + 1));                            \
+        const T zx = ((T)obs[0] - x) * inv_s;                                 \
+        const T zy = ((T)obs[1] - y) * inv_s;                                 \
+        const T qx = zx * zx * inv_nu;                                        \
+        const T qy = zy * zy * inv_nu;                                        \
+        return c2 - half_nu1 * (LOG1P(qx) + LOG1P(qy));                       \
+    }                                                                         \
+    void vo_pf_init_##SFX(size_t N, uint32_t seed, const vo_model *m,         \
+        const double obs[2], T *state, T *ll_out)                             \
+    {                                                                         \
+        _Pragma("omp parallel for schedule(static)")                          \
+        for (size_t i = 0; i < N; ++i) {                                      \
+            vo_philox e;                                                      \
+            vo_particle_engine(&e, 0, seed, i);                               \
+            T x, y, vx, vy;                                                   \
+            PAIR(&e, (T)m->sd_pos0, &x, &y);                                  \
+            PAIR(&e, (T)m->sd_vel0, &vx, &vy);                                \
+            state[0 * N + i] = x;                                             \
+            state[1 * N + i] = y;                                             \
+            state[2 * N + i] = vx;                                            \
+            state[3 * N + i] = vy;                                            \
+            ll_out[i] = vo_ll_##SFX(m, obs, x, y);                            \
+        }                                                                     \
+    }                                                                         \
+    void vo_pf_move_##SFX(size_t N, size_t t, uint32_t seed,                  \
+        const vo_model *m, const double obs[2], T *state, T *ll_out)          \
+    {                                                                         \
+        const T dt = (T)m->dt;                                                \
+        const T h = (T)(0.5 * m->dt * m->dt);                                 \
+        _Pragma("omp parallel for schedule(static)")                          \
+        for (size_t i = 0; i < N; ++i) {                                      \
+            vo_philox e;                                                      \
+            vo_particle_engine(&e, t, seed, i);                               \
+            T ax, ay;                                                         \
+            PAIR(&e, (T)m->sigma_a, &ax, &ay);                                \
+            const T x = state[0 * N + i], y = state[1 * N + i];               \
+            const T vx = state[2 * N + i], vy = state[3 * N + i];             \
+            const T nx = x + dt * vx + h * ax;                                \
+            const T ny = y + dt * vy + h * ay;                                \
+            state[0 * N + i] = nx;                                            \
+            state[1 * N + i] = ny;                                            \
+            state[2 * N + i] = vx + dt * ax;                                  \
+            state[3 * N + i] = vy + dt * ay;                                  \
+            ll_out[i] = vo_ll_##SFX(m, obs, nx, ny);                          \
+        }                                                                     \
+    }
+
+VO_DEFINE_PF_KERNELS(double, f64, vo_pair_d, log1p, double)
+VO_DEFINE_PF_KERNELS(float, f32, vo_pair_f, log1pf, float)
+
+void vo_pf_simulate(
+    uint32_t seed, size_t T, const vo_model *m, double *truth, double *obs)
+{
+    /* CounterEngine(seed): key {seed, 0}, counter 0 */
+    vo_eng e;
+    e.kind = 0;
+    const uint32_t key[2] = {seed, 0};
+    const uint32_t ctr[4] = {0, 0, 0, 0};
+    vo_philox_init(&e.p, key, ctr);
+    vo_normal_d st_normal = {0, 1, 0, 0};
+    vo_gamma st_gamma;
+    vo_gamma_init(&st_gamma, m->nu / 2, 2);
+    double x, y, vx, vy;
+    vo_pair_d(&e.p, m->sd_pos0, &x, &y);
+    vo_pair_d(&e.p, m->sd_vel0, &vx, &vy);
+    const double h = 0.5 * m->dt * m->dt;
+    for (size_t t = 0; t != T; ++t) {
+        if (t > 0) {
+            double ax, ay;
+            vo_pair_d(&e.p, m->sigma_a, &ax, &ay);
+            x = x + m->dt * vx + h * ax;
+            y = y + m->dt * vy + h * ay;
+            vx = vx + m->dt * ax;
+            vy = vy + m->dt * ay;
+        }
+        truth[4 * t + 0] = x;
+        truth[4 * t + 1] = y;
+        truth[4 * t + 2] = vx;
+        truth[4 * t + 3] = vy;
+        double ex, ey;
+        {
+            const double z = vo_normal_d_draw(&st_normal, &e);
+            ex = z * sqrt(m->nu / vo_gamma_draw(&st_gamma, &e));
+        }
+        {
+            const double z = vo_normal_d_draw(&st_normal, &e);
+            ey = z * sqrt(m->nu / vo_gamma_draw(&st_gamma, &e));
+        }
+        obs[2 * t + 0] = x + m->obs_scale * ex;
+        obs[2 * t + 1] = y + m->obs_scale * ey;
+    }
+}
+
+/* Particle::resample + Sampler::do_resample; returns 1 if resampled */
+static int vo_pf_resample(int scheme, double threshold, size_t N,
+    vo_philox *reng, double *W, double *ess, int *rep, int *idx,
+    void *state, int precision)
+{
+    const int resampled = *ess < threshold * (double)N;
+    if (resampled) {
+        vo_resample(scheme, N, N, reng, W, rep);
+        vo_resample_trans_rep_index(N, N, rep, idx);
+        if (precision == 32) {
+            float *s = (float *)state;
+            _Pragma("omp parallel for schedule(static)")
+            for (size_t i = 0; i < N; ++i)
+                for (size_t d = 0; d != 4; ++d)
+                    s[d * N + i] = s[d * N + (size_t)idx[i]];
+        } else {
+            double *s = (double *)state;
+            _Pragma("omp parallel for schedule(static)")
+            for (size_t i = 0; i < N; ++i)
+                for (size_t d = 0; d != 4; ++d)
+                    s[d * N + i] = s[d * N + (size_t)idx[i]];
+        }
+        *ess = vo_weight_set_equal(N, W);
+    }
+    return resampled;
+}
+
+static void vo_pf_mean(size_t N, const void *state, int precision,
+    const double *W, double out[2])
+{
+    for (size_t d = 0; d != 2; ++d) {
+        double s = 0;
+        if (precision == 32) {
+            const float *st = (const float *)state + d * N;
+            for (size_t i = 0; i != N; ++i)
+                s += (double)st[i] * W[i];
+        } else {
+            const double *st = (const double *)state + d * N;
+            for (size_t i = 0; i != N; ++i)
+                s += st[i] * W[i];
+        }
+        out[d] = s;
+    }
+}
+
+int vo_pf_run(int precision, size_t N, size_t T, uint32_t seed, int scheme,
+    double threshold, const vo_model *m, const double *obs, int threads,
+    double *mean_out, double *ess_out, int *resampled_out, double *logz_out)
+{
+#ifdef _OPENMP
+    int saved_threads = omp_get_max_threads();
+    if (threads > 0)
+        omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    const size_t esz = precision == 32 ? sizeof(float) : sizeof(double);
+    void *state = malloc(esz * 4 * N);
+    double *W = (double *)malloc(sizeof(double) * N);
+    double *ll = (double *)malloc(sizeof(double) * N);
+    float *llf = (float *)malloc(sizeof(float) * N);
+    int *rep = (int *)malloc(sizeof(int) * N);
+    int *idx = (int *)malloc(sizeof(int) * N);
+    vo_philox reng;
+    const uint32_t rkey[2] = {0, seed};
+    const uint32_t rctr[4] = {0, 0, 1, 0};
+    vo_philox_init(&reng, rkey, rctr);
+    double ess = vo_weight_set_equal(N, W);
+    double logz = 0;
+    for (size_t t = 0; t != T; ++t) {
+        if (precision == 32) {
+            if (t == 0)
+                vo_pf_init_f32(N, seed, m, obs, (float *)state, llf);
+            else
+                vo_pf_move_f32(N, t, seed, m, obs + 2 * t, (float *)state, llf);
+            for (size_t i = 0; i != N; ++i)
+                ll[i] = (double)llf[i];
+        } else {
+            if (t == 0)
+                vo_pf_init_f64(N, seed, m, obs, (double *)state, ll);
+            else
+                vo_pf_move_f64(N, t, seed, m, obs + 2 * t, (double *)state, ll);
+        }
+        double mx = -INFINITY;
+        for (size_t i = 0; i != N; ++i)
+            if (mx < ll[i])
+                mx = ll[i];
+        double s = 0;
+        if (t == 0) {
+            for (size_t i = 0; i != N; ++i)
+                s += exp(ll[i] - mx);
+            logz += mx + log(s / (double)N);
+            double *tmp = (double *)malloc(sizeof(double) * N);
+            ess = vo_weight_set_log(N, ll, tmp);
+            memcpy(W, tmp, sizeof(double) * N);
+            free(tmp);
+        } else {
+            for (size_t i = 0; i != N; ++i)
+                s += W[i] * exp(ll[i] - mx);
+            logz += mx + log(s);
+            for (size_t i = 0; i != N; ++i)
+                W[i] = log(W[i]);
+            for (size_t i = 0; i != N; ++i)
+                W[i] = W[i] + ll[i];
+            ess = vo_weight_post_set_log(N, W);
+        }
+        logz_out[t] = logz;
+        ess_out[t] = ess;
+        resampled_out[t] = vo_pf_resample(
+            scheme, threshold, N, &reng, W, &ess, rep, idx, state, precision);
+        vo_pf_mean(N, state, precision, W, mean_out + 2 * t);
+    }
+    free(state);
+    free(W);
+    free(ll);
+    free(llf);
+    free(rep);
+    free(idx);
+#ifdef _OPENMP
+    omp_set_num_threads(saved_threads);
+#endif
+    return 0;
+}
