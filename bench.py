@@ -1,0 +1,375 @@
+"""Benchmark: the large single bootstrap filter on GB300.
+
+Workload: the 4D constant-velocity tracking model with Student-t (nu 10,
+scale 0.5) position observations simulated from the model (seed 0), T = 200
+steps, N = 2^24 particles, FP32 SoA state, FP64 block-level log-sum-exp, an
+exact 64-bit fixed-point CDF, systematic resampling when ESS < N / 2.
+One bench step = one complete filter run (initialize + 199 iterations) =
+N * T particle-steps.  The metric is particle-steps per second.
+
+    value  device-resident: observations already in HBM (vsmc_cuda_pf_run_device)
+    e2e    through the C ABI with pinned host buffers (vsmc_cuda_pf_run):
+           observations copied in, histories copied out, every step
+    roofline  the fused move / likelihood / weight kernel, timed with CUDA
+           events on the filter's stream, against the measured HBM copy peak
+    cpu_baseline  the oracle's C restatement of the reference filter on the
+           host cores (OpenMP), on a bounded sample of the workload
+
+`--impl reference` times the reference arm: the oracle restatement of the
+reference's CPU filter (the reference tree is not present on the GPU host),
+rank 0 only.
+
+Multi-GPU (torchrun): every rank runs an independent filter replica (the path
+does not shard across filters); value = all ranks' particle-steps / max time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_PARTICLES = 1 << 24
+T_STEPS = 200
+SCHEME = 2  # systematic
+THRESHOLD = 0.5
+L2_BYTES = 126 * 1024 * 1024
+BYTES_PER_PARTICLE_STEP = 40  # 16 state read + 16 state write + 4 lw read + 4 lw write
+METRIC = "particle-steps/sec (plain bootstrap filter)"
+UNIT = "particle-steps/s"
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}",
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"],
+                    "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_setup(gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def simulate_obs(vc, T, seed=0):
+    """Observations simulated on the device by the product simulator."""
+    import torch
+    truth = torch.zeros(4 * T, dtype=torch.float64, device="cuda")
+    obs = torch.zeros(2 * T, dtype=torch.float64, device="cuda")
+    m = vc.default_model()
+    vc.call("vsmc_cuda_cv_simulate", seed, T, ctypes.byref(m),
+            truth.data_ptr(), obs.data_ptr(),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    return obs
+
+
+def cpu_filter_rate(n, T, threads=0, seed=0):
+    """Oracle restatement of the reference filter on host cores (FP32 state,
+    systematic, ESS < N/2); returns (particle-steps/s, seconds, threads)."""
+    from oracle import binding
+    port = binding.port()
+    m = binding.default_model()
+    tr = np.zeros(4 * T)
+    ob = np.zeros(2 * T)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    port.vo_pf_simulate(seed, T, ctypes.byref(m), P(tr), P(ob))
+    mean = np.zeros(2 * T)
+    ess = np.zeros(T)
+    res = np.zeros(T, np.int32)
+    logz = np.zeros(T)
+    t0 = time.perf_counter()
+    port.vo_pf_run(32, n, T, 1, SCHEME, THRESHOLD, ctypes.byref(m), P(ob),
+                   threads, P(mean), P(ess), P(res), P(logz))
+    dt = time.perf_counter() - t0
+    nthreads = threads if threads > 0 else (os.cpu_count() or 1)
+    return n * T / dt, dt, nthreads
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    n, T = 1 << 20, 50
+    for _ in range(args.warmup):
+        cpu_filter_rate(n, T)
+    total = 0.0
+    rates = []
+    for _ in range(args.steps):
+        r, dt, threads = cpu_filter_rate(n, T)
+        total += dt
+        rates.append(r)
+    value = n * T * args.steps / total
+    sample = (f"N=2^20 particles x T={T} steps per bench step (the "
+              f"N=2^24, T=200 workload scaled down), FP32 state, systematic")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (observations simulated from the model, seed 0)",
+        "config": {"workload": "large single bootstrap filter (CPU sample)",
+                   "particles": n, "steps_T": T, "scheme": "systematic",
+                   "threshold": THRESHOLD},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_PARTICLES)
+    ap.add_argument("--T", type=int, default=T_STEPS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import vsmc_gb300 as vc
+    vc.lib()
+    n, T = args.n, args.T
+    # a dedicated (non-legacy) stream: the filter captures its step in a graph
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    obs_dev = simulate_obs(vc, T, seed=0)
+    pf = vc.ParticleFilter(n, 32, SCHEME, THRESHOLD, seed=1 + rank,
+                           max_steps=T, stream=sptr)
+
+    # ---- device-resident timed region
+    for _ in range(args.warmup):
+        pf.run_device(T, obs_dev.data_ptr())
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        pf.run_device(T, obs_dev.data_ptr())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    hist = pf.history(T)
+
+    # ---- fused step kernel alone (roofline), same stream, CUDA events
+    nk = 50
+    evk0 = torch.cuda.Event(enable_timing=True)
+    evk1 = torch.cuda.Event(enable_timing=True)
+    pf.run_device(T, obs_dev.data_ptr())
+    for _ in range(5):
+        pf.launch_step_kernel()
+    evk0.record(stream)
+    for _ in range(nk):
+        pf.launch_step_kernel()
+    evk1.record(stream)
+    torch.cuda.synchronize()
+    kernel_ms = evk0.elapsed_time(evk1) / nk
+
+    # ---- end to end through the C ABI with pinned host buffers
+    obs_host = torch.empty((T, 2), dtype=torch.float64, pin_memory=True)
+    obs_host.copy_(obs_dev.view(T, 2).cpu())
+    out_mean = torch.empty((T, 2), dtype=torch.float64, pin_memory=True)
+    out_ess = torch.empty(T, dtype=torch.float64, pin_memory=True)
+    out_res = torch.empty(T, dtype=torch.int32, pin_memory=True)
+    out_logz = torch.empty(T, dtype=torch.float64, pin_memory=True)
+    L = vc.lib()
+
+    def e2e_run():
+        vc.check(L.vsmc_cuda_pf_run(pf.handle, T, obs_host.data_ptr(),
+                                    out_mean.data_ptr(), out_ess.data_ptr(),
+                                    out_res.data_ptr(), out_logz.data_ptr()),
+                 "vsmc_cuda_pf_run")
+
+    for _ in range(2):
+        e2e_run()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(2, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_run()  # synchronizes: histories are in host memory on return
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clocks.stop()
+    pf.close()
+
+    ms_max = max_over_ranks(ms, world)
+    e2e_max = max_over_ranks(e2e_s, world)
+    psteps = float(n) * T
+    value = world * psteps * args.steps / (ms_max / 1000.0)
+    e2e_value = world * psteps * e2e_steps / e2e_max
+    peak, peak_kind = measured_peaks()
+    achieved = BYTES_PER_PARTICLE_STEP * n / (kernel_ms / 1000.0) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_pf32_step.json")
+    if os.path.exists(prof):
+        with open(prof) as fh:
+            per_particle = json.load(fh).get("dram_bytes_per_particle")
+        if per_particle:
+            traffic = per_particle * n
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        r, dt, threads = cpu_filter_rate(1 << 20, 20)
+        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "N=2^20 particles x T=20 steps (one run), FP32 state, "
+                         "systematic, oracle restatement of the reference "
+                         "filter, OpenMP move / copy, sequential weights and "
+                         "resampling as in the reference"}
+
+    if rank == 0:
+        launches_per_run = 1 + 5 + 6 * (T - 1) + 1 + 1
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (observations simulated from the model on the "
+                    "device, seed 0)",
+            "config": {
+                "workload": "large single bootstrap filter: 4D constant "
+                            "velocity, Student-t(10, 0.5) observations",
+                "particles": n, "steps_T": T, "scheme": "systematic",
+                "threshold": THRESHOLD, "state": "fp32 SoA",
+                "reduction": "fp64 block-level log-sum-exp",
+                "cdf": "exact 64-bit fixed point",
+                "l2": "inputs larger than L2 (state 256 MiB + log-weights "
+                      "64 MiB at N=2^24); no flush",
+                "replicas": world,
+                "resampled_steps_last_run": int(hist["resampled"].sum()),
+                "final_log_evidence": float(hist["logz"][-1]),
+            },
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": 16 * T,
+                    "d2h_bytes_per_step": (16 + 8 + 4 + 8) * T},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind,
+                         "kernel": "k_pf32_step (fused move / likelihood / "
+                                   "log-weight / FP64 reduction)",
+                         "kernel_ms": kernel_ms,
+                         "bytes_per_launch": BYTES_PER_PARTICLE_STEP * n,
+                         "traffic": traffic},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": launches_per_run * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,340 @@
+/* vsmc_cuda.h - C ABI of libvsmc_cuda, the GB300 (sm_103a) backend for the
+ * vSMC particle-filter step.
+ *
+ * Conventions (every entry point):
+ *   - returns an int status: VSMC_CUDA_OK (0) or a negative vsmc_cuda_status;
+ *   - array arguments are DEVICE pointers unless the comment says "host";
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream); work
+ *     is enqueued on it and the call returns without waiting, except where a
+ *     comment says the call synchronizes;
+ *   - lengths are size_t and must be below 2^31 (int32 replication / index
+ *     arrays, as the reference's C ABI uses int);
+ *   - index arrays are int32, weights double, states SoA ([dim][N]).
+ *
+ * Each declaration names the reference interface it replaces (path inside the
+ * vSMC source tree, file:line).  The reference's own C ABI is
+ * include/vsmc/vsmc.h; its C++ API is the Sampler / Particle / Weight /
+ * StateMatrix / Monitor templates in include/vsmc/core/. */
+#ifndef VSMC_CUDA_H
+#define VSMC_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- status */
+
+typedef enum {
+    VSMC_CUDA_OK = 0,
+    VSMC_CUDA_ERR_ARG = -1,       /* null pointer / bad enum / bad argument */
+    VSMC_CUDA_ERR_SIZE = -2,      /* length out of the supported range */
+    VSMC_CUDA_ERR_NONFINITE = -3, /* NaN, inf or negative weight */
+    VSMC_CUDA_ERR_TIMEOUT = -4,   /* a bounded device wait gave up */
+    VSMC_CUDA_ERR_CUDA = -5,      /* CUDA runtime error (see last_cuda_error) */
+    VSMC_CUDA_ERR_ALLOC = -6,     /* device allocation failed */
+    VSMC_CUDA_ERR_INTERNAL = -7   /* an internal consistency check failed */
+} vsmc_cuda_status;
+
+const char *vsmc_cuda_status_string(int status);
+/* cudaError_t value of the last CUDA failure seen by the library (0 = none) */
+int vsmc_cuda_last_cuda_error(void);
+int vsmc_cuda_version(void); /* major * 10000 + minor * 100 + patch */
+
+/* --------------------------------------------------------- RNG engines */
+
+typedef enum {
+    VSMC_CUDA_PHILOX4X32 = 0,  /* vsmc::Philox4x32   (rng/philox.hpp:309) */
+    VSMC_CUDA_THREEFRY4X64 = 1 /* vsmc::Threefry4x64 (rng/threefry.hpp:389) */
+} vsmc_cuda_rng_kind;
+
+/* Host-side engine state: the CounterEngine<Gen> state of
+ * rng/counter.hpp:288-496 made explicit.  Philox4x32 uses the low 32 bits of
+ * key[0..1] and ctr[0..3]; Threefry4x64 uses all four 64-bit limbs.
+ * index is the next word of the current block (4 = block exhausted); the
+ * current block itself is gen(ctr), so it is not stored.
+ * Replaces the opaque `vsmc_rng` of include/vsmc/vsmc.h:48-50. */
+typedef struct {
+    int32_t kind;
+    uint32_t index;
+    uint64_t key[4];
+    uint64_t ctr[4];
+} vsmc_cuda_rng;
+
+/* CounterEngine(seed): key = {seed, 0, ...}, ctr = 0 (rng/counter.hpp:309-314).
+ * Replaces vsmc_rng_init / vsmc_rng_seed (vsmc.h:55-58, lib/src/vsmc_rng.cpp:68-78). */
+int vsmc_cuda_rng_init(vsmc_cuda_rng *rng, int kind, uint64_t seed);
+/* CounterEngine::key(k): sets the key and resets ctr to 0
+ * (rng/counter.hpp:341-345); n = number of limbs given.
+ * Replaces vsmc_rng_set_key (vsmc.h:64, lib/src/vsmc_rng.cpp:89-98). */
+int vsmc_cuda_rng_set_key(vsmc_cuda_rng *rng, int n, const uint64_t *key);
+/* CounterEngine::ctr(c): sets the counter, drops the buffered block
+ * (rng/counter.hpp:335-339).  Replaces vsmc_rng_set_ctr (vsmc.h:70). */
+int vsmc_cuda_rng_set_ctr(vsmc_cuda_rng *rng, int n, const uint64_t *ctr);
+
+/* Counter-addressed blocks: block b (0-based) = gen(ctr0 + b + 1, key), the
+ * reference's pre-increment convention (rng/philox.hpp:263-269), so
+ * ctr0 = engine.ctr() reproduces the engine's scalar stream.  out receives
+ * 4 * nblocks words.  Replaces PhiloxGenerator::operator() /
+ * ThreefryGenerator::operator() (rng/philox.hpp:263-294,
+ * rng/threefry.hpp:329-366) applied over a range of counters. */
+int vsmc_cuda_philox4x32_blocks(const uint32_t key[2], const uint32_t ctr0[4],
+    size_t nblocks, uint32_t *out, void *stream);
+int vsmc_cuda_threefry4x64_blocks(const uint64_t key[4],
+    const uint64_t ctr0[4], size_t nblocks, uint64_t *out, void *stream);
+
+/* n raw words through the engine's bulk path, bit-exact with
+ * CounterEngine::operator()(n, r) (rng/counter.hpp:357-390), including its
+ * counter handling for blocks whose low limb is all ones
+ * (rng/counter.hpp:78-89, 230-262).  r is uint32_t* (Philox) or uint64_t*
+ * (Threefry).  `rng` (host) is advanced.  Replaces vsmc_rng_rand
+ * (vsmc.h:74, lib/src/vsmc_rng.cpp:124-129) and rng_rand
+ * (rng/counter.hpp:499-504). */
+int vsmc_cuda_rng_rand(vsmc_cuda_rng *rng, size_t n, void *r, void *stream);
+
+/* u01_distribution: n reals in [0,1), same words and values as the
+ * reference batch path (rng/u01_distribution.hpp:215-233).  `rng` advanced.
+ * Replaces vsmc_rng_u01 (vsmc.h:161, lib/src/vsmc_rng.cpp:203). */
+int vsmc_cuda_rng_u01(vsmc_cuda_rng *rng, size_t n, double *r, void *stream);
+int vsmc_cuda_rng_u01_f32(vsmc_cuda_rng *rng, size_t n, float *r, void *stream);
+
+/* normal_distribution: n normals, the reference batch layout (per 1024
+ * chunk: first half sine branch, second half cosine branch; an odd n takes
+ * two more words for the last value) (rng/normal_distribution.hpp:222-267).
+ * Values agree with the reference within libm accuracy.  `rng` advanced.
+ * Replaces vsmc_rng_normal (vsmc.h:147, lib/src/vsmc_rng.cpp:213). */
+int vsmc_cuda_rng_normal(vsmc_cuda_rng *rng, size_t n, double *r, double mean,
+    double stddev, void *stream);
+int vsmc_cuda_rng_normal_f32(vsmc_cuda_rng *rng, size_t n, float *r,
+    float mean, float stddev, void *stream);
+
+/* Independent streams with the scalar distribution semantics: stream s is
+ * the engine (kind, key) placed at counter {0, s, 0, 0}; it yields
+ * per_stream variates into r[s * per_stream + k] exactly as successive
+ * calls of NormalDistribution<double>(mean, sd) (rng/normal_distribution.hpp:
+ * 199-216) or StudentTDistribution<double>(df) (rng/student_t_distribution.hpp:
+ * 78-91, gamma by rng/gamma_distribution.hpp:132-216) on that engine. */
+int vsmc_cuda_normal_streams(int kind, const uint64_t key[4], size_t nstreams,
+    size_t per_stream, double mean, double stddev, double *r, void *stream);
+int vsmc_cuda_student_t_streams(int kind, const uint64_t key[4],
+    size_t nstreams, size_t per_stream, double df, double *r, void *stream);
+
+/* u01 sequence array forms (rng/u01_sequence.hpp:53-89).  Replace
+ * vsmc_rng_u01_sorted / _stratified / _systematic (vsmc.h:76-83).  The
+ * sorted form's running log sum is the reference's left-to-right sum
+ * bit for bit; log/exp come from CUDA's libm. */
+int vsmc_cuda_u01_sorted(size_t n, const double *u01, double *u01seq,
+    void *stream);
+int vsmc_cuda_u01_stratified(size_t n, const double *u01, double *u01seq,
+    void *stream);
+int vsmc_cuda_u01_systematic(size_t n, double u01, double *u01seq,
+    void *stream);
+
+/* --------------------------------------------------------------- sums */
+
+/* Left-to-right double sum s_i = (...((0 + x_0) + x_1) ... + x_i) of n
+ * non-negative finite values, bit-identical to a sequential loop (the order
+ * std::accumulate and the reference's resampling CDF use,
+ * resample/transform.hpp:61-69, core/weight.hpp:228).  prefix may be NULL
+ * (only *total_dev is written); total_dev (device, 1 double) may be NULL.
+ * Returns VSMC_CUDA_ERR_NONFINITE for a negative or non-finite input;
+ * synchronizes the stream to report it. */
+int vsmc_cuda_sequential_sum(size_t n, const double *x, double *prefix,
+    double *total_dev, void *stream);
+
+/* ---------------------------------------------------------- resampling */
+
+typedef enum {
+    VSMC_CUDA_MULTINOMIAL = 0,
+    VSMC_CUDA_STRATIFIED = 1,
+    VSMC_CUDA_SYSTEMATIC = 2,
+    VSMC_CUDA_RESIDUAL = 3,
+    VSMC_CUDA_RESIDUAL_STRATIFIED = 4,
+    VSMC_CUDA_RESIDUAL_SYSTEMATIC = 5
+} vsmc_cuda_resample_scheme; /* = vsmc::ResampleScheme (internal/defines.hpp:57-64) */
+
+/* Replication counts from m normalized weights and n uniforms, identical to
+ * the reference's two-pointer loop (resample/transform.hpp:43-71) for the
+ * same inputs, including unsorted uniforms (counted up to the first
+ * uniform above each cumulative weight).
+ * Replaces vsmc_resample_trans_u01_rep (vsmc.h:286, lib/src/vsmc_resample.cpp:48-53). */
+int vsmc_cuda_resample_trans_u01_rep(size_t m, size_t n, const double *weight,
+    const double *u01, int *replication, void *stream);
+/* Parent index per uniform (resample/transform.hpp:75-96).
+ * Replaces vsmc_resample_trans_u01_index (vsmc.h:288). */
+int vsmc_cuda_resample_trans_u01_index(size_t m, size_t n,
+    const double *weight, const double *u01, int *index, void *stream);
+/* Replication counts -> parent indices with the reference's slot layout:
+ * for m == n a parent keeps its own slot and empty slots are filled, in
+ * order, by surplus copies of parents taken in order
+ * (resample/transform.hpp:100-134).
+ * Replaces vsmc_resample_trans_rep_index (vsmc.h:290). */
+int vsmc_cuda_resample_trans_rep_index(size_t m, size_t n,
+    const int *replication, int *index, void *stream);
+/* Parent indices -> replication counts (resample/transform.hpp:138-150).
+ * Replaces vsmc_resample_trans_index_rep (vsmc.h:292). */
+int vsmc_cuda_resample_trans_index_rep(size_t m, size_t n, const int *index,
+    int *replication, void *stream);
+/* Residual split (resample/transform.hpp:155-168): resid = frac(n * w)
+ * normalized by its left-to-right sum, integ = integer parts; *r_host gets
+ * n - sum(integ).  Synchronizes the stream.
+ * Replaces vsmc_resample_trans_residual (vsmc.h:294). */
+int vsmc_cuda_resample_trans_residual(size_t m, size_t n,
+    const double *weight, double *resid, int *integ, size_t *r_host,
+    void *stream);
+
+/* Resampling schemes with an engine: counts identical to the reference
+ * functors for the same weights and engine state, and the engine advanced by
+ * exactly the words the reference consumes.  Multinomial / Residual build
+ * their sorted uniforms with CUDA's log/exp, so a uniform can differ from the
+ * reference's in the last bit; every other scheme is bit-exact end to end.
+ * `rng` (host) is advanced; the call synchronizes the stream.  Philox4x32
+ * engines only.  Replaces vsmc_resample_<scheme> and vsmc_resample
+ * (vsmc.h:277-310, lib/src/vsmc_resample.cpp:84-116) and
+ * Resample<Scheme>::operator() (resample/multinomial.hpp:46-52,
+ * stratified.hpp:46-52, systematic.hpp:46-52, residual.hpp:46-57,
+ * residual_stratified.hpp:46-57, residual_systematic.hpp:46-57). */
+int vsmc_cuda_resample(size_t m, size_t n, vsmc_cuda_rng *rng,
+    const double *weight, int *replication, int scheme, void *stream);
+int vsmc_cuda_resample_multinomial(size_t m, size_t n, vsmc_cuda_rng *rng,
+    const double *weight, int *replication, void *stream);
+int vsmc_cuda_resample_stratified(size_t m, size_t n, vsmc_cuda_rng *rng,
+    const double *weight, int *replication, void *stream);
+int vsmc_cuda_resample_systematic(size_t m, size_t n, vsmc_cuda_rng *rng,
+    const double *weight, int *replication, void *stream);
+int vsmc_cuda_resample_residual(size_t m, size_t n, vsmc_cuda_rng *rng,
+    const double *weight, int *replication, void *stream);
+int vsmc_cuda_resample_residual_stratified(size_t m, size_t n,
+    vsmc_cuda_rng *rng, const double *weight, int *replication, void *stream);
+int vsmc_cuda_resample_residual_systematic(size_t m, size_t n,
+    vsmc_cuda_rng *rng, const double *weight, int *replication, void *stream);
+
+/* In-place particle copy state[d][dst] = state[d][index[dst]] for a SoA
+ * state of `dim` rows of n values; safe in place for indices produced by
+ * vsmc_cuda_resample_trans_rep_index (every parent keeps its slot).
+ * Replaces StateMatrix<ColMajor,Dim,T>::copy (core/state_matrix.hpp:357-364)
+ * and StateOMP::copy (smp/backend_omp.hpp:53-59). */
+int vsmc_cuda_state_copy_f32(size_t n, size_t dim, const int *index,
+    float *state, void *stream);
+int vsmc_cuda_state_copy_f64(size_t n, size_t dim, const int *index,
+    double *state, void *stream);
+
+/* ------------------------------------------------------------- weights */
+
+/* The Weight class on device (core/weight.hpp:67-230).  W holds normalized
+ * weights (n doubles); *ess_dev (device, 1 double) receives 1 / sum W^2.
+ * Sums run left to right in the reference's order, so set() is bit-exact;
+ * set_log / add_log use CUDA's exp / log.
+ *   set:       Weight::set (weight.hpp:115-120)     W = w / sum(w)
+ *   set_log:   Weight::set_log (weight.hpp:145-149) W = exp(lw - max) normalized
+ *   add_log:   Weight::add_log (weight.hpp:168-173) W = W * exp(l) normalized
+ *   set_equal: Weight::set_equal (weight.hpp:99-103) */
+int vsmc_cuda_weight_set(size_t n, const double *w, double *W,
+    double *ess_dev, void *stream);
+int vsmc_cuda_weight_set_log(size_t n, const double *lw, double *W,
+    double *ess_dev, void *stream);
+int vsmc_cuda_weight_add_log(size_t n, const double *l, double *W,
+    double *ess_dev, void *stream);
+int vsmc_cuda_weight_set_equal(size_t n, double *W, double *ess_dev,
+    void *stream);
+
+/* Weighted mean of each SoA row: out_dev[d] = sum_i W_i * state[d][i] for
+ * d < dim (the Monitor::eval dgemv, core/monitor.hpp:252-267). */
+int vsmc_cuda_monitor_mean_f64(size_t n, size_t dim, const double *state,
+    const double *W, double *out_dev, void *stream);
+int vsmc_cuda_monitor_mean_f32(size_t n, size_t dim, const float *state,
+    const double *W, double *out_dev, void *stream);
+
+/* ------------------------------------------------------ particle filter */
+
+/* Constant-velocity tracking model with Student-t position observations:
+ * state (x, y, vx, vy); x_t = F x_{t-1} + G a_t, a ~ N(0, sigma_a^2 I2);
+ * prior x, y ~ N(0, sd_pos0^2), vx, vy ~ N(0, sd_vel0^2); observation
+ * (x, y) + obs_scale * t_nu per coordinate.  The user move of
+ * example/pf/include/pf.hpp:154-170 in this model's form. */
+typedef struct {
+    double dt, sigma_a, obs_scale, nu, sd_pos0, sd_vel0;
+} vsmc_cuda_cv_model;
+
+typedef struct vsmc_cuda_pf vsmc_cuda_pf; /* opaque */
+
+/* A bootstrap filter over n particles.
+ *   precision 64: FP64 state; weights kept as the reference's Weight class
+ *     (normalized doubles, left-to-right sums) and resampled by the exact
+ *     scheme path above -- the reference's arithmetic step for step.
+ *   precision 32: FP32 SoA state and log-weights in one fused move /
+ *     likelihood / reduction kernel; FP64 block-level log-sum-exp; an exact
+ *     64-bit fixed-point CDF for resampling.
+ * `stream` NULL gives the filter a private non-blocking stream (the legacy
+ * stream cannot be captured in a CUDA graph); vsmc_cuda_pf_stream returns
+ * the stream in use.
+ * Particle streams: Philox4x32 key {step, seed}, counter {0, particle, 0, 0};
+ * resampling engine key {0, seed} from counter {0, 0, 1, 0}.
+ * Replaces Sampler<T>(N, scheme, threshold) (core/sampler.hpp:107-114) with
+ * a CUDA state / move / weight / monitor (smp/backend_omp.hpp:45-133 are the
+ * CPU siblings). */
+int vsmc_cuda_pf_create(vsmc_cuda_pf **pf, size_t n, int precision,
+    int scheme, double threshold, uint32_t seed,
+    const vsmc_cuda_cv_model *model, size_t max_steps, void *stream);
+int vsmc_cuda_pf_destroy(vsmc_cuda_pf *pf);
+/* Sampler::initialize (core/sampler.hpp:443-455) with observation obs_dev[0..1]
+ * (device, 2 doubles). */
+int vsmc_cuda_pf_initialize(vsmc_cuda_pf *pf, const double *obs_dev);
+/* Sampler::iterate() (core/sampler.hpp:464-476) with observation obs_dev[0..1]. */
+int vsmc_cuda_pf_iterate(vsmc_cuda_pf *pf, const double *obs_dev);
+/* initialize + (T-1) iterates over obs_dev[2t..2t+1] (device), recording
+ * per step: mean (2 doubles), ESS, resampled flag and cumulative log
+ * evidence into the device histories. */
+int vsmc_cuda_pf_run_device(vsmc_cuda_pf *pf, size_t T, const double *obs_dev);
+/* Whole run through host buffers (the end-to-end entry point): copies the
+ * T x 2 observations in, runs, copies the histories out, synchronizes.
+ * Any output pointer may be NULL. */
+int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
+    double *mean_host, double *ess_host, int *resampled_host,
+    double *logz_host);
+/* Copy the first T recorded history entries to host (synchronizes). */
+int vsmc_cuda_pf_history(vsmc_cuda_pf *pf, size_t T, double *mean_host,
+    double *ess_host, int *resampled_host, double *logz_host);
+/* Device views: SoA state (4 rows x, y, vx, vy, each of stride
+ * ((n + 255) / 256) * 256 elements, float or double by precision), and the
+ * weight array (precision 64: normalized W doubles; precision 32: float
+ * log-weights; after a resampling step every weight is equal and the stored
+ * log-weights are stale until the next step). */
+int vsmc_cuda_pf_state(vsmc_cuda_pf *pf, void **state_dev, void **weight_dev);
+int vsmc_cuda_pf_stream(vsmc_cuda_pf *pf, void **stream);
+/* Enable (1) / disable (0) capturing each filter step in a CUDA graph and
+ * replaying it (precision 32 only; default on). */
+int vsmc_cuda_pf_use_graph(vsmc_cuda_pf *pf, int on);
+/* Profiling hook (precision 32, after initialize): launch only the fused
+ * move / likelihood / weight-reduction kernel of one step on the filter's
+ * stream, without the resampling kernels.  Steps past max_steps reuse the
+ * last observation and record no history.  No reference counterpart: it
+ * times the dominant kernel of MoveOMP::operator() + Weight::add_log
+ * (smp/backend_omp.hpp:93-105, core/weight.hpp:168-173). */
+int vsmc_cuda_pf_launch_step_kernel(vsmc_cuda_pf *pf);
+
+/* One move + log-likelihood step on caller-owned SoA state (kernel-level
+ * parity entry point): t == 0 draws the prior, t > 0 propagates.  ll
+ * receives the per-particle log-likelihood of obs (host, 2 doubles). */
+int vsmc_cuda_cv_move_f64(size_t n, size_t t, uint32_t seed,
+    const vsmc_cuda_cv_model *model, const double obs[2], double *state,
+    double *ll, void *stream);
+int vsmc_cuda_cv_move_f32(size_t n, size_t t, uint32_t seed,
+    const vsmc_cuda_cv_model *model, const double obs[2], float *state,
+    float *ll, void *stream);
+
+/* Simulate T steps of the model from the Philox4x32 engine seeded with seed
+ * (truth: T x 4, obs: T x 2, device), prior pairs and acceleration pairs from
+ * fresh NormalDistribution<double> objects, observation noise from one
+ * StudentTDistribution<double>(nu) kept for the whole run. */
+int vsmc_cuda_cv_simulate(uint32_t seed, size_t T,
+    const vsmc_cuda_cv_model *model, double *truth, double *obs,
+    void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VSMC_CUDA_H */

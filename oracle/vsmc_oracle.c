@@ -1306,3 +1306,65 @@ int vo_pf_run(int precision, size_t N, size_t T, uint32_t seed, int scheme,
 #endif
     return 0;
 }
+
+/* =====================================================================
+ * Test helper: place an engine at (key, ctr), take k scalar words, then run
+ * one operation -- op 0: n words through the bulk path; 1 / 2:
+ * u01_distribution in f64 / f32; 3 / 4: normal_distribution in f64 / f32
+ * (mean, sd).  The engine state afterwards goes to ctr_out / index_out.
+ * Words and u01 values of a 32-bit engine are written as uint32 / real.
+ * ===================================================================== */
+void vo_engine_run(int kind, const uint64_t key[4], const uint64_t ctr[4],
+    size_t k, int op, size_t n, double mean, double sd, void *out,
+    uint64_t ctr_out[4], uint32_t *index_out)
+{
+    vo_eng e;
+    vo_eng_init(&e, kind, key, ctr);
+    for (size_t i = 0; i != k; ++i) {
+        if (kind == 0)
+            (void)vo_philox_next(&e.p);
+        else
+            (void)vo_threefry_next(&e.t);
+    }
+    if (op == 0) {
+        if (kind == 0)
+            vo_philox_rand(&e.p, n, (uint32_t *)out);
+        else
+            vo_threefry_rand(&e.t, n, (uint64_t *)out);
+    } else if (op == 1) {
+        vo_u01_distribution_d(&e, n, (double *)out);
+    } else if (op == 2) {
+        vo_u01_distribution_f(&e, n, (float *)out);
+    } else if (op == 3 || op == 4) {
+        const size_t kk = 1024, m = n / kk, l = n % kk;
+        if (op == 3) {
+            double *r = (double *)out;
+            for (size_t i = 0; i != m; ++i, r += kk)
+                vo_normal_impl_d(&e, kk, r, mean, sd);
+            vo_normal_impl_d(&e, l, r, mean, sd);
+            if (n % 2 != 0) {
+                const double u = vo_eng_u01d(&e), v = vo_eng_u01d(&e);
+                r[l - 1] = mean + sd * sqrt(-2 * log(u)) * cos(VO_PI_2 * v);
+            }
+        } else {
+            float *r = (float *)out;
+            const float fm = (float)mean, fs = (float)sd;
+            for (size_t i = 0; i != m; ++i, r += kk)
+                vo_normal_impl_f(&e, kk, r, fm, fs);
+            vo_normal_impl_f(&e, l, r, fm, fs);
+            if (n % 2 != 0) {
+                const float u = vo_eng_u01f(&e), v = vo_eng_u01f(&e);
+                r[l - 1] = fm + fs * sqrtf(-2 * logf(u)) * cosf(VO_PI_2F * v);
+            }
+        }
+    }
+    if (kind == 0) {
+        for (int i = 0; i != 4; ++i)
+            ctr_out[i] = e.p.ctr[i];
+        *index_out = e.p.index;
+    } else {
+        for (int i = 0; i != 4; ++i)
+            ctr_out[i] = e.t.ctr[i];
+        *index_out = e.t.index;
+    }
+}

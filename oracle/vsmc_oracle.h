@@ -137,6 +137,11 @@ void vo_pf_init_f32(size_t N, uint32_t seed, const vo_model *m,
     const double obs[2], float *state, float *ll_out);
 double vo_student_t_norm_const(double nu, double s);
 
+/* test helper: k scalar words, then one bulk / u01 / normal batch operation */
+void vo_engine_run(int kind, const uint64_t key[4], const uint64_t ctr[4],
+    size_t k, int op, size_t n, double mean, double sd, void *out,
+    uint64_t ctr_out[4], uint32_t *index_out);
+
 #ifdef __cplusplus
 }
 #endif

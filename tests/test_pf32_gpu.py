@@ -1,0 +1,169 @@
+"""FP32 / FP64 move + likelihood kernels, the simulator, and the FP32 fused
+filter against the oracle."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import P, dev, host
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(vc):
+    return vc.default_model()
+
+
+def _omodel():
+    from oracle.binding import default_model
+    return default_model()
+
+
+@pytest.mark.parametrize("t", [0, 1, 7])
+@pytest.mark.parametrize("n", [1, 3, 1000, 4097])
+def test_cv_move_f32_matches_oracle(vc, port, t, n):
+    rng = np.random.default_rng(t * 1000 + n)
+    state = rng.normal(0, 2, (4, n)).astype(np.float32)
+    obs = np.array([0.7, -1.3])
+    ds = dev(state.copy())
+    ll = dev(np.zeros(n, np.float32))
+    m = _model(vc)
+    vc.call("vsmc_cuda_cv_move_f32", n, t, 12345, ctypes.byref(m), P(obs),
+            ds.data_ptr(), ll.data_ptr(), None)
+    s_ref = state.copy()
+    l_ref = np.zeros(n, np.float32)
+    om = _omodel()
+    if t == 0:
+        port.vo_pf_init_f32(n, 12345, ctypes.byref(om), P(obs), P(s_ref),
+                            P(l_ref))
+    else:
+        port.vo_pf_move_f32(n, t, 12345, ctypes.byref(om), P(obs), P(s_ref),
+                            P(l_ref))
+    got_s = host(ds)
+    got_l = host(ll)
+    # FP32 kernel vs FP32 restatement: 1e-5 relative (absolute below 1)
+    np.testing.assert_allclose(got_s, s_ref, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(got_l, l_ref, rtol=1e-5, atol=1e-4)
+
+
+@pytest.mark.parametrize("t", [0, 1, 50])
+def test_cv_move_f32_vs_fp64_reference(vc, port, t):
+    """FP32 kernel against the FP64 computation on identical inputs."""
+    n = 2048
+    rng = np.random.default_rng(t)
+    state64 = rng.normal(0, 2, (4, n))
+    state32 = state64.astype(np.float32)
+    obs = np.array([1.5, 0.25])
+    ds = dev(state32.copy())
+    ll = dev(np.zeros(n, np.float32))
+    m = _model(vc)
+    vc.call("vsmc_cuda_cv_move_f32", n, t, 9, ctypes.byref(m), P(obs),
+            ds.data_ptr(), ll.data_ptr(), None)
+    s_ref = state32.astype(np.float64)
+    l_ref = np.zeros(n)
+    om = _omodel()
+    if t == 0:
+        port.vo_pf_init_f64(n, 9, ctypes.byref(om), P(obs), P(s_ref), P(l_ref))
+    else:
+        port.vo_pf_move_f64(n, t, 9, ctypes.byref(om), P(obs), P(s_ref),
+                            P(l_ref))
+    # the FP32 radius uniform is (0,1] with 24 bits, the FP64 one [0,1) with
+    # 32 bits: compare the move only where both draw the same radius
+    got = host(ds).astype(np.float64)
+    err = np.abs(got - s_ref) / np.maximum(1.0, np.abs(s_ref))
+    assert np.quantile(err, 0.99) < 1e-5
+
+
+@pytest.mark.parametrize("t", [0, 1, 99])
+@pytest.mark.parametrize("n", [1, 5, 3000])
+def test_cv_move_f64_matches_oracle(vc, port, t, n):
+    rng = np.random.default_rng(t + 17 * n)
+    state = rng.normal(0, 2, (4, n))
+    obs = np.array([-0.3, 2.2])
+    ds = dev(state.copy())
+    ll = dev(np.zeros(n))
+    m = _model(vc)
+    vc.call("vsmc_cuda_cv_move_f64", n, t, 77, ctypes.byref(m), P(obs),
+            ds.data_ptr(), ll.data_ptr(), None)
+    s_ref = state.copy()
+    l_ref = np.zeros(n)
+    om = _omodel()
+    if t == 0:
+        port.vo_pf_init_f64(n, 77, ctypes.byref(om), P(obs), P(s_ref),
+                            P(l_ref))
+    else:
+        port.vo_pf_move_f64(n, t, 77, ctypes.byref(om), P(obs), P(s_ref),
+                            P(l_ref))
+    np.testing.assert_allclose(host(ds), s_ref, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(host(ll), l_ref, rtol=1e-12, atol=1e-12)
+
+
+def test_simulate_matches_oracle(vc, port):
+    import torch
+    T = 200
+    truth = torch.zeros(4 * T, dtype=torch.float64, device="cuda")
+    obs = torch.zeros(2 * T, dtype=torch.float64, device="cuda")
+    m = _model(vc)
+    vc.call("vsmc_cuda_cv_simulate", 0, T, ctypes.byref(m), truth.data_ptr(),
+            obs.data_ptr(), None)
+    tr = np.zeros(4 * T)
+    ob = np.zeros(2 * T)
+    port.vo_pf_simulate(0, T, ctypes.byref(_omodel()), P(tr), P(ob))
+    np.testing.assert_allclose(host(truth), tr, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(host(obs), ob, rtol=1e-12, atol=1e-12)
+
+
+def _obs(port, T=100, seed=0):
+    tr = np.zeros(4 * T)
+    ob = np.zeros(2 * T)
+    port.vo_pf_simulate(seed, T, ctypes.byref(_omodel()), P(tr), P(ob))
+    return ob.reshape(T, 2), tr.reshape(T, 4)
+
+
+def _oracle_pf(port, prec, n, T, seed, scheme, obs):
+    mean = np.zeros(2 * T)
+    ess = np.zeros(T)
+    res = np.zeros(T, np.int32)
+    logz = np.zeros(T)
+    port.vo_pf_run(prec, n, T, seed, scheme, 0.5, ctypes.byref(_omodel()),
+                   P(np.ascontiguousarray(obs)), 0, P(mean), P(ess), P(res),
+                   P(logz))
+    return {"mean": mean.reshape(T, 2), "ess": ess, "resampled": res,
+            "logz": logz}
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("graph", [True, False])
+def test_pf32_filter_tracks_oracle(vc, port, scheme, graph):
+    """Same particle streams and resampling engine as the oracle's FP32
+    filter; the CDFs differ (fixed-point vs left-to-right FP64), so compare
+    with tolerances well inside the Monte Carlo error."""
+    T, n = 100, 1 << 14
+    obs, truth = _obs(port, T)
+    pf = vc.ParticleFilter(n, 32, scheme, 0.5, seed=3, max_steps=T)
+    pf.use_graph(graph)
+    g = pf.run(obs)
+    pf.close()
+    o = _oracle_pf(port, 32, n, T, 3, scheme, obs)
+    # step 0 is identical up to FP32 rounding
+    assert abs(g["ess"][0] - o["ess"][0]) / o["ess"][0] < 1e-4
+    assert abs(g["logz"][0] - o["logz"][0]) < 1e-4
+    # whole run: means and evidence within Monte Carlo error
+    assert np.abs(g["mean"] - o["mean"]).max() < 0.2
+    assert abs(g["logz"][-1] - o["logz"][-1]) < 1.0
+    assert np.abs(g["mean"] - truth[:, :2]).mean() < 0.5
+    assert g["resampled"].sum() > 5
+
+
+def test_pf32_reproducible_and_graph_equal(vc, port):
+    T, n = 60, 50000
+    obs, _ = _obs(port, T, seed=4)
+    outs = []
+    for graph in (True, False, True):
+        pf = vc.ParticleFilter(n, 32, 2, 0.5, seed=8, max_steps=T)
+        pf.use_graph(graph)
+        outs.append(pf.run(obs))
+        pf.close()
+    for o in outs[1:]:
+        for k in ("mean", "ess", "resampled", "logz"):
+            assert np.array_equal(o[k], outs[0][k]), k

@@ -1,0 +1,269 @@
+"""vsmc_gb300 -- GB300 (sm_103a) backend for the vSMC particle-filter step.
+
+The product is the C-ABI library ``libvsmc_cuda.so`` declared in
+``include/vsmc_cuda.h``.  This module loads it with ctypes, declares every
+prototype, and exposes thin Python wrappers that mirror the reference's C ABI
+(``vsmc_rng_*``, ``vsmc_resample_*`` of include/vsmc/vsmc.h) and its
+Sampler-level filter.  Arrays are device pointers (ints); callers usually pass
+``tensor.data_ptr()`` of CUDA tensors.
+
+There is no CPU fallback: if the CUDA library is missing or fails to load,
+``lib()`` raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = _build.LIB
+
+VP = ctypes.c_void_p
+SZ = ctypes.c_size_t
+I32 = ctypes.c_int
+U32 = ctypes.c_uint32
+U64 = ctypes.c_uint64
+F64 = ctypes.c_double
+F32 = ctypes.c_float
+
+# status codes (vsmc_cuda_status)
+OK = 0
+ERR_ARG = -1
+ERR_SIZE = -2
+ERR_NONFINITE = -3
+ERR_TIMEOUT = -4
+ERR_CUDA = -5
+ERR_ALLOC = -6
+ERR_INTERNAL = -7
+
+PHILOX4X32 = 0
+THREEFRY4X64 = 1
+
+# vsmc::ResampleScheme order (internal/defines.hpp:57-64)
+MULTINOMIAL = 0
+STRATIFIED = 1
+SYSTEMATIC = 2
+RESIDUAL = 3
+RESIDUAL_STRATIFIED = 4
+RESIDUAL_SYSTEMATIC = 5
+SCHEMES = {
+    "multinomial": MULTINOMIAL,
+    "stratified": STRATIFIED,
+    "systematic": SYSTEMATIC,
+    "residual": RESIDUAL,
+    "residual_stratified": RESIDUAL_STRATIFIED,
+    "residual_systematic": RESIDUAL_SYSTEMATIC,
+}
+
+
+class Rng(ctypes.Structure):
+    """vsmc_cuda_rng: explicit CounterEngine state (kind, index, key, ctr)."""
+    _fields_ = [("kind", ctypes.c_int32), ("index", ctypes.c_uint32),
+                ("key", U64 * 4), ("ctr", U64 * 4)]
+
+
+class CvModel(ctypes.Structure):
+    """vsmc_cuda_cv_model."""
+    _fields_ = [("dt", F64), ("sigma_a", F64), ("obs_scale", F64),
+                ("nu", F64), ("sd_pos0", F64), ("sd_vel0", F64)]
+
+
+def default_model():
+    """The benchmark tracking model: dt 0.1, acceleration sd 1, Student-t
+    (nu 10, scale 0.5) observations, prior position sd 2, velocity sd 1."""
+    return CvModel(0.1, 1.0, 0.5, 10.0, 2.0, 1.0)
+
+
+_RNGP = ctypes.POINTER(Rng)
+_MODELP = ctypes.POINTER(CvModel)
+
+# name -> (restype, argtypes)
+PROTOTYPES = {
+    "vsmc_cuda_status_string": (ctypes.c_char_p, [I32]),
+    "vsmc_cuda_last_cuda_error": (I32, []),
+    "vsmc_cuda_version": (I32, []),
+    "vsmc_cuda_rng_init": (I32, [_RNGP, I32, U64]),
+    "vsmc_cuda_rng_set_key": (I32, [_RNGP, I32, VP]),
+    "vsmc_cuda_rng_set_ctr": (I32, [_RNGP, I32, VP]),
+    "vsmc_cuda_philox4x32_blocks": (I32, [VP, VP, SZ, VP, VP]),
+    "vsmc_cuda_threefry4x64_blocks": (I32, [VP, VP, SZ, VP, VP]),
+    "vsmc_cuda_rng_rand": (I32, [_RNGP, SZ, VP, VP]),
+    "vsmc_cuda_rng_u01": (I32, [_RNGP, SZ, VP, VP]),
+    "vsmc_cuda_rng_u01_f32": (I32, [_RNGP, SZ, VP, VP]),
+    "vsmc_cuda_rng_normal": (I32, [_RNGP, SZ, VP, F64, F64, VP]),
+    "vsmc_cuda_rng_normal_f32": (I32, [_RNGP, SZ, VP, F32, F32, VP]),
+    "vsmc_cuda_normal_streams": (I32, [I32, VP, SZ, SZ, F64, F64, VP, VP]),
+    "vsmc_cuda_student_t_streams": (I32, [I32, VP, SZ, SZ, F64, VP, VP]),
+    "vsmc_cuda_u01_sorted": (I32, [SZ, VP, VP, VP]),
+    "vsmc_cuda_u01_stratified": (I32, [SZ, VP, VP, VP]),
+    "vsmc_cuda_u01_systematic": (I32, [SZ, F64, VP, VP]),
+    "vsmc_cuda_sequential_sum": (I32, [SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_resample_trans_u01_rep": (I32, [SZ, SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_resample_trans_u01_index": (I32, [SZ, SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_resample_trans_rep_index": (I32, [SZ, SZ, VP, VP, VP]),
+    "vsmc_cuda_resample_trans_index_rep": (I32, [SZ, SZ, VP, VP, VP]),
+    "vsmc_cuda_resample_trans_residual": (
+        I32, [SZ, SZ, VP, VP, VP, ctypes.POINTER(SZ), VP]),
+    "vsmc_cuda_resample": (I32, [SZ, SZ, _RNGP, VP, VP, I32, VP]),
+    "vsmc_cuda_resample_multinomial": (I32, [SZ, SZ, _RNGP, VP, VP, VP]),
+    "vsmc_cuda_resample_stratified": (I32, [SZ, SZ, _RNGP, VP, VP, VP]),
+    "vsmc_cuda_resample_systematic": (I32, [SZ, SZ, _RNGP, VP, VP, VP]),
+    "vsmc_cuda_resample_residual": (I32, [SZ, SZ, _RNGP, VP, VP, VP]),
+    "vsmc_cuda_resample_residual_stratified": (
+        I32, [SZ, SZ, _RNGP, VP, VP, VP]),
+    "vsmc_cuda_resample_residual_systematic": (
+        I32, [SZ, SZ, _RNGP, VP, VP, VP]),
+    "vsmc_cuda_state_copy_f32": (I32, [SZ, SZ, VP, VP, VP]),
+    "vsmc_cuda_state_copy_f64": (I32, [SZ, SZ, VP, VP, VP]),
+    "vsmc_cuda_weight_set": (I32, [SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_weight_set_log": (I32, [SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_weight_add_log": (I32, [SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_weight_set_equal": (I32, [SZ, VP, VP, VP]),
+    "vsmc_cuda_monitor_mean_f64": (I32, [SZ, SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_monitor_mean_f32": (I32, [SZ, SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_pf_create": (
+        I32, [ctypes.POINTER(VP), SZ, I32, I32, F64, U32, _MODELP, SZ, VP]),
+    "vsmc_cuda_pf_destroy": (I32, [VP]),
+    "vsmc_cuda_pf_initialize": (I32, [VP, VP]),
+    "vsmc_cuda_pf_iterate": (I32, [VP, VP]),
+    "vsmc_cuda_pf_run_device": (I32, [VP, SZ, VP]),
+    "vsmc_cuda_pf_run": (I32, [VP, SZ, VP, VP, VP, VP, VP]),
+    "vsmc_cuda_pf_history": (I32, [VP, SZ, VP, VP, VP, VP]),
+    "vsmc_cuda_pf_state": (I32, [VP, ctypes.POINTER(VP), ctypes.POINTER(VP)]),
+    "vsmc_cuda_pf_stream": (I32, [VP, ctypes.POINTER(VP)]),
+    "vsmc_cuda_pf_use_graph": (I32, [VP, I32]),
+    "vsmc_cuda_pf_launch_step_kernel": (I32, [VP]),
+    "vsmc_cuda_cv_move_f64": (I32, [SZ, SZ, U32, _MODELP, VP, VP, VP, VP]),
+    "vsmc_cuda_cv_move_f32": (I32, [SZ, SZ, U32, _MODELP, VP, VP, VP, VP]),
+    "vsmc_cuda_cv_simulate": (I32, [U32, SZ, _MODELP, VP, VP, VP]),
+}
+
+_LIB = None
+
+
+class VsmcCudaError(RuntimeError):
+    def __init__(self, status, where=""):
+        msg = _status_text(status)
+        if status == ERR_CUDA:
+            try:
+                msg += f", cudaError {lib().vsmc_cuda_last_cuda_error()}"
+            except Exception:  # pragma: no cover
+                pass
+        super().__init__(f"{where}: status {status} ({msg})" if where else msg)
+        self.status = status
+
+
+def _status_text(status):
+    try:
+        return lib().vsmc_cuda_status_string(status).decode()
+    except Exception:  # pragma: no cover - only when the library is broken
+        return "unknown"
+
+
+def lib(auto_build=True):
+    """The loaded libvsmc_cuda (prototypes declared).  Raises if absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        if not auto_build:
+            raise OSError(f"{LIB_PATH} is not built")
+        _build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def check(status, where=""):
+    if status != OK:
+        raise VsmcCudaError(status, where)
+    return status
+
+
+def call(name, *args):
+    """Call an entry point and raise VsmcCudaError on a non-zero status."""
+    return check(getattr(lib(), name)(*args), name)
+
+
+def rng(kind=PHILOX4X32, seed=0, key=None, ctr=None):
+    """A vsmc_cuda_rng placed like CounterEngine(seed), then key(k), ctr(c)."""
+    r = Rng()
+    call("vsmc_cuda_rng_init", ctypes.byref(r), kind, seed)
+    if key is not None:
+        k = (U64 * 4)(*[int(v) for v in key] + [0] * (4 - len(key)))
+        call("vsmc_cuda_rng_set_key", ctypes.byref(r), len(key), k)
+    if ctr is not None:
+        c = (U64 * 4)(*[int(v) for v in ctr] + [0] * (4 - len(ctr)))
+        call("vsmc_cuda_rng_set_ctr", ctypes.byref(r), len(ctr), c)
+    return r
+
+
+class ParticleFilter:
+    """A device-resident bootstrap filter (vsmc_cuda_pf) -- the Sampler<T>
+    of the reference with the CUDA state / move / weight / monitor."""
+
+    def __init__(self, n, precision=32, scheme=SYSTEMATIC, threshold=0.5,
+                 seed=0, model=None, max_steps=256, stream=None):
+        self.n = n
+        self.precision = precision
+        self.model = model if model is not None else default_model()
+        h = VP()
+        call("vsmc_cuda_pf_create", ctypes.byref(h), n, precision, scheme,
+             threshold, seed, ctypes.byref(self.model), max_steps, stream)
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            lib().vsmc_cuda_pf_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def launch_step_kernel(self):
+        call("vsmc_cuda_pf_launch_step_kernel", self.handle)
+
+    def use_graph(self, on):
+        call("vsmc_cuda_pf_use_graph", self.handle, 1 if on else 0)
+
+    def run(self, obs):
+        """Whole run through host buffers; obs is a (T, 2) float64 array."""
+        import numpy as np
+        obs = np.ascontiguousarray(obs, dtype=np.float64)
+        T = obs.shape[0]
+        mean = np.zeros((T, 2))
+        ess = np.zeros(T)
+        res = np.zeros(T, dtype=np.int32)
+        logz = np.zeros(T)
+        call("vsmc_cuda_pf_run", self.handle, T, obs.ctypes.data,
+             mean.ctypes.data, ess.ctypes.data, res.ctypes.data,
+             logz.ctypes.data)
+        return {"mean": mean, "ess": ess, "resampled": res, "logz": logz}
+
+    def run_device(self, T, obs_dev_ptr):
+        call("vsmc_cuda_pf_run_device", self.handle, T, obs_dev_ptr)
+
+    def history(self, T):
+        import numpy as np
+        mean = np.zeros((T, 2))
+        ess = np.zeros(T)
+        res = np.zeros(T, dtype=np.int32)
+        logz = np.zeros(T)
+        call("vsmc_cuda_pf_history", self.handle, T, mean.ctypes.data,
+             ess.ctypes.data, res.ctypes.data, logz.ctypes.data)
+        return {"mean": mean, "ess": ess, "resampled": res, "logz": logz}
+
+    def state_ptrs(self):
+        s, w = VP(), VP()
+        call("vsmc_cuda_pf_state", self.handle, ctypes.byref(s),
+             ctypes.byref(w))
+        return s.value, w.value

@@ -1,0 +1,149 @@
+// Model entry points: one move / log-likelihood step on caller-owned state
+// (the kernel-level parity hook) and the observation simulator.
+#include "common.cuh"
+#include "pf_model.cuh"
+#include "rng_device.cuh"
+
+using namespace vsmc_cuda;
+
+namespace vsmc_cuda
+{
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cv_move(uint32_t n, uint32_t t,
+    uint32_t seed, CvConst<T> c, T ox, T oy, T *x, T *y, T *vx, T *vy, T *ll)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const u32x4 w = particle_block(t, seed, i);
+        T X, Y, VX, VY;
+        if (t == 0) {
+            T z1, z2, z3, z4;
+            if constexpr (sizeof(T) == 4) {
+                normal_pair_f(w.x, w.y, z1, z2);
+                normal_pair_f(w.z, w.w, z3, z4);
+            } else {
+                normal_pair_d(w.x, w.y, z1, z2);
+                normal_pair_d(w.z, w.w, z3, z4);
+            }
+            X = c.sd_pos0 * z1;
+            Y = c.sd_pos0 * z2;
+            VX = c.sd_vel0 * z3;
+            VY = c.sd_vel0 * z4;
+        } else {
+            X = x[i];
+            Y = y[i];
+            VX = vx[i];
+            VY = vy[i];
+            T z1, z2;
+            if constexpr (sizeof(T) == 4)
+                normal_pair_f(w.x, w.y, z1, z2);
+            else
+                normal_pair_d(w.x, w.y, z1, z2);
+            cv_move(c, c.sigma_a * z1, c.sigma_a * z2, X, Y, VX, VY);
+        }
+        x[i] = X;
+        y[i] = Y;
+        vx[i] = VX;
+        vy[i] = VY;
+        ll[i] = cv_loglik(c, ox, oy, X, Y);
+    }
+}
+
+// Sequential simulation on one thread (T is small): a Philox4x32 engine
+// seeded with `seed`, fresh NormalDistribution<double> pairs for the prior
+// and the accelerations, one StudentTDistribution<double>(nu) for the noise.
+__global__ void k_cv_simulate(uint32_t seed, uint32_t T, double dt,
+    double sigma_a, double obs_scale, double nu, double sd_pos0,
+    double sd_vel0, double *truth, double *obs)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0)
+        return;
+    PhiloxScalar eng(PhiloxScalar::key_t{seed, 0u}, 0);
+    StudentTScalar st(nu);
+    auto pair = [&](double sd, double &a, double &b) {
+        NormalScalar<double> nd(0, sd);
+        a = nd(eng);
+        b = nd(eng);
+    };
+    double x, y, vx, vy;
+    pair(sd_pos0, x, y);
+    pair(sd_vel0, vx, vy);
+    const double h = 0.5 * dt * dt;
+    for (uint32_t t = 0; t < T; ++t) {
+        if (t > 0) {
+            double ax, ay;
+            pair(sigma_a, ax, ay);
+            x = __dadd_rn(__dadd_rn(x, __dmul_rn(dt, vx)), __dmul_rn(h, ax));
+            y = __dadd_rn(__dadd_rn(y, __dmul_rn(dt, vy)), __dmul_rn(h, ay));
+            vx = __dadd_rn(vx, __dmul_rn(dt, ax));
+            vy = __dadd_rn(vy, __dmul_rn(dt, ay));
+        }
+        truth[4 * t + 0] = x;
+        truth[4 * t + 1] = y;
+        truth[4 * t + 2] = vx;
+        truth[4 * t + 3] = vy;
+        const double ex = st(eng);
+        const double ey = st(eng);
+        obs[2 * t + 0] = __dadd_rn(x, __dmul_rn(obs_scale, ex));
+        obs[2 * t + 1] = __dadd_rn(y, __dmul_rn(obs_scale, ey));
+    }
+}
+
+template <typename T>
+static int cv_move_impl(size_t n, size_t t, uint32_t seed,
+    const vsmc_cuda_cv_model *model, const double obs[2], T *state, T *ll,
+    void *stream)
+{
+    if (!valid_cv_model(model) || obs == nullptr ||
+        ((state == nullptr || ll == nullptr) && n))
+        return VSMC_CUDA_ERR_ARG;
+    if (n >= (size_t(1) << 31) || t > 0xFFFFFFFFull)
+        return VSMC_CUDA_ERR_SIZE;
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    const CvConst<T> c = make_cv_const<T>(*model);
+    const int grid = grid_for(n, 256, 1, 8);
+    k_cv_move<T><<<grid, 256, 0, as_stream(stream)>>>(static_cast<uint32_t>(n),
+        static_cast<uint32_t>(t), seed, c, static_cast<T>(obs[0]),
+        static_cast<T>(obs[1]), state, state + n, state + 2 * n,
+        state + 3 * n, ll);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+} // namespace vsmc_cuda
+
+extern "C" {
+
+int vsmc_cuda_cv_move_f64(size_t n, size_t t, uint32_t seed,
+    const vsmc_cuda_cv_model *model, const double obs[2], double *state,
+    double *ll, void *stream)
+{
+    return cv_move_impl<double>(n, t, seed, model, obs, state, ll, stream);
+}
+
+int vsmc_cuda_cv_move_f32(size_t n, size_t t, uint32_t seed,
+    const vsmc_cuda_cv_model *model, const double obs[2], float *state,
+    float *ll, void *stream)
+{
+    return cv_move_impl<float>(n, t, seed, model, obs, state, ll, stream);
+}
+
+int vsmc_cuda_cv_simulate(uint32_t seed, size_t T,
+    const vsmc_cuda_cv_model *model, double *truth, double *obs, void *stream)
+{
+    if (!valid_cv_model(model) || truth == nullptr || obs == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (T == 0)
+        return VSMC_CUDA_OK;
+    if (T > 0xFFFFFFFFull)
+        return VSMC_CUDA_ERR_SIZE;
+    k_cv_simulate<<<1, 32, 0, as_stream(stream)>>>(seed,
+        static_cast<uint32_t>(T), model->dt, model->sigma_a, model->obs_scale,
+        model->nu, model->sd_pos0, model->sd_vel0, truth, obs);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,467 @@
+// Particle-filter driver and the model entry points of the C ABI.
+//
+// The filter is the reference's Sampler<T> loop (core/sampler.hpp:443-476,
+// 735-785) for the bootstrap filter of the pf example: weight by the
+// observation, record ESS, resample when ESS < threshold * N
+// (core/particle.hpp:170-197), record the weighted position mean
+// (core/monitor.hpp:242-268) and the log-evidence increment
+// log sum_i W_{t-1,i} exp(l_{t,i}) (user_guide/tex/smc.tex:176-182).
+#include "pf_internal.cuh"
+#include "pf32.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <new>
+
+using namespace vsmc_cuda;
+
+namespace vsmc_cuda
+{
+
+static Pf32Args make_args32(vsmc_cuda_pf *pf)
+{
+    Pf32Args a;
+    float *s = static_cast<float *>(pf->state);
+    a.x = s;
+    a.y = s + pf->stride;
+    a.vx = s + 2 * pf->stride;
+    a.vy = s + 3 * pf->stride;
+    a.lw = static_cast<float *>(pf->weight);
+    a.n = static_cast<uint32_t>(pf->n);
+    a.seed = pf->seed;
+    a.max_steps = static_cast<uint32_t>(pf->max_steps);
+    a.threshold = pf->threshold;
+    a.c = make_cv_const<float>(pf->model);
+    a.obs = pf->obs;
+    a.part = pf->part;
+    a.sc = pf->sc;
+    a.h_mean = pf->h_mean;
+    a.h_ess = pf->h_ess;
+    a.h_logz = pf->h_logz;
+    a.h_res = pf->h_res;
+    return a;
+}
+
+static Rs32Args make_rs_args32(vsmc_cuda_pf *pf)
+{
+    Rs32Args r;
+    float *s = static_cast<float *>(pf->state);
+    r.lw = static_cast<const float *>(pf->weight);
+    r.x = s;
+    r.y = s + pf->stride;
+    r.vx = s + 2 * pf->stride;
+    r.vy = s + 3 * pf->stride;
+    r.n = static_cast<uint32_t>(pf->n);
+    r.shift = pf->shift;
+    r.chunk = pf->chunk_rs;
+    r.scheme = pf->scheme;
+    r.qpart = pf->qpart;
+    r.epart = pf->epart;
+    r.cpart = pf->cpart;
+    r.mpart = pf->mpart;
+    r.rep = pf->rep;
+    r.marks = pf->marks;
+    r.empties = pf->empties;
+    r.sc = pf->sc;
+    return r;
+}
+
+// the kernels of one FP32 step after the first
+static int launch_step32(vsmc_cuda_pf *pf)
+{
+    const Pf32Args a = make_args32(pf);
+    const Rs32Args r = make_rs_args32(pf);
+    cudaStream_t st = pf->stream;
+    k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, st>>>(a);
+    k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_count<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_assign<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_markmax<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_gather<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+static int launch_first32(vsmc_cuda_pf *pf)
+{
+    const Pf32Args a = make_args32(pf);
+    const Rs32Args r = make_rs_args32(pf);
+    cudaStream_t st = pf->stream;
+    k_pf32_step<true><<<pf->grid_step, kPfBlock, 0, st>>>(a);
+    k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_count<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_assign<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_markmax<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_gather<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+static int step32(vsmc_cuda_pf *pf)
+{
+    if (!pf->use_graph)
+        return launch_step32(pf);
+    if (pf->graph_exec == nullptr) {
+        VSMC_CUDA_TRY(cudaStreamBeginCapture(
+            pf->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = launch_step32(pf);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(pf->stream, &g);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+        VSMC_CUDA_TRY(e);
+        pf->graph = g;
+        VSMC_CUDA_TRY(cudaGraphInstantiate(&pf->graph_exec, g, 0));
+    }
+    VSMC_CUDA_TRY(cudaGraphLaunch(pf->graph_exec, pf->stream));
+    return VSMC_CUDA_OK;
+}
+
+static int final_mean32(vsmc_cuda_pf *pf)
+{
+    const Pf32Args a = make_args32(pf);
+    const int grid = grid_for(pf->n, kPfBlock, 8, 2);
+    k_pf32_final_mean<<<grid, kPfBlock, 0, pf->stream>>>(
+        a, static_cast<uint32_t>(pf->t - 1));
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+__global__ void k_reset_scalars(PfScalars *sc, uint32_t seed)
+{
+    PfScalars z;
+    z.M = 0;
+    z.S = 0;
+    z.logz = 0;
+    z.ess = 0;
+    z.Q = 0;
+    z.step = 0;
+    z.resampled = 1;
+    z.done = 0;
+    z.err = 0;
+    z.nempty = 0;
+    z.rindex = 4;
+    // resampling engine: key {0, seed}, counter {0, 0, 1, 0}
+    z.rkey[0] = 0;
+    z.rkey[1] = seed;
+    z.rctr[0] = 0;
+    z.rctr[1] = 0;
+    z.rctr[2] = 1;
+    z.rctr[3] = 0;
+    *sc = z;
+}
+
+static int reset_scalars(vsmc_cuda_pf *pf)
+{
+    k_reset_scalars<<<1, 1, 0, pf->stream>>>(pf->sc, pf->seed);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+static void free_all(vsmc_cuda_pf *pf)
+{
+    if (pf->graph_exec)
+        cudaGraphExecDestroy(pf->graph_exec);
+    if (pf->graph)
+        cudaGraphDestroy(pf->graph);
+    void *ptrs[] = {pf->state, pf->weight, pf->obs, pf->h_mean, pf->h_ess,
+        pf->h_logz, pf->h_res, pf->sc, pf->part, pf->qpart, pf->epart,
+        pf->cpart, pf->mpart, pf->rep, pf->marks, pf->empties};
+    for (void *p : ptrs)
+        if (p)
+            cudaFree(p);
+    if (pf->p64)
+        pf64_destroy(pf);
+    if (pf->own_stream && pf->stream)
+        cudaStreamDestroy(pf->stream);
+    pf->stream = nullptr;
+}
+
+template <typename T>
+static int dalloc(T **p, size_t count)
+{
+    void *q = nullptr;
+    VSMC_CUDA_TRY(cudaMalloc(&q, sizeof(T) * (count ? count : 1)));
+    *p = static_cast<T *>(q);
+    return VSMC_CUDA_OK;
+}
+
+static int sync_and_check(vsmc_cuda_pf *pf)
+{
+    VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
+    uint32_t err = 0;
+    VSMC_CUDA_TRY(cudaMemcpy(&err, &pf->sc->err, sizeof(err),
+        cudaMemcpyDeviceToHost));
+    if (err & DEV_ERR_NONFINITE)
+        return VSMC_CUDA_ERR_NONFINITE;
+    if (err)
+        return VSMC_CUDA_ERR_INTERNAL;
+    return VSMC_CUDA_OK;
+}
+
+} // namespace vsmc_cuda
+
+extern "C" {
+
+int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
+    int scheme, double threshold, uint32_t seed,
+    const vsmc_cuda_cv_model *model, size_t max_steps, void *stream)
+{
+    if (out == nullptr || !valid_cv_model(model) ||
+        (precision != 32 && precision != 64) || std::isnan(threshold))
+        return VSMC_CUDA_ERR_ARG;
+    *out = nullptr;
+    if (n < 1 || n >= (size_t(1) << 31) || max_steps < 1 ||
+        max_steps > (size_t(1) << 31))
+        return VSMC_CUDA_ERR_SIZE;
+    if (scheme < VSMC_CUDA_MULTINOMIAL || scheme > VSMC_CUDA_RESIDUAL_SYSTEMATIC)
+        return VSMC_CUDA_ERR_ARG;
+    if (precision == 32 && scheme != VSMC_CUDA_STRATIFIED &&
+        scheme != VSMC_CUDA_SYSTEMATIC)
+        return VSMC_CUDA_ERR_ARG;
+    vsmc_cuda_pf *pf = new (std::nothrow) vsmc_cuda_pf;
+    if (pf == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    pf->n = n;
+    pf->stride = (n + 255) / 256 * 256;
+    pf->precision = precision;
+    pf->scheme = scheme;
+    pf->threshold = threshold;
+    pf->seed = seed;
+    pf->model = *model;
+    pf->max_steps = max_steps;
+    pf->stream = as_stream(stream);
+    if (pf->stream == nullptr) {
+        // the legacy stream cannot be captured into a graph: use a private one
+        if (cudaStreamCreateWithFlags(&pf->stream, cudaStreamNonBlocking) !=
+            cudaSuccess) {
+            delete pf;
+            return VSMC_CUDA_ERR_CUDA;
+        }
+        pf->own_stream = true;
+    }
+    int rc = VSMC_CUDA_OK;
+    const size_t esz = precision == 32 ? sizeof(float) : sizeof(double);
+#define PF_TRY(x)                                                             \
+    do {                                                                      \
+        rc = (x);                                                             \
+        if (rc != VSMC_CUDA_OK) {                                             \
+            free_all(pf);                                                     \
+            delete pf;                                                        \
+            return rc;                                                        \
+        }                                                                     \
+    } while (0)
+    PF_TRY(dalloc(reinterpret_cast<char **>(&pf->state), esz * 4 * pf->stride));
+    PF_TRY(dalloc(reinterpret_cast<char **>(&pf->weight), esz * n));
+    PF_TRY(dalloc(&pf->obs, 2 * max_steps));
+    PF_TRY(dalloc(&pf->h_mean, 2 * max_steps));
+    PF_TRY(dalloc(&pf->h_ess, max_steps));
+    PF_TRY(dalloc(&pf->h_logz, max_steps));
+    PF_TRY(dalloc(&pf->h_res, max_steps));
+    PF_TRY(dalloc(&pf->sc, 1));
+    if (precision == 32) {
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &occ, k_pf32_step<false>, kPfBlock, 0) != cudaSuccess ||
+            occ < 1)
+            occ = 4;
+        const size_t ntiles = (n + kPfTile - 1) / kPfTile;
+        size_t g = static_cast<size_t>(num_sms()) * static_cast<size_t>(occ);
+        pf->grid_step = static_cast<int>(ntiles < g ? ntiles : g);
+        size_t grs = static_cast<size_t>(num_sms()) * 4;
+        size_t chunk = (n + grs - 1) / grs;
+        chunk = (chunk + kPfTile - 1) / kPfTile * kPfTile;
+        pf->chunk_rs = static_cast<uint32_t>(chunk);
+        pf->grid_rs = static_cast<int>((n + chunk - 1) / chunk);
+        int lg = 0;
+        while ((size_t(1) << lg) < n)
+            ++lg;
+        pf->shift = static_cast<uint32_t>(63 - lg);
+        PF_TRY(dalloc(&pf->part, pf->grid_step > 1024 ? pf->grid_step : 1024));
+        PF_TRY(dalloc(&pf->qpart, pf->grid_rs));
+        PF_TRY(dalloc(&pf->epart, pf->grid_rs));
+        PF_TRY(dalloc(&pf->cpart, pf->grid_rs));
+        PF_TRY(dalloc(&pf->mpart, pf->grid_rs));
+        PF_TRY(dalloc(&pf->rep, n));
+        PF_TRY(dalloc(&pf->marks, n));
+        PF_TRY(dalloc(&pf->empties, n));
+        if (cudaMemsetAsync(pf->marks, 0, sizeof(uint32_t) * n, pf->stream) !=
+            cudaSuccess)
+            PF_TRY(VSMC_CUDA_ERR_CUDA);
+    } else {
+        PF_TRY(pf64_create(pf));
+    }
+    PF_TRY(reset_scalars(pf));
+#undef PF_TRY
+    *out = pf;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_destroy(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr)
+        return VSMC_CUDA_OK;
+    cudaStreamSynchronize(pf->stream);
+    free_all(pf);
+    delete pf;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_launch_step_kernel(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr || pf->precision != 32 || pf->t == 0)
+        return VSMC_CUDA_ERR_ARG;
+    const Pf32Args a = make_args32(pf);
+    k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
+    VSMC_CUDA_CHECK_LAUNCH();
+    ++pf->t;
+    pf->mean_pending = true;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_use_graph(vsmc_cuda_pf *pf, int on)
+{
+    if (pf == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    pf->use_graph = on != 0;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_stream(vsmc_cuda_pf *pf, void **stream)
+{
+    if (pf == nullptr || stream == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    *stream = pf->stream;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_state(vsmc_cuda_pf *pf, void **state_dev, void **weight_dev)
+{
+    if (pf == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (state_dev)
+        *state_dev = pf->state;
+    if (weight_dev)
+        *weight_dev = pf->weight;
+    return VSMC_CUDA_OK;
+}
+
+static int pf_begin(vsmc_cuda_pf *pf)
+{
+    int rc = reset_scalars(pf);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    pf->t = 0;
+    pf->mean_pending = false;
+    rc = pf->precision == 32 ? launch_first32(pf) : pf64_step(pf, true);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    pf->t = 1;
+    pf->mean_pending = true;
+    return VSMC_CUDA_OK;
+}
+
+static int pf_next(vsmc_cuda_pf *pf)
+{
+    const int rc = pf->precision == 32 ? step32(pf) : pf64_step(pf, false);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    ++pf->t;
+    pf->mean_pending = true;
+    return VSMC_CUDA_OK;
+}
+
+static int pf_flush_mean(vsmc_cuda_pf *pf)
+{
+    if (!pf->mean_pending || pf->t == 0)
+        return VSMC_CUDA_OK;
+    const int rc =
+        pf->precision == 32 ? final_mean32(pf) : pf64_final_mean(pf);
+    if (rc == VSMC_CUDA_OK)
+        pf->mean_pending = false;
+    return rc;
+}
+
+int vsmc_cuda_pf_initialize(vsmc_cuda_pf *pf, const double *obs_dev)
+{
+    if (pf == nullptr || obs_dev == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(pf->obs, obs_dev, 2 * sizeof(double),
+        cudaMemcpyDeviceToDevice, pf->stream));
+    return pf_begin(pf);
+}
+
+int vsmc_cuda_pf_iterate(vsmc_cuda_pf *pf, const double *obs_dev)
+{
+    if (pf == nullptr || obs_dev == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (pf->t == 0)
+        return VSMC_CUDA_ERR_ARG;
+    if (pf->t >= pf->max_steps)
+        return VSMC_CUDA_ERR_SIZE;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(pf->obs + 2 * pf->t, obs_dev,
+        2 * sizeof(double), cudaMemcpyDeviceToDevice, pf->stream));
+    return pf_next(pf);
+}
+
+int vsmc_cuda_pf_run_device(vsmc_cuda_pf *pf, size_t T, const double *obs_dev)
+{
+    if (pf == nullptr || obs_dev == nullptr || T == 0)
+        return VSMC_CUDA_ERR_ARG;
+    if (T > pf->max_steps)
+        return VSMC_CUDA_ERR_SIZE;
+    if (obs_dev != pf->obs)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(pf->obs, obs_dev, 2 * T * sizeof(double),
+            cudaMemcpyDeviceToDevice, pf->stream));
+    int rc = pf_begin(pf);
+    for (size_t t = 1; rc == VSMC_CUDA_OK && t < T; ++t)
+        rc = pf_next(pf);
+    if (rc == VSMC_CUDA_OK)
+        rc = pf_flush_mean(pf);
+    return rc;
+}
+
+int vsmc_cuda_pf_history(vsmc_cuda_pf *pf, size_t T, double *mean_host,
+    double *ess_host, int *resampled_host, double *logz_host)
+{
+    if (pf == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (T > pf->t)
+        return VSMC_CUDA_ERR_SIZE;
+    int rc = pf_flush_mean(pf);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    cudaStream_t st = pf->stream;
+    if (mean_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(mean_host, pf->h_mean,
+            2 * T * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (ess_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(ess_host, pf->h_ess, T * sizeof(double),
+            cudaMemcpyDeviceToHost, st));
+    if (resampled_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(resampled_host, pf->h_res,
+            T * sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (logz_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(logz_host, pf->h_logz,
+            T * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return sync_and_check(pf);
+}
+
+int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
+    double *mean_host, double *ess_host, int *resampled_host,
+    double *logz_host)
+{
+    if (pf == nullptr || obs_host == nullptr || T == 0)
+        return VSMC_CUDA_ERR_ARG;
+    if (T > pf->max_steps)
+        return VSMC_CUDA_ERR_SIZE;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(pf->obs, obs_host, 2 * T * sizeof(double),
+        cudaMemcpyHostToDevice, pf->stream));
+    int rc = vsmc_cuda_pf_run_device(pf, T, pf->obs);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    return vsmc_cuda_pf_history(
+        pf, T, mean_host, ess_host, resampled_host, logz_host);
+}
+
+} // extern "C"

@@ -1,0 +1,67 @@
+// Data layout of the FP32 filter step (device structs shared by the driver).
+#pragma once
+
+#include "common.cuh"
+#include "pf_model.cuh"
+
+namespace vsmc_cuda
+{
+
+constexpr int kPfBlock = 256;
+constexpr int kPfTile = kPfBlock * 4; // particles per block iteration
+
+// FP64 per-block record of the fused step
+struct MovePartial {
+    double sx, sy, sw; // previous-step monitor sums
+    double m, s, s2;   // new log-weights: block max, sum exp, sum exp^2
+};
+
+// Device-resident filter scalars (one per filter)
+struct PfScalars {
+    double M;    // max of the stored log-weights after the last weighting
+    double S;    // sum exp(lw - M)
+    double logz; // cumulative log-evidence
+    double ess;
+    uint64_t Q;          // fixed-point CDF total of the pending resample
+    uint32_t step;       // next step index t
+    int32_t resampled;   // last step resampled: stored lw are stale
+    uint32_t done;       // completion counter of the fused step
+    uint32_t err;        // DEV_ERR_* bits
+    uint32_t nempty;     // empty slots of the pending resample
+    uint32_t rindex;     // resampling engine: next word index in gen(rctr)
+    uint32_t rkey[2];
+    uint32_t rctr[4];
+};
+
+struct Pf32Args {
+    float *x, *y, *vx, *vy, *lw;
+    uint32_t n;
+    uint32_t seed;
+    uint32_t max_steps; // history / observation capacity
+    double threshold;
+    CvConst<float> c;
+    const double *obs; // T x 2 observations (device)
+    MovePartial *part;
+    PfScalars *sc;
+    double *h_mean, *h_ess, *h_logz;
+    int *h_res;
+};
+
+struct Rs32Args {
+    const float *lw;
+    float *x, *y, *vx, *vy;
+    uint32_t n;
+    uint32_t shift;  // fixed-point K
+    uint32_t chunk;  // particles per block (multiple of kPfTile)
+    int scheme;      // VSMC_CUDA_STRATIFIED or VSMC_CUDA_SYSTEMATIC
+    uint64_t *qpart; // per-block sum of q
+    uint32_t *epart; // per-block empty count
+    uint32_t *cpart; // per-block copy count (sum of rep)
+    uint32_t *mpart; // per-block max of marks
+    int32_t *rep;
+    uint32_t *marks;   // N entries, zero between resamples
+    uint32_t *empties; // N entries
+    PfScalars *sc;
+};
+
+} // namespace vsmc_cuda

@@ -1,0 +1,61 @@
+// Host-side filter object shared by the FP32 and FP64 drivers.
+#pragma once
+
+#include "common.cuh"
+#include "pf32_types.cuh"
+
+namespace vsmc_cuda
+{
+
+struct Pf64State; // FP64 driver state (pf64.cu)
+
+} // namespace vsmc_cuda
+
+struct vsmc_cuda_pf {
+    size_t n = 0;
+    size_t stride = 0; // SoA row stride (n rounded up to 256 elements)
+    int precision = 32;
+    int scheme = VSMC_CUDA_SYSTEMATIC;
+    double threshold = 0.5;
+    uint32_t seed = 0;
+    vsmc_cuda_cv_model model = {};
+    size_t max_steps = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false; // created here when the caller passed NULL
+    size_t t = 0;           // next step on the host side
+    bool mean_pending = false;
+    bool use_graph = true;
+
+    // device buffers
+    void *state = nullptr;  // 4 rows of `stride` (float or double)
+    void *weight = nullptr; // FP32: log-weights (float); FP64: W (double)
+    double *obs = nullptr;  // max_steps x 2
+    double *h_mean = nullptr, *h_ess = nullptr, *h_logz = nullptr;
+    int *h_res = nullptr;
+    vsmc_cuda::PfScalars *sc = nullptr;
+
+    // FP32 fused-step workspace
+    int grid_step = 0;
+    int grid_rs = 0;
+    uint32_t chunk_rs = 0;
+    uint32_t shift = 0;
+    vsmc_cuda::MovePartial *part = nullptr;
+    uint64_t *qpart = nullptr;
+    uint32_t *epart = nullptr, *cpart = nullptr, *mpart = nullptr;
+    int32_t *rep = nullptr;
+    uint32_t *marks = nullptr, *empties = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    vsmc_cuda::Pf64State *p64 = nullptr;
+};
+
+namespace vsmc_cuda
+{
+
+int pf64_create(vsmc_cuda_pf *pf);
+void pf64_destroy(vsmc_cuda_pf *pf);
+int pf64_step(vsmc_cuda_pf *pf, bool first);
+int pf64_final_mean(vsmc_cuda_pf *pf);
+
+} // namespace vsmc_cuda

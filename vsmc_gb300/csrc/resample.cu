@@ -1,0 +1,1114 @@
+// Resampling transforms, schemes, particle copy, weights and the monitor mean
+// on the device, with the reference's arithmetic.
+//
+// Cumulative weights and normalizing sums are the reference's left-to-right
+// sums bit for bit (seqsum.cu).  Counting uniforms against the CDF follows the
+// two-pointer loop of resample/transform.hpp:43-71: after particle i the loop
+// has consumed every uniform before the first one above cdf_i, so with the
+// prefix maximum pm_j of the uniforms, F(cdf_i) = #{j : pm_j <= cdf_i} and
+// rep_i = F(cdf_i) - F(cdf_{i-1}); the last particle takes the rest.
+#include "common.cuh"
+#include "rng_device.cuh"
+#include "scan.cuh"
+#include "seqsum.cuh"
+#include "resample_internal.cuh"
+
+#include <cmath>
+#include <cstring>
+
+namespace vsmc_cuda
+{
+
+namespace
+{
+
+constexpr int kB = 256;
+
+int grid1(size_t n) { return grid_for(n ? n : 1, kB, 4, 8); }
+
+#define GRID_LOOP(i, n)                                                       \
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; \
+         i < (n); i += static_cast<size_t>(gridDim.x) * blockDim.x)
+
+// ------------------------------------------------------------ elementwise
+
+__global__ void k_fill_i32(size_t n, int *p, int v)
+{
+    GRID_LOOP(i, n) p[i] = v;
+}
+
+__global__ void k_set_one(int *p, int v)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        *p = v;
+}
+
+// max-scan key: NaN compares as "above everything", as the reference's
+// `u <= accw` test is false for NaN
+__device__ __forceinline__ double key_of(double u)
+{
+    return isnan(u) ? INFINITY : u;
+}
+
+struct LoadKey {
+    const double *u;
+    __device__ double operator()(size_t i) const { return key_of(u[i]); }
+};
+
+struct StoreD {
+    double *p;
+    __device__ void operator()(size_t i, double v) const { p[i] = v; }
+};
+
+// #{j < n : pm_j <= x} (pm non-decreasing)
+__device__ __forceinline__ size_t upper_count(
+    const double *pm, size_t n, double x)
+{
+    size_t lo = 0, hi = n;
+    while (lo < hi) {
+        const size_t mid = lo + (hi - lo) / 2;
+        if (pm[mid] <= x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// #{i < m : s_i < x} (s non-decreasing): the first i with s_i >= x
+__device__ __forceinline__ size_t lower_count(
+    const double *s, size_t m, double x)
+{
+    size_t lo = 0, hi = m;
+    while (lo < hi) {
+        const size_t mid = lo + (hi - lo) / 2;
+        if (s[mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_counts(size_t m, size_t n, const double *cdf,
+    const double *pm, uint32_t *F)
+{
+    GRID_LOOP(i, m - 1) F[i] = static_cast<uint32_t>(upper_count(pm, n, cdf[i]));
+}
+
+__global__ void k_rep_from_counts(size_t m, size_t n, const uint32_t *F,
+    int *rep, const int *integ)
+{
+    GRID_LOOP(i, m)
+    {
+        const uint32_t hi = i + 1 < m ? F[i] : static_cast<uint32_t>(n);
+        const uint32_t lo = i > 0 ? F[i - 1] : 0u;
+        int r = static_cast<int>(hi - lo);
+        if (integ)
+            r += integ[i];
+        rep[i] = r;
+    }
+}
+
+__global__ void k_index_from_cdf(size_t m, size_t n, const double *cdf,
+    const double *pm, int *idx)
+{
+    GRID_LOOP(j, n)
+    idx[j] = static_cast<int>(lower_count(cdf, m - 1, pm[j]));
+}
+
+// ---------------------------------------------- uniforms from the engine
+// word k of the scalar stream of (key, ctr, index): gen(ctr + (index+k)/4)
+struct EngineState {
+    uint32_t k0, k1;
+    uint32_t c[4];
+    uint32_t index;
+};
+
+__device__ __forceinline__ uint32_t stream_word(const EngineState &e, size_t k)
+{
+    const uint64_t pos = static_cast<uint64_t>(e.index) + k;
+    uint32_t c[4] = {e.c[0], e.c[1], e.c[2], e.c[3]};
+    ctr32_add(c, pos / 4);
+    const u32x4 b = philox4x32_10(c[0], c[1], c[2], c[3], e.k0, e.k1);
+    const uint32_t i = static_cast<uint32_t>(pos % 4);
+    return i == 0 ? b.x : (i == 1 ? b.y : (i == 2 ? b.z : b.w));
+}
+
+// U01SequenceStratified: u_j = U_j * delta + j * delta
+__global__ void k_stratified_seq(EngineState e, size_t n, double *u)
+{
+    const double delta = 1.0 / static_cast<double>(n);
+    GRID_LOOP(j, n)
+    {
+        const double U = u01_co_d(stream_word(e, j));
+        u[j] = __dadd_rn(__dmul_rn(U, delta),
+            __dmul_rn(static_cast<double>(j), delta));
+    }
+}
+
+// U01SequenceSystematic: u0 = U * delta, u_j = u0 + j * delta
+__global__ void k_systematic_seq(EngineState e, size_t n, double *u)
+{
+    const double delta = 1.0 / static_cast<double>(n);
+    const double u0 = __dmul_rn(u01_co_d(stream_word(e, 0)), delta);
+    GRID_LOOP(j, n)
+    u[j] = __dadd_rn(u0, __dmul_rn(static_cast<double>(j), delta));
+}
+
+// U01SequenceSorted terms: -log(U_j) / (n - j), summed left to right below
+__global__ void k_sorted_terms(EngineState e, size_t n, double *t)
+{
+    GRID_LOOP(j, n)
+    {
+        const double U = u01_co_d(stream_word(e, j));
+        t[j] = -(log(U) / static_cast<double>(n - j));
+    }
+}
+
+__global__ void k_sorted_terms_arr(size_t n, const double *u01, double *t)
+{
+    GRID_LOOP(j, n) t[j] = -(log(u01[j]) / static_cast<double>(n - j));
+}
+
+// u_j = 1 - exp(lmax_j), lmax_j = -prefix_j
+__global__ void k_sorted_finish(size_t n, const double *neg_lmax, double *u)
+{
+    GRID_LOOP(j, n) u[j] = 1.0 - exp(-neg_lmax[j]);
+}
+
+__global__ void k_stratified_arr(size_t n, const double *u01, double *out)
+{
+    const double delta = 1.0 / static_cast<double>(n);
+    GRID_LOOP(i, n)
+    out[i] = __dadd_rn(__dmul_rn(u01[i], delta),
+        __dmul_rn(static_cast<double>(i), delta));
+}
+
+__global__ void k_systematic_terms(size_t n, double u01, double *t)
+{
+    const double delta = 1.0 / static_cast<double>(n);
+    GRID_LOOP(i, n) t[i] = i == 0 ? __dmul_rn(u01, delta) : delta;
+}
+
+// --------------------------------------------------------------- residual
+
+__global__ void k_residual_split(
+    size_t m, size_t n, const double *w, double *resid, int *integ)
+{
+    const double coeff = static_cast<double>(n);
+    GRID_LOOP(i, m)
+    {
+        const double x = __dmul_rn(coeff, w[i]);
+        const double ip = trunc(x);
+        resid[i] = x - ip; // modf: exact
+        integ[i] = static_cast<int>(ip);
+    }
+}
+
+__global__ void k_scale(size_t m, const double *total, double *v)
+{
+    const double inv = 1.0 / *total;
+    GRID_LOOP(i, m) v[i] = __dmul_rn(inv, v[i]);
+}
+
+// ------------------------------------------------------------ rep -> index
+
+struct I2 {
+    int32_t a, b;
+};
+
+struct OpI2 {
+    __device__ __forceinline__ I2 operator()(const I2 &x, const I2 &y) const
+    {
+        return {x.a + y.a, x.b + y.b};
+    }
+};
+
+struct OpMaxI {
+    __device__ __forceinline__ int32_t operator()(int32_t x, int32_t y) const
+    {
+        return x < y ? y : x;
+    }
+};
+
+// (empty flag, surplus) for m == n; (rep, 0) for m != n
+struct LoadES {
+    const int *rep;
+    bool square;
+    __device__ I2 operator()(size_t i) const
+    {
+        const int r = rep[i];
+        if (square)
+            return {r == 0 ? 1 : 0, r > 1 ? r - 1 : 0};
+        return {r, 0};
+    }
+};
+
+struct StoreI2 {
+    I2 *p;
+    __device__ void operator()(size_t i, I2 v) const { p[i] = v; }
+};
+
+// marks: rank of the first surplus copy of p (m == n), or first output slot
+// of p (m != n), gets p + 1
+__global__ void k_marks(size_t m, bool square, const int *rep, const I2 *incl,
+    int *marks, size_t nmarks, uint32_t *err)
+{
+    GRID_LOOP(p, m)
+    {
+        const int r = rep[p];
+        if (r < 0) {
+            atomicOr(err, DEV_ERR_INTERNAL);
+            continue;
+        }
+        if (square) {
+            if (r > 1) {
+                const int first = incl[p].b - (r - 1); // exclusive surplus
+                if (first >= 0 && static_cast<size_t>(first) < nmarks)
+                    marks[first] = static_cast<int>(p) + 1;
+                else
+                    atomicOr(err, DEV_ERR_INTERNAL);
+            }
+        } else if (r > 0) {
+            const int first = incl[p].a - r;
+            if (first >= 0 && static_cast<size_t>(first) < nmarks)
+                marks[first] = static_cast<int>(p) + 1;
+            else
+                atomicOr(err, DEV_ERR_INTERNAL);
+        }
+    }
+}
+
+struct LoadI {
+    const int *p;
+    __device__ int32_t operator()(size_t i) const { return p[i]; }
+};
+
+struct StoreI {
+    int *p;
+    __device__ void operator()(size_t i, int32_t v) const { p[i] = v; }
+};
+
+__global__ void k_index_square(size_t n, const int *rep, const I2 *incl,
+    const int *src_of_rank, size_t nrank, int *idx, uint32_t *err)
+{
+    GRID_LOOP(d, n)
+    {
+        if (rep[d] != 0) {
+            idx[d] = static_cast<int>(d);
+        } else {
+            const int k = incl[d].a - 1; // exclusive empty rank
+            if (k >= 0 && static_cast<size_t>(k) < nrank && src_of_rank[k] > 0)
+                idx[d] = src_of_rank[k] - 1;
+            else
+                atomicOr(err, DEV_ERR_INTERNAL);
+        }
+    }
+}
+
+__global__ void k_index_flat(size_t total, const int *src, int *idx)
+{
+    GRID_LOOP(d, total) idx[d] = src[d] - 1;
+}
+
+__global__ void k_hist(size_t m, size_t n, const int *idx, int *rep,
+    uint32_t *err)
+{
+    GRID_LOOP(i, n)
+    {
+        const int p = idx[i];
+        if (p < 0 || static_cast<size_t>(p) >= m)
+            atomicOr(err, DEV_ERR_INTERNAL);
+        else
+            atomicAdd(rep + p, 1);
+    }
+}
+
+// --------------------------------------------------------------- copying
+
+__global__ void k_check_fixed_points(size_t n, const int *idx, uint32_t *err)
+{
+    GRID_LOOP(d, n)
+    {
+        const int s = idx[d];
+        if (s < 0 || static_cast<size_t>(s) >= n || idx[s] != s)
+            atomicOr(err, DEV_ERR_INTERNAL);
+    }
+}
+
+template <typename T>
+__global__ void k_copy_state(size_t n, size_t dim, size_t ld, const int *idx,
+    T *state, const uint32_t *err)
+{
+    if (*err)
+        return;
+    GRID_LOOP(d, n)
+    {
+        const size_t s = static_cast<size_t>(idx[d]);
+        if (s != d)
+            for (size_t r = 0; r < dim; ++r)
+                state[r * ld + d] = state[r * ld + s];
+    }
+}
+
+// ---------------------------------------------------------------- weights
+
+struct OpMaxD {
+    __device__ __forceinline__ double operator()(double a, double b) const
+    {
+        return a < b ? b : a;
+    }
+};
+
+__global__ void k_reduce_max(size_t n, const double *v, double *part)
+{
+    double m = -INFINITY;
+    GRID_LOOP(i, n) m = fmax(m, v[i]);
+    __shared__ double sh[kB / 32 + 1];
+    m = block_reduce(m, OpMaxD(), -static_cast<double>(INFINITY), sh);
+    if (threadIdx.x == 0)
+        part[blockIdx.x] = m;
+}
+
+__global__ void k_max_parts(int nb, double *part)
+{
+    double m = -INFINITY;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
+        m = fmax(m, part[b]);
+    __shared__ double sh[kB / 32 + 1];
+    m = block_reduce(m, OpMaxD(), -static_cast<double>(INFINITY), sh);
+    if (threadIdx.x == 0)
+        part[0] = m;
+}
+
+// W = exp(lw - max)  (post_set_log -> normalize(true), weight.hpp:202-229)
+__global__ void k_exp_shift(size_t n, const double *lw, const double *mx,
+    double *W)
+{
+    const double m = *mx;
+    GRID_LOOP(i, n) W[i] = exp(lw[i] - m);
+}
+
+// W = log(W) + l  (add_log, weight.hpp:168-173)
+__global__ void k_log_add(size_t n, const double *l, double *W)
+{
+    GRID_LOOP(i, n) W[i] = __dadd_rn(log(W[i]), l[i]);
+}
+
+__global__ void k_square(size_t n, const double *W, double *sq)
+{
+    GRID_LOOP(i, n) sq[i] = __dmul_rn(W[i], W[i]);
+}
+
+__global__ void k_inv_total(const double *total, double *ess)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        *ess = 1.0 / *total;
+}
+
+__global__ void k_fill_d(size_t n, double *p, double v)
+{
+    GRID_LOOP(i, n) p[i] = v;
+}
+
+// ---------------------------------------------------------------- monitor
+
+template <typename T>
+__global__ void k_wsum(size_t n, size_t dim, size_t ld, const T *state,
+    const double *W, double *part)
+{
+    __shared__ double sh[kB / 32 + 1];
+    for (size_t d = 0; d < dim; ++d) {
+        double s = 0;
+        GRID_LOOP(i, n) s += W[i] * static_cast<double>(state[d * ld + i]);
+        s = block_reduce(s, OpAdd(), 0.0, sh);
+        if (threadIdx.x == 0)
+            part[d * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+__global__ void k_wsum_final(size_t dim, int nb, const double *part,
+    double *out)
+{
+    if (threadIdx.x < dim && blockIdx.x == 0) {
+        double s = 0;
+        for (int b = 0; b < nb; ++b)
+            s += part[threadIdx.x * nb + b];
+        out[threadIdx.x] = s;
+    }
+}
+
+EngineState engine_state(const vsmc_cuda_rng &r)
+{
+    EngineState e;
+    e.k0 = static_cast<uint32_t>(r.key[0]);
+    e.k1 = static_cast<uint32_t>(r.key[1]);
+    for (int i = 0; i < 4; ++i)
+        e.c[i] = static_cast<uint32_t>(r.ctr[i]);
+    e.index = r.index;
+    return e;
+}
+
+// advance the host engine by k words of the scalar stream
+void engine_advance_host(vsmc_cuda_rng &r, uint64_t k)
+{
+    if (k == 0)
+        return;
+    const uint64_t last = static_cast<uint64_t>(r.index) + k - 1;
+    uint32_t c[4] = {static_cast<uint32_t>(r.ctr[0]),
+        static_cast<uint32_t>(r.ctr[1]), static_cast<uint32_t>(r.ctr[2]),
+        static_cast<uint32_t>(r.ctr[3])};
+    ctr32_add(c, last / 4);
+    for (int i = 0; i < 4; ++i)
+        r.ctr[i] = c[i];
+    r.index = static_cast<uint32_t>(last % 4) + 1;
+}
+
+bool size_ok(size_t n) { return n < (size_t(1) << 31); }
+
+} // namespace
+
+// ------------------------------------------------------- internal entries
+
+// rep for m weights against n uniforms u (device); integ added if non-null
+int u01_rep_device(size_t m, size_t n, const double *w, const double *u,
+    int *rep, const int *integ, uint32_t *err, Scratch &scratch,
+    cudaStream_t st)
+{
+    if (m == 0)
+        return VSMC_CUDA_OK;
+    if (m == 1 || n == 0) {
+        if (m == 1) {
+            k_set_one<<<1, 32, 0, st>>>(rep, static_cast<int>(n));
+            VSMC_CUDA_CHECK_LAUNCH();
+            if (integ)
+                k_rep_from_counts<<<1, 32, 0, st>>>(1, n, nullptr, rep, integ);
+        } else {
+            k_fill_i32<<<grid1(m), kB, 0, st>>>(m, rep, 0);
+            VSMC_CUDA_CHECK_LAUNCH();
+            if (integ) {
+                uint32_t *F = scratch.get<uint32_t>(m);
+                if (F == nullptr)
+                    return VSMC_CUDA_ERR_ALLOC;
+                VSMC_CUDA_TRY(cudaMemsetAsync(F, 0, sizeof(uint32_t) * m, st));
+                k_rep_from_counts<<<grid1(m), kB, 0, st>>>(m, 0, F, rep, integ);
+            }
+        }
+        VSMC_CUDA_CHECK_LAUNCH();
+        return VSMC_CUDA_OK;
+    }
+    double *cdf = scratch.get<double>(m - 1);
+    double *pm = scratch.get<double>(n);
+    double *pp = scratch.get<double>(scan_parts(n));
+    uint32_t *F = scratch.get<uint32_t>(m);
+    if (!cdf || !pm || !pp || !F)
+        return VSMC_CUDA_ERR_ALLOC;
+    int rc = seqsum_device(m - 1, w, cdf, nullptr, err, scratch, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    rc = device_scan(n, LoadKey{u}, StoreD{pm}, OpMaxD(), -static_cast<double>(INFINITY), pp, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    k_counts<<<grid1(m), kB, 0, st>>>(m, n, cdf, pm, F);
+    k_rep_from_counts<<<grid1(m), kB, 0, st>>>(m, n, F, rep, integ);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+int rep_index_device(size_t m, size_t n, const int *rep, int *idx,
+    uint32_t *err, Scratch &scratch, cudaStream_t st)
+{
+    if (m == 0 || n == 0)
+        return VSMC_CUDA_OK;
+    const bool square = m == n;
+    I2 *incl = scratch.get<I2>(m);
+    I2 *pp = scratch.get<I2>(scan_parts(m));
+    if (!incl || !pp)
+        return VSMC_CUDA_ERR_ALLOC;
+    int rc = device_scan(m, LoadES{rep, square}, StoreI2{incl}, OpI2(),
+        I2{0, 0}, pp, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    // the number of ranks / slots is needed on the host to size the scan
+    I2 tot;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(
+        &tot, incl + (m - 1), sizeof(I2), cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    size_t nmarks;
+    if (square) {
+        if (tot.a != tot.b || tot.a < 0)
+            return VSMC_CUDA_ERR_ARG; // counts do not sum to n
+        nmarks = static_cast<size_t>(tot.a);
+    } else {
+        if (tot.a < 0 || static_cast<size_t>(tot.a) > n)
+            return VSMC_CUDA_ERR_ARG;
+        nmarks = static_cast<size_t>(tot.a);
+    }
+    if (nmarks == 0) {
+        if (square)
+            k_index_square<<<grid1(n), kB, 0, st>>>(
+                n, rep, incl, nullptr, 0, idx, err);
+        VSMC_CUDA_CHECK_LAUNCH();
+        return VSMC_CUDA_OK;
+    }
+    int *marks = scratch.get<int>(nmarks);
+    int *srcs = scratch.get<int>(nmarks);
+    int *pm = scratch.get<int>(scan_parts(nmarks));
+    if (!marks || !srcs || !pm)
+        return VSMC_CUDA_ERR_ALLOC;
+    VSMC_CUDA_TRY(cudaMemsetAsync(marks, 0, sizeof(int) * nmarks, st));
+    k_marks<<<grid1(m), kB, 0, st>>>(m, square, rep, incl, marks, nmarks, err);
+    VSMC_CUDA_CHECK_LAUNCH();
+    rc = device_scan(nmarks, LoadI{marks}, StoreI{srcs}, OpMaxI(), 0, pm, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    if (square)
+        k_index_square<<<grid1(n), kB, 0, st>>>(
+            n, rep, incl, srcs, nmarks, idx, err);
+    else
+        k_index_flat<<<grid1(nmarks), kB, 0, st>>>(nmarks, srcs, idx);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+// residual split; *R_dev receives n - sum(integ) (device size_t)
+int residual_device(size_t m, size_t n, const double *w, double *resid,
+    int *integ, size_t *R_host, uint32_t *err, Scratch &scratch,
+    cudaStream_t st)
+{
+    if (m == 0) {
+        *R_host = n;
+        return VSMC_CUDA_OK;
+    }
+    k_residual_split<<<grid1(m), kB, 0, st>>>(m, n, w, resid, integ);
+    VSMC_CUDA_CHECK_LAUNCH();
+    double *total = scratch.get<double>(1);
+    int *isum = scratch.get<int>(1);
+    int *pp = scratch.get<int>(scan_parts(m));
+    int *ipref = scratch.get<int>(m);
+    if (!total || !isum || !pp || !ipref)
+        return VSMC_CUDA_ERR_ALLOC;
+    int rc = seqsum_device(m, resid, nullptr, total, err, scratch, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    k_scale<<<grid1(m), kB, 0, st>>>(m, total, resid);
+    VSMC_CUDA_CHECK_LAUNCH();
+    rc = device_scan(m, LoadI{integ}, StoreI{ipref}, OpAdd(), 0, pp, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    int R = 0;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(
+        &R, ipref + (m - 1), sizeof(int), cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    *R_host = n - static_cast<size_t>(R);
+    return VSMC_CUDA_OK;
+}
+
+// words a lazily read uniform sequence of length n consumed, given the counts
+// (the loop reads up to the first uniform above the second-to-last CDF value)
+int consumed_words(size_t m, size_t n, const int *rep_dev, const int *integ_dev,
+    cudaStream_t st, uint64_t *words)
+{
+    *words = 0;
+    if (m < 2 || n == 0)
+        return VSMC_CUDA_OK;
+    int last = 0, ilast = 0;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(
+        &last, rep_dev + (m - 1), sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (integ_dev)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(&ilast, integ_dev + (m - 1),
+            sizeof(int), cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    const size_t tail = static_cast<size_t>(last - ilast);
+    const size_t jf = n - tail;
+    *words = jf < n ? jf + 1 : n;
+    return VSMC_CUDA_OK;
+}
+
+int scheme_device(size_t m, size_t n, vsmc_cuda_rng *rng, const double *w,
+    int *rep, int scheme, Scratch &scratch, cudaStream_t st)
+{
+    uint32_t *err = scratch.get<uint32_t>(1);
+    if (err == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    VSMC_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    const bool residual = scheme >= VSMC_CUDA_RESIDUAL;
+    const int base = residual ? scheme - VSMC_CUDA_RESIDUAL : scheme;
+    const double *wt = w;
+    int *integ = nullptr;
+    size_t N = n;
+    int rc;
+    if (residual) {
+        double *resid = scratch.get<double>(m);
+        integ = scratch.get<int>(m);
+        if (!resid || !integ)
+            return VSMC_CUDA_ERR_ALLOC;
+        rc = residual_device(m, n, w, resid, integ, &N, err, scratch, st);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+        wt = resid;
+    }
+    const EngineState es = engine_state(*rng);
+    double *u = scratch.get<double>(N);
+    if (u == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    if (N > 0) {
+        if (base == VSMC_CUDA_STRATIFIED) {
+            k_stratified_seq<<<grid1(N), kB, 0, st>>>(es, N, u);
+        } else if (base == VSMC_CUDA_SYSTEMATIC) {
+            k_systematic_seq<<<grid1(N), kB, 0, st>>>(es, N, u);
+        } else {
+            double *t = scratch.get<double>(N);
+            if (t == nullptr)
+                return VSMC_CUDA_ERR_ALLOC;
+            k_sorted_terms<<<grid1(N), kB, 0, st>>>(es, N, t);
+            VSMC_CUDA_CHECK_LAUNCH();
+            rc = seqsum_device(N, t, t, nullptr, err, scratch, st, true);
+            if (rc != VSMC_CUDA_OK)
+                return rc;
+            k_sorted_finish<<<grid1(N), kB, 0, st>>>(N, t, u);
+        }
+        VSMC_CUDA_CHECK_LAUNCH();
+    }
+    rc = u01_rep_device(m, N, wt, u, rep, integ, err, scratch, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    uint64_t words = 0;
+    if (base == VSMC_CUDA_SYSTEMATIC) {
+        words = 1; // the sequence constructor draws once
+    } else if (m >= 1) {
+        rc = consumed_words(m, N, rep, integ, st, &words);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+    }
+    int status = VSMC_CUDA_OK;
+    rc = read_err(err, st, &status);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    if (status != VSMC_CUDA_OK)
+        return status;
+    engine_advance_host(*rng, words);
+    return VSMC_CUDA_OK;
+}
+
+// Weight::normalize(use_log) on W in place: sum, scale, ESS (weight.hpp:208-229)
+int weight_normalize_device(size_t n, double *W, double *ess_dev,
+    uint32_t *err, Scratch &scratch, cudaStream_t st)
+{
+    double *total = scratch.get<double>(1);
+    double *sq = scratch.get<double>(n);
+    double *tsq = scratch.get<double>(1);
+    if (!total || !sq || !tsq)
+        return VSMC_CUDA_ERR_ALLOC;
+    int rc = seqsum_device(n, W, nullptr, total, err, scratch, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    k_scale<<<grid1(n), kB, 0, st>>>(n, total, W);
+    k_square<<<grid1(n), kB, 0, st>>>(n, W, sq);
+    VSMC_CUDA_CHECK_LAUNCH();
+    rc = seqsum_device(n, sq, nullptr, tsq, err, scratch, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    if (ess_dev) {
+        k_inv_total<<<1, 32, 0, st>>>(tsq, ess_dev);
+        VSMC_CUDA_CHECK_LAUNCH();
+    }
+    return VSMC_CUDA_OK;
+}
+
+// post_set_log: subtract the max, exponentiate, normalize
+int weight_post_set_log_device(size_t n, double *W, double *ess_dev,
+    uint32_t *err, Scratch &scratch, cudaStream_t st)
+{
+    const int nb = grid1(n);
+    double *part = scratch.get<double>(nb);
+    if (part == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    k_reduce_max<<<nb, kB, 0, st>>>(n, W, part);
+    k_max_parts<<<1, kB, 0, st>>>(nb, part);
+    k_exp_shift<<<grid1(n), kB, 0, st>>>(n, W, part, W);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return weight_normalize_device(n, W, ess_dev, err, scratch, st);
+}
+
+int weight_set_equal_device(size_t n, double *W, double *ess_dev,
+    uint32_t *err, Scratch &scratch, cudaStream_t st)
+{
+    k_fill_d<<<grid1(n), kB, 0, st>>>(n, W, 1.0 / static_cast<double>(n));
+    VSMC_CUDA_CHECK_LAUNCH();
+    return weight_normalize_device(n, W, ess_dev, err, scratch, st);
+}
+
+int weight_add_log_device(size_t n, const double *l, double *W,
+    double *ess_dev, uint32_t *err, Scratch &scratch, cudaStream_t st)
+{
+    k_log_add<<<grid1(n), kB, 0, st>>>(n, l, W);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return weight_post_set_log_device(n, W, ess_dev, err, scratch, st);
+}
+
+template <typename T>
+int monitor_mean_device(size_t n, size_t dim, size_t ld, const T *state,
+    const double *W, double *out, Scratch &scratch, cudaStream_t st)
+{
+    const int nb = grid_for(n, kB, 8, 2);
+    double *part = scratch.get<double>(dim * nb);
+    if (part == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    k_wsum<T><<<nb, kB, 0, st>>>(n, dim, ld, state, W, part);
+    k_wsum_final<<<1, 32, 0, st>>>(dim, nb, part, out);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+template int monitor_mean_device<float>(size_t, size_t, size_t, const float *,
+    const double *, double *, Scratch &, cudaStream_t);
+template int monitor_mean_device<double>(size_t, size_t, size_t,
+    const double *, const double *, double *, Scratch &, cudaStream_t);
+
+template <typename T>
+int state_copy_device(size_t n, size_t dim, size_t ld, const int *idx,
+    T *state, uint32_t *err, cudaStream_t st)
+{
+    k_check_fixed_points<<<grid1(n), kB, 0, st>>>(n, idx, err);
+    k_copy_state<T><<<grid1(n), kB, 0, st>>>(n, dim, ld, idx, state, err);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+template int state_copy_device<float>(
+    size_t, size_t, size_t, const int *, float *, uint32_t *, cudaStream_t);
+template int state_copy_device<double>(
+    size_t, size_t, size_t, const int *, double *, uint32_t *, cudaStream_t);
+
+} // namespace vsmc_cuda
+
+using namespace vsmc_cuda;
+
+namespace
+{
+
+// run `body(err, scratch)` with a fresh error word, then report it
+template <typename F>
+int with_err(void *stream, F body)
+{
+    cudaStream_t st = as_stream(stream);
+    Scratch scratch(st);
+    uint32_t *err = scratch.get<uint32_t>(1);
+    if (err == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    VSMC_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    int rc = body(err, scratch, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    int status = VSMC_CUDA_OK;
+    rc = read_err(err, st, &status);
+    return rc != VSMC_CUDA_OK ? rc : status;
+}
+
+bool valid_philox(const vsmc_cuda_rng *r)
+{
+    return r != nullptr && r->kind == VSMC_CUDA_PHILOX4X32 && r->index >= 1 &&
+        r->index <= 4;
+}
+
+} // namespace
+
+extern "C" {
+
+int vsmc_cuda_u01_sorted(size_t n, const double *u01, double *u01seq,
+    void *stream)
+{
+    if ((u01 == nullptr || u01seq == nullptr) && n)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        double *t = sc.get<double>(n);
+        if (t == nullptr)
+            return static_cast<int>(VSMC_CUDA_ERR_ALLOC);
+        k_sorted_terms_arr<<<grid1(n), kB, 0, st>>>(n, u01, t);
+        VSMC_CUDA_CHECK_LAUNCH();
+        int rc = seqsum_device(n, t, t, nullptr, err, sc, st, true);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+        k_sorted_finish<<<grid1(n), kB, 0, st>>>(n, t, u01seq);
+        VSMC_CUDA_CHECK_LAUNCH();
+        return static_cast<int>(VSMC_CUDA_OK);
+    });
+}
+
+int vsmc_cuda_u01_stratified(size_t n, const double *u01, double *u01seq,
+    void *stream)
+{
+    if ((u01 == nullptr || u01seq == nullptr) && n)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    k_stratified_arr<<<grid1(n), kB, 0, as_stream(stream)>>>(n, u01, u01seq);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_u01_systematic(size_t n, double u01, double *u01seq,
+    void *stream)
+{
+    if (u01seq == nullptr && n)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        double *t = sc.get<double>(n);
+        if (t == nullptr)
+            return static_cast<int>(VSMC_CUDA_ERR_ALLOC);
+        k_systematic_terms<<<grid1(n), kB, 0, st>>>(n, u01, t);
+        VSMC_CUDA_CHECK_LAUNCH();
+        return seqsum_device(n, t, u01seq, nullptr, err, sc, st);
+    });
+}
+
+int vsmc_cuda_resample_trans_u01_rep(size_t m, size_t n, const double *weight,
+    const double *u01, int *replication, void *stream)
+{
+    if ((m && (weight == nullptr || replication == nullptr)) ||
+        (n && m > 1 && u01 == nullptr))
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(m) || !size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        return u01_rep_device(m, n, weight, u01, replication, nullptr, err,
+            sc, st);
+    });
+}
+
+int vsmc_cuda_resample_trans_u01_index(size_t m, size_t n,
+    const double *weight, const double *u01, int *index, void *stream)
+{
+    if (m == 0 || n == 0)
+        return VSMC_CUDA_OK;
+    if (weight == nullptr || u01 == nullptr || index == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(m) || !size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        if (m == 1) {
+            k_fill_i32<<<grid1(n), kB, 0, st>>>(n, index, 0);
+            VSMC_CUDA_CHECK_LAUNCH();
+            return static_cast<int>(VSMC_CUDA_OK);
+        }
+        double *cdf = sc.get<double>(m - 1);
+        double *pm = sc.get<double>(n);
+        double *pp = sc.get<double>(scan_parts(n));
+        if (!cdf || !pm || !pp)
+            return static_cast<int>(VSMC_CUDA_ERR_ALLOC);
+        int rc = seqsum_device(m - 1, weight, cdf, nullptr, err, sc, st);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+        rc = device_scan(
+            n, LoadKey{u01}, StoreD{pm}, OpMaxD(), -static_cast<double>(INFINITY), pp, st);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+        k_index_from_cdf<<<grid1(n), kB, 0, st>>>(m, n, cdf, pm, index);
+        VSMC_CUDA_CHECK_LAUNCH();
+        return static_cast<int>(VSMC_CUDA_OK);
+    });
+}
+
+int vsmc_cuda_resample_trans_rep_index(size_t m, size_t n,
+    const int *replication, int *index, void *stream)
+{
+    if (m == 0 || n == 0)
+        return VSMC_CUDA_OK;
+    if (replication == nullptr || index == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(m) || !size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        return rep_index_device(m, n, replication, index, err, sc, st);
+    });
+}
+
+int vsmc_cuda_resample_trans_index_rep(size_t m, size_t n, const int *index,
+    int *replication, void *stream)
+{
+    if (m == 0 || n == 0)
+        return VSMC_CUDA_OK;
+    if (replication == nullptr || index == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(m) || !size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        (void)sc;
+        VSMC_CUDA_TRY(cudaMemsetAsync(replication, 0, sizeof(int) * m, st));
+        k_hist<<<grid1(n), kB, 0, st>>>(m, n, index, replication, err);
+        VSMC_CUDA_CHECK_LAUNCH();
+        return static_cast<int>(VSMC_CUDA_OK);
+    });
+}
+
+int vsmc_cuda_resample_trans_residual(size_t m, size_t n,
+    const double *weight, double *resid, int *integ, size_t *r_host,
+    void *stream)
+{
+    if (r_host == nullptr ||
+        (m && (weight == nullptr || resid == nullptr || integ == nullptr)))
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(m) || !size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        return residual_device(m, n, weight, resid, integ, r_host, err, sc, st);
+    });
+}
+
+int vsmc_cuda_resample(size_t m, size_t n, vsmc_cuda_rng *rng,
+    const double *weight, int *replication, int scheme, void *stream)
+{
+    if (!valid_philox(rng) || scheme < VSMC_CUDA_MULTINOMIAL ||
+        scheme > VSMC_CUDA_RESIDUAL_SYSTEMATIC ||
+        (m && (weight == nullptr || replication == nullptr)))
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(m) || !size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    cudaStream_t st = as_stream(stream);
+    Scratch scratch(st);
+    return scheme_device(m, n, rng, weight, replication, scheme, scratch, st);
+}
+
+#define VSMC_CUDA_SCHEME_ENTRY(name, id)                                      \
+    int vsmc_cuda_resample_##name(size_t m, size_t n, vsmc_cuda_rng *rng,     \
+        const double *weight, int *replication, void *stream)                 \
+    {                                                                         \
+        return vsmc_cuda_resample(m, n, rng, weight, replication, id, stream); \
+    }
+
+VSMC_CUDA_SCHEME_ENTRY(multinomial, VSMC_CUDA_MULTINOMIAL)
+VSMC_CUDA_SCHEME_ENTRY(stratified, VSMC_CUDA_STRATIFIED)
+VSMC_CUDA_SCHEME_ENTRY(systematic, VSMC_CUDA_SYSTEMATIC)
+VSMC_CUDA_SCHEME_ENTRY(residual, VSMC_CUDA_RESIDUAL)
+VSMC_CUDA_SCHEME_ENTRY(residual_stratified, VSMC_CUDA_RESIDUAL_STRATIFIED)
+VSMC_CUDA_SCHEME_ENTRY(residual_systematic, VSMC_CUDA_RESIDUAL_SYSTEMATIC)
+
+int vsmc_cuda_state_copy_f32(size_t n, size_t dim, const int *index,
+    float *state, void *stream)
+{
+    if (n && (index == nullptr || state == nullptr))
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    if (n == 0 || dim == 0)
+        return VSMC_CUDA_OK;
+    const int rc = with_err(stream, [&](uint32_t *err, Scratch &, cudaStream_t st) -> int {
+        return state_copy_device<float>(n, dim, n, index, state, err, st);
+    });
+    return rc == VSMC_CUDA_ERR_INTERNAL ? VSMC_CUDA_ERR_ARG : rc;
+}
+
+int vsmc_cuda_state_copy_f64(size_t n, size_t dim, const int *index,
+    double *state, void *stream)
+{
+    if (n && (index == nullptr || state == nullptr))
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    if (n == 0 || dim == 0)
+        return VSMC_CUDA_OK;
+    const int rc = with_err(stream, [&](uint32_t *err, Scratch &, cudaStream_t st) -> int {
+        return state_copy_device<double>(n, dim, n, index, state, err, st);
+    });
+    return rc == VSMC_CUDA_ERR_INTERNAL ? VSMC_CUDA_ERR_ARG : rc;
+}
+
+int vsmc_cuda_weight_set(size_t n, const double *w, double *W,
+    double *ess_dev, void *stream)
+{
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    if (w == nullptr || W == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        if (W != w)
+            VSMC_CUDA_TRY(cudaMemcpyAsync(W, w, sizeof(double) * n,
+                cudaMemcpyDeviceToDevice, st));
+        return weight_normalize_device(n, W, ess_dev, err, sc, st);
+    });
+}
+
+int vsmc_cuda_weight_set_log(size_t n, const double *lw, double *W,
+    double *ess_dev, void *stream)
+{
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    if (lw == nullptr || W == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        if (W != lw)
+            VSMC_CUDA_TRY(cudaMemcpyAsync(W, lw, sizeof(double) * n,
+                cudaMemcpyDeviceToDevice, st));
+        return weight_post_set_log_device(n, W, ess_dev, err, sc, st);
+    });
+}
+
+int vsmc_cuda_weight_add_log(size_t n, const double *l, double *W,
+    double *ess_dev, void *stream)
+{
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    if (l == nullptr || W == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        return weight_add_log_device(n, l, W, ess_dev, err, sc, st);
+    });
+}
+
+int vsmc_cuda_weight_set_equal(size_t n, double *W, double *ess_dev,
+    void *stream)
+{
+    if (n == 0)
+        return VSMC_CUDA_OK;
+    if (W == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n))
+        return VSMC_CUDA_ERR_SIZE;
+    return with_err(stream, [&](uint32_t *err, Scratch &sc, cudaStream_t st) -> int {
+        return weight_set_equal_device(n, W, ess_dev, err, sc, st);
+    });
+}
+
+int vsmc_cuda_monitor_mean_f64(size_t n, size_t dim, const double *state,
+    const double *W, double *out_dev, void *stream)
+{
+    if (state == nullptr || W == nullptr || out_dev == nullptr || dim > 32)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n) || n == 0)
+        return VSMC_CUDA_ERR_SIZE;
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    return monitor_mean_device<double>(n, dim, n, state, W, out_dev, sc, st);
+}
+
+int vsmc_cuda_monitor_mean_f32(size_t n, size_t dim, const float *state,
+    const double *W, double *out_dev, void *stream)
+{
+    if (state == nullptr || W == nullptr || out_dev == nullptr || dim > 32)
+        return VSMC_CUDA_ERR_ARG;
+    if (!size_ok(n) || n == 0)
+        return VSMC_CUDA_ERR_SIZE;
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    return monitor_mean_device<float>(n, dim, n, state, W, out_dev, sc, st);
+}
+
+} // extern "C"

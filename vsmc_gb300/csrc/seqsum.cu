@@ -1,0 +1,297 @@
+// Left-to-right double summation, bit-identical to a sequential loop, in
+// parallel.
+//
+// The reference accumulates its resampling CDF and its normalizing sums one
+// element at a time (resample/transform.hpp:61-69, core/weight.hpp:224-229,
+// resample/transform.hpp:164).  For non-negative terms the running sum s is
+// non-decreasing, and while s_{i-1} and s_i stay in one binade [2^e, 2^(e+1))
+// every partial sum is a multiple of u = 2^(e-52), so
+//     s_i = fl(s_{i-1} + x_i) = s_{i-1} + rint(x_i / u) * u
+// whenever x_i / u is not exactly half-way (a tie rounds to even, which
+// depends on s_{i-1}).  The increment rint(x_i / u) is an exact integer that
+// does not depend on s_{i-1}, so runs of such elements are an exact integer
+// prefix sum.  What is left -- the first element, elements whose running sum
+// may cross a power of two, ties, and sums too small for the relative
+// bounds -- is a short list of breakpoints, evaluated in order by one thread
+// with real IEEE additions.  The binade of every running sum is taken from an
+// approximate parallel prefix P with the margin 2^-19 relative, far above
+// both |P - exact| and |sequential - exact| <= (n - 1) 2^-53 (n < 2^31).
+#include "common.cuh"
+#include "scan.cuh"
+#include "seqsum.cuh"
+
+#include <cmath>
+
+namespace vsmc_cuda
+{
+
+namespace
+{
+
+struct RF {
+    uint64_t r; // integer increment in units of the element's binade ulp
+    uint32_t f; // 1 = breakpoint
+    uint32_t pad;
+};
+
+struct OpRF {
+    __device__ __forceinline__ RF operator()(const RF &a, const RF &b) const
+    {
+        return {a.r + b.r, a.f + b.f, 0};
+    }
+};
+
+constexpr double kMargin = 0x1p-19;
+
+// exact power of two (ldexp scales without rounding)
+__device__ __forceinline__ double pow2(int k) { return ldexp(1.0, k); }
+
+__device__ __forceinline__ int binade(double v)
+{
+    return static_cast<int>((__double_as_longlong(v) >> 52) & 0x7FF) - 1023;
+}
+
+// classification of element i from the approximate prefix P
+struct Class {
+    bool regular;
+    int e;      // binade of s_{i-1} and s_i (regular only)
+    uint64_t r; // rint(x_i / 2^(e-52)) (regular only)
+};
+
+__device__ __forceinline__ Class classify(size_t i, const double *x,
+    const double *P, uint32_t *err, bool allow_inf)
+{
+    Class c = {false, 0, 0};
+    const double xi = x[i];
+    if (!(xi >= 0.0) || (isinf(xi) && !allow_inf)) {
+        if (err)
+            atomicOr(err, DEV_ERR_NONFINITE);
+        return c;
+    }
+    if (isinf(xi))
+        return c;
+    if (i == 0)
+        return c;
+    const double lo = P[i - 1] * (1.0 - kMargin);
+    const double hi = P[i] * (1.0 + kMargin);
+    if (!(lo >= 0x1p-1000) || !isfinite(hi))
+        return c;
+    const int e = binade(lo);
+    if (binade(hi) != e)
+        return c;
+    const double y = ldexp(xi, 52 - e); // exact
+    const double fl = floor(y);
+    if (y - fl == 0.5) // tie: rounding depends on the running sum's parity
+        return c;
+    c.regular = true;
+    c.e = e;
+    c.r = static_cast<uint64_t>(rint(y));
+    return c;
+}
+
+struct LoadX {
+    const double *x;
+    __device__ double operator()(size_t i) const { return x[i]; }
+};
+
+struct StoreD {
+    double *p;
+    __device__ void operator()(size_t i, double v) const { p[i] = v; }
+};
+
+struct LoadRF {
+    const double *x;
+    const double *P;
+    bool allow_inf;
+    __device__ RF operator()(size_t i) const
+    {
+        const Class c = classify(i, x, P, nullptr, allow_inf);
+        return {c.regular ? c.r : 0ull, c.regular ? 0u : 1u, 0u};
+    }
+};
+
+struct StoreRF {
+    RF *p;
+    __device__ void operator()(size_t i, RF v) const { p[i] = v; }
+};
+
+// breakpoint records, in order
+__global__ void __launch_bounds__(256) k_breakpoints(size_t n,
+    const double *x, const double *P, const RF *C, uint32_t *bidx,
+    uint64_t *bcr, uint32_t *err, bool allow_inf)
+{
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+         i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const Class c = classify(i, x, P, err, allow_inf);
+        if (!c.regular) {
+            const uint32_t k = C[i].f - 1;
+            bidx[k] = static_cast<uint32_t>(i);
+            bcr[k] = C[i].r; // r_i = 0, so also the count through i - 1
+        }
+    }
+}
+
+// One block walks the breakpoints in order with real additions.
+__global__ void __launch_bounds__(256) k_fixup(size_t n, const double *x,
+    const double *P, const RF *C, const uint32_t *bidx, const uint64_t *bcr,
+    double *sb, double *total, uint32_t *err, bool allow_inf)
+{
+    __shared__ double s_xb[256];
+    __shared__ uint32_t s_b[256];
+    __shared__ uint64_t s_crm1[256];
+    __shared__ int s_em1[256];
+    __shared__ int s_reg_m1[256];
+    const uint32_t nbk = C[n - 1].f;
+    double S = 0.0;          // value at the previous breakpoint
+    uint32_t bprev = 0;
+    uint64_t crprev = 0;
+    for (uint32_t c0 = 0; c0 < nbk; c0 += 256) {
+        const uint32_t k = c0 + threadIdx.x;
+        if (k < nbk) {
+            const uint32_t b = bidx[k];
+            s_b[threadIdx.x] = b;
+            s_xb[threadIdx.x] = x[b];
+            if (b > 0) {
+                const Class cm = classify(b - 1, x, P, nullptr, allow_inf);
+                s_reg_m1[threadIdx.x] = cm.regular ? 1 : 0;
+                s_em1[threadIdx.x] = cm.e;
+                s_crm1[threadIdx.x] = C[b - 1].r;
+            } else {
+                s_reg_m1[threadIdx.x] = 0;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t m = nbk - c0 < 256 ? nbk - c0 : 256;
+            for (uint32_t j = 0; j < m; ++j) {
+                const uint32_t b = s_b[j];
+                double sp;
+                if (c0 + j == 0) {
+                    sp = 0.0;
+                    if (b != 0)
+                        atomicOr(err, DEV_ERR_INTERNAL);
+                } else if (!s_reg_m1[j]) {
+                    sp = S; // b - 1 is the previous breakpoint
+                    if (b - 1 != bprev)
+                        atomicOr(err, DEV_ERR_INTERNAL);
+                } else {
+                    sp = S + static_cast<double>(s_crm1[j] - crprev) *
+                            pow2(s_em1[j] - 52);
+                }
+                S = __dadd_rn(sp, s_xb[j]);
+                sb[c0 + j] = S;
+                bprev = b;
+                crprev = bcr[c0 + j];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total != nullptr) {
+        const Class cl = classify(n - 1, x, P, nullptr, allow_inf);
+        if (cl.regular)
+            *total = S + static_cast<double>(C[n - 1].r - crprev) *
+                    pow2(cl.e - 52);
+        else
+            *total = S;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_prefix_out(size_t n, const double *x,
+    const double *P, const RF *C, const uint64_t *bcr, const double *sb,
+    double *out, uint32_t *err, bool allow_inf)
+{
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+         i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const Class c = classify(i, x, P, nullptr, allow_inf);
+        const uint32_t k = C[i].f - 1;
+        double s;
+        if (!c.regular) {
+            s = sb[k];
+        } else {
+            s = sb[k] + static_cast<double>(C[i].r - bcr[k]) *
+                    pow2(c.e - 52);
+            const double lo = pow2(c.e);
+            if (!(s >= lo && s < 2.0 * lo))
+                atomicOr(err, DEV_ERR_BOUND);
+        }
+        out[i] = s;
+    }
+}
+
+} // namespace
+
+int seqsum_device(size_t n, const double *x, double *prefix, double *total,
+    uint32_t *err, Scratch &scratch, cudaStream_t st, bool allow_inf)
+{
+    if (n == 0) {
+        if (total)
+            VSMC_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(double), st));
+        return VSMC_CUDA_OK;
+    }
+    if (n >= (size_t(1) << 31))
+        return VSMC_CUDA_ERR_SIZE;
+    const size_t nb = scan_parts(n);
+    double *P = scratch.get<double>(n);
+    double *pd = scratch.get<double>(nb);
+    RF *C = scratch.get<RF>(n);
+    RF *pr = scratch.get<RF>(nb);
+    uint32_t *bidx = scratch.get<uint32_t>(n);
+    uint64_t *bcr = scratch.get<uint64_t>(n);
+    double *sb = scratch.get<double>(n);
+    if (!P || !pd || !C || !pr || !bidx || !bcr || !sb)
+        return VSMC_CUDA_ERR_ALLOC;
+    int rc = device_scan(n, LoadX{x}, StoreD{P}, OpAdd(), 0.0, pd, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    rc = device_scan(
+        n, LoadRF{x, P, allow_inf}, StoreRF{C}, OpRF(), RF{0, 0, 0}, pr, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    const int grid = grid_for(n, 256, 4, 8);
+    k_breakpoints<<<grid, 256, 0, st>>>(n, x, P, C, bidx, bcr, err, allow_inf);
+    k_fixup<<<1, 256, 0, st>>>(
+        n, x, P, C, bidx, bcr, sb, total, err, allow_inf);
+    if (prefix)
+        k_prefix_out<<<grid, 256, 0, st>>>(
+            n, x, P, C, bcr, sb, prefix, err, allow_inf);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+int read_err(uint32_t *err_dev, cudaStream_t st, int *status)
+{
+    uint32_t e = 0;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(
+        &e, err_dev, sizeof(e), cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (e & DEV_ERR_NONFINITE)
+        *status = VSMC_CUDA_ERR_NONFINITE;
+    else if (e)
+        *status = VSMC_CUDA_ERR_INTERNAL;
+    else
+        *status = VSMC_CUDA_OK;
+    return VSMC_CUDA_OK;
+}
+
+} // namespace vsmc_cuda
+
+using namespace vsmc_cuda;
+
+extern "C" int vsmc_cuda_sequential_sum(size_t n, const double *x,
+    double *prefix, double *total_dev, void *stream)
+{
+    if ((x == nullptr && n) || (prefix == nullptr && total_dev == nullptr))
+        return VSMC_CUDA_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    Scratch scratch(st);
+    uint32_t *err = scratch.get<uint32_t>(1);
+    if (err == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    VSMC_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    int rc = seqsum_device(n, x, prefix, total_dev, err, scratch, st);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    int status = VSMC_CUDA_OK;
+    rc = read_err(err, st, &status);
+    return rc != VSMC_CUDA_OK ? rc : status;
+}
