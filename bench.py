@@ -135,13 +135,25 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
+    """The largest x over all ranks (the slowest rank's time)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_seed(rank):
+    """Each rank runs an independent filter replica with its own seed."""
+    return 1 + rank
+
+
+def aggregate_rate(units_per_rank, world, seconds_max):
+    """Whole-job throughput: every rank's units over the slowest rank's time."""
+    return world * units_per_rank / seconds_max
 
 
 def simulate_obs(vc, T, seed=0):
@@ -238,7 +250,7 @@ def main():
     torch.cuda.set_stream(stream)
     sptr = ctypes.c_void_p(stream.cuda_stream)
     obs_dev = simulate_obs(vc, T, seed=0)
-    pf = vc.ParticleFilter(n, 32, SCHEME, THRESHOLD, seed=1 + rank,
+    pf = vc.ParticleFilter(n, 32, SCHEME, THRESHOLD, seed=replica_seed(rank),
                            max_steps=T, stream=sptr)
 
     # ---- device-resident timed region
@@ -306,8 +318,8 @@ def main():
     ms_max = max_over_ranks(ms, world)
     e2e_max = max_over_ranks(e2e_s, world)
     psteps = float(n) * T
-    value = world * psteps * args.steps / (ms_max / 1000.0)
-    e2e_value = world * psteps * e2e_steps / e2e_max
+    value = aggregate_rate(psteps * args.steps, world, ms_max / 1000.0)
+    e2e_value = aggregate_rate(psteps * e2e_steps, world, e2e_max)
     peak, peak_kind = measured_peaks()
     achieved = BYTES_PER_PARTICLE_STEP * n / (kernel_ms / 1000.0) / 1e9
     traffic = None

@@ -211,6 +211,20 @@ int vsmc_cuda_resample_residual_stratified(size_t m, size_t n,
 int vsmc_cuda_resample_residual_systematic(size_t m, size_t n,
     vsmc_cuda_rng *rng, const double *weight, int *replication, void *stream);
 
+/* Resampling on an integer CDF, as the precision-32 filter does it: q holds
+ * n non-negative 64-bit weights whose total stays below 2^63; uniform j
+ * (stratified: its own word; systematic: one shared word a of the engine)
+ * is u_j = (j + a 2^-32) / n and counts toward the first i with
+ * u_j <= (q_0 + ... + q_i) / total, compared exactly in integers.  The last
+ * slot takes the rest, as in resample/transform.hpp:70.  replication (n) and
+ * index (n, the reference slot layout of resample/transform.hpp:116-133) are
+ * device outputs (either may be NULL); the engine consumes the words the
+ * reference's U01SequenceStratified / U01SequenceSystematic would
+ * (rng/u01_sequence.hpp:177-259).  Synchronizes the stream.  No reference
+ * counterpart for the integer CDF itself (the reference sums doubles). */
+int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
+    vsmc_cuda_rng *rng, int *replication, int *index, void *stream);
+
 /* In-place particle copy state[d][dst] = state[d][index[dst]] for a SoA
  * state of `dim` rows of n values; safe in place for indices produced by
  * vsmc_cuda_resample_trans_rep_index (every parent keeps its slot).
@@ -301,7 +315,11 @@ int vsmc_cuda_pf_history(vsmc_cuda_pf *pf, size_t T, double *mean_host,
  * ((n + 255) / 256) * 256 elements, float or double by precision), and the
  * weight array (precision 64: normalized W doubles; precision 32: float
  * log-weights; after a resampling step every weight is equal and the stored
- * log-weights are stale until the next step). */
+ * log-weights are stale until the next step).  Precision 32 keeps the state
+ * in two buffers that alternate every step (a step reads one and writes the
+ * other, gathering resampled particles on the way), so the state pointer is
+ * valid until the next step; the call applies a pending resampling gather
+ * first (and may synchronize the stream to do so). */
 int vsmc_cuda_pf_state(vsmc_cuda_pf *pf, void **state_dev, void **weight_dev);
 int vsmc_cuda_pf_stream(vsmc_cuda_pf *pf, void **stream);
 /* Enable (1) / disable (0) capturing each filter step in a CUDA graph and

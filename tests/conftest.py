@@ -39,10 +39,25 @@ def P(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+_KEEP = []
+
+
 def dev(a):
-    """numpy -> CUDA tensor (same dtype)."""
+    """numpy -> CUDA tensor (same dtype).
+
+    The tensor is also kept in a per-test list: `dev(x).data_ptr()` passed
+    straight to a C call would otherwise let the temporary be freed at once,
+    and the caching allocator could hand the same block to the next dev()."""
     import torch
-    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    _KEEP.append(t)
+    return t
+
+
+@pytest.fixture(autouse=True)
+def _release_kept_tensors():
+    yield
+    _KEEP.clear()
 
 
 def host(t):

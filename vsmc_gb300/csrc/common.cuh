@@ -9,6 +9,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 
 #include "../../include/vsmc_cuda.h"
 
@@ -320,8 +321,7 @@ class Scratch
 
     private:
     cudaStream_t stream_;
-    void *ptrs_[32] = {};
-    int count_ = 0;
+    std::vector<void *> ptrs_;
 };
 
 } // namespace vsmc_cuda

@@ -47,21 +47,20 @@ int grid_for(
 
 Scratch::~Scratch()
 {
-    for (int i = 0; i < count_; ++i)
-        cudaFreeAsync(ptrs_[i], stream_);
+    // stream-ordered: each block is released after the work queued before
+    for (void *p : ptrs_)
+        cudaFreeAsync(p, stream_);
 }
 
 void *Scratch::alloc(size_t bytes)
 {
-    if (count_ >= 32)
-        return nullptr;
     void *p = nullptr;
     cudaError_t e = cudaMallocAsync(&p, bytes ? bytes : 1, stream_);
     if (e != cudaSuccess) {
         set_last_cuda_error(e);
         return nullptr;
     }
-    ptrs_[count_++] = p;
+    ptrs_.push_back(p);
     return p;
 }
 

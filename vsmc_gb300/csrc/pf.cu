@@ -18,15 +18,29 @@ using namespace vsmc_cuda;
 namespace vsmc_cuda
 {
 
+static float *buf32(vsmc_cuda_pf *pf, int which)
+{
+    return static_cast<float *>(which == 0 ? pf->state : pf->state2);
+}
+
+// A = the current state buffer, B = the other one
 static Pf32Args make_args32(vsmc_cuda_pf *pf)
 {
-    Pf32Args a;
-    float *s = static_cast<float *>(pf->state);
-    a.x = s;
-    a.y = s + pf->stride;
-    a.vx = s + 2 * pf->stride;
-    a.vy = s + 3 * pf->stride;
+    Pf32Args a = {};
+    const float *A = buf32(pf, pf->cur);
+    float *B = buf32(pf, 1 - pf->cur);
+    const size_t ld = pf->stride;
+    a.ax = A;
+    a.ay = A + ld;
+    a.avx = A + 2 * ld;
+    a.avy = A + 3 * ld;
+    a.bx = B;
+    a.by = B + ld;
+    a.bvx = B + 2 * ld;
+    a.bvy = B + 3 * ld;
     a.lw = static_cast<float *>(pf->weight);
+    a.idx = pf->idx;
+    a.srcs = pf->empties;
     a.n = static_cast<uint32_t>(pf->n);
     a.seed = pf->seed;
     a.max_steps = static_cast<uint32_t>(pf->max_steps);
@@ -44,13 +58,9 @@ static Pf32Args make_args32(vsmc_cuda_pf *pf)
 
 static Rs32Args make_rs_args32(vsmc_cuda_pf *pf)
 {
-    Rs32Args r;
-    float *s = static_cast<float *>(pf->state);
+    Rs32Args r = {};
     r.lw = static_cast<const float *>(pf->weight);
-    r.x = s;
-    r.y = s + pf->stride;
-    r.vx = s + 2 * pf->stride;
-    r.vy = s + 3 * pf->stride;
+    r.q = nullptr; // the log-weights are the input
     r.n = static_cast<uint32_t>(pf->n);
     r.shift = pf->shift;
     r.chunk = pf->chunk_rs;
@@ -60,60 +70,68 @@ static Rs32Args make_rs_args32(vsmc_cuda_pf *pf)
     r.cpart = pf->cpart;
     r.mpart = pf->mpart;
     r.rep = pf->rep;
+    r.idx = pf->idx;
     r.marks = pf->marks;
-    r.empties = pf->empties;
+    r.srcs = pf->empties;
     r.sc = pf->sc;
     return r;
 }
 
-// the kernels of one FP32 step after the first
-static int launch_step32(vsmc_cuda_pf *pf)
+static void launch_resample32(vsmc_cuda_pf *pf)
 {
-    const Pf32Args a = make_args32(pf);
     const Rs32Args r = make_rs_args32(pf);
     cudaStream_t st = pf->stream;
-    k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, st>>>(a);
     k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     k_rs32_count<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     k_rs32_assign<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     k_rs32_markmax<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    k_rs32_gather<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    k_rs32_fill<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+}
+
+// the kernels of one FP32 step (reads buffer cur, writes the other)
+static int launch_step32(vsmc_cuda_pf *pf, bool first)
+{
+    const Pf32Args a = make_args32(pf);
+    if (first)
+        k_pf32_step<true><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
+    else
+        k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
+    launch_resample32(pf);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
 }
 
 static int launch_first32(vsmc_cuda_pf *pf)
 {
-    const Pf32Args a = make_args32(pf);
-    const Rs32Args r = make_rs_args32(pf);
-    cudaStream_t st = pf->stream;
-    k_pf32_step<true><<<pf->grid_step, kPfBlock, 0, st>>>(a);
-    k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    k_rs32_count<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    k_rs32_assign<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    k_rs32_markmax<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    k_rs32_gather<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    VSMC_CUDA_CHECK_LAUNCH();
-    return VSMC_CUDA_OK;
+    const int rc = launch_step32(pf, true);
+    if (rc == VSMC_CUDA_OK)
+        pf->cur = 1 - pf->cur;
+    return rc;
 }
 
 static int step32(vsmc_cuda_pf *pf)
 {
-    if (!pf->use_graph)
-        return launch_step32(pf);
-    if (pf->graph_exec == nullptr) {
+    if (!pf->use_graph) {
+        const int rc = launch_step32(pf, false);
+        if (rc == VSMC_CUDA_OK)
+            pf->cur = 1 - pf->cur;
+        return rc;
+    }
+    const int par = pf->cur;
+    if (pf->graph_exec[par] == nullptr) {
         VSMC_CUDA_TRY(cudaStreamBeginCapture(
             pf->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = launch_step32(pf);
+        const int rc = launch_step32(pf, false);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(pf->stream, &g);
         if (rc != VSMC_CUDA_OK)
             return rc;
         VSMC_CUDA_TRY(e);
-        pf->graph = g;
-        VSMC_CUDA_TRY(cudaGraphInstantiate(&pf->graph_exec, g, 0));
+        pf->graph[par] = g;
+        VSMC_CUDA_TRY(cudaGraphInstantiate(&pf->graph_exec[par], g, 0));
     }
-    VSMC_CUDA_TRY(cudaGraphLaunch(pf->graph_exec, pf->stream));
+    VSMC_CUDA_TRY(cudaGraphLaunch(pf->graph_exec[par], pf->stream));
+    pf->cur = 1 - pf->cur;
     return VSMC_CUDA_OK;
 }
 
@@ -124,6 +142,24 @@ static int final_mean32(vsmc_cuda_pf *pf)
     k_pf32_final_mean<<<grid, kPfBlock, 0, pf->stream>>>(
         a, static_cast<uint32_t>(pf->t - 1));
     VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+// apply a pending resampling gather to the stored state (host-side views)
+static int materialize32(vsmc_cuda_pf *pf)
+{
+    int32_t gather = 0;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(&gather, &pf->sc->gather, sizeof(gather),
+        cudaMemcpyDeviceToHost, pf->stream));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
+    if (!gather)
+        return VSMC_CUDA_OK;
+    const Pf32Args a = make_args32(pf);
+    k_pf32_materialize<<<grid_for(pf->n, kPfBlock, 4, 8), kPfBlock, 0,
+        pf->stream>>>(a);
+    k_pf32_clear_gather<<<1, 1, 0, pf->stream>>>(pf->sc);
+    VSMC_CUDA_CHECK_LAUNCH();
+    pf->cur = 1 - pf->cur;
     return VSMC_CUDA_OK;
 }
 
@@ -160,13 +196,16 @@ static int reset_scalars(vsmc_cuda_pf *pf)
 
 static void free_all(vsmc_cuda_pf *pf)
 {
-    if (pf->graph_exec)
-        cudaGraphExecDestroy(pf->graph_exec);
-    if (pf->graph)
-        cudaGraphDestroy(pf->graph);
-    void *ptrs[] = {pf->state, pf->weight, pf->obs, pf->h_mean, pf->h_ess,
-        pf->h_logz, pf->h_res, pf->sc, pf->part, pf->qpart, pf->epart,
-        pf->cpart, pf->mpart, pf->rep, pf->marks, pf->empties};
+    for (int k = 0; k < 2; ++k) {
+        if (pf->graph_exec[k])
+            cudaGraphExecDestroy(pf->graph_exec[k]);
+        if (pf->graph[k])
+            cudaGraphDestroy(pf->graph[k]);
+    }
+    void *ptrs[] = {pf->state, pf->state2, pf->weight, pf->obs, pf->h_mean,
+        pf->h_ess, pf->h_logz, pf->h_res, pf->sc, pf->part, pf->qpart,
+        pf->epart, pf->cpart, pf->mpart, pf->rep, pf->idx, pf->marks,
+        pf->empties};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -282,7 +321,10 @@ int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
         PF_TRY(dalloc(&pf->epart, pf->grid_rs));
         PF_TRY(dalloc(&pf->cpart, pf->grid_rs));
         PF_TRY(dalloc(&pf->mpart, pf->grid_rs));
-        PF_TRY(dalloc(&pf->rep, n));
+        PF_TRY(dalloc(reinterpret_cast<char **>(&pf->state2),
+            esz * 4 * pf->stride));
+        PF_TRY(dalloc(&pf->rep, n + 4));
+        PF_TRY(dalloc(&pf->idx, pf->stride));
         PF_TRY(dalloc(&pf->marks, n));
         PF_TRY(dalloc(&pf->empties, n));
         if (cudaMemsetAsync(pf->marks, 0, sizeof(uint32_t) * n, pf->stream) !=
@@ -314,8 +356,73 @@ int vsmc_cuda_pf_launch_step_kernel(vsmc_cuda_pf *pf)
     const Pf32Args a = make_args32(pf);
     k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
     VSMC_CUDA_CHECK_LAUNCH();
+    pf->cur = 1 - pf->cur;
     ++pf->t;
     pf->mean_pending = true;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
+    vsmc_cuda_rng *rng, int *replication, int *index, void *stream)
+{
+    if (q == nullptr || reinterpret_cast<uintptr_t>(q) % alignof(uint64_t) ||
+        rng == nullptr || rng->kind != VSMC_CUDA_PHILOX4X32 ||
+        rng->index < 1 || rng->index > 4 ||
+        (scheme != VSMC_CUDA_STRATIFIED && scheme != VSMC_CUDA_SYSTEMATIC))
+        return VSMC_CUDA_ERR_ARG;
+    if (n < 2 || n >= (size_t(1) << 31))
+        return VSMC_CUDA_ERR_SIZE;
+    cudaStream_t st = as_stream(stream);
+    Scratch scratch(st);
+    const size_t grs0 = static_cast<size_t>(num_sms()) * 4;
+    size_t chunk = (n + grs0 - 1) / grs0;
+    chunk = (chunk + kPfTile - 1) / kPfTile * kPfTile;
+    const int grid = static_cast<int>((n + chunk - 1) / chunk);
+    Rs32Args r = {};
+    r.q = q;
+    r.n = static_cast<uint32_t>(n);
+    r.chunk = static_cast<uint32_t>(chunk);
+    r.scheme = scheme;
+    r.qpart = scratch.get<uint64_t>(grid);
+    r.epart = scratch.get<uint32_t>(grid);
+    r.cpart = scratch.get<uint32_t>(grid);
+    r.mpart = scratch.get<uint32_t>(grid);
+    r.rep = scratch.get<int32_t>(n + 4);
+    r.idx = scratch.get<int32_t>(n + 4);
+    r.marks = scratch.get<uint32_t>(n);
+    r.srcs = scratch.get<uint32_t>(n);
+    r.sc = scratch.get<PfScalars>(1);
+    if (!r.qpart || !r.epart || !r.cpart || !r.mpart || !r.rep || !r.idx ||
+        !r.marks || !r.srcs || !r.sc)
+        return VSMC_CUDA_ERR_ALLOC;
+    VSMC_CUDA_TRY(cudaMemsetAsync(r.marks, 0, sizeof(uint32_t) * n, st));
+    k_rs32_setup<<<1, 1, 0, st>>>(r.sc, static_cast<uint32_t>(rng->key[0]),
+        static_cast<uint32_t>(rng->key[1]), static_cast<uint32_t>(rng->ctr[0]),
+        static_cast<uint32_t>(rng->ctr[1]), static_cast<uint32_t>(rng->ctr[2]),
+        static_cast<uint32_t>(rng->ctr[3]), rng->index);
+    k_rs32_qsum<<<grid, kPfBlock, 0, st>>>(r);
+    k_rs32_count<<<grid, kPfBlock, 0, st>>>(r);
+    k_rs32_assign<<<grid, kPfBlock, 0, st>>>(r);
+    k_rs32_markmax<<<grid, kPfBlock, 0, st>>>(r);
+    k_rs32_fill<<<grid, kPfBlock, 0, st>>>(r);
+    VSMC_CUDA_CHECK_LAUNCH();
+    if (index)
+        k_rs32_decode<<<grid_for(n, kPfBlock, 4, 8), kPfBlock, 0, st>>>(r, index);
+    if (replication)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(replication, r.rep, sizeof(int) * n,
+            cudaMemcpyDeviceToDevice, st));
+    VSMC_CUDA_CHECK_LAUNCH();
+    PfScalars sc;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(
+        &sc, r.sc, sizeof(sc), cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (sc.err & DEV_ERR_NONFINITE)
+        return VSMC_CUDA_ERR_NONFINITE;
+    if (sc.err)
+        return VSMC_CUDA_ERR_INTERNAL;
+    for (int i = 0; i < 4; ++i)
+        rng->ctr[i] = sc.rctr[i];
+    rng->index = sc.rindex;
     return VSMC_CUDA_OK;
 }
 
@@ -339,8 +446,13 @@ int vsmc_cuda_pf_state(vsmc_cuda_pf *pf, void **state_dev, void **weight_dev)
 {
     if (pf == nullptr)
         return VSMC_CUDA_ERR_ARG;
+    if (pf->precision == 32) {
+        const int rc = materialize32(pf);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+    }
     if (state_dev)
-        *state_dev = pf->state;
+        *state_dev = pf->precision == 32 ? buf32(pf, pf->cur) : pf->state;
     if (weight_dev)
         *weight_dev = pf->weight;
     return VSMC_CUDA_OK;

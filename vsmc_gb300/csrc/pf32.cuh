@@ -43,8 +43,9 @@ __device__ __forceinline__ void lse_push(float v, float &m, float &s, float &s2)
     }
 }
 
-__device__ __forceinline__ void lse_merge(
-    double &m, double &s, double &s2, double m2, double t, double t2)
+// merge (m2, t, t2) into (m, s, s2): max, sum exp(v - m), sum exp(2(v - m))
+__device__ __forceinline__ void lse_merge_f(
+    float &m, float &s, float &s2, float m2, float t, float t2)
 {
     if (!(m2 > -INFINITY))
         return;
@@ -55,12 +56,12 @@ __device__ __forceinline__ void lse_merge(
         return;
     }
     if (m2 > m) {
-        const double e = exp(m - m2);
+        const float e = __expf(m - m2);
         s = s * e + t;
         s2 = s2 * e * e + t2;
         m = m2;
     } else {
-        const double e = exp(m2 - m);
+        const float e = __expf(m2 - m);
         s += t * e;
         s2 += t2 * e * e;
     }
@@ -106,90 +107,139 @@ __device__ __forceinline__ void engine_advance(PfScalars &sc, uint64_t k)
     sc.rindex = static_cast<uint32_t>(last % 4) + 1;
 }
 
-// Fixed-point comparison setup shared by the count kernels.
+// Counting uniforms against the fixed-point CDF.
+//
+// Uniform j is u_j = (j + a_j 2^-32) / N with a 32-bit word a_j.  With the
+// integer CDF C_i and total Q, u_j <= C / Q  <=>  (j 2^32 + a_j) Q <= C N 2^32
+// <=>  j Q + G_j <= C N  with G_j = ceil(a_j Q / 2^32) < Q, since both sides
+// are integers.  The counts follow from one exact floor(C N / Q) with its
+// remainder per CDF value.
 struct CountP {
     uint64_t Q;  // CDF total
-    uint64_t D;  // N * 2^32
+    uint64_t G;  // systematic: ceil(a Q / 2^32) (one word for every j)
     uint32_t n;
     int sh;      // Q >> sh < 2^24
     float scale; // n / (Q >> sh)
 };
 
-__device__ __forceinline__ CountP make_count_params(uint64_t Q, uint32_t n)
+__device__ __forceinline__ uint64_t ceil_aq(uint32_t a, uint64_t Q)
+{
+    const uint64_t hi = __umul64hi(static_cast<uint64_t>(a), Q); // < 2^32
+    const uint64_t lo = static_cast<uint64_t>(a) * Q;
+    return ((hi << 32) | (lo >> 32)) + ((lo & 0xFFFFFFFFull) != 0 ? 1 : 0);
+}
+
+__device__ __forceinline__ CountP make_count_params(
+    uint64_t Q, uint32_t n, uint32_t a_sys)
 {
     CountP p;
     p.Q = Q;
-    p.D = static_cast<uint64_t>(n) << 32;
+    p.G = ceil_aq(a_sys, Q);
     p.n = n;
     const int bits = 64 - __clzll(static_cast<long long>(Q));
     p.sh = bits > 24 ? bits - 24 : 0;
-    p.scale = static_cast<float>(n) / static_cast<float>(Q >> p.sh);
+    p.scale = static_cast<float>(n) /
+        __uint2float_rz(static_cast<uint32_t>(Q >> p.sh));
     return p;
 }
 
-// Number of uniforms u_j = (j + a_j 2^-32) / N (j < N) with u_j <= C / Q.
-// The u_j are strictly increasing, so this is also the index of the first
-// uniform above C.  a(j) returns a_j.  The float estimate is within a few
-// units; the 128-bit checks make the answer exact.
-template <typename AFn>
-__device__ __forceinline__ uint32_t count_le(
-    uint64_t C, const CountP &p, AFn a, uint32_t &err)
+// j = floor((C n - G) / Q) and r = (C n - G) - j Q; false if C n < G
+__device__ __forceinline__ bool cn_divmod(uint64_t C, uint64_t G,
+    const CountP &p, long long &j, uint64_t &r, uint32_t &err)
 {
-    const U128 X = mul_u64(C, p.D);
-    auto cond = [&](long long jj) -> bool {
-        const uint64_t num = (static_cast<uint64_t>(jj) << 32) + a(jj);
-        return le_u128(mul_u64(num, p.Q), X);
-    };
-    const long long nn = static_cast<long long>(p.n);
-    const float f = static_cast<float>(static_cast<uint32_t>(C >> p.sh)) * p.scale;
-    long long j = static_cast<long long>(floorf(f)) - 1; // estimate of the answer - 1
-    if (j > nn - 1)
-        j = nn - 1;
-    if (j < -1)
-        j = -1;
-    // walk a few steps from the estimate; the largest j with cond(j) is the
-    // answer - 1 (cond is monotone: true then false)
-    for (int g = 0; g < 8 && j >= 0 && !cond(j); ++g)
-        --j;
-    long long lo, hi; // cond(lo) true or lo == -1; cond(hi) false or hi == n
-    if (j >= 0 && !cond(j)) {
-        lo = -1;
-        hi = j;
-    } else {
-        for (int g = 0; g < 8 && j + 1 < nn && cond(j + 1); ++g)
-            ++j;
-        if (j + 1 >= nn || !cond(j + 1))
-            return static_cast<uint32_t>(j + 1);
-        lo = j + 1;
-        hi = nn;
+    uint64_t xh = __umul64hi(C, static_cast<uint64_t>(p.n));
+    uint64_t xl = C * static_cast<uint64_t>(p.n);
+    if (xl < G) {
+        if (xh == 0)
+            return false;
+        --xh;
     }
-    // estimate was far off (very large N): exact bisection
+    xl -= G;
+    // estimate within a few units of the answer
+    const float f =
+        __uint2float_rz(static_cast<uint32_t>(C >> p.sh)) * p.scale;
+    long long jj = static_cast<long long>(__float2int_rz(f)) - 2;
+    if (jj < 0)
+        jj = 0;
+    if (jj > static_cast<long long>(p.n))
+        jj = static_cast<long long>(p.n);
+    // R = X - jj Q, 128-bit; walk down while negative, up while >= Q
+    const uint64_t ph = __umul64hi(static_cast<uint64_t>(jj), p.Q);
+    const uint64_t pl = static_cast<uint64_t>(jj) * p.Q;
+    uint64_t rl = xl - pl;
+    uint64_t rh = xh - ph - (xl < pl ? 1 : 0);
     int guard = 0;
-    while (hi - lo > 1) {
-        const long long mid = lo + (hi - lo) / 2;
-        if (cond(mid))
-            lo = mid;
-        else
-            hi = mid;
+    while (static_cast<long long>(rh) < 0) { // X < jj Q
+        --jj;
+        const uint64_t t = rl + p.Q;
+        rh += (t < rl ? 1 : 0);
+        rl = t;
         if (++guard > 64) {
             err |= DEV_ERR_BOUND;
             break;
         }
     }
-    return static_cast<uint32_t>(lo + 1);
+    guard = 0;
+    while (rh != 0 || rl >= p.Q) {
+        ++jj;
+        rh -= (rl < p.Q ? 1 : 0);
+        rl -= p.Q;
+        if (++guard > 64) {
+            err |= DEV_ERR_BOUND;
+            break;
+        }
+    }
+    j = jj;
+    r = rl;
+    return true;
 }
 
+// F(C) = number of uniforms <= C / Q (= index of the first one above).
+// sys: every uniform shares a_sys (systematic); otherwise a_j is word j of
+// the resampling engine (stratified).
+__device__ __forceinline__ uint32_t count_F(uint64_t C, const CountP &p,
+    bool sys, const PfScalars &sc, uint32_t &err)
+{
+    long long j;
+    uint64_t r;
+    if (sys) {
+        if (!cn_divmod(C, p.G, p, j, r, err))
+            return 0;
+        const long long F = j + 1;
+        return static_cast<uint32_t>(F < p.n ? F : p.n);
+    }
+    cn_divmod(C, 0, p, j, r, err);
+    if (j >= static_cast<long long>(p.n))
+        return p.n;
+    const uint32_t aj = engine_word(sc, static_cast<uint64_t>(j));
+    return static_cast<uint32_t>(j) + (ceil_aq(aj, p.Q) <= r ? 1u : 0u);
+}
+
+// floor(w * 2^shift) for w = exp(lw - M) in (0, 1], by integer operations on
+// the float's bits (no 64-bit conversion instruction)
 __device__ __forceinline__ uint64_t fixed_q(float lw, float M, uint32_t shift)
 {
     if (!(lw > -INFINITY))
         return 0;
-    const float w = __expf(lw - M); // in (0, 1]
-    return __float2ull_rz(ldexpf(fminf(w, 1.0f), static_cast<int>(shift)));
+    const float w = fminf(__expf(lw - M), 1.0f);
+    const uint32_t bits = __float_as_uint(w);
+    const int e = static_cast<int>(bits >> 23); // biased exponent
+    if (e == 0)
+        return 0; // below 2^-126: floor(w 2^shift) == 0 for shift <= 63
+    const uint64_t mant = (bits & 0x7FFFFFu) | 0x800000u;
+    const int sh = e - 150 + static_cast<int>(shift); // w = mant * 2^(e-150)
+    if (sh >= 0)
+        return mant << sh;
+    if (sh <= -64)
+        return 0;
+    return mant >> (-sh);
 }
 
 // ------------------------------------------------------------ fused step
 
 // Per-particle body of the fused kernel.  First: draw the prior at t = 0.
+// x..vy hold the particle as read (after any resampling gather) on entry and
+// the moved particle on exit.
 template <bool First>
 __device__ __forceinline__ void step_one(const Pf32Args &a, uint32_t i,
     uint32_t t, float ox, float oy, int resampled, float Mprev, float &x,
@@ -220,11 +270,70 @@ __device__ __forceinline__ void step_one(const Pf32Args &a, uint32_t i,
     lse_push(lw, m, s, s2);
 }
 
+__device__ __forceinline__ float4 ld4(const float *p, uint32_t i)
+{
+    return __ldcs(reinterpret_cast<const float4 *>(p + i));
+}
+
+__device__ __forceinline__ void st4(float *p, uint32_t i, float4 v)
+{
+    __stcs(reinterpret_cast<float4 *>(p + i), v);
+}
+
+// source slot of slot i after a resample: idx[i] >= 0 is the slot itself
+// (a parent), idx[i] = -(e + 1) is the e-th empty slot, filled from srcs[e]
+__device__ __forceinline__ uint32_t source_of(
+    const int32_t *idx, const uint32_t *srcs, int32_t v)
+{
+    return v >= 0 ? static_cast<uint32_t>(v) : __ldcg(srcs + (-v - 1));
+    (void)idx;
+}
+
+// Reads the state of particles i0..i0+3 (gathered through idx after a
+// resample).
+__device__ __forceinline__ void load_group(const Pf32Args &a, uint32_t i0,
+    bool gather, float4 &X, float4 &Y, float4 &VX, float4 &VY)
+{
+    if (gather) {
+        const int4 I = __ldcs(reinterpret_cast<const int4 *>(a.idx + i0));
+        const int b = static_cast<int>(i0);
+        if (I.x == b && I.y == b + 1 && I.z == b + 2 && I.w == b + 3) {
+            X = ld4(a.ax, i0);
+            Y = ld4(a.ay, i0);
+            VX = ld4(a.avx, i0);
+            VY = ld4(a.avy, i0);
+        } else {
+            uint32_t s0 = source_of(a.idx, a.srcs, I.x);
+            uint32_t s1 = source_of(a.idx, a.srcs, I.y);
+            uint32_t s2 = source_of(a.idx, a.srcs, I.z);
+            uint32_t s3 = source_of(a.idx, a.srcs, I.w);
+            if (max(max(s0, s1), max(s2, s3)) >= a.n) {
+                // an index outside the particles: record it, read slot 0
+                atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+                s0 = s0 < a.n ? s0 : 0;
+                s1 = s1 < a.n ? s1 : 0;
+                s2 = s2 < a.n ? s2 : 0;
+                s3 = s3 < a.n ? s3 : 0;
+            }
+            X = make_float4(a.ax[s0], a.ax[s1], a.ax[s2], a.ax[s3]);
+            Y = make_float4(a.ay[s0], a.ay[s1], a.ay[s2], a.ay[s3]);
+            VX = make_float4(a.avx[s0], a.avx[s1], a.avx[s2], a.avx[s3]);
+            VY = make_float4(a.avy[s0], a.avy[s1], a.avy[s2], a.avy[s3]);
+        }
+    } else {
+        X = ld4(a.ax, i0);
+        Y = ld4(a.ay, i0);
+        VX = ld4(a.avx, i0);
+        VY = ld4(a.avy, i0);
+    }
+}
+
 template <bool First>
 __global__ void __launch_bounds__(kPfBlock) k_pf32_step(const Pf32Args a)
 {
     const uint32_t t = a.sc->step;
     const int resampled = First ? 1 : a.sc->resampled;
+    const bool gather = First ? false : (a.sc->gather != 0);
     const float Mprev = First ? 0.0f : static_cast<float>(a.sc->M);
     // steps past the capacity (profiling loops) reuse the last observation
     // and record nothing
@@ -240,14 +349,8 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_step(const Pf32Args a)
         if (i0 + 3 < n) {
             float4 X, Y, VX, VY, LW;
             if (!First) {
-                X = __ldcs(reinterpret_cast<const float4 *>(a.x + i0));
-                Y = __ldcs(reinterpret_cast<const float4 *>(a.y + i0));
-                VX = __ldcs(reinterpret_cast<const float4 *>(a.vx + i0));
-                VY = __ldcs(reinterpret_cast<const float4 *>(a.vy + i0));
-                if (!resampled)
-                    LW = __ldcs(reinterpret_cast<const float4 *>(a.lw + i0));
-                else
-                    LW = make_float4(0, 0, 0, 0);
+                load_group(a, i0, gather, X, Y, VX, VY);
+                LW = resampled ? make_float4(0, 0, 0, 0) : ld4(a.lw, i0);
             }
             step_one<First>(a, i0 + 0, t, ox, oy, resampled, Mprev, X.x, Y.x,
                 VX.x, VY.x, LW.x, m, s, s2, sx, sy, sw);
@@ -257,63 +360,77 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_step(const Pf32Args a)
                 VX.z, VY.z, LW.z, m, s, s2, sx, sy, sw);
             step_one<First>(a, i0 + 3, t, ox, oy, resampled, Mprev, X.w, Y.w,
                 VX.w, VY.w, LW.w, m, s, s2, sx, sy, sw);
-            __stcs(reinterpret_cast<float4 *>(a.x + i0), X);
-            __stcs(reinterpret_cast<float4 *>(a.y + i0), Y);
-            __stcs(reinterpret_cast<float4 *>(a.vx + i0), VX);
-            __stcs(reinterpret_cast<float4 *>(a.vy + i0), VY);
-            __stcs(reinterpret_cast<float4 *>(a.lw + i0), LW);
+            st4(a.bx, i0, X);
+            st4(a.by, i0, Y);
+            st4(a.bvx, i0, VX);
+            st4(a.bvy, i0, VY);
+            st4(a.lw, i0, LW);
         } else {
             for (uint32_t i = i0; i < n && i < i0 + 4; ++i) {
                 float X = 0, Y = 0, VX = 0, VY = 0, LW = 0;
                 if (!First) {
-                    X = a.x[i];
-                    Y = a.y[i];
-                    VX = a.vx[i];
-                    VY = a.vy[i];
+                    uint32_t src =
+                        gather ? source_of(a.idx, a.srcs, a.idx[i]) : i;
+                    if (src >= a.n) {
+                        atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+                        src = 0;
+                    }
+                    X = a.ax[src];
+                    Y = a.ay[src];
+                    VX = a.avx[src];
+                    VY = a.avy[src];
                     LW = resampled ? 0.0f : a.lw[i];
                 }
                 step_one<First>(a, i, t, ox, oy, resampled, Mprev, X, Y, VX,
                     VY, LW, m, s, s2, sx, sy, sw);
-                a.x[i] = X;
-                a.y[i] = Y;
-                a.vx[i] = VX;
-                a.vy[i] = VY;
+                a.bx[i] = X;
+                a.by[i] = Y;
+                a.bvx[i] = VX;
+                a.bvy[i] = VY;
                 a.lw[i] = LW;
             }
         }
     }
 
-    // ---- block reduction: FP32 per thread, FP64 across warps
-    double dm = m, ds = s, ds2 = s2, dsx = sx, dsy = sy, dsw = sw;
+    // ---- warp level in FP32
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        const double om = __shfl_xor_sync(0xFFFFFFFFu, dm, d);
-        const double os = __shfl_xor_sync(0xFFFFFFFFu, ds, d);
-        const double os2 = __shfl_xor_sync(0xFFFFFFFFu, ds2, d);
-        lse_merge(dm, ds, ds2, om, os, os2);
-        dsx += __shfl_xor_sync(0xFFFFFFFFu, dsx, d);
-        dsy += __shfl_xor_sync(0xFFFFFFFFu, dsy, d);
-        dsw += __shfl_xor_sync(0xFFFFFFFFu, dsw, d);
+        const float om = __shfl_xor_sync(0xFFFFFFFFu, m, d);
+        const float os = __shfl_xor_sync(0xFFFFFFFFu, s, d);
+        const float os2 = __shfl_xor_sync(0xFFFFFFFFu, s2, d);
+        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, d);
+        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, d);
+        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, d);
+        lse_merge_f(m, s, s2, om, os, os2);
     }
-    __shared__ double sh[6][kPfBlock / 32];
+    // ---- block and grid level: FP64 accumulation, FP32 rescale factors
+    __shared__ float shm[kPfBlock / 32];
+    __shared__ double sh[5][kPfBlock / 32];
     __shared__ bool is_last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) {
-        sh[0][wid] = dsx;
-        sh[1][wid] = dsy;
-        sh[2][wid] = dsw;
-        sh[3][wid] = dm;
-        sh[4][wid] = ds;
-        sh[5][wid] = ds2;
+        shm[wid] = m;
+        sh[0][wid] = s;
+        sh[1][wid] = s2;
+        sh[2][wid] = sx;
+        sh[3][wid] = sy;
+        sh[4][wid] = sw;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        MovePartial p = {0, 0, 0, -INFINITY, 0, 0};
+        float mb = -INFINITY;
+        for (int w = 0; w < kPfBlock / 32; ++w)
+            mb = fmaxf(mb, shm[w]);
+        MovePartial p = {0, 0, 0, mb, 0, 0};
         for (int w = 0; w < kPfBlock / 32; ++w) {
-            p.sx += sh[0][w];
-            p.sy += sh[1][w];
-            p.sw += sh[2][w];
-            lse_merge(p.m, p.s, p.s2, sh[3][w], sh[4][w], sh[5][w]);
+            p.sx += sh[2][w];
+            p.sy += sh[3][w];
+            p.sw += sh[4][w];
+            if (shm[w] > -INFINITY) {
+                const double f = __expf(shm[w] - mb);
+                p.s += sh[0][w] * f;
+                p.s2 += sh[1][w] * f * f;
+            }
         }
         a.part[blockIdx.x] = p;
         __threadfence();
@@ -323,43 +440,50 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_step(const Pf32Args a)
     if (!is_last)
         return;
 
-    // ---- last block: combine all block records in FP64
+    // ---- last block: combine every block's record
     __threadfence();
-    double M = -INFINITY, S = 0, S2 = 0, SX = 0, SY = 0, SW = 0;
+    float M = -INFINITY;
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+        M = fmaxf(M, static_cast<float>(a.part[b].m));
+    __shared__ float shmax[kPfBlock / 32 + 1];
+    M = block_reduce(M, OpMax(), -INFINITY, shmax);
+    double S = 0, S2 = 0, SX = 0, SY = 0, SW = 0;
     for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
         const MovePartial p = a.part[b];
         SX += p.sx;
         SY += p.sy;
         SW += p.sw;
-        lse_merge(M, S, S2, p.m, p.s, p.s2);
+        if (p.m > -INFINITY) {
+            const double f = __expf(static_cast<float>(p.m) - M);
+            S += p.s * f;
+            S2 += p.s2 * f * f;
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        const double om = __shfl_xor_sync(0xFFFFFFFFu, M, d);
-        const double os = __shfl_xor_sync(0xFFFFFFFFu, S, d);
-        const double os2 = __shfl_xor_sync(0xFFFFFFFFu, S2, d);
-        lse_merge(M, S, S2, om, os, os2);
+        S += __shfl_xor_sync(0xFFFFFFFFu, S, d);
+        S2 += __shfl_xor_sync(0xFFFFFFFFu, S2, d);
         SX += __shfl_xor_sync(0xFFFFFFFFu, SX, d);
         SY += __shfl_xor_sync(0xFFFFFFFFu, SY, d);
         SW += __shfl_xor_sync(0xFFFFFFFFu, SW, d);
     }
     __syncthreads();
     if (lane == 0) {
-        sh[0][wid] = SX;
-        sh[1][wid] = SY;
-        sh[2][wid] = SW;
-        sh[3][wid] = M;
-        sh[4][wid] = S;
-        sh[5][wid] = S2;
+        sh[0][wid] = S;
+        sh[1][wid] = S2;
+        sh[2][wid] = SX;
+        sh[3][wid] = SY;
+        sh[4][wid] = SW;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double M1 = -INFINITY, S1 = 0, S21 = 0, SX1 = 0, SY1 = 0, SW1 = 0;
+        double S1 = 0, S21 = 0, SX1 = 0, SY1 = 0, SW1 = 0;
         for (int w = 0; w < kPfBlock / 32; ++w) {
-            SX1 += sh[0][w];
-            SY1 += sh[1][w];
-            SW1 += sh[2][w];
-            lse_merge(M1, S1, S21, sh[3][w], sh[4][w], sh[5][w]);
+            S1 += sh[0][w];
+            S21 += sh[1][w];
+            SX1 += sh[2][w];
+            SY1 += sh[3][w];
+            SW1 += sh[4][w];
         }
         PfScalars &sc = *a.sc;
         const double prev_mass = First ? static_cast<double>(n) : SW1;
@@ -369,6 +493,7 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_step(const Pf32Args a)
             a.h_mean[2 * (t - 1) + 1] = SY1 / SW1;
         }
         const double ess = S1 * S1 / S21;
+        const double M1 = static_cast<double>(M);
         sc.logz += M1 + log(S1) - log(prev_mass);
         if (!(S1 > 0) || !(ess > 0))
             sc.err |= DEV_ERR_NONFINITE;
@@ -382,6 +507,7 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_step(const Pf32Args a)
         sc.S = S1;
         sc.ess = ess;
         sc.resampled = flag;
+        sc.gather = 0; // every block has read it; a resample sets it again
         sc.step = t + 1;
         sc.done = 0;
     }
@@ -392,13 +518,19 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_final_mean(
     const Pf32Args a, uint32_t t_rec)
 {
     const int resampled = a.sc->resampled;
+    const bool gather = a.sc->gather != 0;
     const float M = static_cast<float>(a.sc->M);
     double sx = 0, sy = 0, sw = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
          i += gridDim.x * blockDim.x) {
+        uint32_t src = gather ? source_of(a.idx, a.srcs, a.idx[i]) : i;
+        if (src >= a.n) {
+            atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+            src = 0;
+        }
         const float w = resampled ? 1.0f : __expf(a.lw[i] - M);
-        sx += w * a.x[i];
-        sy += w * a.y[i];
+        sx += w * a.ax[src];
+        sy += w * a.ay[src];
         sw += w;
     }
     __shared__ double sh[3][kPfBlock / 32];
@@ -444,6 +576,30 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_final_mean(
     a.sc->done = 0;
 }
 
+// B = A gathered through idx (materializes a pending resample)
+__global__ void __launch_bounds__(kPfBlock) k_pf32_materialize(
+    const Pf32Args a)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += gridDim.x * blockDim.x) {
+        uint32_t src = source_of(a.idx, a.srcs, a.idx[i]);
+        if (src >= a.n) {
+            atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+            src = 0;
+        }
+        a.bx[i] = a.ax[src];
+        a.by[i] = a.ay[src];
+        a.bvx[i] = a.avx[src];
+        a.bvy[i] = a.avy[src];
+    }
+}
+
+__global__ void k_pf32_clear_gather(PfScalars *sc)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        sc->gather = 0;
+}
+
 // ------------------------------------------------------------ resampling
 
 __device__ __forceinline__ void chunk_range(
@@ -457,7 +613,14 @@ __device__ __forceinline__ void chunk_range(
         hi = n;
 }
 
-// block sum of q over the block's chunk
+__device__ __forceinline__ uint64_t q_at(
+    const Rs32Args &a, uint32_t i, float M)
+{
+    return a.q ? a.q[i] : fixed_q(a.lw[i], M, a.shift);
+}
+
+// block sum of q over the block's chunk (two groups of four per thread in
+// flight)
 __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
 {
     if (!a.sc->resampled)
@@ -466,8 +629,21 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
     uint32_t lo, hi;
     chunk_range(a.n, a.chunk, lo, hi);
     uint64_t acc = 0;
-    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-        acc += fixed_q(a.lw[i], M, a.shift);
+    for (uint32_t base = lo; base < hi; base += 2 * kPfTile) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t i0 = base + h * kPfTile + threadIdx.x * 4;
+            if (i0 + 3 < hi && a.q == nullptr) {
+                const float4 v =
+                    __ldcg(reinterpret_cast<const float4 *>(a.lw + i0));
+                acc += fixed_q(v.x, M, a.shift) + fixed_q(v.y, M, a.shift) +
+                    fixed_q(v.z, M, a.shift) + fixed_q(v.w, M, a.shift);
+            } else {
+                for (uint32_t i = i0; i < hi && i < i0 + 4; ++i)
+                    acc += q_at(a, i, M);
+            }
+        }
+    }
     __shared__ uint64_t sh[kPfBlock / 32 + 1];
     acc = block_reduce(acc, OpAdd(), uint64_t(0), sh);
     if (threadIdx.x == 0)
@@ -490,20 +666,8 @@ __device__ __forceinline__ void block_prefix_of_parts(
     all = block_reduce(q, OpAdd(), T(0), sh);
 }
 
-struct StratA {
-    const PfScalars *sc;
-    __device__ uint64_t operator()(long long j) const
-    {
-        return engine_word(*sc, static_cast<uint64_t>(j));
-    }
-};
-
-struct SystA {
-    uint64_t a0;
-    __device__ uint64_t operator()(long long) const { return a0; }
-};
-
-// Replication counts from the fixed-point CDF; per-block empty counts.
+// Replication counts from the fixed-point CDF; per-block empty and copy
+// counts.
 __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
 {
     if (!a.sc->resampled)
@@ -513,52 +677,86 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     chunk_range(a.n, a.chunk, lo, hi);
     __shared__ uint64_t shq[kPfBlock / 32 + 1];
     __shared__ uint32_t she[kPfBlock / 32 + 1];
+    __shared__ uint32_t lastF[kPfBlock / 32];
+    __shared__ uint32_t carryF;
     uint64_t offset, Q;
     block_prefix_of_parts(a.qpart, blockIdx.x, gridDim.x, offset, Q, shq);
     if (blockIdx.x == 0 && threadIdx.x == 0)
         a.sc->Q = Q;
-    const CountP cp = make_count_params(Q, a.n);
-    const uint64_t a0 = engine_word(*a.sc, 0);
-    StratA strat{a.sc};
-    SystA syst{a0};
+    const PfScalars sc = *a.sc;
+    const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
+    const CountP cp = make_count_params(Q, a.n, engine_word(sc, 0));
     uint32_t err = 0;
+    if (threadIdx.x == 0)
+        carryF = lo == 0 ? 0u : count_F(offset, cp, sys, sc, err);
     uint32_t empties = 0, copies = 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (uint32_t base = lo; base < hi; base += kPfTile) {
         const uint32_t i0 = base + threadIdx.x * 4;
         uint64_t q[4];
+        if (i0 + 3 < hi && a.q == nullptr) {
+            const float4 v = __ldcg(reinterpret_cast<const float4 *>(a.lw + i0));
+            q[0] = fixed_q(v.x, M, a.shift);
+            q[1] = fixed_q(v.y, M, a.shift);
+            q[2] = fixed_q(v.z, M, a.shift);
+            q[3] = fixed_q(v.w, M, a.shift);
+        } else {
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            q[k] = (i0 + k < hi) ? fixed_q(a.lw[i0 + k], M, a.shift) : 0;
+            for (int k = 0; k < 4; ++k)
+                q[k] = (i0 + k < hi) ? q_at(a, i0 + k, M) : 0;
+        }
         const uint64_t tsum = q[0] + q[1] + q[2] + q[3];
         uint64_t tile_total;
         const uint64_t incl =
             block_inclusive_scan(tsum, OpAdd(), uint64_t(0), shq, &tile_total);
-        uint64_t C = offset + incl - tsum; // exclusive prefix of this thread
-        uint32_t Fprev = a.scheme == VSMC_CUDA_STRATIFIED
-            ? count_le(C, cp, strat, err)
-            : count_le(C, cp, syst, err);
-        if (i0 == 0)
-            Fprev = 0;
+        uint64_t C = offset + incl - tsum;
+        uint32_t F[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const uint32_t i = i0 + k;
-            if (i >= hi)
-                break;
             C += q[k];
-            uint32_t F;
-            if (i + 1 == a.n)
-                F = a.n; // the last particle takes the rest
+            const uint32_t i = i0 + k;
+            if (i + 1 >= a.n)
+                F[k] = a.n; // the last particle takes the rest
+            else if (i < hi)
+                F[k] = count_F(C, cp, sys, sc, err);
             else
-                F = a.scheme == VSMC_CUDA_STRATIFIED
-                    ? count_le(C, cp, strat, err)
-                    : count_le(C, cp, syst, err);
-            const int32_t r = static_cast<int32_t>(F - Fprev);
-            a.rep[i] = r;
-            empties += r == 0 ? 1u : 0u;
-            copies += static_cast<uint32_t>(r);
-            Fprev = F;
+                F[k] = 0;
         }
+        // F before this thread's first particle: the previous thread's last
+        uint32_t Fprev = __shfl_up_sync(0xFFFFFFFFu, F[3], 1);
+        if (lane == 31)
+            lastF[wid] = F[3];
+        __syncthreads();
+        if (lane == 0)
+            Fprev = wid == 0 ? carryF : lastF[wid - 1];
+        __syncthreads();
+        int32_t r[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            r[k] = static_cast<int32_t>(F[k] - Fprev);
+            Fprev = F[k];
+        }
+        if (i0 + 3 < hi) {
+            *reinterpret_cast<int4 *>(a.rep + i0) = make_int4(r[0], r[1], r[2], r[3]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                empties += r[k] == 0 ? 1u : 0u;
+                copies += static_cast<uint32_t>(r[k]);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (i0 + k < hi) {
+                    a.rep[i0 + k] = r[k];
+                    empties += r[k] == 0 ? 1u : 0u;
+                    copies += static_cast<uint32_t>(r[k]);
+                }
+        }
+        // the next tile starts after the last particle of this one
+        if (threadIdx.x == blockDim.x - 1)
+            carryF = F[3];
         offset += tile_total;
+        __syncthreads();
     }
     if (err)
         atomicOr(&a.sc->err, err);
@@ -570,10 +768,12 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     }
 }
 
-// Slot assignment: marks[surplus rank of p] = p + 1 for parents with two or
-// more copies, empties[empty rank of d] = d.  With c = copies before slot i
-// and e = empty slots before i, the first surplus rank of i is c - (i - e)
-// (every non-empty slot before i keeps one of its copies).
+// Slot assignment.  With c = copies before slot i and e = empty slots before
+// i, the first surplus rank of i is c - (i - e) (every non-empty slot before
+// i keeps one of its copies).  idx[i] = i for a parent (it keeps its slot),
+// idx[i] = -(e + 1) for the e-th empty slot (its source is srcs[e], filled
+// below); marks[first surplus rank of a parent with two or more copies] =
+// parent + 1.
 __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
 {
     if (!a.sc->resampled)
@@ -588,6 +788,7 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         PfScalars &sc = *a.sc;
         sc.nempty = etotal;
+        sc.gather = 1;
         if (ctotal != a.n)
             sc.err |= DEV_ERR_INTERNAL;
         // words the scheme consumed: U01SequenceSystematic draws once in its
@@ -604,15 +805,24 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
     for (uint32_t base = lo; base < hi; base += kPfTile) {
         const uint32_t i0 = base + threadIdx.x * 4;
         int32_t r[4];
+        if (i0 + 3 < hi) {
+            const int4 v = __ldcg(reinterpret_cast<const int4 *>(a.rep + i0));
+            r[0] = v.x;
+            r[1] = v.y;
+            r[2] = v.z;
+            r[3] = v.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                r[k] = (i0 + k < hi) ? a.rep[i0 + k] : -1;
+        }
         uint32_t tr = 0, te = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            r[k] = (i0 + k < hi) ? a.rep[i0 + k] : -1;
+        for (int k = 0; k < 4; ++k)
             if (r[k] >= 0) {
                 tr += static_cast<uint32_t>(r[k]);
                 te += r[k] == 0 ? 1u : 0u;
             }
-        }
         const uint64_t v = (static_cast<uint64_t>(tr) << 32) | te;
         uint64_t tot;
         const uint64_t incl =
@@ -620,25 +830,34 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         const uint64_t ex = incl - v;
         uint32_t c = coff + static_cast<uint32_t>(ex >> 32);
         uint32_t e = eoff + static_cast<uint32_t>(ex & 0xFFFFFFFFu);
+        int32_t out[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            if (r[k] < 0)
-                break;
             const uint32_t i = i0 + k;
             if (r[k] == 0) {
-                if (e < a.n)
-                    a.empties[e] = i;
-                else
-                    atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+                out[k] = -static_cast<int32_t>(e) - 1;
                 ++e;
-            } else if (r[k] >= 2) {
-                const uint32_t rank = c - (i - e);
-                if (rank < a.n)
-                    a.marks[rank] = i + 1;
-                else
-                    atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+            } else {
+                out[k] = static_cast<int32_t>(i);
+                if (r[k] >= 2) {
+                    const uint32_t rank = c - (i - e);
+                    if (rank < a.n)
+                        a.marks[rank] = i + 1;
+                    else
+                        atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+                }
             }
-            c += static_cast<uint32_t>(r[k]);
+            if (r[k] > 0)
+                c += static_cast<uint32_t>(r[k]);
+        }
+        if (i0 + 3 < hi) {
+            *reinterpret_cast<int4 *>(a.idx + i0) =
+                make_int4(out[0], out[1], out[2], out[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (r[k] >= 0)
+                    a.idx[i0 + k] = out[k];
         }
         coff += static_cast<uint32_t>(tot >> 32);
         eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
@@ -648,7 +867,8 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
 __device__ __forceinline__ void rank_range(
     uint32_t K, uint32_t &lo, uint32_t &hi)
 {
-    const uint32_t per = (K + gridDim.x - 1) / gridDim.x;
+    uint32_t per = (K + gridDim.x - 1) / gridDim.x;
+    per = (per + 3) / 4 * 4;
     lo = blockIdx.x * per;
     hi = lo + per;
     if (lo > K)
@@ -657,7 +877,7 @@ __device__ __forceinline__ void rank_range(
         hi = K;
 }
 
-// per-block max of the marks over the block's share of the K surplus ranks
+// per-block max of the marks over the block's share of the surplus ranks
 __global__ void __launch_bounds__(kPfBlock) k_rs32_markmax(const Rs32Args a)
 {
     if (!a.sc->resampled)
@@ -665,17 +885,21 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_markmax(const Rs32Args a)
     uint32_t lo, hi;
     rank_range(min(a.sc->nempty, a.n), lo, hi);
     uint32_t mx = 0;
-    for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
-        mx = max(mx, a.marks[k]);
+    for (uint32_t k0 = lo + threadIdx.x * 4; k0 < hi; k0 += 4 * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k0 + k < hi)
+                mx = max(mx, __ldcg(a.marks + k0 + k));
+    }
     __shared__ uint32_t sh[kPfBlock / 32 + 1];
     mx = block_reduce(mx, OpMax(), 0u, sh);
     if (threadIdx.x == 0)
         a.mpart[blockIdx.x] = mx;
 }
 
-// Running max of the marks gives the parent of each surplus rank; copy the
-// parent into the empty slot of the same rank, and clear the marks.
-__global__ void __launch_bounds__(kPfBlock) k_rs32_gather(const Rs32Args a)
+// Running max of the marks gives the parent of each surplus rank:
+// srcs[k] = that parent; the marks are cleared for the next resample.
+__global__ void __launch_bounds__(kPfBlock) k_rs32_fill(const Rs32Args a)
 {
     if (!a.sc->resampled)
         return;
@@ -686,28 +910,72 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_gather(const Rs32Args a)
     for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x)
         carry = max(carry, a.mpart[b]);
     carry = block_reduce(carry, OpMax(), 0u, sh);
-    for (uint32_t base = lo; base < hi; base += blockDim.x) {
-        const uint32_t k = base + threadIdx.x;
-        const uint32_t mk = k < hi ? a.marks[k] : 0u;
-        uint32_t tot;
-        uint32_t run = block_inclusive_scan(mk, OpMax(), 0u, sh, &tot);
-        run = max(run, carry);
-        carry = max(carry, tot);
-        if (k < hi) {
-            const uint32_t src = run - 1;
-            const uint32_t dst = a.empties[k];
-            if (run == 0 || src >= a.n || dst >= a.n) {
-                atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
-                continue;
-            }
-            a.x[dst] = a.x[src];
-            a.y[dst] = a.y[src];
-            a.vx[dst] = a.vx[src];
-            a.vy[dst] = a.vy[src];
-            if (mk)
-                a.marks[k] = 0;
+    for (uint32_t base = lo; base < hi; base += 4 * blockDim.x) {
+        const uint32_t k0 = base + threadIdx.x * 4;
+        uint32_t mk[4], run[4];
+        uint32_t tmax = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            mk[k] = k0 + k < hi ? __ldcg(a.marks + k0 + k) : 0u;
+            tmax = max(tmax, mk[k]);
+            run[k] = tmax;
         }
+        uint32_t tot;
+        const uint32_t incl = block_inclusive_scan(tmax, OpMax(), 0u, sh, &tot);
+        uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+        if ((threadIdx.x & 31) == 0)
+            before = 0;
+        // the exclusive max of the block scan is not available per lane 0
+        // from the shuffle; recompute it from the inclusive value
+        __shared__ uint32_t shl[kPfBlock / 32];
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 31)
+            shl[wid] = incl;
+        __syncthreads();
+        if (lane == 0 && wid > 0)
+            before = shl[wid - 1];
+        __syncthreads();
+        before = max(before, carry);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k0 + k < hi) {
+                const uint32_t rk = max(run[k], before);
+                if (rk == 0 || rk - 1 >= a.n)
+                    atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+                else
+                    a.srcs[k0 + k] = rk - 1;
+                if (mk[k])
+                    a.marks[k0 + k] = 0;
+            }
+        }
+        carry = max(carry, tot);
     }
+}
+
+// parent index of every slot from the encoded idx (reference layout)
+__global__ void __launch_bounds__(kPfBlock) k_rs32_decode(
+    const Rs32Args a, int32_t *parent)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += gridDim.x * blockDim.x) {
+        const int32_t v = a.idx[i];
+        parent[i] = v >= 0 ? v : static_cast<int32_t>(a.srcs[-v - 1]);
+    }
+}
+
+__global__ void k_rs32_setup(PfScalars *sc, uint32_t k0, uint32_t k1,
+    uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t index)
+{
+    PfScalars z = {};
+    z.resampled = 1;
+    z.rkey[0] = k0;
+    z.rkey[1] = k1;
+    z.rctr[0] = c0;
+    z.rctr[1] = c1;
+    z.rctr[2] = c2;
+    z.rctr[3] = c3;
+    z.rindex = index;
+    *sc = z;
 }
 
 } // namespace vsmc_cuda

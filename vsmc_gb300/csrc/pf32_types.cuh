@@ -24,7 +24,8 @@ struct PfScalars {
     double ess;
     uint64_t Q;          // fixed-point CDF total of the pending resample
     uint32_t step;       // next step index t
-    int32_t resampled;   // last step resampled: stored lw are stale
+    int32_t resampled;   // last step resampled: weights equal, lw stale
+    int32_t gather;      // state must be read through idx (after a resample)
     uint32_t done;       // completion counter of the fused step
     uint32_t err;        // DEV_ERR_* bits
     uint32_t nempty;     // empty slots of the pending resample
@@ -33,8 +34,14 @@ struct PfScalars {
     uint32_t rctr[4];
 };
 
+// The state lives in two SoA buffers; a step reads one (A) and writes the
+// other (B).  After a resample, A is read through the parent index idx.
 struct Pf32Args {
-    float *x, *y, *vx, *vy, *lw;
+    const float *ax, *ay, *avx, *avy; // state in
+    float *bx, *by, *bvx, *bvy;       // state out
+    float *lw;                        // log-weights (in place)
+    const int32_t *idx;               // parent of each slot after a resample
+    const uint32_t *srcs;             // sources of the empty slots, by rank
     uint32_t n;
     uint32_t seed;
     uint32_t max_steps; // history / observation capacity
@@ -49,7 +56,7 @@ struct Pf32Args {
 
 struct Rs32Args {
     const float *lw;
-    float *x, *y, *vx, *vy;
+    const uint64_t *q; // integer weights given directly (lw unused), or null
     uint32_t n;
     uint32_t shift;  // fixed-point K
     uint32_t chunk;  // particles per block (multiple of kPfTile)
@@ -59,8 +66,9 @@ struct Rs32Args {
     uint32_t *cpart; // per-block copy count (sum of rep)
     uint32_t *mpart; // per-block max of marks
     int32_t *rep;
+    int32_t *idx;      // per slot: itself (>= 0) or -(empty rank + 1)
     uint32_t *marks;   // N entries, zero between resamples
-    uint32_t *empties; // N entries
+    uint32_t *srcs;    // N entries: source of the k-th empty slot
     PfScalars *sc;
 };
 

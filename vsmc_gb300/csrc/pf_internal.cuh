@@ -28,6 +28,8 @@ struct vsmc_cuda_pf {
 
     // device buffers
     void *state = nullptr;  // 4 rows of `stride` (float or double)
+    void *state2 = nullptr; // FP32: second buffer; a step reads one, writes the other
+    int cur = 0;            // FP32: buffer holding the current state (0: state)
     void *weight = nullptr; // FP32: log-weights (float); FP64: W (double)
     double *obs = nullptr;  // max_steps x 2
     double *h_mean = nullptr, *h_ess = nullptr, *h_logz = nullptr;
@@ -43,9 +45,10 @@ struct vsmc_cuda_pf {
     uint64_t *qpart = nullptr;
     uint32_t *epart = nullptr, *cpart = nullptr, *mpart = nullptr;
     int32_t *rep = nullptr;
+    int32_t *idx = nullptr;
     uint32_t *marks = nullptr, *empties = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr}; // by buffer parity
 
     vsmc_cuda::Pf64State *p64 = nullptr;
 };
