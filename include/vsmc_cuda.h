@@ -225,6 +225,25 @@ int vsmc_cuda_resample_residual_systematic(size_t m, size_t n,
 int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
     vsmc_cuda_rng *rng, int *replication, int *index, void *stream);
 
+/* vsmc_cuda_resample_fixed without any allocation, for callers that must not
+ * allocate device memory while they run (inside an allocator or memory-pool
+ * callback, or in a loop that reserved all device memory beforehand).  Same
+ * arguments, results and engine advance as vsmc_cuda_resample_fixed; its
+ * scratch is one fixed array of about 4 MiB in the library's device image.
+ *   - n must be at most VSMC_CUDA_RESAMPLE_FIXED_NOALLOC_MAX_N, otherwise
+ *     VSMC_CUDA_ERR_SIZE is returned before any device work;
+ *   - the first call on each device (that device current) looks up the
+ *     array's address and may load the library's device code: make it
+ *     before any stream capture;
+ *   - all callers on a device share the array, so calls whose work overlaps
+ *     in time (other streams, other host threads) race and give wrong
+ *     results: order them on one stream;
+ *   - synchronizes the stream.
+ * No reference counterpart (the reference allocates nothing on a device). */
+#define VSMC_CUDA_RESAMPLE_FIXED_NOALLOC_MAX_N (1u << 18)
+int vsmc_cuda_resample_fixed_noalloc(size_t n, const uint64_t *q, int scheme,
+    vsmc_cuda_rng *rng, int *replication, int *index, void *stream);
+
 /* In-place particle copy state[d][dst] = state[d][index[dst]] for a SoA
  * state of `dim` rows of n values; safe in place for indices produced by
  * vsmc_cuda_resample_trans_rep_index (every parent keeps its slot).

@@ -114,6 +114,8 @@ PROTOTYPES = {
     "vsmc_cuda_resample_residual_systematic": (
         I32, [SZ, SZ, _RNGP, VP, VP, VP]),
     "vsmc_cuda_resample_fixed": (I32, [SZ, VP, I32, _RNGP, VP, VP, VP]),
+    "vsmc_cuda_resample_fixed_noalloc": (I32, [SZ, VP, I32, _RNGP, VP, VP,
+                                               VP]),
     "vsmc_cuda_state_copy_f32": (I32, [SZ, SZ, VP, VP, VP]),
     "vsmc_cuda_state_copy_f64": (I32, [SZ, SZ, VP, VP, VP]),
     "vsmc_cuda_weight_set": (I32, [SZ, VP, VP, VP, VP]),

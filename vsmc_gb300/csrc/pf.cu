@@ -11,6 +11,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 using namespace vsmc_cuda;
@@ -577,3 +578,152 @@ int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
 }
 
 } // extern "C"
+
+// ------------------------------------------------------------------------
+// Integer-CDF resampling that allocates nothing.
+//
+// vsmc_cuda_resample_fixed takes its scratch (partial sums, replication
+// counts, slot marks, empty-slot sources, engine scalars) from
+// cudaMallocAsync on every call.  Some callers cannot allocate at call time:
+// code that runs inside a memory-pool or allocator callback (allocating
+// there re-enters the allocator), loops that have reserved all device memory
+// up front or must keep allocator calls out of a latency budget, and hosts
+// whose allocator is locked while they run.  The variant below takes the same
+// scratch from one fixed array in the library's device image instead.
+//
+// Limits and rules for its users:
+//   * n <= VSMC_CUDA_RESAMPLE_FIXED_NOALLOC_MAX_N (2^18 particles); larger n
+//     is rejected with VSMC_CUDA_ERR_SIZE before any device work.  The array
+//     is about 4 MiB, present on every device the library is loaded on.
+//   * The first call on each device (with that device current) looks up the
+//     array's address with cudaGetSymbolAddress, which may load the
+//     library's device code; make that first call before any stream capture.
+//   * The array is shared by all callers on a device: two calls whose work
+//     overlaps in time (different streams, or different host threads) race
+//     on it and give wrong results.  Order them on one stream.
+//   * The slot marks must be zero when counting starts; each call clears them
+//     with cudaMemsetAsync on its stream (no allocation).  Everything else
+//     in the array is fully written before it is read.
+namespace vsmc_cuda
+{
+
+constexpr size_t kNoAllocMaxN = VSMC_CUDA_RESAMPLE_FIXED_NOALLOC_MAX_N;
+// chunk >= kPfTile particles per block, so at most this many blocks
+constexpr size_t kNoAllocMaxBlocks = (kNoAllocMaxN + kPfTile - 1) / kPfTile;
+
+constexpr size_t na_align(size_t b) { return (b + 255) / 256 * 256; }
+
+// byte offsets of the pieces inside the array, each on a 256-byte boundary
+constexpr size_t kNaSc = 0;
+constexpr size_t kNaQpart = kNaSc + na_align(sizeof(PfScalars));
+constexpr size_t kNaEpart =
+    kNaQpart + na_align(sizeof(uint64_t) * kNoAllocMaxBlocks);
+constexpr size_t kNaCpart =
+    kNaEpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
+constexpr size_t kNaMpart =
+    kNaCpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
+constexpr size_t kNaRep =
+    kNaMpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
+constexpr size_t kNaIdx = kNaRep + na_align(sizeof(int32_t) * (kNoAllocMaxN + 4));
+constexpr size_t kNaMarks =
+    kNaIdx + na_align(sizeof(int32_t) * (kNoAllocMaxN + 4));
+constexpr size_t kNaSrcs = kNaMarks + na_align(sizeof(uint32_t) * kNoAllocMaxN);
+constexpr size_t kNaBytes = kNaSrcs + na_align(sizeof(uint32_t) * kNoAllocMaxN);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+static std::mutex g_noalloc_mutex;
+static unsigned char *g_noalloc_ptr[kNaMaxDevices] = {};
+
+// Address of the array on the current device (looked up once per device).
+static int noalloc_scratch(unsigned char **out)
+{
+    int dev = -1;
+    VSMC_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNaMaxDevices)
+        return VSMC_CUDA_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_last_cuda_error(e);
+            return VSMC_CUDA_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return VSMC_CUDA_OK;
+}
+
+} // namespace vsmc_cuda
+
+extern "C" int vsmc_cuda_resample_fixed_noalloc(size_t n, const uint64_t *q,
+    int scheme, vsmc_cuda_rng *rng, int *replication, int *index,
+    void *stream)
+{
+    if (q == nullptr || reinterpret_cast<uintptr_t>(q) % alignof(uint64_t) ||
+        rng == nullptr || rng->kind != VSMC_CUDA_PHILOX4X32 ||
+        rng->index < 1 || rng->index > 4 ||
+        (scheme != VSMC_CUDA_STRATIFIED && scheme != VSMC_CUDA_SYSTEMATIC))
+        return VSMC_CUDA_ERR_ARG;
+    if (n < 2 || n > kNoAllocMaxN)
+        return VSMC_CUDA_ERR_SIZE;
+    unsigned char *base = nullptr;
+    const int rc = noalloc_scratch(&base);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    cudaStream_t st = as_stream(stream);
+    const size_t grs0 = static_cast<size_t>(num_sms()) * 4;
+    size_t chunk = (n + grs0 - 1) / grs0;
+    chunk = (chunk + kPfTile - 1) / kPfTile * kPfTile;
+    const size_t grid = (n + chunk - 1) / chunk;
+    if (grid > kNoAllocMaxBlocks)
+        return VSMC_CUDA_ERR_INTERNAL;
+    Rs32Args r = {};
+    r.q = q;
+    r.n = static_cast<uint32_t>(n);
+    r.chunk = static_cast<uint32_t>(chunk);
+    r.scheme = scheme;
+    r.sc = reinterpret_cast<PfScalars *>(base + kNaSc);
+    r.qpart = reinterpret_cast<uint64_t *>(base + kNaQpart);
+    r.epart = reinterpret_cast<uint32_t *>(base + kNaEpart);
+    r.cpart = reinterpret_cast<uint32_t *>(base + kNaCpart);
+    r.mpart = reinterpret_cast<uint32_t *>(base + kNaMpart);
+    r.rep = reinterpret_cast<int32_t *>(base + kNaRep);
+    r.idx = reinterpret_cast<int32_t *>(base + kNaIdx);
+    r.marks = reinterpret_cast<uint32_t *>(base + kNaMarks);
+    r.srcs = reinterpret_cast<uint32_t *>(base + kNaSrcs);
+    VSMC_CUDA_TRY(cudaMemsetAsync(r.marks, 0, sizeof(uint32_t) * n, st));
+    k_rs32_setup<<<1, 1, 0, st>>>(r.sc, static_cast<uint32_t>(rng->key[0]),
+        static_cast<uint32_t>(rng->key[1]), static_cast<uint32_t>(rng->ctr[0]),
+        static_cast<uint32_t>(rng->ctr[1]), static_cast<uint32_t>(rng->ctr[2]),
+        static_cast<uint32_t>(rng->ctr[3]), rng->index);
+    const int g = static_cast<int>(grid);
+    k_rs32_qsum<<<g, kPfBlock, 0, st>>>(r);
+    k_rs32_count<<<g, kPfBlock, 0, st>>>(r);
+    k_rs32_assign<<<g, kPfBlock, 0, st>>>(r);
+    k_rs32_markmax<<<g, kPfBlock, 0, st>>>(r);
+    k_rs32_fill<<<g, kPfBlock, 0, st>>>(r);
+    VSMC_CUDA_CHECK_LAUNCH();
+    if (index)
+        k_rs32_decode<<<grid_for(n, kPfBlock, 4, 8), kPfBlock, 0, st>>>(
+            r, index);
+    if (replication)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(replication, r.rep, sizeof(int) * n,
+            cudaMemcpyDeviceToDevice, st));
+    VSMC_CUDA_CHECK_LAUNCH();
+    PfScalars sc;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(
+        &sc, r.sc, sizeof(sc), cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (sc.err & DEV_ERR_NONFINITE)
+        return VSMC_CUDA_ERR_NONFINITE;
+    if (sc.err)
+        return VSMC_CUDA_ERR_INTERNAL;
+    for (int i = 0; i < 4; ++i)
+        rng->ctr[i] = sc.rctr[i];
+    rng->index = sc.rindex;
+    return VSMC_CUDA_OK;
+}
