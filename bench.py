@@ -225,6 +225,163 @@ def run_reference(args):
     return 0
 
 
+def batched_spec(nf, seed):
+    """Batched-filter workload: per filter acceleration sd ~ U(0.5, 2),
+    observation scale ~ U(0.2, 1), particles log-uniform in [2^8, 2^16],
+    horizon uniform in [50, 500]; seeded."""
+    import vsmc_gb300 as vc
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(2.0 ** 8), np.log(2.0 ** 16), nf))
+    n = np.minimum(np.round(n), 2 ** 16).astype(np.uint32)
+    T = rng.integers(50, 501, nf).astype(np.uint32)
+    models = []
+    for _ in range(nf):
+        m = vc.default_model()
+        m.sigma_a = float(rng.uniform(0.5, 2.0))
+        m.obs_scale = float(rng.uniform(0.2, 1.0))
+        models.append(m)
+    return n, T, models
+
+
+def run_batched(args):
+    """4096 independent filters stepped together (one persistent step kernel
+    and one per-filter resampling kernel per step, the run as one graph)."""
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import vsmc_gb300 as vc
+    vc.lib()
+    nf = args.filters
+    n, T, models = batched_spec(nf, 20261203 + rank)
+    seeds = (np.arange(nf) + (rank << 20)).astype(np.uint32)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    b = vc.FilterBatch(n, T, seeds, models, scheme=vc.STRATIFIED,
+                       stream=ctypes.c_void_p(stream.cuda_stream))
+    obs = torch.zeros(2 * b.total_steps, dtype=torch.float64, device="cuda")
+    b.simulate(obs.data_ptr())
+    tune_ms = b.autotune(obs.data_ptr(), steps=args.tune_steps)
+    shape = b.shape()
+    for _ in range(args.warmup):
+        b.run_device(obs.data_ptr())
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.run_device(obs.data_ptr())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    hist = b.history()
+    # end to end: pinned host observations in, histories out, every run
+    TT = b.total_steps
+    obs_h = torch.empty(2 * TT, dtype=torch.float64, pin_memory=True)
+    obs_h.copy_(obs.cpu())
+    mean_h = torch.empty(2 * TT, dtype=torch.float64, pin_memory=True)
+    ess_h = torch.empty(TT, dtype=torch.float64, pin_memory=True)
+    res_h = torch.empty(TT, dtype=torch.int32, pin_memory=True)
+    logz_h = torch.empty(TT, dtype=torch.float64, pin_memory=True)
+    L = vc.lib()
+
+    def e2e_run():
+        vc.check(L.vsmc_cuda_batch_run(b.handle, obs_h.data_ptr(),
+                                       mean_h.data_ptr(), ess_h.data_ptr(),
+                                       res_h.data_ptr(), logz_h.data_ptr()),
+                 "vsmc_cuda_batch_run")
+
+    e2e_run()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(2, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_run()
+    e2e_s = time.perf_counter() - t0
+    clocks.stop()
+    psteps = float(b.particle_steps())
+    b.close()
+    ms_max = max_over_ranks(ms, world)
+    e2e_max = max_over_ranks(e2e_s, world)
+    value = aggregate_rate(psteps * args.steps, world, ms_max / 1000.0)
+    peak, peak_kind = measured_peaks()
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import binding
+        port = binding.port()
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        obs_np = obs_h.numpy().reshape(-1, 2)
+        offs = np.concatenate([[0], np.cumsum(T.astype(np.int64))])
+        done = 0.0
+        t0 = time.perf_counter()
+        k = 0
+        while k < nf and time.perf_counter() - t0 < 10.0:
+            Tk = int(T[k])
+            om = binding.default_model()
+            om.sigma_a = models[k].sigma_a
+            om.obs_scale = models[k].obs_scale
+            o = np.ascontiguousarray(obs_np[offs[k]:offs[k + 1]])
+            z = np.zeros(2 * Tk)
+            e = np.zeros(Tk)
+            r = np.zeros(Tk, np.int32)
+            lz = np.zeros(Tk)
+            port.vo_pf_run(32, int(n[k]), Tk, int(seeds[k]), 1, 0.5,
+                           ctypes.byref(om), P(o), 0, P(z), P(e), P(r), P(lz))
+            done += float(n[k]) * Tk
+            k += 1
+        dt = time.perf_counter() - t0
+        cpu = {"value": done / dt, "unit": UNIT,
+               "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"the first {k} filters of the batch, one after "
+                         "another, oracle restatement (OpenMP move)"}
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/sec (batched bootstrap filters)",
+            "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (each filter's observations simulated from "
+                    "its own model on the device)",
+            "config": {"workload": f"{nf} batched filters: particles "
+                                   "log-uniform [2^8, 2^16], horizons "
+                                   "U[50, 500], sigma_a U(0.5, 2), obs scale "
+                                   "U(0.2, 1), stratified, ESS < N/2",
+                       "particle_steps_per_run": psteps,
+                       "shape_ppt_block": list(shape),
+                       "autotune_ms": [float(x) for x in tune_ms],
+                       "resampled_fraction": float(np.mean(
+                           [h["resampled"].mean() for h in hist])),
+                       "l2": "state 2 x 4 x 4 B x sum N >> L2; no flush"},
+            "e2e": {"value": aggregate_rate(psteps * e2e_steps, world,
+                                            e2e_max),
+                    "unit": UNIT, "h2d_bytes_per_step": 16 * TT,
+                    "d2h_bytes_per_step": (16 + 8 + 4 + 8) * TT},
+            "roofline": {"bound": "hbm",
+                         "achieved": BYTES_PER_PARTICLE_STEP * psteps /
+                         (ms_max / args.steps / 1000.0) / 1e9,
+                         "peak": peak, "unit": "GB/s",
+                         "peak_source": peak_kind,
+                         "scope": "whole run (step + resampling kernels), "
+                                  "40 B per particle-step"},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": (1 + 2 * (int(T.max()) + 1)) * args.steps,
+        }
+        line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -234,10 +391,16 @@ def main():
     ap.add_argument("--n", type=int, default=N_PARTICLES)
     ap.add_argument("--T", type=int, default=T_STEPS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "batched"])
+    ap.add_argument("--filters", type=int, default=4096)
+    ap.add_argument("--tune-steps", type=int, default=60)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     args.warmup = max(args.warmup, 3)
+    if args.workload == "batched":
+        return run_batched(args)
 
     import torch
     rank, world, local = dist_setup(args.gpus)

@@ -70,3 +70,25 @@ def test_host_side_status_and_engine_setup(libpath):
     bad = vc.CvModel(0.1, 1.0, -0.5, 10.0, 2.0, 1.0)
     assert vc.lib().vsmc_cuda_pf_create(ctypes.byref(h), 10, 32, 2, 0.5, 0,
                                         ctypes.byref(bad), 10, None) == vc.ERR_ARG
+
+
+def test_batch_create_validates_before_device_work():
+    import ctypes
+    import numpy as np
+    import vsmc_gb300 as vc
+    L = vc.lib()
+    h = ctypes.c_void_p()
+    m = (vc.CvModel * 2)(vc.default_model(), vc.default_model())
+    T = np.array([5, 5], np.uint32)
+    seeds = np.array([1, 2], np.uint32)
+    bad_n = np.array([1, 10], np.uint32)
+    assert L.vsmc_cuda_batch_create(ctypes.byref(h), 2, bad_n.ctypes.data,
+                                    T.ctypes.data, m, seeds.ctypes.data, 1,
+                                    0.5, None) == vc.ERR_SIZE
+    n = np.array([10, 10], np.uint32)
+    assert L.vsmc_cuda_batch_create(ctypes.byref(h), 2, n.ctypes.data,
+                                    T.ctypes.data, m, seeds.ctypes.data, 0,
+                                    0.5, None) == vc.ERR_ARG
+    assert L.vsmc_cuda_batch_create(ctypes.byref(h), 0, n.ctypes.data,
+                                    T.ctypes.data, m, seeds.ctypes.data, 1,
+                                    0.5, None) == vc.ERR_SIZE

@@ -136,6 +136,18 @@ PROTOTYPES = {
     "vsmc_cuda_pf_stream": (I32, [VP, ctypes.POINTER(VP)]),
     "vsmc_cuda_pf_use_graph": (I32, [VP, I32]),
     "vsmc_cuda_pf_launch_step_kernel": (I32, [VP]),
+    "vsmc_cuda_batch_create": (
+        I32, [ctypes.POINTER(VP), SZ, VP, VP, VP, VP, I32, F64, VP]),
+    "vsmc_cuda_batch_destroy": (I32, [VP]),
+    "vsmc_cuda_batch_stream": (I32, [VP, ctypes.POINTER(VP)]),
+    "vsmc_cuda_batch_simulate": (I32, [VP, VP, VP]),
+    "vsmc_cuda_batch_run_device": (I32, [VP, VP]),
+    "vsmc_cuda_batch_run": (I32, [VP, VP, VP, VP, VP, VP]),
+    "vsmc_cuda_batch_history": (I32, [VP, VP, VP, VP, VP]),
+    "vsmc_cuda_batch_set_shape": (I32, [VP, I32, I32]),
+    "vsmc_cuda_batch_get_shape": (I32, [VP, ctypes.POINTER(I32),
+                                        ctypes.POINTER(I32)]),
+    "vsmc_cuda_batch_autotune": (I32, [VP, VP, I32, VP]),
     "vsmc_cuda_cv_move_f64": (I32, [SZ, SZ, U32, _MODELP, VP, VP, VP, VP]),
     "vsmc_cuda_cv_move_f32": (I32, [SZ, SZ, U32, _MODELP, VP, VP, VP, VP]),
     "vsmc_cuda_cv_simulate": (I32, [U32, SZ, _MODELP, VP, VP, VP]),
@@ -205,6 +217,110 @@ def rng(kind=PHILOX4X32, seed=0, key=None, ctr=None):
         c = (U64 * 4)(*[int(v) for v in ctr] + [0] * (4 - len(ctr)))
         call("vsmc_cuda_rng_set_ctr", ctypes.byref(r), len(ctr), c)
     return r
+
+
+class FilterBatch:
+    """Independent FP32 bootstrap filters stepped together
+    (vsmc_cuda_batch): n, T, seeds are sequences, models a sequence of
+    CvModel (default: the default model for every filter)."""
+
+    def __init__(self, n, T, seeds, models=None, scheme=STRATIFIED,
+                 threshold=0.5, stream=None):
+        import numpy as np
+        self.n = np.ascontiguousarray(n, dtype=np.uint32)
+        self.T = np.ascontiguousarray(T, dtype=np.uint32)
+        self.seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        nf = len(self.n)
+        if models is None:
+            models = [default_model() for _ in range(nf)]
+        self.models = (CvModel * nf)(*models)
+        self.offsets = np.concatenate([[0], np.cumsum(self.T.astype(np.int64))])
+        h = VP()
+        call("vsmc_cuda_batch_create", ctypes.byref(h), nf,
+             self.n.ctypes.data, self.T.ctypes.data, self.models,
+             self.seeds.ctypes.data, scheme, threshold, stream)
+        self.handle = h
+
+    @property
+    def total_steps(self):
+        return int(self.offsets[-1])
+
+    def particle_steps(self):
+        """Sum over the filters of particles x horizon."""
+        return int(sum(int(a) * int(b) for a, b in zip(self.n, self.T)))
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            lib().vsmc_cuda_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stream(self):
+        s = VP()
+        call("vsmc_cuda_batch_stream", self.handle, ctypes.byref(s))
+        return s.value
+
+    def simulate(self, obs_dev_ptr, truth_dev_ptr=None):
+        call("vsmc_cuda_batch_simulate", self.handle, truth_dev_ptr,
+             obs_dev_ptr)
+
+    def run_device(self, obs_dev_ptr):
+        call("vsmc_cuda_batch_run_device", self.handle, obs_dev_ptr)
+
+    def _split(self, mean, ess, res, logz):
+        out = []
+        for f in range(len(self.n)):
+            a, b = int(self.offsets[f]), int(self.offsets[f + 1])
+            out.append({"mean": mean[a:b], "ess": ess[a:b],
+                        "resampled": res[a:b], "logz": logz[a:b]})
+        return out
+
+    def history(self):
+        """Per-filter histories of the last run (list of dicts)."""
+        import numpy as np
+        TT = self.total_steps
+        mean = np.zeros((TT, 2))
+        ess = np.zeros(TT)
+        res = np.zeros(TT, dtype=np.int32)
+        logz = np.zeros(TT)
+        call("vsmc_cuda_batch_history", self.handle, mean.ctypes.data,
+             ess.ctypes.data, res.ctypes.data, logz.ctypes.data)
+        return self._split(mean, ess, res, logz)
+
+    def run(self, obs):
+        """Whole run through host buffers; obs is (sum T, 2) float64."""
+        import numpy as np
+        obs = np.ascontiguousarray(obs, dtype=np.float64)
+        TT = self.total_steps
+        mean = np.zeros((TT, 2))
+        ess = np.zeros(TT)
+        res = np.zeros(TT, dtype=np.int32)
+        logz = np.zeros(TT)
+        call("vsmc_cuda_batch_run", self.handle, obs.ctypes.data,
+             mean.ctypes.data, ess.ctypes.data, res.ctypes.data,
+             logz.ctypes.data)
+        return self._split(mean, ess, res, logz)
+
+    def set_shape(self, ppt, block):
+        call("vsmc_cuda_batch_set_shape", self.handle, ppt, block)
+
+    def shape(self):
+        p, b = I32(), I32()
+        call("vsmc_cuda_batch_get_shape", self.handle, ctypes.byref(p),
+             ctypes.byref(b))
+        return p.value, b.value
+
+    def autotune(self, obs_dev_ptr, steps=50):
+        import numpy as np
+        ms = np.zeros(6, dtype=np.float32)
+        call("vsmc_cuda_batch_autotune", self.handle, obs_dev_ptr, steps,
+             ms.ctypes.data)
+        return ms
 
 
 class ParticleFilter:

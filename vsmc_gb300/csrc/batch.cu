@@ -1,0 +1,1205 @@
+// Batched FP32 bootstrap filters.
+//
+// Thousands of independent filters, each with its own particle count,
+// horizon, model constants and seed, advance together: per global step one
+// persistent kernel moves, weights and reduces the particles of every filter
+// still running, and one kernel resamples, one block per filter, the filters
+// whose ESS fell below the threshold.  A whole run (every step of the longest
+// horizon) is one CUDA graph.
+//
+// Filter f behaves exactly as a single precision-32 filter (pf.cu) with seed
+// seeds[f]: the same particle streams (Philox4x32 key {step, seed}, counter
+// {0, particle, 0, 0}), the same FP32 move / likelihood / log-weight
+// arithmetic, the same resampling engine (key {0, seed}, counter {0, 0, 1, 0})
+// and the same exact fixed-point counting, so its particles, counts and
+// resampling decisions match; only the order of the FP64 block sums differs.
+//
+// Layout.  Filters are stored by horizon, longest first, so the filters still
+// running at step t are a prefix and so are their tiles (a tile is
+// kBlock * kPPT consecutive particles of one filter).  Particle arrays are the
+// filters' segments concatenated, each starting on a multiple of 4 elements.
+// Resampling indices are local to the filter's segment.
+//
+// The step and tile shapes (threads per block, particles per thread) are
+// chosen by vsmc_cuda_batch_autotune from timed runs of the actual batch.
+//
+// No reference counterpart: the reference would run one Sampler<T> per
+// filter (core/sampler.hpp:107-114) with the pf example's move
+// (example/pf/include/pf.hpp:154-170).
+#include "cv_sim.cuh"
+#include "pf32_dev.cuh"
+#include "pf_model.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+using namespace vsmc_cuda;
+
+namespace vsmc_cuda
+{
+
+// Static description of one filter (internal order).
+struct BFilter {
+    uint32_t n;        // particles
+    uint32_t off;      // first particle in the concatenated arrays
+    uint32_t tile0;    // first tile of the step kernel
+    uint32_t ntiles;   // tiles of the step kernel
+    uint32_t T;        // horizon: steps 0..T-1, step T records the last mean
+    uint32_t obs_off;  // first observation pair (caller's filter order)
+    uint32_t hist_off; // first history entry (caller's filter order)
+    uint32_t seed;
+    uint32_t shift;    // fixed-point K = 63 - ceil(log2 n)
+    uint32_t pad;
+    CvConst<float> c;
+};
+
+struct BatchArgs {
+    const BFilter *flt;
+    PfScalars *st;               // dynamic state, one per filter
+    const uint32_t *tile_filter; // filter of each tile
+    const uint32_t *active;      // [tmax + 1] tiles of the filters with T >= t
+    const uint32_t *res_order;   // filters by particle count, largest first
+    const float *ax, *ay, *avx, *avy; // state in
+    float *bx, *by, *bvx, *bvy;       // state out
+    float *lw;
+    int32_t *rep, *idx;
+    uint32_t *marks, *srcs;
+    MovePartial *part; // per tile
+    const double *obs;
+    double *h_mean, *h_ess, *h_logz;
+    int *h_res;
+    uint32_t *step; // global step counter
+    uint32_t nfilters, tmax;
+    int scheme;
+    double threshold;
+};
+
+// The FP32 per-particle body of the single filter (step_one in pf32.cuh),
+// with the filter's constants and seed.
+template <bool First>
+__device__ __forceinline__ void batch_one(const CvConst<float> &c,
+    uint32_t seed, uint32_t i, uint32_t t, float ox, float oy, int resampled,
+    float Mprev, float &x, float &y, float &vx, float &vy, float &lw, float &m,
+    float &s, float &s2, float &sx, float &sy, float &sw)
+{
+    const u32x4 w = particle_block(t, seed, i);
+    float lw_old = 0.0f;
+    if (First) {
+        float z1, z2, z3, z4;
+        normal_pair_f(w.x, w.y, z1, z2);
+        normal_pair_f(w.z, w.w, z3, z4);
+        x = c.sd_pos0 * z1;
+        y = c.sd_pos0 * z2;
+        vx = c.sd_vel0 * z3;
+        vy = c.sd_vel0 * z4;
+    } else {
+        lw_old = resampled ? 0.0f : lw - Mprev;
+        const float wo = resampled ? 1.0f : __expf(lw_old);
+        sx += wo * x;
+        sy += wo * y;
+        sw += wo;
+        float z1, z2;
+        normal_pair_f(w.x, w.y, z1, z2);
+        cv_move(c, c.sigma_a * z1, c.sigma_a * z2, x, y, vx, vy);
+    }
+    lw = lw_old + cv_loglik(c, ox, oy, x, y);
+    lse_push(lw, m, s, s2);
+}
+
+template <int kPPT>
+__device__ __forceinline__ void load_run(const float *p, float (&v)[kPPT])
+{
+    if constexpr (kPPT == 4) {
+        const float4 q = __ldcs(reinterpret_cast<const float4 *>(p));
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+        v[3] = q.w;
+    } else if constexpr (kPPT == 2) {
+        const float2 q = __ldcs(reinterpret_cast<const float2 *>(p));
+        v[0] = q.x;
+        v[1] = q.y;
+    } else {
+        v[0] = __ldcs(p);
+    }
+}
+
+template <int kPPT>
+__device__ __forceinline__ void store_run(float *p, const float (&v)[kPPT])
+{
+    if constexpr (kPPT == 4) {
+        __stcs(reinterpret_cast<float4 *>(p),
+            make_float4(v[0], v[1], v[2], v[3]));
+    } else if constexpr (kPPT == 2) {
+        __stcs(reinterpret_cast<float2 *>(p), make_float2(v[0], v[1]));
+    } else {
+        __stcs(p, v[0]);
+    }
+}
+
+// One global step of every running filter.  A filter at t < T moves and
+// weights its particles; at t == T it only records the weighted mean of its
+// final particles.  The last tile of a filter to finish combines the
+// filter's tile records in FP64.
+template <int kBlock, int kPPT, bool First>
+__global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
+{
+    constexpr uint32_t kTile = kBlock * kPPT;
+    constexpr int kW = kBlock / 32;
+    const uint32_t t = *a.step;
+    const uint32_t ntiles = t <= a.tmax ? a.active[t] : 0u;
+    __shared__ float shm[kW];
+    __shared__ double sh[5][kW];
+    __shared__ float shmax[kW + 1];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t f = a.tile_filter[tile];
+        const BFilter F = a.flt[f];
+        PfScalars &S = a.st[f];
+        const bool mon = !First && t == F.T;
+        const int resampled = First ? 1 : S.resampled;
+        const bool gather = First ? false : (S.gather != 0);
+        const float Mprev = First ? 0.0f : static_cast<float>(S.M);
+        float ox = 0.0f, oy = 0.0f;
+        if (!mon) {
+            ox = static_cast<float>(a.obs[2 * (F.obs_off + t) + 0]);
+            oy = static_cast<float>(a.obs[2 * (F.obs_off + t) + 1]);
+        }
+        float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
+        const uint32_t i0 = (tile - F.tile0) * kTile + threadIdx.x * kPPT;
+        const bool full = i0 + kPPT <= F.n;
+        float X[kPPT], Y[kPPT], VX[kPPT], VY[kPPT], LW[kPPT];
+#pragma unroll
+        for (int k = 0; k < kPPT; ++k)
+            X[k] = Y[k] = VX[k] = VY[k] = LW[k] = 0.0f;
+        if (!First) {
+            const uint32_t g0 = F.off + i0;
+            if (!gather && full) {
+                load_run<kPPT>(a.ax + g0, X);
+                load_run<kPPT>(a.ay + g0, Y);
+                load_run<kPPT>(a.avx + g0, VX);
+                load_run<kPPT>(a.avy + g0, VY);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kPPT; ++k) {
+                    const uint32_t i = i0 + k;
+                    if (i < F.n) {
+                        uint32_t src = i;
+                        if (gather) {
+                            const int32_t v = a.idx[F.off + i];
+                            const uint32_t e = static_cast<uint32_t>(-(v + 1));
+                            src = v >= 0 ? static_cast<uint32_t>(v)
+                                         : (e < F.n ? __ldcg(a.srcs + F.off + e)
+                                                    : F.n);
+                            if (src >= F.n) {
+                                atomicOr(&S.err, DEV_ERR_INTERNAL);
+                                src = 0;
+                            }
+                        }
+                        X[k] = a.ax[F.off + src];
+                        Y[k] = a.ay[F.off + src];
+                        VX[k] = a.avx[F.off + src];
+                        VY[k] = a.avy[F.off + src];
+                    }
+                }
+            }
+            if (!resampled) {
+                if (full) {
+                    load_run<kPPT>(a.lw + g0, LW);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kPPT; ++k)
+                        if (i0 + k < F.n)
+                            LW[k] = a.lw[g0 + k];
+                }
+            }
+        }
+        if (mon) {
+#pragma unroll
+            for (int k = 0; k < kPPT; ++k)
+                if (i0 + k < F.n) {
+                    const float wo = resampled ? 1.0f : __expf(LW[k] - Mprev);
+                    sx += wo * X[k];
+                    sy += wo * Y[k];
+                    sw += wo;
+                }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kPPT; ++k)
+                if (i0 + k < F.n)
+                    batch_one<First>(F.c, F.seed, i0 + k, t, ox, oy,
+                        resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k], m,
+                        s, s2, sx, sy, sw);
+            const uint32_t g0 = F.off + i0;
+            if (full) {
+                store_run<kPPT>(a.bx + g0, X);
+                store_run<kPPT>(a.by + g0, Y);
+                store_run<kPPT>(a.bvx + g0, VX);
+                store_run<kPPT>(a.bvy + g0, VY);
+                store_run<kPPT>(a.lw + g0, LW);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kPPT; ++k)
+                    if (i0 + k < F.n) {
+                        a.bx[g0 + k] = X[k];
+                        a.by[g0 + k] = Y[k];
+                        a.bvx[g0 + k] = VX[k];
+                        a.bvy[g0 + k] = VY[k];
+                        a.lw[g0 + k] = LW[k];
+                    }
+            }
+        }
+
+        // ---- tile record: FP32 within a warp, FP64 across warps
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            const float om = __shfl_xor_sync(0xFFFFFFFFu, m, d);
+            const float os = __shfl_xor_sync(0xFFFFFFFFu, s, d);
+            const float os2 = __shfl_xor_sync(0xFFFFFFFFu, s2, d);
+            sx += __shfl_xor_sync(0xFFFFFFFFu, sx, d);
+            sy += __shfl_xor_sync(0xFFFFFFFFu, sy, d);
+            sw += __shfl_xor_sync(0xFFFFFFFFu, sw, d);
+            lse_merge_f(m, s, s2, om, os, os2);
+        }
+        if (lane == 0) {
+            shm[wid] = m;
+            sh[0][wid] = s;
+            sh[1][wid] = s2;
+            sh[2][wid] = sx;
+            sh[3][wid] = sy;
+            sh[4][wid] = sw;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float mb = -INFINITY;
+            for (int w = 0; w < kW; ++w)
+                mb = fmaxf(mb, shm[w]);
+            MovePartial p = {0, 0, 0, mb, 0, 0};
+            for (int w = 0; w < kW; ++w) {
+                p.sx += sh[2][w];
+                p.sy += sh[3][w];
+                p.sw += sh[4][w];
+                if (shm[w] > -INFINITY) {
+                    const double fct = __expf(shm[w] - mb);
+                    p.s += sh[0][w] * fct;
+                    p.s2 += sh[1][w] * fct * fct;
+                }
+            }
+            a.part[tile] = p;
+            __threadfence();
+            is_last = atomicAdd(&S.done, 1u) == F.ntiles - 1;
+        }
+        __syncthreads();
+        if (is_last) {
+            // ---- the filter's last tile: combine its tile records
+            __threadfence();
+            float M = -INFINITY;
+            for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock)
+                M = fmaxf(M, static_cast<float>(a.part[F.tile0 + b].m));
+            M = block_reduce(M, OpMax(), -INFINITY, shmax);
+            double S1 = 0, S2 = 0, SX = 0, SY = 0, SW = 0;
+            for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock) {
+                const MovePartial p = a.part[F.tile0 + b];
+                SX += p.sx;
+                SY += p.sy;
+                SW += p.sw;
+                if (p.m > -INFINITY) {
+                    const double fct = __expf(static_cast<float>(p.m) - M);
+                    S1 += p.s * fct;
+                    S2 += p.s2 * fct * fct;
+                }
+            }
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                S1 += __shfl_xor_sync(0xFFFFFFFFu, S1, d);
+                S2 += __shfl_xor_sync(0xFFFFFFFFu, S2, d);
+                SX += __shfl_xor_sync(0xFFFFFFFFu, SX, d);
+                SY += __shfl_xor_sync(0xFFFFFFFFu, SY, d);
+                SW += __shfl_xor_sync(0xFFFFFFFFu, SW, d);
+            }
+            if (lane == 0) {
+                sh[0][wid] = S1;
+                sh[1][wid] = S2;
+                sh[2][wid] = SX;
+                sh[3][wid] = SY;
+                sh[4][wid] = SW;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double T1 = 0, T2 = 0, TX = 0, TY = 0, TW = 0;
+                for (int w = 0; w < kW; ++w) {
+                    T1 += sh[0][w];
+                    T2 += sh[1][w];
+                    TX += sh[2][w];
+                    TY += sh[3][w];
+                    TW += sh[4][w];
+                }
+                if (mon) {
+                    a.h_mean[2 * (F.hist_off + F.T - 1) + 0] = TX / TW;
+                    a.h_mean[2 * (F.hist_off + F.T - 1) + 1] = TY / TW;
+                    S.resampled = 0; // finished: nothing left to resample
+                    S.gather = 0;
+                } else {
+                    const double prev_mass =
+                        First ? static_cast<double>(F.n) : TW;
+                    if (!First) {
+                        a.h_mean[2 * (F.hist_off + t - 1) + 0] = TX / TW;
+                        a.h_mean[2 * (F.hist_off + t - 1) + 1] = TY / TW;
+                    }
+                    const double ess = T1 * T1 / T2;
+                    const double M1 = static_cast<double>(M);
+                    S.logz += M1 + log(T1) - log(prev_mass);
+                    if (!(T1 > 0) || !(ess > 0))
+                        S.err |= DEV_ERR_NONFINITE;
+                    const int flag =
+                        ess < a.threshold * static_cast<double>(F.n) ? 1 : 0;
+                    a.h_ess[F.hist_off + t] = ess;
+                    a.h_logz[F.hist_off + t] = S.logz;
+                    a.h_res[F.hist_off + t] = flag;
+                    S.M = M1;
+                    S.S = T1;
+                    S.ess = ess;
+                    S.resampled = flag;
+                    S.gather = 0;
+                    S.step = t + 1;
+                }
+                S.done = 0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Resampling of one filter by one block (kB threads, 4 particles each per
+// chunk): the fixed-point total, the counts, the slot assignment and the
+// empty-slot sources, as the single filter's k_rs32_* kernels do over the
+// whole grid.  The filter's arrays stay in L2 between the passes.
+template <int kB>
+__global__ void __launch_bounds__(kB) k_batch_resample(const BatchArgs a)
+{
+    constexpr int kW = kB / 32;
+    constexpr uint32_t kChunk = kB * 4;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(a.step, 1u); // every step kernel block has read it
+    if (blockIdx.x >= a.nfilters)
+        return;
+    const uint32_t f = a.res_order[blockIdx.x];
+    PfScalars &S = a.st[f];
+    if (!S.resampled)
+        return;
+    const BFilter F = a.flt[f];
+    const uint32_t n = F.n;
+    const float M = static_cast<float>(S.M);
+    const float *lw = a.lw + F.off;
+    int32_t *rep = a.rep + F.off;
+    int32_t *idx = a.idx + F.off;
+    uint32_t *marks = a.marks + F.off;
+    uint32_t *srcs = a.srcs + F.off;
+    __shared__ uint64_t sh64[kW + 1];
+    __shared__ uint32_t sh32[kW + 1];
+    __shared__ QR shqr[kW];
+    __shared__ uint32_t lastF[kW];
+    __shared__ uint32_t carryF;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t err = 0;
+
+    // ---- A: fixed-point total
+    uint64_t acc = 0;
+    for (uint32_t i0 = threadIdx.x * 4; i0 < n; i0 += kChunk) {
+        if (i0 + 3 < n) {
+            const float4 v = __ldcg(reinterpret_cast<const float4 *>(lw + i0));
+            acc += fixed_q(v.x, M, F.shift) + fixed_q(v.y, M, F.shift) +
+                fixed_q(v.z, M, F.shift) + fixed_q(v.w, M, F.shift);
+        } else {
+            for (uint32_t i = i0; i < n; ++i)
+                acc += fixed_q(lw[i], M, F.shift);
+        }
+    }
+    const uint64_t Q = block_reduce(acc, OpAdd(), uint64_t(0), sh64);
+    if (Q == 0) {
+        if (threadIdx.x == 0)
+            atomicOr(&S.err, DEV_ERR_NONFINITE);
+        return;
+    }
+    const PfScalars sc = S;
+    const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
+    const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
+    const float invQ = __frcp_rn(__ull2float_rn(Q));
+    WordCache wc;
+    wc.blk = ~0ull;
+
+    // ---- B: counts.  Start: X = 0 * n - G.
+    QR carry;
+    if (sys && cp.G > 0) {
+        carry.j = 0;
+        carry.r = Q - cp.G;
+    } else {
+        carry.j = 1;
+        carry.r = 0;
+    }
+    if (threadIdx.x == 0)
+        carryF = 0;
+    __syncthreads();
+    uint32_t empties = 0, copies = 0;
+    for (uint32_t base = 0; base < n; base += kChunk) {
+        const uint32_t i0 = base + threadIdx.x * 4;
+        uint64_t q[4];
+        if (i0 + 3 < n) {
+            const float4 v = __ldcg(reinterpret_cast<const float4 *>(lw + i0));
+            q[0] = fixed_q(v.x, M, F.shift);
+            q[1] = fixed_q(v.y, M, F.shift);
+            q[2] = fixed_q(v.z, M, F.shift);
+            q[3] = fixed_q(v.w, M, F.shift);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                q[k] = i0 + k < n ? fixed_q(lw[i0 + k], M, F.shift) : 0;
+        }
+        QR loc[4];
+        QR ac = {0, 0};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            qr_push(ac, q[k], n, false, Q, invQ, cp, err);
+            loc[k] = ac;
+        }
+        QR total;
+        const QR ex = block_exclusive_qr<kB>(ac, Q, shqr, &total);
+        const QR st = qr_add(carry, ex, Q);
+        uint32_t Fv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = i0 + k;
+            if (i + 1 >= n)
+                Fv[k] = n; // the last particle takes the rest
+            else
+                Fv[k] = f_of(qr_add(st, loc[k], Q), sys, n, Q, sc, wc);
+        }
+        uint32_t Fprev = __shfl_up_sync(0xFFFFFFFFu, Fv[3], 1);
+        if (lane == 31)
+            lastF[wid] = Fv[3];
+        __syncthreads();
+        if (lane == 0)
+            Fprev = wid == 0 ? carryF : lastF[wid - 1];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int32_t r = static_cast<int32_t>(Fv[k] - Fprev);
+            Fprev = Fv[k];
+            if (i0 + k < n) {
+                rep[i0 + k] = r;
+                empties += r == 0 ? 1u : 0u;
+                copies += static_cast<uint32_t>(r);
+            }
+        }
+        if (threadIdx.x == kB - 1)
+            carryF = Fv[3];
+        carry = qr_add(carry, total, Q);
+        __syncthreads();
+    }
+    copies = block_reduce(copies, OpAdd(), 0u, sh32);
+    const uint32_t nempty = block_reduce(empties, OpAdd(), 0u, sh32);
+    if (copies != n)
+        err |= DEV_ERR_INTERNAL;
+
+    // ---- C: slots.  idx[i] = i for a parent, -(e + 1) for the e-th empty
+    // slot; marks[first surplus rank of a parent with two or more copies] =
+    // parent + 1.
+    uint32_t coff = 0, eoff = 0;
+    for (uint32_t base = 0; base < n; base += kChunk) {
+        const uint32_t i0 = base + threadIdx.x * 4;
+        int32_t r[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            r[k] = i0 + k < n ? rep[i0 + k] : -1;
+        uint32_t tr = 0, te = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (r[k] >= 0) {
+                tr += static_cast<uint32_t>(r[k]);
+                te += r[k] == 0 ? 1u : 0u;
+            }
+        const uint64_t v = (static_cast<uint64_t>(tr) << 32) | te;
+        uint64_t tot;
+        const uint64_t incl =
+            block_inclusive_scan(v, OpAdd(), uint64_t(0), sh64, &tot);
+        const uint64_t exv = incl - v;
+        uint32_t c = coff + static_cast<uint32_t>(exv >> 32);
+        uint32_t e = eoff + static_cast<uint32_t>(exv & 0xFFFFFFFFu);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = i0 + k;
+            if (r[k] < 0)
+                continue;
+            if (r[k] == 0) {
+                idx[i] = -static_cast<int32_t>(e) - 1;
+                ++e;
+            } else {
+                idx[i] = static_cast<int32_t>(i);
+                if (r[k] >= 2) {
+                    const uint32_t rank = c - (i - e);
+                    if (rank < n)
+                        marks[rank] = i + 1;
+                    else
+                        err |= DEV_ERR_INTERNAL;
+                }
+                c += static_cast<uint32_t>(r[k]);
+            }
+        }
+        coff += static_cast<uint32_t>(tot >> 32);
+        eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
+    }
+    __syncthreads();
+
+    // ---- D: the parent of surplus rank k is the running max of the marks
+    uint32_t run_carry = 0;
+    for (uint32_t base = 0; base < nempty; base += kChunk) {
+        const uint32_t k0 = base + threadIdx.x * 4;
+        uint32_t mk[4], run[4];
+        uint32_t tmax = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            mk[k] = k0 + k < nempty ? marks[k0 + k] : 0u;
+            tmax = max(tmax, mk[k]);
+            run[k] = tmax;
+        }
+        uint32_t tot;
+        const uint32_t incl =
+            block_inclusive_scan(tmax, OpMax(), 0u, sh32, &tot);
+        uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+        if (lane == 31)
+            lastF[wid] = incl;
+        __syncthreads();
+        if (lane == 0)
+            before = wid > 0 ? lastF[wid - 1] : 0u;
+        __syncthreads();
+        before = max(before, run_carry);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k0 + k < nempty) {
+                const uint32_t rk = max(run[k], before);
+                if (rk == 0 || rk - 1 >= n)
+                    err |= DEV_ERR_INTERNAL;
+                srcs[k0 + k] = rk - 1;
+                if (mk[k])
+                    marks[k0 + k] = 0;
+            }
+        }
+        run_carry = max(run_carry, tot);
+    }
+    __syncthreads();
+    if (err)
+        atomicOr(&S.err, err);
+    if (threadIdx.x == 0) {
+        S.nempty = nempty;
+        S.Q = Q;
+        S.gather = 1;
+        // the words U01SequenceSystematic / U01SequenceStratified consume
+        // (rng/u01_sequence.hpp:177-259, resample/transform.hpp:61-70)
+        if (sys) {
+            engine_advance(S, 1);
+        } else {
+            const uint32_t jf = n - static_cast<uint32_t>(rep[n - 1]);
+            engine_advance(S, jf < n ? jf + 1 : n);
+        }
+    }
+}
+
+__global__ void k_batch_reset(PfScalars *st, const BFilter *flt, uint32_t nf,
+    uint32_t *step)
+{
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f == 0)
+        *step = 0;
+    if (f >= nf)
+        return;
+    PfScalars z = {};
+    z.resampled = 1;
+    z.rindex = 4;
+    z.rkey[0] = 0;
+    z.rkey[1] = flt[f].seed;
+    z.rctr[2] = 1;
+    st[f] = z;
+}
+
+// each filter's observations from its own model and seed (one thread each)
+__global__ void k_batch_simulate(const vsmc_cuda_cv_model *models,
+    const uint32_t *seeds, const uint32_t *T, const uint32_t *obs_off,
+    uint32_t nf, double *truth, double *obs)
+{
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf)
+        return;
+    const vsmc_cuda_cv_model m = models[f];
+    cv_simulate_seq(seeds[f], T[f], m.dt, m.sigma_a, m.obs_scale, m.nu,
+        m.sd_pos0, m.sd_vel0, truth ? truth + 4 * obs_off[f] : nullptr,
+        obs + 2 * obs_off[f]);
+}
+
+constexpr int kResBlock = 512;
+
+struct Shape {
+    int ppt, block;
+};
+constexpr Shape kShapes[] = {
+    {1, 128}, {2, 128}, {4, 128}, {1, 256}, {2, 256}, {4, 256}};
+constexpr int kNumShapes = 6;
+
+template <int kBlock, int kPPT>
+static cudaError_t launch_step_t(bool first, int grid, const BatchArgs &a,
+    cudaStream_t st)
+{
+    if (first)
+        k_batch_step<kBlock, kPPT, true><<<grid, kBlock, 0, st>>>(a);
+    else
+        k_batch_step<kBlock, kPPT, false><<<grid, kBlock, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_step(
+    Shape s, bool first, int grid, const BatchArgs &a, cudaStream_t st)
+{
+    if (s.block == 128) {
+        if (s.ppt == 1)
+            return launch_step_t<128, 1>(first, grid, a, st);
+        if (s.ppt == 2)
+            return launch_step_t<128, 2>(first, grid, a, st);
+        return launch_step_t<128, 4>(first, grid, a, st);
+    }
+    if (s.ppt == 1)
+        return launch_step_t<256, 1>(first, grid, a, st);
+    if (s.ppt == 2)
+        return launch_step_t<256, 2>(first, grid, a, st);
+    return launch_step_t<256, 4>(first, grid, a, st);
+}
+
+template <int kBlock, int kPPT>
+static int occupancy_t()
+{
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ, k_batch_step<kBlock, kPPT, false>, kBlock, 0) !=
+            cudaSuccess ||
+        occ < 1)
+        occ = 2;
+    return occ;
+}
+
+static int occupancy(Shape s)
+{
+    if (s.block == 128)
+        return s.ppt == 1 ? occupancy_t<128, 1>()
+                          : (s.ppt == 2 ? occupancy_t<128, 2>()
+                                        : occupancy_t<128, 4>());
+    return s.ppt == 1 ? occupancy_t<256, 1>()
+                      : (s.ppt == 2 ? occupancy_t<256, 2>()
+                                    : occupancy_t<256, 4>());
+}
+
+} // namespace vsmc_cuda
+
+struct vsmc_cuda_batch {
+    uint32_t nf = 0;
+    uint32_t tmax = 0;
+    int scheme = VSMC_CUDA_STRATIFIED;
+    double threshold = 0.5;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    Shape shape = {4, 256};
+    // caller order
+    std::vector<uint32_t> n, T, seeds;
+    std::vector<vsmc_cuda_cv_model> models;
+    std::vector<uint32_t> obs_off; // prefix sums of T (caller order)
+    size_t total_T = 0;
+    // internal order: horizon descending
+    std::vector<uint32_t> order;     // internal -> caller
+    std::vector<uint32_t> res_order; // internal filters by n descending
+    std::vector<BFilter> flt;        // internal order
+    std::vector<uint32_t> tile_filter, active;
+    size_t total_particles = 0; // with padding
+    size_t max_tiles = 0;
+    // device
+    BFilter *d_flt = nullptr;
+    PfScalars *d_st = nullptr;
+    uint32_t *d_tile_filter = nullptr, *d_active = nullptr,
+             *d_res_order = nullptr, *d_step = nullptr;
+    float *d_state[2] = {nullptr, nullptr};
+    float *d_lw = nullptr;
+    int32_t *d_rep = nullptr, *d_idx = nullptr;
+    uint32_t *d_marks = nullptr, *d_srcs = nullptr;
+    MovePartial *d_part = nullptr;
+    double *d_obs = nullptr;
+    double *d_mean = nullptr, *d_ess = nullptr, *d_logz = nullptr;
+    int *d_res = nullptr;
+    // run graph (for one observation pointer and shape)
+    cudaGraphExec_t graph = nullptr;
+    const double *graph_obs = nullptr;
+    Shape graph_shape = {0, 0};
+};
+
+namespace vsmc_cuda
+{
+
+template <typename T>
+static int balloc(T **p, size_t count)
+{
+    void *q = nullptr;
+    VSMC_CUDA_TRY(cudaMalloc(&q, sizeof(T) * (count ? count : 1)));
+    *p = static_cast<T *>(q);
+    return VSMC_CUDA_OK;
+}
+
+static void batch_free(vsmc_cuda_batch *b)
+{
+    if (b->graph)
+        cudaGraphExecDestroy(b->graph);
+    void *ptrs[] = {b->d_flt, b->d_st, b->d_tile_filter, b->d_active,
+        b->d_res_order, b->d_step, b->d_state[0], b->d_state[1], b->d_lw,
+        b->d_rep, b->d_idx, b->d_marks, b->d_srcs, b->d_part, b->d_obs,
+        b->d_mean, b->d_ess, b->d_logz, b->d_res};
+    for (void *p : ptrs)
+        if (p)
+            cudaFree(p);
+    if (b->own_stream && b->stream)
+        cudaStreamDestroy(b->stream);
+}
+
+// tile tables for a shape (host + device)
+static int batch_layout(vsmc_cuda_batch *b, Shape s)
+{
+    const uint32_t tile = static_cast<uint32_t>(s.ppt * s.block);
+    b->tile_filter.clear();
+    for (uint32_t k = 0; k < b->nf; ++k) {
+        BFilter &F = b->flt[k];
+        F.tile0 = static_cast<uint32_t>(b->tile_filter.size());
+        F.ntiles = (F.n + tile - 1) / tile;
+        for (uint32_t j = 0; j < F.ntiles; ++j)
+            b->tile_filter.push_back(k);
+    }
+    if (b->tile_filter.size() > b->max_tiles)
+        return VSMC_CUDA_ERR_INTERNAL;
+    // filters are sorted by T descending: those with T >= t are a prefix
+    b->active.assign(b->tmax + 1, 0);
+    uint32_t k = b->nf;
+    for (uint32_t t = 0; t <= b->tmax; ++t) {
+        while (k > 0 && b->flt[k - 1].T < t)
+            --k;
+        b->active[t] = k == 0 ? 0 : b->flt[k - 1].tile0 + b->flt[k - 1].ntiles;
+    }
+    cudaStream_t st = b->stream;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(b->d_flt, b->flt.data(),
+        sizeof(BFilter) * b->nf, cudaMemcpyHostToDevice, st));
+    VSMC_CUDA_TRY(cudaMemcpyAsync(b->d_tile_filter, b->tile_filter.data(),
+        sizeof(uint32_t) * b->tile_filter.size(), cudaMemcpyHostToDevice, st));
+    VSMC_CUDA_TRY(cudaMemcpyAsync(b->d_active, b->active.data(),
+        sizeof(uint32_t) * b->active.size(), cudaMemcpyHostToDevice, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    b->shape = s;
+    return VSMC_CUDA_OK;
+}
+
+static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
+{
+    BatchArgs a = {};
+    const size_t ld = b->total_particles;
+    const float *A = b->d_state[cur];
+    float *B = b->d_state[1 - cur];
+    a.flt = b->d_flt;
+    a.st = b->d_st;
+    a.tile_filter = b->d_tile_filter;
+    a.active = b->d_active;
+    a.res_order = b->d_res_order;
+    a.ax = A;
+    a.ay = A + ld;
+    a.avx = A + 2 * ld;
+    a.avy = A + 3 * ld;
+    a.bx = B;
+    a.by = B + ld;
+    a.bvx = B + 2 * ld;
+    a.bvy = B + 3 * ld;
+    a.lw = b->d_lw;
+    a.rep = b->d_rep;
+    a.idx = b->d_idx;
+    a.marks = b->d_marks;
+    a.srcs = b->d_srcs;
+    a.part = b->d_part;
+    a.obs = obs;
+    a.h_mean = b->d_mean;
+    a.h_ess = b->d_ess;
+    a.h_logz = b->d_logz;
+    a.h_res = b->d_res;
+    a.step = b->d_step;
+    a.nfilters = b->nf;
+    a.tmax = b->tmax;
+    a.scheme = b->scheme;
+    a.threshold = b->threshold;
+    return a;
+}
+
+// enqueue a whole run (reset + steps 0..nsteps-1) on the batch's stream;
+// grid = the step kernel's persistent grid for the current shape
+static int enqueue_run(
+    vsmc_cuda_batch *b, const double *obs, int nsteps, int grid)
+{
+    cudaStream_t st = b->stream;
+    k_batch_reset<<<(b->nf + 255) / 256, 256, 0, st>>>(
+        b->d_st, b->d_flt, b->nf, b->d_step);
+    VSMC_CUDA_CHECK_LAUNCH();
+    for (int t = 0; t < nsteps; ++t) {
+        const BatchArgs a = batch_args(b, obs, t & 1);
+        VSMC_CUDA_TRY(launch_step(b->shape, t == 0, grid, a, st));
+        k_batch_resample<kResBlock><<<b->nf, kResBlock, 0, st>>>(a);
+        VSMC_CUDA_CHECK_LAUNCH();
+    }
+    return VSMC_CUDA_OK;
+}
+
+static int check_errors(vsmc_cuda_batch *b)
+{
+    std::vector<PfScalars> st(b->nf);
+    VSMC_CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_st,
+        sizeof(PfScalars) * b->nf, cudaMemcpyDeviceToHost, b->stream));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    uint32_t err = 0;
+    for (const PfScalars &s : st)
+        err |= s.err;
+    if (err & DEV_ERR_NONFINITE)
+        return VSMC_CUDA_ERR_NONFINITE;
+    if (err)
+        return VSMC_CUDA_ERR_INTERNAL;
+    return VSMC_CUDA_OK;
+}
+
+} // namespace vsmc_cuda
+
+extern "C" {
+
+int vsmc_cuda_batch_create(vsmc_cuda_batch **out, size_t nfilters,
+    const uint32_t *n, const uint32_t *T, const vsmc_cuda_cv_model *models,
+    const uint32_t *seeds, int scheme, double threshold, void *stream)
+{
+    if (out == nullptr || n == nullptr || T == nullptr || models == nullptr ||
+        seeds == nullptr || std::isnan(threshold) ||
+        (scheme != VSMC_CUDA_STRATIFIED && scheme != VSMC_CUDA_SYSTEMATIC))
+        return VSMC_CUDA_ERR_ARG;
+    *out = nullptr;
+    if (nfilters < 1 || nfilters > (size_t(1) << 24))
+        return VSMC_CUDA_ERR_SIZE;
+    size_t total = 0, totalT = 0, tiles = 0;
+    uint32_t tmax = 0;
+    for (size_t f = 0; f < nfilters; ++f) {
+        if (!valid_cv_model(&models[f]))
+            return VSMC_CUDA_ERR_ARG;
+        if (n[f] < 2 || n[f] > (1u << 30) || T[f] < 1 || T[f] > (1u << 24))
+            return VSMC_CUDA_ERR_SIZE;
+        total += (static_cast<size_t>(n[f]) + 3) / 4 * 4;
+        totalT += T[f];
+        tiles += (n[f] + 127) / 128; // the smallest tile
+        tmax = std::max(tmax, T[f]);
+    }
+    if (total >= (size_t(1) << 31) || totalT >= (size_t(1) << 31))
+        return VSMC_CUDA_ERR_SIZE;
+    vsmc_cuda_batch *b = new (std::nothrow) vsmc_cuda_batch;
+    if (b == nullptr)
+        return VSMC_CUDA_ERR_ALLOC;
+    b->nf = static_cast<uint32_t>(nfilters);
+    b->tmax = tmax;
+    b->scheme = scheme;
+    b->threshold = threshold;
+    b->n.assign(n, n + nfilters);
+    b->T.assign(T, T + nfilters);
+    b->seeds.assign(seeds, seeds + nfilters);
+    b->models.assign(models, models + nfilters);
+    b->total_T = totalT;
+    b->total_particles = total;
+    b->max_tiles = tiles;
+    b->obs_off.resize(nfilters);
+    size_t acc = 0;
+    for (size_t f = 0; f < nfilters; ++f) {
+        b->obs_off[f] = static_cast<uint32_t>(acc);
+        acc += T[f];
+    }
+    b->order.resize(nfilters);
+    for (uint32_t f = 0; f < nfilters; ++f)
+        b->order[f] = f;
+    std::stable_sort(b->order.begin(), b->order.end(),
+        [&](uint32_t x, uint32_t y) { return T[x] > T[y]; });
+    b->flt.resize(nfilters);
+    size_t off = 0;
+    for (uint32_t k = 0; k < nfilters; ++k) {
+        const uint32_t f = b->order[k];
+        BFilter &F = b->flt[k];
+        F = BFilter{};
+        F.n = n[f];
+        F.off = static_cast<uint32_t>(off);
+        off += (static_cast<size_t>(n[f]) + 3) / 4 * 4;
+        F.T = T[f];
+        F.obs_off = b->obs_off[f];
+        F.hist_off = b->obs_off[f];
+        F.seed = seeds[f];
+        int lg = 0;
+        while ((size_t(1) << lg) < n[f])
+            ++lg;
+        F.shift = static_cast<uint32_t>(63 - lg);
+        F.c = make_cv_const<float>(models[f]);
+    }
+    b->res_order.resize(nfilters);
+    for (uint32_t k = 0; k < nfilters; ++k)
+        b->res_order[k] = k;
+    std::stable_sort(b->res_order.begin(), b->res_order.end(),
+        [&](uint32_t x, uint32_t y) { return b->flt[x].n > b->flt[y].n; });
+
+    b->stream = as_stream(stream);
+    if (b->stream == nullptr) {
+        if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) !=
+            cudaSuccess) {
+            delete b;
+            return VSMC_CUDA_ERR_CUDA;
+        }
+        b->own_stream = true;
+    }
+    int rc = VSMC_CUDA_OK;
+#define B_TRY(x)                                                              \
+    do {                                                                      \
+        rc = (x);                                                             \
+        if (rc != VSMC_CUDA_OK) {                                             \
+            batch_free(b);                                                    \
+            delete b;                                                         \
+            return rc;                                                        \
+        }                                                                     \
+    } while (0)
+    B_TRY(balloc(&b->d_flt, nfilters));
+    B_TRY(balloc(&b->d_st, nfilters));
+    B_TRY(balloc(&b->d_tile_filter, tiles));
+    B_TRY(balloc(&b->d_active, tmax + 1));
+    B_TRY(balloc(&b->d_res_order, nfilters));
+    B_TRY(balloc(&b->d_step, 1));
+    B_TRY(balloc(&b->d_state[0], 4 * total));
+    B_TRY(balloc(&b->d_state[1], 4 * total));
+    B_TRY(balloc(&b->d_lw, total));
+    B_TRY(balloc(&b->d_rep, total));
+    B_TRY(balloc(&b->d_idx, total));
+    B_TRY(balloc(&b->d_marks, total));
+    B_TRY(balloc(&b->d_srcs, total));
+    B_TRY(balloc(&b->d_part, tiles));
+    B_TRY(balloc(&b->d_obs, 2 * totalT));
+    B_TRY(balloc(&b->d_mean, 2 * totalT));
+    B_TRY(balloc(&b->d_ess, totalT));
+    B_TRY(balloc(&b->d_logz, totalT));
+    B_TRY(balloc(&b->d_res, totalT));
+    if (cudaMemsetAsync(b->d_marks, 0, sizeof(uint32_t) * total, b->stream) !=
+        cudaSuccess)
+        B_TRY(VSMC_CUDA_ERR_CUDA);
+    if (cudaMemsetAsync(b->d_mean, 0, sizeof(double) * 2 * totalT,
+            b->stream) != cudaSuccess)
+        B_TRY(VSMC_CUDA_ERR_CUDA);
+    if (cudaMemcpyAsync(b->d_res_order, b->res_order.data(),
+            sizeof(uint32_t) * nfilters, cudaMemcpyHostToDevice,
+            b->stream) != cudaSuccess)
+        B_TRY(VSMC_CUDA_ERR_CUDA);
+    B_TRY(batch_layout(b, b->shape));
+#undef B_TRY
+    *out = b;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_destroy(vsmc_cuda_batch *b)
+{
+    if (b == nullptr)
+        return VSMC_CUDA_OK;
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    delete b;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_stream(vsmc_cuda_batch *b, void **stream)
+{
+    if (b == nullptr || stream == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    *stream = b->stream;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_simulate(vsmc_cuda_batch *b, double *truth_dev,
+    double *obs_dev)
+{
+    if (b == nullptr || obs_dev == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    vsmc_cuda_cv_model *dm = nullptr;
+    uint32_t *dseed = nullptr, *dT = nullptr, *doff = nullptr;
+    cudaStream_t st = b->stream;
+    Scratch scratch(st);
+    dm = scratch.get<vsmc_cuda_cv_model>(b->nf);
+    dseed = scratch.get<uint32_t>(b->nf);
+    dT = scratch.get<uint32_t>(b->nf);
+    doff = scratch.get<uint32_t>(b->nf);
+    if (!dm || !dseed || !dT || !doff)
+        return VSMC_CUDA_ERR_ALLOC;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(dm, b->models.data(),
+        sizeof(vsmc_cuda_cv_model) * b->nf, cudaMemcpyHostToDevice, st));
+    VSMC_CUDA_TRY(cudaMemcpyAsync(dseed, b->seeds.data(),
+        sizeof(uint32_t) * b->nf, cudaMemcpyHostToDevice, st));
+    VSMC_CUDA_TRY(cudaMemcpyAsync(dT, b->T.data(), sizeof(uint32_t) * b->nf,
+        cudaMemcpyHostToDevice, st));
+    VSMC_CUDA_TRY(cudaMemcpyAsync(doff, b->obs_off.data(),
+        sizeof(uint32_t) * b->nf, cudaMemcpyHostToDevice, st));
+    k_batch_simulate<<<(b->nf + 63) / 64, 64, 0, st>>>(
+        dm, dseed, dT, doff, b->nf, truth_dev, obs_dev);
+    VSMC_CUDA_CHECK_LAUNCH();
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_run_device(vsmc_cuda_batch *b, const double *obs_dev)
+{
+    if (b == nullptr || obs_dev == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    const int nsteps = static_cast<int>(b->tmax) + 1;
+    if (b->graph == nullptr || b->graph_obs != obs_dev ||
+        b->graph_shape.ppt != b->shape.ppt ||
+        b->graph_shape.block != b->shape.block) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        const int grid = num_sms() * occupancy(b->shape);
+        VSMC_CUDA_TRY(cudaStreamBeginCapture(
+            b->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_run(b, obs_dev, nsteps, grid);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (rc != VSMC_CUDA_OK) {
+            if (g)
+                cudaGraphDestroy(g);
+            return rc;
+        }
+        VSMC_CUDA_TRY(e);
+        const cudaError_t ei = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        VSMC_CUDA_TRY(ei);
+        b->graph_obs = obs_dev;
+        b->graph_shape = b->shape;
+    }
+    VSMC_CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_history(vsmc_cuda_batch *b, double *mean_host,
+    double *ess_host, int *resampled_host, double *logz_host)
+{
+    if (b == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    const int rc = check_errors(b);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    cudaStream_t st = b->stream;
+    const size_t TT = b->total_T;
+    if (mean_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(mean_host, b->d_mean,
+            sizeof(double) * 2 * TT, cudaMemcpyDeviceToHost, st));
+    if (ess_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(ess_host, b->d_ess, sizeof(double) * TT,
+            cudaMemcpyDeviceToHost, st));
+    if (resampled_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(resampled_host, b->d_res,
+            sizeof(int) * TT, cudaMemcpyDeviceToHost, st));
+    if (logz_host)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(logz_host, b->d_logz,
+            sizeof(double) * TT, cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_run(vsmc_cuda_batch *b, const double *obs_host,
+    double *mean_host, double *ess_host, int *resampled_host,
+    double *logz_host)
+{
+    if (b == nullptr || obs_host == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(b->d_obs, obs_host,
+        sizeof(double) * 2 * b->total_T, cudaMemcpyHostToDevice, b->stream));
+    const int rc = vsmc_cuda_batch_run_device(b, b->d_obs);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    return vsmc_cuda_batch_history(
+        b, mean_host, ess_host, resampled_host, logz_host);
+}
+
+int vsmc_cuda_batch_set_shape(vsmc_cuda_batch *b, int ppt, int block)
+{
+    if (b == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    for (int k = 0; k < kNumShapes; ++k)
+        if (kShapes[k].ppt == ppt && kShapes[k].block == block)
+            return batch_layout(b, kShapes[k]);
+    return VSMC_CUDA_ERR_ARG;
+}
+
+int vsmc_cuda_batch_get_shape(vsmc_cuda_batch *b, int *ppt, int *block)
+{
+    if (b == nullptr || ppt == nullptr || block == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    *ppt = b->shape.ppt;
+    *block = b->shape.block;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_autotune(vsmc_cuda_batch *b, const double *obs_dev,
+    int steps, float *ms_host)
+{
+    if (b == nullptr || obs_dev == nullptr || steps < 1)
+        return VSMC_CUDA_ERR_ARG;
+    const int nsteps = std::min(steps, static_cast<int>(b->tmax) + 1);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    VSMC_CUDA_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return VSMC_CUDA_ERR_CUDA;
+    }
+    int best = -1;
+    float best_ms = 0;
+    int rc = VSMC_CUDA_OK;
+    for (int k = 0; k < kNumShapes && rc == VSMC_CUDA_OK; ++k) {
+        rc = batch_layout(b, kShapes[k]);
+        if (rc != VSMC_CUDA_OK)
+            break;
+        const int grid = num_sms() * occupancy(b->shape);
+        rc = enqueue_run(b, obs_dev, nsteps, grid); // warm-up
+        if (rc != VSMC_CUDA_OK)
+            break;
+        if (cudaEventRecord(e0, b->stream) != cudaSuccess) {
+            rc = VSMC_CUDA_ERR_CUDA;
+            break;
+        }
+        rc = enqueue_run(b, obs_dev, nsteps, grid);
+        if (rc != VSMC_CUDA_OK)
+            break;
+        float ms = 0;
+        if (cudaEventRecord(e1, b->stream) != cudaSuccess ||
+            cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+            rc = VSMC_CUDA_ERR_CUDA;
+            break;
+        }
+        if (ms_host)
+            ms_host[k] = ms;
+        if (best < 0 || ms < best_ms) {
+            best = k;
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    rc = check_errors(b);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    return batch_layout(b, kShapes[best]);
+}
+
+} // extern "C"

@@ -3,6 +3,7 @@
 #include "common.cuh"
 #include "pf_model.cuh"
 #include "rng_device.cuh"
+#include "cv_sim.cuh"
 
 using namespace vsmc_cuda;
 
@@ -50,44 +51,15 @@ __global__ void __launch_bounds__(256) k_cv_move(uint32_t n, uint32_t t,
     }
 }
 
-// Sequential simulation on one thread (T is small): a Philox4x32 engine
-// seeded with `seed`, fresh NormalDistribution<double> pairs for the prior
-// and the accelerations, one StudentTDistribution<double>(nu) for the noise.
+// Sequential simulation on one thread (T is small); see cv_sim.cuh.
 __global__ void k_cv_simulate(uint32_t seed, uint32_t T, double dt,
     double sigma_a, double obs_scale, double nu, double sd_pos0,
     double sd_vel0, double *truth, double *obs)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0)
         return;
-    PhiloxScalar eng(PhiloxScalar::key_t{seed, 0u}, 0);
-    StudentTScalar st(nu);
-    auto pair = [&](double sd, double &a, double &b) {
-        NormalScalar<double> nd(0, sd);
-        a = nd(eng);
-        b = nd(eng);
-    };
-    double x, y, vx, vy;
-    pair(sd_pos0, x, y);
-    pair(sd_vel0, vx, vy);
-    const double h = 0.5 * dt * dt;
-    for (uint32_t t = 0; t < T; ++t) {
-        if (t > 0) {
-            double ax, ay;
-            pair(sigma_a, ax, ay);
-            x = __dadd_rn(__dadd_rn(x, __dmul_rn(dt, vx)), __dmul_rn(h, ax));
-            y = __dadd_rn(__dadd_rn(y, __dmul_rn(dt, vy)), __dmul_rn(h, ay));
-            vx = __dadd_rn(vx, __dmul_rn(dt, ax));
-            vy = __dadd_rn(vy, __dmul_rn(dt, ay));
-        }
-        truth[4 * t + 0] = x;
-        truth[4 * t + 1] = y;
-        truth[4 * t + 2] = vx;
-        truth[4 * t + 3] = vy;
-        const double ex = st(eng);
-        const double ey = st(eng);
-        obs[2 * t + 0] = __dadd_rn(x, __dmul_rn(obs_scale, ex));
-        obs[2 * t + 1] = __dadd_rn(y, __dmul_rn(obs_scale, ey));
-    }
+    cv_simulate_seq(seed, T, dt, sigma_a, obs_scale, nu, sd_pos0, sd_vel0,
+        truth, obs);
 }
 
 template <typename T>

@@ -21,219 +21,10 @@
 #include "common.cuh"
 #include "pf_model.cuh"
 #include "pf32_types.cuh"
+#include "pf32_dev.cuh"
 
 namespace vsmc_cuda
 {
-
-// ------------------------------------------------------- small utilities
-
-__device__ __forceinline__ void lse_push(float v, float &m, float &s, float &s2)
-{
-    if (!(v > -INFINITY)) // -inf and NaN carry no weight
-        return;
-    if (v > m) {
-        const float e = __expf(m - v);
-        s = s * e + 1.0f;
-        s2 = s2 * e * e + 1.0f;
-        m = v;
-    } else {
-        const float e = __expf(v - m);
-        s += e;
-        s2 += e * e;
-    }
-}
-
-// merge (m2, t, t2) into (m, s, s2): max, sum exp(v - m), sum exp(2(v - m))
-__device__ __forceinline__ void lse_merge_f(
-    float &m, float &s, float &s2, float m2, float t, float t2)
-{
-    if (!(m2 > -INFINITY))
-        return;
-    if (!(m > -INFINITY)) {
-        m = m2;
-        s = t;
-        s2 = t2;
-        return;
-    }
-    if (m2 > m) {
-        const float e = __expf(m - m2);
-        s = s * e + t;
-        s2 = s2 * e * e + t2;
-        m = m2;
-    } else {
-        const float e = __expf(m2 - m);
-        s += t * e;
-        s2 += t2 * e * e;
-    }
-}
-
-// 64 x 64 -> 128 bit product, compared as (hi, lo)
-struct U128 {
-    uint64_t hi, lo;
-};
-
-__device__ __forceinline__ U128 mul_u64(uint64_t a, uint64_t b)
-{
-    return {__umul64hi(a, b), a * b};
-}
-
-__device__ __forceinline__ bool le_u128(const U128 &a, const U128 &b)
-{
-    return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo);
-}
-
-// word k (k >= 0) of the scalar stream of an engine at (key, ctr, index):
-// gen(ctr + (index + k) / 4)[(index + k) % 4]
-__device__ __forceinline__ uint32_t engine_word(const PfScalars &sc, uint64_t k)
-{
-    const uint64_t pos = static_cast<uint64_t>(sc.rindex) + k;
-    uint32_t c[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
-    ctr32_add(c, pos / 4);
-    const u32x4 b = philox4x32_10(c[0], c[1], c[2], c[3], sc.rkey[0], sc.rkey[1]);
-    const uint32_t i = static_cast<uint32_t>(pos % 4);
-    return i == 0 ? b.x : (i == 1 ? b.y : (i == 2 ? b.z : b.w));
-}
-
-// advance the engine by k >= 1 words
-__device__ __forceinline__ void engine_advance(PfScalars &sc, uint64_t k)
-{
-    if (k == 0)
-        return;
-    const uint64_t last = static_cast<uint64_t>(sc.rindex) + k - 1;
-    uint32_t c[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
-    ctr32_add(c, last / 4);
-    for (int i = 0; i < 4; ++i)
-        sc.rctr[i] = c[i];
-    sc.rindex = static_cast<uint32_t>(last % 4) + 1;
-}
-
-// Counting uniforms against the fixed-point CDF.
-//
-// Uniform j is u_j = (j + a_j 2^-32) / N with a 32-bit word a_j.  With the
-// integer CDF C_i and total Q, u_j <= C / Q  <=>  (j 2^32 + a_j) Q <= C N 2^32
-// <=>  j Q + G_j <= C N  with G_j = ceil(a_j Q / 2^32) < Q, since both sides
-// are integers.  The counts follow from one exact floor(C N / Q) with its
-// remainder per CDF value.
-struct CountP {
-    uint64_t Q;  // CDF total
-    uint64_t G;  // systematic: ceil(a Q / 2^32) (one word for every j)
-    uint32_t n;
-    int sh;      // Q >> sh < 2^24
-    float scale; // n / (Q >> sh)
-};
-
-__device__ __forceinline__ uint64_t ceil_aq(uint32_t a, uint64_t Q)
-{
-    const uint64_t hi = __umul64hi(static_cast<uint64_t>(a), Q); // < 2^32
-    const uint64_t lo = static_cast<uint64_t>(a) * Q;
-    return ((hi << 32) | (lo >> 32)) + ((lo & 0xFFFFFFFFull) != 0 ? 1 : 0);
-}
-
-__device__ __forceinline__ CountP make_count_params(
-    uint64_t Q, uint32_t n, uint32_t a_sys)
-{
-    CountP p;
-    p.Q = Q;
-    p.G = ceil_aq(a_sys, Q);
-    p.n = n;
-    const int bits = 64 - __clzll(static_cast<long long>(Q));
-    p.sh = bits > 24 ? bits - 24 : 0;
-    p.scale = static_cast<float>(n) /
-        __uint2float_rz(static_cast<uint32_t>(Q >> p.sh));
-    return p;
-}
-
-// j = floor((C n - G) / Q) and r = (C n - G) - j Q; false if C n < G
-__device__ __forceinline__ bool cn_divmod(uint64_t C, uint64_t G,
-    const CountP &p, long long &j, uint64_t &r, uint32_t &err)
-{
-    uint64_t xh = __umul64hi(C, static_cast<uint64_t>(p.n));
-    uint64_t xl = C * static_cast<uint64_t>(p.n);
-    if (xl < G) {
-        if (xh == 0)
-            return false;
-        --xh;
-    }
-    xl -= G;
-    // estimate within a few units of the answer
-    const float f =
-        __uint2float_rz(static_cast<uint32_t>(C >> p.sh)) * p.scale;
-    long long jj = static_cast<long long>(__float2int_rz(f)) - 2;
-    if (jj < 0)
-        jj = 0;
-    if (jj > static_cast<long long>(p.n))
-        jj = static_cast<long long>(p.n);
-    // R = X - jj Q, 128-bit; walk down while negative, up while >= Q
-    const uint64_t ph = __umul64hi(static_cast<uint64_t>(jj), p.Q);
-    const uint64_t pl = static_cast<uint64_t>(jj) * p.Q;
-    uint64_t rl = xl - pl;
-    uint64_t rh = xh - ph - (xl < pl ? 1 : 0);
-    int guard = 0;
-    while (static_cast<long long>(rh) < 0) { // X < jj Q
-        --jj;
-        const uint64_t t = rl + p.Q;
-        rh += (t < rl ? 1 : 0);
-        rl = t;
-        if (++guard > 64) {
-            err |= DEV_ERR_BOUND;
-            break;
-        }
-    }
-    guard = 0;
-    while (rh != 0 || rl >= p.Q) {
-        ++jj;
-        rh -= (rl < p.Q ? 1 : 0);
-        rl -= p.Q;
-        if (++guard > 64) {
-            err |= DEV_ERR_BOUND;
-            break;
-        }
-    }
-    j = jj;
-    r = rl;
-    return true;
-}
-
-// F(C) = number of uniforms <= C / Q (= index of the first one above).
-// sys: every uniform shares a_sys (systematic); otherwise a_j is word j of
-// the resampling engine (stratified).
-__device__ __forceinline__ uint32_t count_F(uint64_t C, const CountP &p,
-    bool sys, const PfScalars &sc, uint32_t &err)
-{
-    long long j;
-    uint64_t r;
-    if (sys) {
-        if (!cn_divmod(C, p.G, p, j, r, err))
-            return 0;
-        const long long F = j + 1;
-        return static_cast<uint32_t>(F < p.n ? F : p.n);
-    }
-    cn_divmod(C, 0, p, j, r, err);
-    if (j >= static_cast<long long>(p.n))
-        return p.n;
-    const uint32_t aj = engine_word(sc, static_cast<uint64_t>(j));
-    return static_cast<uint32_t>(j) + (ceil_aq(aj, p.Q) <= r ? 1u : 0u);
-}
-
-// floor(w * 2^shift) for w = exp(lw - M) in (0, 1], by integer operations on
-// the float's bits (no 64-bit conversion instruction)
-__device__ __forceinline__ uint64_t fixed_q(float lw, float M, uint32_t shift)
-{
-    if (!(lw > -INFINITY))
-        return 0;
-    const float w = fminf(__expf(lw - M), 1.0f);
-    const uint32_t bits = __float_as_uint(w);
-    const int e = static_cast<int>(bits >> 23); // biased exponent
-    if (e == 0)
-        return 0; // below 2^-126: floor(w 2^shift) == 0 for shift <= 63
-    const uint64_t mant = (bits & 0x7FFFFFu) | 0x800000u;
-    const int sh = e - 150 + static_cast<int>(shift); // w = mant * 2^(e-150)
-    if (sh >= 0)
-        return mant << sh;
-    if (sh <= -64)
-        return 0;
-    return mant >> (-sh);
-}
 
 // ------------------------------------------------------------ fused step
 
@@ -329,7 +120,7 @@ __device__ __forceinline__ void load_group(const Pf32Args &a, uint32_t i0,
 }
 
 template <bool First>
-__global__ void __launch_bounds__(kPfBlock) k_pf32_step(const Pf32Args a)
+__global__ void __launch_bounds__(kPfBlock, 5) k_pf32_step(const Pf32Args a)
 {
     const uint32_t t = a.sc->step;
     const int resampled = First ? 1 : a.sc->resampled;
@@ -619,7 +410,7 @@ __device__ __forceinline__ uint64_t q_at(
     return a.q ? a.q[i] : fixed_q(a.lw[i], M, a.shift);
 }
 
-// block sum of q over the block's chunk (two groups of four per thread in
+// block sum of q over the block's chunk (four groups of four per thread in
 // flight)
 __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
 {
@@ -629,16 +420,22 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
     uint32_t lo, hi;
     chunk_range(a.n, a.chunk, lo, hi);
     uint64_t acc = 0;
-    for (uint32_t base = lo; base < hi; base += 2 * kPfTile) {
+    constexpr int kG = 4;
+    for (uint32_t base = lo; base < hi; base += kG * kPfTile) {
+        if (a.q == nullptr && base + kG * kPfTile <= hi) {
+            float4 v[kG];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t i0 = base + h * kPfTile + threadIdx.x * 4;
-            if (i0 + 3 < hi && a.q == nullptr) {
-                const float4 v =
-                    __ldcg(reinterpret_cast<const float4 *>(a.lw + i0));
-                acc += fixed_q(v.x, M, a.shift) + fixed_q(v.y, M, a.shift) +
-                    fixed_q(v.z, M, a.shift) + fixed_q(v.w, M, a.shift);
-            } else {
+            for (int h = 0; h < kG; ++h)
+                v[h] = __ldcg(reinterpret_cast<const float4 *>(
+                    a.lw + base + h * kPfTile + threadIdx.x * 4));
+#pragma unroll
+            for (int h = 0; h < kG; ++h)
+                acc += fixed_q(v[h].x, M, a.shift) +
+                    fixed_q(v[h].y, M, a.shift) +
+                    fixed_q(v[h].z, M, a.shift) + fixed_q(v[h].w, M, a.shift);
+        } else {
+            for (int h = 0; h < kG; ++h) {
+                const uint32_t i0 = base + h * kPfTile + threadIdx.x * 4;
                 for (uint32_t i = i0; i < hi && i < i0 + 4; ++i)
                     acc += q_at(a, i, M);
             }
@@ -676,26 +473,56 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     uint32_t lo, hi;
     chunk_range(a.n, a.chunk, lo, hi);
     __shared__ uint64_t shq[kPfBlock / 32 + 1];
+    __shared__ QR shqr[kPfBlock / 32];
     __shared__ uint32_t she[kPfBlock / 32 + 1];
     __shared__ uint32_t lastF[kPfBlock / 32];
     __shared__ uint32_t carryF;
+    __shared__ QR start0;
     uint64_t offset, Q;
     block_prefix_of_parts(a.qpart, blockIdx.x, gridDim.x, offset, Q, shq);
     if (blockIdx.x == 0 && threadIdx.x == 0)
         a.sc->Q = Q;
     const PfScalars sc = *a.sc;
     const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
-    const CountP cp = make_count_params(Q, a.n, engine_word(sc, 0));
+    const bool checked = a.q != nullptr;
+    const uint32_t n = a.n;
+    const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
+    const float invQ = __frcp_rn(__ull2float_rn(Q));
+    WordCache wc;
+    wc.blk = ~0ull;
     uint32_t err = 0;
-    if (threadIdx.x == 0)
-        carryF = lo == 0 ? 0u : count_F(offset, cp, sys, sc, err);
+    if (threadIdx.x == 0) {
+        // the block's first CDF value, offset, by one 128-bit division
+        const uint64_t G = sys ? cp.G : 0;
+        long long j;
+        uint64_t r;
+        QR s;
+        if (cn_divmod(offset, G, cp, j, r, err)) {
+            s.j = static_cast<uint32_t>(j + 1);
+            s.r = r;
+        } else { // offset n < G < Q: X = -(G - offset n)
+            s.j = 0;
+            s.r = Q - (G - offset * static_cast<uint64_t>(n));
+        }
+        start0 = s;
+        carryF = lo == 0 ? 0u : f_of(s, sys, n, Q, sc, wc);
+    }
+    __syncthreads();
+    QR carry = start0;
     uint32_t empties = 0, copies = 0;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // the next tile's log-weights are loaded while this one is counted
+    float4 nxt = make_float4(0, 0, 0, 0);
+    if (!checked && lo + threadIdx.x * 4 + 3 < hi)
+        nxt = __ldcg(reinterpret_cast<const float4 *>(
+            a.lw + lo + threadIdx.x * 4));
     for (uint32_t base = lo; base < hi; base += kPfTile) {
         const uint32_t i0 = base + threadIdx.x * 4;
+        const float4 v = nxt;
+        if (!checked && i0 + kPfTile + 3 < hi)
+            nxt = __ldcg(reinterpret_cast<const float4 *>(a.lw + i0 + kPfTile));
         uint64_t q[4];
-        if (i0 + 3 < hi && a.q == nullptr) {
-            const float4 v = __ldcg(reinterpret_cast<const float4 *>(a.lw + i0));
+        if (i0 + 3 < hi && !checked) {
             q[0] = fixed_q(v.x, M, a.shift);
             q[1] = fixed_q(v.y, M, a.shift);
             q[2] = fixed_q(v.z, M, a.shift);
@@ -705,20 +532,25 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
             for (int k = 0; k < 4; ++k)
                 q[k] = (i0 + k < hi) ? q_at(a, i0 + k, M) : 0;
         }
-        const uint64_t tsum = q[0] + q[1] + q[2] + q[3];
-        uint64_t tile_total;
-        const uint64_t incl =
-            block_inclusive_scan(tsum, OpAdd(), uint64_t(0), shq, &tile_total);
-        uint64_t C = offset + incl - tsum;
+        // positions after each of this thread's particles, from its start
+        QR loc[4];
+        QR acc = {0, 0};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            qr_push(acc, q[k], n, checked, Q, invQ, cp, err);
+            loc[k] = acc;
+        }
+        QR tile_total;
+        const QR ex = block_exclusive_qr(acc, Q, shqr, &tile_total);
+        const QR st = qr_add(carry, ex, Q);
         uint32_t F[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            C += q[k];
             const uint32_t i = i0 + k;
-            if (i + 1 >= a.n)
-                F[k] = a.n; // the last particle takes the rest
+            if (i + 1 >= n)
+                F[k] = n; // the last particle takes the rest
             else if (i < hi)
-                F[k] = count_F(C, cp, sys, sc, err);
+                F[k] = f_of(qr_add(st, loc[k], Q), sys, n, Q, sc, wc);
             else
                 F[k] = 0;
         }
@@ -755,7 +587,7 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
         // the next tile starts after the last particle of this one
         if (threadIdx.x == blockDim.x - 1)
             carryF = F[3];
-        offset += tile_total;
+        carry = qr_add(carry, tile_total, Q);
         __syncthreads();
     }
     if (err)
@@ -766,6 +598,20 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
         a.epart[blockIdx.x] = empties;
         a.cpart[blockIdx.x] = copies;
     }
+}
+
+// counts of slots i0..i0+3 below hi (-1 past hi)
+__device__ __forceinline__ int4 load_rep4(
+    const int32_t *rep, uint32_t i0, uint32_t hi)
+{
+    if (i0 + 3 < hi)
+        return __ldcg(reinterpret_cast<const int4 *>(rep + i0));
+    int4 v;
+    v.x = i0 + 0 < hi ? rep[i0 + 0] : -1;
+    v.y = i0 + 1 < hi ? rep[i0 + 1] : -1;
+    v.z = i0 + 2 < hi ? rep[i0 + 2] : -1;
+    v.w = i0 + 3 < hi ? rep[i0 + 3] : -1;
+    return v;
 }
 
 // Slot assignment.  With c = copies before slot i and e = empty slots before
@@ -802,20 +648,14 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
             engine_advance(sc, jf < a.n ? jf + 1 : a.n);
         }
     }
+    // the next tile's counts are loaded while this one is scanned
+    int4 nxt = load_rep4(a.rep, lo + threadIdx.x * 4, hi);
     for (uint32_t base = lo; base < hi; base += kPfTile) {
         const uint32_t i0 = base + threadIdx.x * 4;
-        int32_t r[4];
-        if (i0 + 3 < hi) {
-            const int4 v = __ldcg(reinterpret_cast<const int4 *>(a.rep + i0));
-            r[0] = v.x;
-            r[1] = v.y;
-            r[2] = v.z;
-            r[3] = v.w;
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                r[k] = (i0 + k < hi) ? a.rep[i0 + k] : -1;
-        }
+        const int4 cur = nxt;
+        if (base + kPfTile < hi)
+            nxt = load_rep4(a.rep, i0 + kPfTile, hi);
+        const int32_t r[4] = {cur.x, cur.y, cur.z, cur.w};
         uint32_t tr = 0, te = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -877,6 +717,20 @@ __device__ __forceinline__ void rank_range(
         hi = K;
 }
 
+// marks k0..k0+3 below hi (0 past hi); k0 is a multiple of 4
+__device__ __forceinline__ uint4 load_marks4(
+    const uint32_t *marks, uint32_t k0, uint32_t hi)
+{
+    if (k0 + 3 < hi)
+        return __ldcg(reinterpret_cast<const uint4 *>(marks + k0));
+    uint4 v;
+    v.x = k0 + 0 < hi ? __ldcg(marks + k0 + 0) : 0u;
+    v.y = k0 + 1 < hi ? __ldcg(marks + k0 + 1) : 0u;
+    v.z = k0 + 2 < hi ? __ldcg(marks + k0 + 2) : 0u;
+    v.w = k0 + 3 < hi ? __ldcg(marks + k0 + 3) : 0u;
+    return v;
+}
+
 // per-block max of the marks over the block's share of the surplus ranks
 __global__ void __launch_bounds__(kPfBlock) k_rs32_markmax(const Rs32Args a)
 {
@@ -885,11 +739,13 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_markmax(const Rs32Args a)
     uint32_t lo, hi;
     rank_range(min(a.sc->nempty, a.n), lo, hi);
     uint32_t mx = 0;
-    for (uint32_t k0 = lo + threadIdx.x * 4; k0 < hi; k0 += 4 * blockDim.x) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k0 + k < hi)
-                mx = max(mx, __ldcg(a.marks + k0 + k));
+    const uint32_t step = 4 * blockDim.x;
+    for (uint32_t k0 = lo + threadIdx.x * 4; k0 < hi; k0 += 2 * step) {
+        const uint4 v = load_marks4(a.marks, k0, hi);
+        const uint4 w = k0 + step < hi ? load_marks4(a.marks, k0 + step, hi)
+                                       : make_uint4(0, 0, 0, 0);
+        mx = max(mx, max(max(v.x, v.y), max(v.z, v.w)));
+        mx = max(mx, max(max(w.x, w.y), max(w.z, w.w)));
     }
     __shared__ uint32_t sh[kPfBlock / 32 + 1];
     mx = block_reduce(mx, OpMax(), 0u, sh);
@@ -906,50 +762,66 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_fill(const Rs32Args a)
     uint32_t lo, hi;
     rank_range(min(a.sc->nempty, a.n), lo, hi);
     __shared__ uint32_t sh[kPfBlock / 32 + 1];
+    __shared__ uint32_t shl[kPfBlock / 32];
     uint32_t carry = 0;
     for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x)
         carry = max(carry, a.mpart[b]);
     carry = block_reduce(carry, OpMax(), 0u, sh);
-    for (uint32_t base = lo; base < hi; base += 4 * blockDim.x) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t step = 4 * blockDim.x;
+    // the next group's marks are loaded while this one is scanned
+    uint4 nxt = load_marks4(a.marks, lo + threadIdx.x * 4, hi);
+    uint32_t err = 0;
+    for (uint32_t base = lo; base < hi; base += step) {
         const uint32_t k0 = base + threadIdx.x * 4;
-        uint32_t mk[4], run[4];
+        const uint4 cur = nxt;
+        if (base + step < hi)
+            nxt = load_marks4(a.marks, k0 + step, hi);
+        const uint32_t mk[4] = {cur.x, cur.y, cur.z, cur.w};
+        uint32_t run[4];
         uint32_t tmax = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            mk[k] = k0 + k < hi ? __ldcg(a.marks + k0 + k) : 0u;
             tmax = max(tmax, mk[k]);
             run[k] = tmax;
         }
         uint32_t tot;
         const uint32_t incl = block_inclusive_scan(tmax, OpMax(), 0u, sh, &tot);
+        // exclusive max: the previous lane's inclusive value, or the
+        // previous warp's total for lane 0
         uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
-        if ((threadIdx.x & 31) == 0)
-            before = 0;
-        // the exclusive max of the block scan is not available per lane 0
-        // from the shuffle; recompute it from the inclusive value
-        __shared__ uint32_t shl[kPfBlock / 32];
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         if (lane == 31)
             shl[wid] = incl;
         __syncthreads();
-        if (lane == 0 && wid > 0)
-            before = shl[wid - 1];
+        if (lane == 0)
+            before = wid > 0 ? shl[wid - 1] : 0u;
         __syncthreads();
         before = max(before, carry);
+        uint32_t out[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            if (k0 + k < hi) {
-                const uint32_t rk = max(run[k], before);
-                if (rk == 0 || rk - 1 >= a.n)
-                    atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
-                else
-                    a.srcs[k0 + k] = rk - 1;
-                if (mk[k])
-                    a.marks[k0 + k] = 0;
-            }
+            const uint32_t rk = max(run[k], before);
+            if (k0 + k < hi && (rk == 0 || rk - 1 >= a.n))
+                err |= DEV_ERR_INTERNAL;
+            out[k] = rk - 1;
         }
+        if (k0 + 3 < hi) {
+            *reinterpret_cast<uint4 *>(a.srcs + k0) =
+                make_uint4(out[0], out[1], out[2], out[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k0 + k < hi)
+                    a.srcs[k0 + k] = out[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (mk[k] && k0 + k < hi)
+                a.marks[k0 + k] = 0;
         carry = max(carry, tot);
     }
+    if (err)
+        atomicOr(&a.sc->err, err);
 }
 
 // parent index of every slot from the encoded idx (reference layout)

@@ -1,0 +1,355 @@
+// Device helpers of the FP32 filters (single and batched): log-sum-exp
+// accumulation, the resampling engine's word stream, and exact counting of
+// systematic / stratified uniforms against a 64-bit fixed-point CDF.
+#pragma once
+
+#include "common.cuh"
+#include "pf32_types.cuh"
+
+namespace vsmc_cuda
+{
+
+// ------------------------------------------------------- small utilities
+
+__device__ __forceinline__ void lse_push(float v, float &m, float &s, float &s2)
+{
+    if (!(v > -INFINITY)) // -inf and NaN carry no weight
+        return;
+    if (v > m) {
+        const float e = __expf(m - v);
+        s = s * e + 1.0f;
+        s2 = s2 * e * e + 1.0f;
+        m = v;
+    } else {
+        const float e = __expf(v - m);
+        s += e;
+        s2 += e * e;
+    }
+}
+
+// merge (m2, t, t2) into (m, s, s2): max, sum exp(v - m), sum exp(2(v - m))
+__device__ __forceinline__ void lse_merge_f(
+    float &m, float &s, float &s2, float m2, float t, float t2)
+{
+    if (!(m2 > -INFINITY))
+        return;
+    if (!(m > -INFINITY)) {
+        m = m2;
+        s = t;
+        s2 = t2;
+        return;
+    }
+    if (m2 > m) {
+        const float e = __expf(m - m2);
+        s = s * e + t;
+        s2 = s2 * e * e + t2;
+        m = m2;
+    } else {
+        const float e = __expf(m2 - m);
+        s += t * e;
+        s2 += t2 * e * e;
+    }
+}
+
+// 64 x 64 -> 128 bit product, compared as (hi, lo)
+struct U128 {
+    uint64_t hi, lo;
+};
+
+__device__ __forceinline__ U128 mul_u64(uint64_t a, uint64_t b)
+{
+    return {__umul64hi(a, b), a * b};
+}
+
+__device__ __forceinline__ bool le_u128(const U128 &a, const U128 &b)
+{
+    return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo);
+}
+
+// word k (k >= 0) of the scalar stream of an engine at (key, ctr, index):
+// gen(ctr + (index + k) / 4)[(index + k) % 4]
+__device__ __forceinline__ uint32_t engine_word(const PfScalars &sc, uint64_t k)
+{
+    const uint64_t pos = static_cast<uint64_t>(sc.rindex) + k;
+    uint32_t c[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
+    ctr32_add(c, pos / 4);
+    const u32x4 b = philox4x32_10(c[0], c[1], c[2], c[3], sc.rkey[0], sc.rkey[1]);
+    const uint32_t i = static_cast<uint32_t>(pos % 4);
+    return i == 0 ? b.x : (i == 1 ? b.y : (i == 2 ? b.z : b.w));
+}
+
+// advance the engine by k >= 1 words
+__device__ __forceinline__ void engine_advance(PfScalars &sc, uint64_t k)
+{
+    if (k == 0)
+        return;
+    const uint64_t last = static_cast<uint64_t>(sc.rindex) + k - 1;
+    uint32_t c[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
+    ctr32_add(c, last / 4);
+    for (int i = 0; i < 4; ++i)
+        sc.rctr[i] = c[i];
+    sc.rindex = static_cast<uint32_t>(last % 4) + 1;
+}
+
+// Counting uniforms against the fixed-point CDF.
+//
+// Uniform j is u_j = (j + a_j 2^-32) / N with a 32-bit word a_j.  With the
+// integer CDF C_i and total Q, u_j <= C / Q  <=>  (j 2^32 + a_j) Q <= C N 2^32
+// <=>  j Q + G_j <= C N  with G_j = ceil(a_j Q / 2^32) < Q, since both sides
+// are integers.  The counts follow from one exact floor(C N / Q) with its
+// remainder per CDF value.
+struct CountP {
+    uint64_t Q;  // CDF total
+    uint64_t G;  // systematic: ceil(a Q / 2^32) (one word for every j)
+    uint32_t n;
+    int sh;      // Q >> sh < 2^24
+    float scale; // n / (Q >> sh)
+};
+
+__device__ __forceinline__ uint64_t ceil_aq(uint32_t a, uint64_t Q)
+{
+    const uint64_t hi = __umul64hi(static_cast<uint64_t>(a), Q); // < 2^32
+    const uint64_t lo = static_cast<uint64_t>(a) * Q;
+    return ((hi << 32) | (lo >> 32)) + ((lo & 0xFFFFFFFFull) != 0 ? 1 : 0);
+}
+
+__device__ __forceinline__ CountP make_count_params(
+    uint64_t Q, uint32_t n, uint32_t a_sys)
+{
+    CountP p;
+    p.Q = Q;
+    p.G = ceil_aq(a_sys, Q);
+    p.n = n;
+    const int bits = 64 - __clzll(static_cast<long long>(Q));
+    p.sh = bits > 24 ? bits - 24 : 0;
+    p.scale = static_cast<float>(n) /
+        __uint2float_rz(static_cast<uint32_t>(Q >> p.sh));
+    return p;
+}
+
+// j = floor((C n - G) / Q) and r = (C n - G) - j Q; false if C n < G
+__device__ __forceinline__ bool cn_divmod(uint64_t C, uint64_t G,
+    const CountP &p, long long &j, uint64_t &r, uint32_t &err)
+{
+    uint64_t xh = __umul64hi(C, static_cast<uint64_t>(p.n));
+    uint64_t xl = C * static_cast<uint64_t>(p.n);
+    if (xl < G) {
+        if (xh == 0)
+            return false;
+        --xh;
+    }
+    xl -= G;
+    // estimate within a few units of the answer
+    const float f =
+        __uint2float_rz(static_cast<uint32_t>(C >> p.sh)) * p.scale;
+    long long jj = static_cast<long long>(__float2int_rz(f)) - 2;
+    if (jj < 0)
+        jj = 0;
+    if (jj > static_cast<long long>(p.n))
+        jj = static_cast<long long>(p.n);
+    // R = X - jj Q, 128-bit; walk down while negative, up while >= Q
+    const uint64_t ph = __umul64hi(static_cast<uint64_t>(jj), p.Q);
+    const uint64_t pl = static_cast<uint64_t>(jj) * p.Q;
+    uint64_t rl = xl - pl;
+    uint64_t rh = xh - ph - (xl < pl ? 1 : 0);
+    int guard = 0;
+    while (static_cast<long long>(rh) < 0) { // X < jj Q
+        --jj;
+        const uint64_t t = rl + p.Q;
+        rh += (t < rl ? 1 : 0);
+        rl = t;
+        if (++guard > 64) {
+            err |= DEV_ERR_BOUND;
+            break;
+        }
+    }
+    guard = 0;
+    while (rh != 0 || rl >= p.Q) {
+        ++jj;
+        rh -= (rl < p.Q ? 1 : 0);
+        rl -= p.Q;
+        if (++guard > 64) {
+            err |= DEV_ERR_BOUND;
+            break;
+        }
+    }
+    j = jj;
+    r = rl;
+    return true;
+}
+
+// floor(w * 2^shift) for w = exp(lw - M) in (0, 1], by integer operations on
+// the float's bits (no 64-bit conversion instruction)
+__device__ __forceinline__ uint64_t fixed_q(float lw, float M, uint32_t shift)
+{
+    if (!(lw > -INFINITY))
+        return 0;
+    const float w = fminf(__expf(lw - M), 1.0f);
+    const uint32_t bits = __float_as_uint(w);
+    const int e = static_cast<int>(bits >> 23); // biased exponent
+    if (e == 0)
+        return 0; // below 2^-126: floor(w 2^shift) == 0 for shift <= 63
+    const uint64_t mant = (bits & 0x7FFFFFu) | 0x800000u;
+    const int sh = e - 150 + static_cast<int>(shift); // w = mant * 2^(e-150)
+    if (sh >= 0)
+        return mant << sh;
+    if (sh <= -64)
+        return 0;
+    return mant >> (-sh);
+}
+
+// A CDF value's position against the uniforms, X = C n - G (G = 0 for
+// stratified), kept as X = (j - 1) Q + r with 0 <= r < Q.  Then F(C) = j
+// (systematic, clamped to n), or j - 1 plus one if uniform j - 1 lies at or
+// below C / Q (stratified).  A step of the CDF adds q n to X, so positions
+// follow from one 128-bit division per block, then only additions.
+struct QR {
+    uint32_t j;
+    uint64_t r;
+};
+
+__device__ __forceinline__ QR qr_add(const QR &a, const QR &b, uint64_t Q)
+{
+    QR c;
+    c.j = a.j + b.j;
+    c.r = a.r + b.r; // both below Q < 2^63: no wrap
+    if (c.r >= Q) {
+        c.r -= Q;
+        ++c.j;
+    }
+    return c;
+}
+
+// Bring r below Q, adding the quotient to j.  A float estimate held below
+// the true quotient removes most of it; each round cuts r / Q by about 2^18,
+// so a few rounds finish (bounded; error bit if the bound is hit).
+__device__ __forceinline__ void qr_reduce(
+    uint64_t &r, uint32_t &j, uint64_t Q, float invQ, uint32_t &err)
+{
+    int guard = 0;
+    while (r >= Q) {
+        const float est = fmaf(__uint2float_rz(static_cast<uint32_t>(r >> 32)),
+                              4294967296.0f,
+                              __uint2float_rz(static_cast<uint32_t>(r))) *
+            invQ;
+        uint32_t d = 1;
+        if (est > 4.0f)
+            d = __float2uint_rz(est * 0.999998f) - 2;
+        r -= static_cast<uint64_t>(d) * Q;
+        j += d;
+        if (++guard > 16) {
+            err |= DEV_ERR_BOUND;
+            break;
+        }
+    }
+}
+
+// q n added to a position.  Filter weights satisfy q <= 2^K and
+// n <= 2^(63 - K), so q n <= 2^63 and r + q n < 2^64; integer weights given
+// by a caller are checked and take the 128-bit division when they do not.
+__device__ __forceinline__ void qr_push(QR &acc, uint64_t q, uint32_t n,
+    bool checked, uint64_t Q, float invQ, const CountP &cp, uint32_t &err)
+{
+    if (checked) {
+        const uint64_t plo = static_cast<uint64_t>(static_cast<uint32_t>(q)) * n;
+        const uint64_t phi = (q >> 32) * n;
+        const uint64_t lo = plo + (phi << 32);
+        const uint64_t hi = (phi >> 32) + (lo < plo ? 1 : 0);
+        const uint64_t s = acc.r + lo;
+        if (hi != 0 || s < lo) {
+            long long jj;
+            uint64_t rr;
+            cn_divmod(q, 0, cp, jj, rr, err);
+            acc = qr_add(acc, QR{static_cast<uint32_t>(jj), rr}, Q);
+            return;
+        }
+        acc.r = s;
+    } else {
+        acc.r += q * n;
+    }
+    qr_reduce(acc.r, acc.j, Q, invQ, err);
+}
+
+// word k of the resampling engine's stream, caching the last Philox block
+struct WordCache {
+    uint64_t blk;
+    u32x4 w;
+};
+
+__device__ __forceinline__ uint32_t cached_word(
+    const PfScalars &sc, uint64_t k, WordCache &c)
+{
+    const uint64_t pos = static_cast<uint64_t>(sc.rindex) + k;
+    const uint64_t b = pos >> 2;
+    if (b != c.blk) {
+        uint32_t ctr[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
+        ctr32_add(ctr, b);
+        c.w = philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], sc.rkey[0],
+            sc.rkey[1]);
+        c.blk = b;
+    }
+    const uint32_t i = static_cast<uint32_t>(pos & 3);
+    return i == 0 ? c.w.x : (i == 1 ? c.w.y : (i == 2 ? c.w.z : c.w.w));
+}
+
+// F from a position (see QR)
+__device__ __forceinline__ uint32_t f_of(const QR &x, bool sys, uint32_t n,
+    uint64_t Q, const PfScalars &sc, WordCache &wc)
+{
+    if (sys)
+        return x.j < n ? x.j : n;
+    if (x.j == 0)
+        return 0;
+    const uint32_t j0 = x.j - 1;
+    if (j0 >= n)
+        return n;
+    return j0 + (ceil_aq(cached_word(sc, j0, wc), Q) <= x.r ? 1u : 0u);
+}
+
+// Block-wide exclusive scan of positions over kBlock threads; *total gets
+// the block's sum; sh holds kBlock / 32 entries.
+template <int kBlock = kPfBlock>
+__device__ __forceinline__ QR block_exclusive_qr(
+    QR v, uint64_t Q, QR *sh, QR *total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int nw = kBlock / 32;
+    QR x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        QR o;
+        o.j = __shfl_up_sync(0xFFFFFFFFu, x.j, d);
+        o.r = __shfl_up_sync(0xFFFFFFFFu, x.r, d);
+        if (lane >= d)
+            x = qr_add(o, x, Q);
+    }
+    if (lane == 31)
+        sh[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        QR w = lane < nw ? sh[lane] : QR{0, 0};
+#pragma unroll
+        for (int d = 1; d < nw; d <<= 1) {
+            QR o;
+            o.j = __shfl_up_sync(0xFFFFFFFFu, w.j, d);
+            o.r = __shfl_up_sync(0xFFFFFFFFu, w.r, d);
+            if (lane >= d)
+                w = qr_add(o, w, Q);
+        }
+        if (lane < nw)
+            sh[lane] = w;
+    }
+    __syncthreads();
+    QR ex;
+    ex.j = __shfl_up_sync(0xFFFFFFFFu, x.j, 1);
+    ex.r = __shfl_up_sync(0xFFFFFFFFu, x.r, 1);
+    if (lane == 0)
+        ex = QR{0, 0};
+    if (wid > 0)
+        ex = qr_add(sh[wid - 1], ex, Q);
+    *total = sh[nw - 1];
+    __syncthreads();
+    return ex;
+}
+
+} // namespace vsmc_cuda

@@ -59,6 +59,8 @@ __device__ __forceinline__ u32x4 particle_block(
 }
 
 // FP32 standard-normal pair: Box-Muller, (0,1] radius uniform, [0,1) angle.
+// The angle 2 pi u goes through sincospi of the exact 2 u (no range
+// reduction, and no rounding of 2 pi u).
 __device__ __forceinline__ void normal_pair_f(uint32_t w0, uint32_t w1,
     float &z1, float &z2)
 {
@@ -66,7 +68,7 @@ __device__ __forceinline__ void normal_pair_f(uint32_t w0, uint32_t w1,
     const float u2 = u01_co_f(w1);
     const float r = sqrtf(-2.0f * logf(u1));
     float sv, cv;
-    sincosf(kPi2f * u2, &sv, &cv);
+    sincospif(2.0f * u2, &sv, &cv);
     z1 = r * cv;
     z2 = r * sv;
 }
@@ -84,6 +86,7 @@ __device__ __forceinline__ void normal_pair_d(uint32_t w0, uint32_t w1,
     z2 = __dmul_rn(u1, sv);
 }
 
+// FP32: log1p(qx) + log1p(qy) as one log1p((1 + qx)(1 + qy) - 1)
 __device__ __forceinline__ float cv_loglik(
     const CvConst<float> &c, float ox, float oy, float x, float y)
 {
@@ -91,7 +94,7 @@ __device__ __forceinline__ float cv_loglik(
     const float zy = (oy - y) * c.inv_s;
     const float qx = zx * zx * c.inv_nu;
     const float qy = zy * zy * c.inv_nu;
-    return c.c2 - c.half_nu1 * (log1pf(qx) + log1pf(qy));
+    return c.c2 - c.half_nu1 * log1pf(fmaf(qx, qy, qx + qy));
 }
 
 __device__ __forceinline__ double cv_loglik(
