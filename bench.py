@@ -258,7 +258,7 @@ def run_batched(args):
     torch.cuda.set_stream(stream)
     b = vc.FilterBatch(n, T, seeds, models, scheme=vc.STRATIFIED,
                        stream=ctypes.c_void_p(stream.cuda_stream))
-    obs = torch.zeros(2 * b.total_steps, dtype=torch.float64, device="cuda")
+    obs = torch.zeros(b.obs_len(), dtype=torch.float64, device="cuda")
     b.simulate(obs.data_ptr())
     tune_ms = b.autotune(obs.data_ptr(), steps=args.tune_steps)
     shape = b.shape()
@@ -282,7 +282,7 @@ def run_batched(args):
     hist = b.history()
     # end to end: pinned host observations in, histories out, every run
     TT = b.total_steps
-    obs_h = torch.empty(2 * TT, dtype=torch.float64, pin_memory=True)
+    obs_h = torch.empty(b.obs_len(), dtype=torch.float64, pin_memory=True)
     obs_h.copy_(obs.cpu())
     mean_h = torch.empty(2 * TT, dtype=torch.float64, pin_memory=True)
     ess_h = torch.empty(TT, dtype=torch.float64, pin_memory=True)
@@ -382,6 +382,127 @@ def run_batched(args):
     return 0
 
 
+def run_learned(args):
+    """Learned proposal vs bootstrap on the bearings-only model: R filters
+    (independent seeds) on one simulated observation sequence; log-evidence
+    SD over the R runs and the error of the posterior mean against an FP64
+    oracle reference; the headline is the bootstrap-equivalent
+    particle-step rate of the learned filter at equal log-evidence SD."""
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import vsmc_gb300 as vc
+    vc.lib()
+    m = vc.bearings_model()
+    T, R = 200, args.replicates
+    obs = torch.zeros(T, dtype=torch.float64, device="cuda")
+    truth = torch.zeros(4 * T, dtype=torch.float64, device="cuda")
+    vc.call("vsmc_cuda_bearings_simulate", 0, T, ctypes.byref(m),
+            truth.data_ptr(), obs.data_ptr(), None)
+    obs_np = obs.cpu().numpy()
+    # ---- training on simulated trajectories
+    prop = vc.Proposal(seed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = prop.train(m, seed=11, ntraj=args.train_traj, T=T,
+                        batch=args.train_batch, steps=args.train_steps,
+                        lr=args.lr)
+    train_s = time.perf_counter() - t0
+    # ---- reference posterior mean (FP64 oracle bootstrap, host cores)
+    ref_mean = None
+    if not args.no_cpu_baseline:
+        from oracle import binding
+        port = binding.port()
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        Nref = args.ref_particles
+        mean = np.zeros(2 * T)
+        ess = np.zeros(T)
+        res = np.zeros(T, np.int32)
+        logz = np.zeros(T)
+        t0 = time.perf_counter()
+        port.vo_bearings_pf_run(64, Nref, T, 123, 1, 0.5,
+                                ctypes.byref(binding.bearings_model()),
+                                P(obs_np), None, 0, P(mean), P(ess), P(res),
+                                P(logz))
+        ref_s = time.perf_counter() - t0
+        ref_mean = mean.reshape(T, 2)
+
+    obs_all = torch.from_numpy(np.tile(obs_np, R)).cuda()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def measure(N, packed):
+        b = vc.FilterBatch([N] * R, [T] * R, np.arange(R) + 1000,
+                           bearings=True, packed=packed,
+                           stream=ctypes.c_void_p(stream.cuda_stream))
+        for _ in range(args.warmup):
+            b.run_device(obs_all.data_ptr())
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            b.run_device(obs_all.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        out = b.history()
+        b.close()
+        logz = np.array([o["logz"][-1] for o in out])
+        means = np.stack([o["mean"] for o in out])  # R x T x 2
+        err = None
+        if ref_mean is not None:
+            err = float(np.sqrt(np.mean((means.mean(axis=0) - ref_mean) ** 2)))
+        return {"N": N, "ms": ms, "rate": N * T * R / (ms / 1000.0),
+                "logz_sd": float(logz.std()), "logz_mean": float(logz.mean()),
+                "mean_rmse_vs_ref": err}
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    learned = measure(args.learned_particles, prop.packed.data_ptr())
+    boot = [measure(N, None) for N in args.boot_particles]
+    clocks.stop()
+    # bootstrap N at the learned filter's log-evidence SD (log-log fit)
+    lx = np.log([b["N"] for b in boot])
+    ly = np.log([b["logz_sd"] for b in boot])
+    slope, icpt = np.polyfit(lx, ly, 1)
+    n_eq = float(np.exp((np.log(learned["logz_sd"]) - icpt) / slope))
+    # bootstrap wall time at n_eq (linear in N between the measured points)
+    ms_eq = float(np.interp(n_eq, [b["N"] for b in boot],
+                            [b["ms"] for b in boot],
+                            left=None, right=None))
+    if n_eq > boot[-1]["N"]:
+        ms_eq = boot[-1]["ms"] * n_eq / boot[-1]["N"]
+    value = n_eq * T * R / (learned["ms"] / 1000.0)
+    line = {
+        "metric": "particle-steps/sec at fixed log-evidence SD "
+                  "(learned proposal, bootstrap-equivalent)",
+        "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": learned["ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 network (fp32 accumulate), fp32 state",
+        "data": "synthetic bearings-only track (seed 0), T=200",
+        "config": {
+            "workload": f"{R} filters x N={args.learned_particles} learned "
+                        f"proposal vs bootstrap N in {args.boot_particles}",
+            "train": {"trajectories": args.train_traj, "steps": T,
+                      "batch": args.train_batch, "lr": args.lr,
+                      "adam_steps": len(losses), "seconds": train_s,
+                      "loss_first": float(losses[:50].mean()),
+                      "loss_last": float(losses[-50:].mean())},
+            "learned": learned, "bootstrap": boot,
+            "bootstrap_n_at_equal_sd": n_eq,
+            "bootstrap_ms_at_equal_sd": ms_eq,
+            "speedup_at_equal_sd": ms_eq / learned["ms"],
+            "reference": {"particles": args.ref_particles, "fp64": True,
+                          "seconds": ref_s} if ref_mean is not None else None,
+        },
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -392,7 +513,16 @@ def main():
     ap.add_argument("--T", type=int, default=T_STEPS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="single",
-                    choices=["single", "batched"])
+                    choices=["single", "batched", "learned"])
+    ap.add_argument("--replicates", type=int, default=1024)
+    ap.add_argument("--learned-particles", type=int, default=1 << 12)
+    ap.add_argument("--boot-particles", type=int, nargs="+",
+                    default=[1 << 12, 1 << 14, 1 << 16])
+    ap.add_argument("--train-traj", type=int, default=1 << 20)
+    ap.add_argument("--train-batch", type=int, default=1 << 16)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--ref-particles", type=int, default=1 << 18)
     ap.add_argument("--filters", type=int, default=4096)
     ap.add_argument("--tune-steps", type=int, default=60)
     args = ap.parse_args()
@@ -401,6 +531,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "learned":
+        return run_learned(args)
 
     import torch
     rank, world, local = dist_setup(args.gpus)

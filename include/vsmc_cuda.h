@@ -352,6 +352,119 @@ int vsmc_cuda_pf_use_graph(vsmc_cuda_pf *pf, int on);
  * (smp/backend_omp.hpp:93-105, core/weight.hpp:168-173). */
 int vsmc_cuda_pf_launch_step_kernel(vsmc_cuda_pf *pf);
 
+/* ------------------------------------- bearings-only model, proposal */
+
+/* Bearings-only tracking: state (x, y, vx, vy); constant velocity with
+ * continuous white-noise acceleration of spectral density q per axis
+ * (Q = q [[dt^3/3, dt^2/2], [dt^2/2, dt]]); bearing observation
+ * atan2(y, x) + N(0, sigma_z^2) from a sensor at the origin; prior
+ * N((x0, y0, vx0, vy0), diag(sd_pos0^2, sd_pos0^2, sd_vel0^2, sd_vel0^2)).
+ * No reference counterpart (the reference's pf example is the position
+ * model above). */
+typedef struct {
+    double dt, q, sigma_z, x0, y0, vx0, vy0, sd_pos0, sd_vel0;
+} vsmc_cuda_bearings_model;
+
+/* Simulate T steps from CounterEngine(seed) (Philox4x32): prior and
+ * transition noise from fresh NormalDistribution<double> pairs (x axis, then
+ * y axis), bearing noise from one NormalDistribution<double>(0, sigma_z)
+ * kept for the run.  truth: T x 4 (may be NULL), obs: T (device). */
+int vsmc_cuda_bearings_simulate(uint32_t seed, size_t T,
+    const vsmc_cuda_bearings_model *model, double *truth, double *obs,
+    void *stream);
+
+/* The proposal network: inputs (x / 10, y / 10, vx, vy, sin z, cos z),
+ * two hidden layers of 64 (GELU, tanh form), outputs (m, l): the mean and
+ * diagonal log-variance of the whitened transition noise nu (x = F x' + L nu,
+ * L = chol(Q)).  Parameters: FP32, *nparams floats (W1[64][6], b1[64],
+ * W2[64][64], b2[64], W3[8][64], b3[8]); the packed copy (BF16 operand
+ * fragments + FP32 biases, *npacked 32-bit words) is what the kernels read. */
+int vsmc_cuda_mlp_sizes(size_t *nparams, size_t *npacked);
+int vsmc_cuda_mlp_init(uint32_t seed, float *params, void *stream);
+int vsmc_cuda_mlp_pack(const float *params, uint32_t *packed, void *stream);
+/* out[B][8] = network(feat[B][6]) (BF16 operands, FP32 accumulation). */
+int vsmc_cuda_mlp_forward(const uint32_t *packed, size_t B, const float *feat,
+    float *out, void *stream);
+/* Mean loss 0.5 sum_d [(nu_d - m_d)^2 exp(-l_d) + l_d] over B rows
+ * (loss_dev: 1 double, may be NULL) and its gradient with respect to the
+ * parameters (grad_dev: nparams floats); the sum over rows is in a fixed
+ * order. */
+int vsmc_cuda_mlp_loss_grad(const uint32_t *packed, size_t B,
+    const float *feat, const float *nu, double *loss_dev, float *grad_dev,
+    void *stream);
+/* Train params in place with Adam (lr): ntraj trajectories simulated from
+ * the model (seed) for T steps give ntraj * (T - 1) stored (x_{t-1}, z_t,
+ * nu_t) samples; then `steps` Adam steps on minibatches of `batch` samples
+ * drawn uniformly with replacement.  loss_host (may be NULL) receives the
+ * mean loss of each minibatch (`steps` values).  Synchronizes. */
+int vsmc_cuda_mlp_train(const vsmc_cuda_bearings_model *model, uint32_t seed,
+    size_t ntraj, size_t T, size_t batch, size_t steps, double lr,
+    float *params, double *loss_host, void *stream);
+/* One FP32 move + weight increment on caller-owned SoA state [4][n]: t == 0
+ * draws the prior; t > 0 draws nu ~ N(0, I) (packed == NULL, bootstrap) or
+ * nu ~ N(m, diag(exp(l))) from the network (packed != NULL).  lw_inc gets
+ * log g(z | x) (+ log N(nu; 0, I) - log N(nu; m, exp(l)) for the learned
+ * proposal).  Particle streams: Philox4x32 key {t, seed}, counter
+ * {0, i, 0, 0}, pre-incremented, two Box-Muller pairs. */
+int vsmc_cuda_bearings_move_f32(size_t n, size_t t, uint32_t seed,
+    const vsmc_cuda_bearings_model *model, double z, const uint32_t *packed,
+    float *state, float *lw_inc, void *stream);
+
+/* ----------------------------------------------------- batched filters */
+
+typedef struct vsmc_cuda_batch vsmc_cuda_batch; /* opaque */
+
+/* nfilters independent precision-32 bootstrap filters run together.  Filter
+ * f has n[f] >= 2 particles, horizon T[f] >= 1, model models[f] and seed
+ * seeds[f] (host arrays).  Per step, one persistent kernel moves, weights and
+ * reduces the particles of every filter still running, and one kernel
+ * resamples (one block per filter) those whose ESS fell below
+ * threshold * n[f]; a whole run is one CUDA graph.  Filter f draws the
+ * streams and makes the counts of a single vsmc_cuda_pf with seed seeds[f]
+ * (the order of its FP64 sums differs).  Observations and histories are the
+ * filters' blocks concatenated in the caller's order: filter f's T[f] steps
+ * start at entry T[0] + ... + T[f-1] (2 doubles per entry for observations
+ * and means).  scheme: stratified or systematic.  No reference counterpart:
+ * the reference runs one Sampler<T> per filter (core/sampler.hpp:107-114). */
+int vsmc_cuda_batch_create(vsmc_cuda_batch **batch, size_t nfilters,
+    const uint32_t *n, const uint32_t *T, const vsmc_cuda_cv_model *models,
+    const uint32_t *seeds, int scheme, double threshold, void *stream);
+/* Bearings-only filters (vsmc_cuda_bearings_model each): the bootstrap
+ * (packed == NULL) or the learned proposal (packed: the packed proposal
+ * network, device, kept by pointer for the batch's lifetime).  Observations
+ * are one bearing per step (filter f's block starts at entry
+ * T[0] + ... + T[f-1]).  The learned kind has a fixed kernel shape (16
+ * particles per warp; set_shape and autotune refuse it). */
+int vsmc_cuda_batch_create_bearings(vsmc_cuda_batch **batch, size_t nfilters,
+    const uint32_t *n, const uint32_t *T,
+    const vsmc_cuda_bearings_model *models, const uint32_t *seeds,
+    const uint32_t *packed, int scheme, double threshold, void *stream);
+int vsmc_cuda_batch_destroy(vsmc_cuda_batch *batch);
+int vsmc_cuda_batch_stream(vsmc_cuda_batch *batch, void **stream);
+/* Each filter's truth (4 per step, may be NULL) and observations simulated
+ * from its own model and seed, as vsmc_cuda_cv_simulate /
+ * vsmc_cuda_bearings_simulate do for one filter (device outputs,
+ * concatenated layout).  Synchronizes. */
+int vsmc_cuda_batch_simulate(vsmc_cuda_batch *batch, double *truth_dev,
+    double *obs_dev);
+/* Run every filter to its horizon over device observations (asynchronous). */
+int vsmc_cuda_batch_run_device(vsmc_cuda_batch *batch, const double *obs_dev);
+/* Host observations in, histories out (the end-to-end entry; synchronizes). */
+int vsmc_cuda_batch_run(vsmc_cuda_batch *batch, const double *obs_host,
+    double *mean_host, double *ess_host, int *resampled_host,
+    double *logz_host);
+/* Copy the histories of the last run to host (synchronizes; NULL skips). */
+int vsmc_cuda_batch_history(vsmc_cuda_batch *batch, double *mean_host,
+    double *ess_host, int *resampled_host, double *logz_host);
+/* Step-kernel shape: particles per thread (1, 2, 4) x threads (128, 256). */
+int vsmc_cuda_batch_set_shape(vsmc_cuda_batch *batch, int ppt, int block);
+int vsmc_cuda_batch_get_shape(vsmc_cuda_batch *batch, int *ppt, int *block);
+/* Time the first `steps` steps of the batch over obs_dev for each shape and
+ * keep the fastest; ms_host (6 floats, may be NULL) receives the times in
+ * the order (1,128) (2,128) (4,128) (1,256) (2,256) (4,256).  Synchronizes. */
+int vsmc_cuda_batch_autotune(vsmc_cuda_batch *batch, const double *obs_dev,
+    int steps, float *ms_host);
+
 /* One move + log-likelihood step on caller-owned SoA state (kernel-level
  * parity entry point): t == 0 draws the prior, t > 0 propagates.  ll
  * receives the per-particle log-likelihood of obs (host, 2 doubles). */

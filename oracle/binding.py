@@ -35,6 +35,20 @@ def default_model():
 
 _MP = ctypes.POINTER(Model)
 
+
+class BModel(ctypes.Structure):
+    """vo_bmodel: the bearings-only tracking model."""
+    _fields_ = [("dt", F64), ("q", F64), ("sigma_z", F64), ("x0", F64),
+                ("y0", F64), ("vx0", F64), ("vy0", F64), ("sd_pos0", F64),
+                ("sd_vel0", F64)]
+
+
+def bearings_model():
+    return BModel(0.1, 1.0, 0.005, 10.0, 10.0, 0.0, 0.0, 1.0, 1.0)
+
+
+_BMP = ctypes.POINTER(BModel)
+
 PORT_PROTOTYPES = {
     "vo_philox4x32_words": (None, [VP, VP, SZ, VP, I32]),
     "vo_threefry4x64_words": (None, [VP, VP, SZ, VP, I32]),
@@ -69,6 +83,13 @@ PORT_PROTOTYPES = {
     "vo_pf_init_f64": (None, [SZ, U32, _MP, VP, VP, VP]),
     "vo_pf_init_f32": (None, [SZ, U32, _MP, VP, VP, VP]),
     "vo_student_t_norm_const": (F64, [F64, F64]),
+    "vo_bearings_simulate": (None, [U32, SZ, _BMP, VP, VP]),
+    "vo_bearings_move_f32": (None, [SZ, SZ, U32, _BMP, F64, VP, VP, VP]),
+    "vo_mlp_forward": (None, [VP, SZ, VP, VP]),
+    "vo_mlp_loss_grad": (None, [VP, SZ, VP, VP, VP, VP]),
+    "vo_mlp_set_rounding": (None, [I32]),
+    "vo_bearings_pf_run": (I32, [I32, SZ, SZ, U32, I32, F64, _BMP, VP, VP,
+                                 I32, VP, VP, VP, VP]),
     "vo_engine_run": (None, [I32, VP, VP, SZ, I32, SZ, F64, F64, VP, VP,
                              VP]),
 }

@@ -1368,3 +1368,390 @@ void vo_engine_run(int kind, const uint64_t key[4], const uint64_t ctr[4],
         *index_out = e.t.index;
     }
 }
+
+/* =====================================================================
+ * Bearings-only tracking and the learned proposal.  Project-written test
+ * infrastructure with no reference counterpart: the simulator (FP64, the
+ * reference's CounterEngine / NormalDistribution draws), the FP32 particle
+ * move and weight increment (bootstrap or learned proposal), the proposal
+ * network's forward pass and loss gradient in FP64 with the device's BF16
+ * operand rounding reproduced, and bearings filters for reference runs.
+ *
+ * Model: per axis [p; v]_t = [p + dt v; v]_{t-1} + L nu, L = chol(Q),
+ * Q = q [[dt^3/3, dt^2/2], [dt^2/2, dt]]; bearing atan2(y, x) + N(0, sz^2).
+ * Proposals draw the whitened noise nu (bootstrap N(0, I); learned
+ * N(m, diag exp(l)) from the network) and weight by
+ * log g(z | x) + log N(nu; 0, I) - log N(nu; m, diag exp(l)).
+ * ===================================================================== */
+static void vo_bchol(const vo_bmodel *m, double *l11, double *l21, double *l22)
+{
+    const double q11 = m->q * m->dt * m->dt * m->dt / 3;
+    const double q12 = m->q * m->dt * m->dt / 2;
+    const double q22 = m->q * m->dt;
+    *l11 = sqrt(q11);
+    *l21 = q12 / *l11;
+    *l22 = sqrt(q22 - *l21 * *l21);
+}
+
+void vo_bearings_simulate(
+    uint32_t seed, size_t T, const vo_bmodel *m, double *truth, double *obs)
+{
+    vo_eng e;
+    e.kind = 0;
+    const uint32_t key[2] = {seed, 0};
+    const uint32_t ctr[4] = {0, 0, 0, 0};
+    vo_philox_init(&e.p, key, ctr);
+    vo_normal_d zn = {0, m->sigma_z, 0, 0};
+    double l11, l21, l22;
+    vo_bchol(m, &l11, &l21, &l22);
+    double x, y, vx, vy, a, b, c, d;
+    vo_pair_d(&e.p, m->sd_pos0, &a, &b);
+    x = m->x0 + a;
+    y = m->y0 + b;
+    vo_pair_d(&e.p, m->sd_vel0, &a, &b);
+    vx = m->vx0 + a;
+    vy = m->vy0 + b;
+    for (size_t t = 0; t != T; ++t) {
+        if (t > 0) {
+            vo_pair_d(&e.p, 1.0, &a, &b);
+            vo_pair_d(&e.p, 1.0, &c, &d);
+            x = (x + m->dt * vx) + l11 * a;
+            vx = vx + (l21 * a + l22 * b);
+            y = (y + m->dt * vy) + l11 * c;
+            vy = vy + (l21 * c + l22 * d);
+        }
+        if (truth) {
+            truth[4 * t + 0] = x;
+            truth[4 * t + 1] = y;
+            truth[4 * t + 2] = vx;
+            truth[4 * t + 3] = vy;
+        }
+        obs[t] = atan2(y, x) + vo_normal_d_draw(&zn, &e);
+    }
+}
+
+/* 1: round the network's tensor-core operands to BF16 and its FP32 values
+ * to float as the device does; 0: exact FP64 (for finite-difference checks
+ * of the gradient) */
+static int vo_mlp_device_rounding = 1;
+
+void vo_mlp_set_rounding(int on)
+{
+    vo_mlp_device_rounding = on;
+}
+
+/* float rounding of a device FP32 value (identity in exact mode) */
+static double vo_rf(double x)
+{
+    return vo_mlp_device_rounding ? (double)(float)x : x;
+}
+
+/* BF16 round to nearest even (finite inputs; identity in exact mode) */
+static double vo_bf16d(double x);
+
+static float vo_bf16(float x)
+{
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    u &= 0xFFFF0000u;
+    memcpy(&x, &u, 4);
+    return x;
+}
+
+static double vo_gelu(double x, double *grad)
+{
+    const double k0 = -1.5957691216057308, k1 = -0.0713548162726009;
+    const double e = exp(x * (k1 * x * x + k0));
+    const double s = 1 / (1 + e);
+    if (grad)
+        *grad = s - x * s * (1 - s) * (3 * k1 * x * x + k0);
+    return x * s;
+}
+
+#define VO_IN 6
+#define VO_HID 64
+#define VO_OUT 8
+#define VO_W1 0
+#define VO_B1 (VO_W1 + VO_HID * VO_IN)
+#define VO_W2 (VO_B1 + VO_HID)
+#define VO_B2 (VO_W2 + VO_HID * VO_HID)
+#define VO_W3 (VO_B2 + VO_HID)
+#define VO_B3 (VO_W3 + VO_OUT * VO_HID)
+#define VO_NP (VO_B3 + VO_OUT)
+
+static double vo_bf16d(double x)
+{
+    return vo_mlp_device_rounding ? (double)vo_bf16((float)x) : x;
+}
+
+typedef struct {
+    double a0[VO_IN];          /* bf16 inputs */
+    double pre1[VO_HID];       /* hidden pre-activations */
+    double a1[VO_HID];         /* bf16 gelu(pre1) */
+    double pre2[VO_HID];
+    double a2[VO_HID];
+    double out[VO_OUT];
+} vo_mlp_row;
+
+static float p_w3(const float *p, int d, int j)
+{
+    return p[VO_W3 + d * VO_HID + j];
+}
+
+/* one row of the forward pass: BF16 weights and activations, FP64 sums */
+static void vo_mlp_row_forward(const float *p, const float *f, vo_mlp_row *r)
+{
+    for (int k = 0; k < VO_IN; ++k)
+        r->a0[k] = vo_bf16d(f[k]);
+    for (int j = 0; j < VO_HID; ++j) {
+        double s = 0;
+        for (int k = 0; k < VO_IN; ++k)
+            s += vo_bf16d(p[VO_W1 + j * VO_IN + k]) * r->a0[k];
+        r->pre1[j] = s + p[VO_B1 + j];
+        r->a1[j] = vo_bf16d(vo_gelu(r->pre1[j], NULL));
+    }
+    for (int j = 0; j < VO_HID; ++j) {
+        double s = 0;
+        for (int k = 0; k < VO_HID; ++k)
+            s += vo_bf16d(p[VO_W2 + j * VO_HID + k]) * r->a1[k];
+        r->pre2[j] = s + p[VO_B2 + j];
+        r->a2[j] = vo_bf16d(vo_gelu(r->pre2[j], NULL));
+    }
+    for (int d = 0; d < VO_OUT; ++d) {
+        double s = 0;
+        for (int k = 0; k < VO_HID; ++k)
+            s += vo_bf16d(p[VO_W3 + d * VO_HID + k]) * r->a2[k];
+        r->out[d] = s + p[VO_B3 + d];
+    }
+}
+
+void vo_mlp_forward(const float *params, size_t B, const float *feat,
+    float *out)
+{
+    _Pragma("omp parallel for schedule(static)")
+    for (size_t i = 0; i < B; ++i) {
+        vo_mlp_row r;
+        vo_mlp_row_forward(params, feat + 6 * i, &r);
+        for (int d = 0; d < VO_OUT; ++d)
+            out[8 * i + d] = (float)r.out[d];
+    }
+}
+
+/* mean loss 0.5 sum_d [(nu_d - m_d)^2 exp(-l_d) + l_d] and its gradient;
+ * the backward data path rounds its operands to BF16 as the device does */
+void vo_mlp_loss_grad(const float *params, size_t B, const float *feat,
+    const float *nu, double *loss, double *grad)
+{
+    for (int i = 0; i < VO_NP; ++i)
+        grad[i] = 0;
+    double L = 0;
+    const double inv_b = 1.0 / (double)B;
+    for (size_t i = 0; i < B; ++i) {
+        vo_mlp_row r;
+        vo_mlp_row_forward(params, feat + 6 * i, &r);
+        double dout[VO_OUT];
+        for (int d = 0; d < 4; ++d) {
+            const double res = nu[4 * i + d] - r.out[d];
+            const double el = exp(-r.out[4 + d]);
+            L += 0.5 * (res * res * el + r.out[4 + d]);
+            dout[d] = vo_rf(-res * el * inv_b);
+            dout[4 + d] = vo_rf(0.5 * (1 - res * res * el) * inv_b);
+        }
+        double dp2[VO_HID], dp1[VO_HID];
+        for (int j = 0; j < VO_HID; ++j) {
+            double s = 0;
+            for (int d = 0; d < VO_OUT; ++d)
+                s += vo_bf16d(p_w3(params, d, j)) * vo_bf16d(dout[d]);
+            double gg;
+            vo_gelu(r.pre2[j], &gg);
+            dp2[j] = vo_rf(s * gg);
+        }
+        for (int k = 0; k < VO_HID; ++k) {
+            double s = 0;
+            for (int j = 0; j < VO_HID; ++j)
+                s += vo_bf16d(params[VO_W2 + j * VO_HID + k]) *
+                    vo_bf16d(dp2[j]);
+            double gg;
+            vo_gelu(r.pre1[k], &gg);
+            dp1[k] = vo_rf(s * gg);
+        }
+        for (int d = 0; d < VO_OUT; ++d) {
+            grad[VO_B3 + d] += dout[d];
+            for (int k = 0; k < VO_HID; ++k)
+                grad[VO_W3 + d * VO_HID + k] += dout[d] * r.a2[k];
+        }
+        for (int j = 0; j < VO_HID; ++j) {
+            grad[VO_B2 + j] += dp2[j];
+            for (int k = 0; k < VO_HID; ++k)
+                grad[VO_W2 + j * VO_HID + k] += dp2[j] * r.a1[k];
+            grad[VO_B1 + j] += dp1[j];
+            for (int k = 0; k < VO_IN; ++k)
+                grad[VO_W1 + j * VO_IN + k] += dp1[j] * r.a0[k];
+        }
+    }
+    *loss = L * inv_b;
+}
+
+static inline double vo_bwrap(double d)
+{
+    return d - VO_PI_2 * nearbyint(d / VO_PI_2);
+}
+
+void vo_bearings_move_f32(size_t N, size_t t, uint32_t seed,
+    const vo_bmodel *m, double z, const float *params, float *state,
+    float *lw_inc)
+{
+    double l11d, l21d, l22d;
+    vo_bchol(m, &l11d, &l21d, &l22d);
+    const float l11 = (float)l11d, l21 = (float)l21d, l22 = (float)l22d;
+    const float dt = (float)m->dt;
+    const float inv_sz = (float)(1 / m->sigma_z);
+    const float ll_c = (float)(-log(m->sigma_z * sqrt(2 * VO_PI)));
+    const float zf = (float)z;
+    const float sz = sinf(zf), cz = cosf(zf);
+    _Pragma("omp parallel for schedule(static)")
+    for (size_t i = 0; i < N; ++i) {
+        vo_philox e;
+        vo_particle_engine(&e, t, seed, i);
+        float ev[4];
+        vo_pair_f(&e, 1.0f, &ev[0], &ev[1]);
+        vo_pair_f(&e, 1.0f, &ev[2], &ev[3]);
+        float x = state[i], y = state[N + i];
+        float vx = state[2 * N + i], vy = state[3 * N + i];
+        float lq = 0;
+        if (t == 0) {
+            x = (float)m->x0 + (float)m->sd_pos0 * ev[0];
+            y = (float)m->y0 + (float)m->sd_pos0 * ev[1];
+            vx = (float)m->vx0 + (float)m->sd_vel0 * ev[2];
+            vy = (float)m->vy0 + (float)m->sd_vel0 * ev[3];
+        } else {
+            float nu[4] = {ev[0], ev[1], ev[2], ev[3]};
+            if (params) {
+                const float f[6] = {x * 0.1f, y * 0.1f, vx, vy, sz, cz};
+                vo_mlp_row r;
+                vo_mlp_row_forward(params, f, &r);
+                for (int d = 0; d < 4; ++d) {
+                    float l = (float)r.out[4 + d];
+                    l = l < -12.0f ? -12.0f : (l > 4.0f ? 4.0f : l);
+                    nu[d] = (float)r.out[d] + expf(0.5f * l) * ev[d];
+                    lq += 0.5f * (ev[d] * ev[d] - nu[d] * nu[d]) + 0.5f * l;
+                }
+            }
+            const float dx = l11 * nu[0], dvx = l21 * nu[0] + l22 * nu[1];
+            const float dy = l11 * nu[2], dvy = l21 * nu[2] + l22 * nu[3];
+            x = (x + dt * vx) + dx;
+            y = (y + dt * vy) + dy;
+            vx = vx + dvx;
+            vy = vy + dvy;
+        }
+        state[i] = x;
+        state[N + i] = y;
+        state[2 * N + i] = vx;
+        state[3 * N + i] = vy;
+        float d = zf - atan2f(y, x);
+        d -= (float)VO_PI_2 * nearbyintf(d / (float)VO_PI_2);
+        const float s = d * inv_sz;
+        lw_inc[i] = ll_c - 0.5f * s * s + lq;
+    }
+}
+
+static void vo_bearings_move_f64(size_t N, size_t t, uint32_t seed,
+    const vo_bmodel *m, double z, double *state, double *ll)
+{
+    double l11, l21, l22;
+    vo_bchol(m, &l11, &l21, &l22);
+    const double ll_c = -log(m->sigma_z * sqrt(2 * VO_PI));
+    _Pragma("omp parallel for schedule(static)")
+    for (size_t i = 0; i < N; ++i) {
+        vo_philox e;
+        vo_particle_engine(&e, t, seed, i);
+        double a, b, c, d;
+        double x = state[i], y = state[N + i];
+        double vx = state[2 * N + i], vy = state[3 * N + i];
+        if (t == 0) {
+            vo_pair_d(&e, m->sd_pos0, &a, &b);
+            vo_pair_d(&e, m->sd_vel0, &c, &d);
+            x = m->x0 + a;
+            y = m->y0 + b;
+            vx = m->vx0 + c;
+            vy = m->vy0 + d;
+        } else {
+            vo_pair_d(&e, 1.0, &a, &b);
+            vo_pair_d(&e, 1.0, &c, &d);
+            x = (x + m->dt * vx) + l11 * a;
+            vx = vx + (l21 * a + l22 * b);
+            y = (y + m->dt * vy) + l11 * c;
+            vy = vy + (l21 * c + l22 * d);
+        }
+        state[i] = x;
+        state[N + i] = y;
+        state[2 * N + i] = vx;
+        state[3 * N + i] = vy;
+        const double s = vo_bwrap(z - atan2(y, x)) / m->sigma_z;
+        ll[i] = ll_c - 0.5 * s * s;
+    }
+}
+
+int vo_bearings_pf_run(int precision, size_t N, size_t T, uint32_t seed,
+    int scheme, double threshold, const vo_bmodel *m, const double *obs,
+    const float *params, int threads, double *mean_out, double *ess_out,
+    int *resampled_out, double *logz_out)
+{
+#ifdef _OPENMP
+    int saved_threads = omp_get_max_threads();
+    if (threads > 0)
+        omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    const size_t esz = precision == 32 ? sizeof(float) : sizeof(double);
+    void *state = calloc(4 * N, esz);
+    double *W = (double *)malloc(sizeof(double) * N);
+    double *ll = (double *)malloc(sizeof(double) * N);
+    float *llf = (float *)malloc(sizeof(float) * N);
+    int *rep = (int *)malloc(sizeof(int) * N);
+    int *idx = (int *)malloc(sizeof(int) * N);
+    vo_philox reng;
+    const uint32_t rkey[2] = {0, seed};
+    const uint32_t rctr[4] = {0, 0, 1, 0};
+    vo_philox_init(&reng, rkey, rctr);
+    double ess = vo_weight_set_equal(N, W);
+    double logz = 0;
+    for (size_t t = 0; t != T; ++t) {
+        if (precision == 32) {
+            vo_bearings_move_f32(
+                N, t, seed, m, obs[t], params, (float *)state, llf);
+            for (size_t i = 0; i != N; ++i)
+                ll[i] = (double)llf[i];
+        } else {
+            vo_bearings_move_f64(N, t, seed, m, obs[t], (double *)state, ll);
+        }
+        double mx = -INFINITY;
+        for (size_t i = 0; i != N; ++i)
+            if (mx < ll[i])
+                mx = ll[i];
+        double s = 0;
+        for (size_t i = 0; i != N; ++i)
+            s += W[i] * exp(ll[i] - mx);
+        logz += mx + log(s);
+        for (size_t i = 0; i != N; ++i)
+            W[i] = log(W[i]) + ll[i];
+        ess = vo_weight_post_set_log(N, W);
+        logz_out[t] = logz;
+        ess_out[t] = ess;
+        resampled_out[t] = vo_pf_resample(
+            scheme, threshold, N, &reng, W, &ess, rep, idx, state, precision);
+        vo_pf_mean(N, state, precision, W, mean_out + 2 * t);
+    }
+    free(state);
+    free(W);
+    free(ll);
+    free(llf);
+    free(rep);
+    free(idx);
+#ifdef _OPENMP
+    omp_set_num_threads(saved_threads);
+#endif
+    return 0;
+}

@@ -137,6 +137,33 @@ void vo_pf_init_f32(size_t N, uint32_t seed, const vo_model *m,
     const double obs[2], float *state, float *ll_out);
 double vo_student_t_norm_const(double nu, double s);
 
+/* ---------------------------- bearings-only model, learned proposal */
+/* project-written (no reference counterpart); see vsmc_oracle.c */
+typedef struct {
+    double dt, q, sigma_z, x0, y0, vx0, vy0, sd_pos0, sd_vel0;
+} vo_bmodel;
+
+void vo_bearings_simulate(
+    uint32_t seed, size_t T, const vo_bmodel *m, double *truth, double *obs);
+/* FP32 move + weight increment (params NULL: bootstrap) on SoA [4][N] */
+void vo_bearings_move_f32(size_t N, size_t t, uint32_t seed,
+    const vo_bmodel *m, double z, const float *params, float *state,
+    float *lw_inc);
+/* proposal network: forward (out[B][8]) and mean loss + gradient (FP64,
+ * BF16 operand rounding as on the device) */
+void vo_mlp_forward(const float *params, size_t B, const float *feat,
+    float *out);
+void vo_mlp_loss_grad(const float *params, size_t B, const float *feat,
+    const float *nu, double *loss, double *grad);
+/* 1 (default): device rounding (BF16 operands, FP32 values); 0: exact */
+void vo_mlp_set_rounding(int on);
+/* bearings filter: precision 64 (bootstrap, FP64 state) or 32 (FP32 state,
+ * bootstrap or learned proposal with params) */
+int vo_bearings_pf_run(int precision, size_t N, size_t T, uint32_t seed,
+    int scheme, double threshold, const vo_bmodel *m, const double *obs,
+    const float *params, int threads, double *mean_out, double *ess_out,
+    int *resampled_out, double *logz_out);
+
 /* test helper: k scalar words, then one bulk / u01 / normal batch operation */
 void vo_engine_run(int kind, const uint64_t key[4], const uint64_t ctr[4],
     size_t k, int op, size_t n, double mean, double sd, void *out,

@@ -68,6 +68,20 @@ class CvModel(ctypes.Structure):
                 ("nu", F64), ("sd_pos0", F64), ("sd_vel0", F64)]
 
 
+class BearingsModel(ctypes.Structure):
+    """vsmc_cuda_bearings_model."""
+    _fields_ = [("dt", F64), ("q", F64), ("sigma_z", F64), ("x0", F64),
+                ("y0", F64), ("vx0", F64), ("vy0", F64), ("sd_pos0", F64),
+                ("sd_vel0", F64)]
+
+
+def bearings_model():
+    """The bearings-only benchmark model: dt 0.1, acceleration spectral
+    density 1, bearing noise sd 0.005 rad, target starting near (10, 10)
+    (position sd 1, velocity sd 1)."""
+    return BearingsModel(0.1, 1.0, 0.005, 10.0, 10.0, 0.0, 0.0, 1.0, 1.0)
+
+
 def default_model():
     """The benchmark tracking model: dt 0.1, acceleration sd 1, Student-t
     (nu 10, scale 0.5) observations, prior position sd 2, velocity sd 1."""
@@ -76,6 +90,7 @@ def default_model():
 
 _RNGP = ctypes.POINTER(Rng)
 _MODELP = ctypes.POINTER(CvModel)
+_BMODELP = ctypes.POINTER(BearingsModel)
 
 # name -> (restype, argtypes)
 PROTOTYPES = {
@@ -138,7 +153,19 @@ PROTOTYPES = {
     "vsmc_cuda_pf_launch_step_kernel": (I32, [VP]),
     "vsmc_cuda_batch_create": (
         I32, [ctypes.POINTER(VP), SZ, VP, VP, VP, VP, I32, F64, VP]),
+    "vsmc_cuda_batch_create_bearings": (
+        I32, [ctypes.POINTER(VP), SZ, VP, VP, VP, VP, VP, I32, F64, VP]),
     "vsmc_cuda_batch_destroy": (I32, [VP]),
+    "vsmc_cuda_bearings_simulate": (I32, [U32, SZ, _BMODELP, VP, VP, VP]),
+    "vsmc_cuda_mlp_sizes": (I32, [ctypes.POINTER(SZ), ctypes.POINTER(SZ)]),
+    "vsmc_cuda_mlp_init": (I32, [U32, VP, VP]),
+    "vsmc_cuda_mlp_pack": (I32, [VP, VP, VP]),
+    "vsmc_cuda_mlp_forward": (I32, [VP, SZ, VP, VP, VP]),
+    "vsmc_cuda_mlp_loss_grad": (I32, [VP, SZ, VP, VP, VP, VP, VP]),
+    "vsmc_cuda_mlp_train": (I32, [_BMODELP, U32, SZ, SZ, SZ, SZ, F64, VP,
+                                  VP, VP]),
+    "vsmc_cuda_bearings_move_f32": (I32, [SZ, SZ, U32, _BMODELP, F64, VP, VP,
+                                          VP, VP]),
     "vsmc_cuda_batch_stream": (I32, [VP, ctypes.POINTER(VP)]),
     "vsmc_cuda_batch_simulate": (I32, [VP, VP, VP]),
     "vsmc_cuda_batch_run_device": (I32, [VP, VP]),
@@ -225,20 +252,33 @@ class FilterBatch:
     CvModel (default: the default model for every filter)."""
 
     def __init__(self, n, T, seeds, models=None, scheme=STRATIFIED,
-                 threshold=0.5, stream=None):
+                 threshold=0.5, stream=None, bearings=False, packed=None):
+        """bearings=True: bearings-only filters (models: BearingsModel),
+        with the learned proposal when packed (device pointer of the packed
+        network) is given; observations are then one bearing per step."""
         import numpy as np
         self.n = np.ascontiguousarray(n, dtype=np.uint32)
         self.T = np.ascontiguousarray(T, dtype=np.uint32)
         self.seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        self.bearings = bearings
+        self.obs_dim = 1 if bearings else 2
         nf = len(self.n)
-        if models is None:
-            models = [default_model() for _ in range(nf)]
-        self.models = (CvModel * nf)(*models)
         self.offsets = np.concatenate([[0], np.cumsum(self.T.astype(np.int64))])
         h = VP()
-        call("vsmc_cuda_batch_create", ctypes.byref(h), nf,
-             self.n.ctypes.data, self.T.ctypes.data, self.models,
-             self.seeds.ctypes.data, scheme, threshold, stream)
+        if bearings:
+            if models is None:
+                models = [bearings_model() for _ in range(nf)]
+            self.models = (BearingsModel * nf)(*models)
+            call("vsmc_cuda_batch_create_bearings", ctypes.byref(h), nf,
+                 self.n.ctypes.data, self.T.ctypes.data, self.models,
+                 self.seeds.ctypes.data, packed, scheme, threshold, stream)
+        else:
+            if models is None:
+                models = [default_model() for _ in range(nf)]
+            self.models = (CvModel * nf)(*models)
+            call("vsmc_cuda_batch_create", ctypes.byref(h), nf,
+                 self.n.ctypes.data, self.T.ctypes.data, self.models,
+                 self.seeds.ctypes.data, scheme, threshold, stream)
         self.handle = h
 
     @property
@@ -264,6 +304,10 @@ class FilterBatch:
         s = VP()
         call("vsmc_cuda_batch_stream", self.handle, ctypes.byref(s))
         return s.value
+
+    def obs_len(self):
+        """Doubles in the concatenated observation array."""
+        return self.obs_dim * self.total_steps
 
     def simulate(self, obs_dev_ptr, truth_dev_ptr=None):
         call("vsmc_cuda_batch_simulate", self.handle, truth_dev_ptr,
@@ -293,7 +337,8 @@ class FilterBatch:
         return self._split(mean, ess, res, logz)
 
     def run(self, obs):
-        """Whole run through host buffers; obs is (sum T, 2) float64."""
+        """Whole run through host buffers; obs: the concatenated
+        observations (sum T x 2 positions, or sum T bearings)."""
         import numpy as np
         obs = np.ascontiguousarray(obs, dtype=np.float64)
         TT = self.total_steps
@@ -321,6 +366,47 @@ class FilterBatch:
         call("vsmc_cuda_batch_autotune", self.handle, obs_dev_ptr, steps,
              ms.ctypes.data)
         return ms
+
+
+class Proposal:
+    """The proposal network's FP32 parameters and packed copy (device)."""
+
+    def __init__(self, seed=0):
+        import torch
+        npar, npk = SZ(), SZ()
+        call("vsmc_cuda_mlp_sizes", ctypes.byref(npar), ctypes.byref(npk))
+        self.nparams, self.npacked = npar.value, npk.value
+        self.params = torch.zeros(self.nparams, dtype=torch.float32,
+                                  device="cuda")
+        self.packed = torch.zeros(self.npacked, dtype=torch.int32,
+                                  device="cuda")
+        call("vsmc_cuda_mlp_init", seed, self.params.data_ptr(), None)
+        self.pack()
+
+    def pack(self):
+        import torch
+        call("vsmc_cuda_mlp_pack", self.params.data_ptr(),
+             self.packed.data_ptr(), None)
+        torch.cuda.synchronize()
+
+    def train(self, model, seed, ntraj, T, batch, steps, lr):
+        """Adam on simulated trajectories; returns the minibatch losses."""
+        import numpy as np
+        losses = np.zeros(steps)
+        call("vsmc_cuda_mlp_train", ctypes.byref(model), seed, ntraj, T,
+             batch, steps, lr, self.params.data_ptr(), losses.ctypes.data,
+             None)
+        self.pack()
+        return losses
+
+    def loss(self, feat_dev_ptr, nu_dev_ptr, B):
+        """Mean loss on B rows (device arrays)."""
+        import torch
+        loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+        grad = torch.zeros(self.nparams, dtype=torch.float32, device="cuda")
+        call("vsmc_cuda_mlp_loss_grad", self.packed.data_ptr(), B,
+             feat_dev_ptr, nu_dev_ptr, loss.data_ptr(), grad.data_ptr(), None)
+        return float(loss.cpu()[0])
 
 
 class ParticleFilter:

@@ -26,7 +26,9 @@
 // No reference counterpart: the reference would run one Sampler<T> per
 // filter (core/sampler.hpp:107-114) with the pf example's move
 // (example/pf/include/pf.hpp:154-170).
+#include "bearings.cuh"
 #include "cv_sim.cuh"
+#include "mlp.cuh"
 #include "pf32_dev.cuh"
 #include "pf_model.cuh"
 
@@ -53,8 +55,16 @@ struct BFilter {
     uint32_t seed;
     uint32_t shift;    // fixed-point K = 63 - ceil(log2 n)
     uint32_t pad;
-    CvConst<float> c;
+    union {
+        CvConst<float> c;   // position / Student-t model
+        BearingsConst bc;   // bearings-only model
+    };
 };
+
+// filter kinds
+constexpr int kKindCv = 0;       // CV + Student-t positions, bootstrap
+constexpr int kKindBearings = 1; // bearings-only, bootstrap
+constexpr int kKindLearned = 2;  // bearings-only, learned proposal
 
 struct BatchArgs {
     const BFilter *flt;
@@ -72,6 +82,7 @@ struct BatchArgs {
     double *h_mean, *h_ess, *h_logz;
     int *h_res;
     uint32_t *step; // global step counter
+    const uint32_t *packed; // proposal network (learned kind)
     uint32_t nfilters, tmax;
     int scheme;
     double threshold;
@@ -140,11 +151,178 @@ __device__ __forceinline__ void store_run(float *p, const float (&v)[kPPT])
     }
 }
 
-// One global step of every running filter.  A filter at t < T moves and
-// weights its particles; at t == T it only records the weighted mean of its
-// final particles.  The last tile of a filter to finish combines the
-// filter's tile records in FP64.
-template <int kBlock, int kPPT, bool First>
+// The tile's record (FP32 within a warp, FP64 across warps) and, in the
+// block that finishes a filter's last tile, the filter's FP64 combination:
+// ESS, log-evidence increment, resampling decision and histories (or, at
+// t == T, the last weighted mean).  All threads of the block call it.
+template <int kBlock, bool First>
+__device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
+    const BFilter &F, PfScalars &S, uint32_t t, bool mon, float m, float s,
+    float s2, float sx, float sy, float sw, float *shm, double (*sh)[kBlock / 32],
+    float *shmax, bool &is_last)
+{
+    constexpr int kW = kBlock / 32;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const float om = __shfl_xor_sync(0xFFFFFFFFu, m, d);
+        const float os = __shfl_xor_sync(0xFFFFFFFFu, s, d);
+        const float os2 = __shfl_xor_sync(0xFFFFFFFFu, s2, d);
+        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, d);
+        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, d);
+        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, d);
+        lse_merge_f(m, s, s2, om, os, os2);
+    }
+    if (lane == 0) {
+        shm[wid] = m;
+        sh[0][wid] = s;
+        sh[1][wid] = s2;
+        sh[2][wid] = sx;
+        sh[3][wid] = sy;
+        sh[4][wid] = sw;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float mb = -INFINITY;
+        for (int w = 0; w < kW; ++w)
+            mb = fmaxf(mb, shm[w]);
+        MovePartial p = {0, 0, 0, mb, 0, 0};
+        for (int w = 0; w < kW; ++w) {
+            p.sx += sh[2][w];
+            p.sy += sh[3][w];
+            p.sw += sh[4][w];
+            if (shm[w] > -INFINITY) {
+                const double fct = __expf(shm[w] - mb);
+                p.s += sh[0][w] * fct;
+                p.s2 += sh[1][w] * fct * fct;
+            }
+        }
+        a.part[tile] = p;
+        __threadfence();
+        is_last = atomicAdd(&S.done, 1u) == F.ntiles - 1;
+    }
+    __syncthreads();
+    if (!is_last)
+        return;
+    // ---- the filter's last tile: combine its tile records
+    __threadfence();
+    float M = -INFINITY;
+    for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock)
+        M = fmaxf(M, static_cast<float>(a.part[F.tile0 + b].m));
+    M = block_reduce(M, OpMax(), -INFINITY, shmax);
+    double S1 = 0, S2 = 0, SX = 0, SY = 0, SW = 0;
+    for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock) {
+        const MovePartial p = a.part[F.tile0 + b];
+        SX += p.sx;
+        SY += p.sy;
+        SW += p.sw;
+        if (p.m > -INFINITY) {
+            const double fct = __expf(static_cast<float>(p.m) - M);
+            S1 += p.s * fct;
+            S2 += p.s2 * fct * fct;
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        S1 += __shfl_xor_sync(0xFFFFFFFFu, S1, d);
+        S2 += __shfl_xor_sync(0xFFFFFFFFu, S2, d);
+        SX += __shfl_xor_sync(0xFFFFFFFFu, SX, d);
+        SY += __shfl_xor_sync(0xFFFFFFFFu, SY, d);
+        SW += __shfl_xor_sync(0xFFFFFFFFu, SW, d);
+    }
+    __syncthreads();
+    if (lane == 0) {
+        sh[0][wid] = S1;
+        sh[1][wid] = S2;
+        sh[2][wid] = SX;
+        sh[3][wid] = SY;
+        sh[4][wid] = SW;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double T1 = 0, T2 = 0, TX = 0, TY = 0, TW = 0;
+        for (int w = 0; w < kW; ++w) {
+            T1 += sh[0][w];
+            T2 += sh[1][w];
+            TX += sh[2][w];
+            TY += sh[3][w];
+            TW += sh[4][w];
+        }
+        if (mon) {
+            a.h_mean[2 * (F.hist_off + F.T - 1) + 0] = TX / TW;
+            a.h_mean[2 * (F.hist_off + F.T - 1) + 1] = TY / TW;
+            S.resampled = 0; // finished: nothing left to resample
+            S.gather = 0;
+        } else {
+            const double prev_mass = First ? static_cast<double>(F.n) : TW;
+            if (!First) {
+                a.h_mean[2 * (F.hist_off + t - 1) + 0] = TX / TW;
+                a.h_mean[2 * (F.hist_off + t - 1) + 1] = TY / TW;
+            }
+            const double ess = T1 * T1 / T2;
+            const double M1 = static_cast<double>(M);
+            S.logz += M1 + log(T1) - log(prev_mass);
+            if (!(T1 > 0) || !(ess > 0))
+                S.err |= DEV_ERR_NONFINITE;
+            const int flag =
+                ess < a.threshold * static_cast<double>(F.n) ? 1 : 0;
+            a.h_ess[F.hist_off + t] = ess;
+            a.h_logz[F.hist_off + t] = S.logz;
+            a.h_res[F.hist_off + t] = flag;
+            S.M = M1;
+            S.S = T1;
+            S.ess = ess;
+            S.resampled = flag;
+            S.gather = 0;
+            S.step = t + 1;
+        }
+        S.done = 0;
+    }
+}
+
+// slot i's source inside the filter after a resample (bounds-checked)
+__device__ __forceinline__ uint32_t batch_source(
+    const BatchArgs &a, const BFilter &F, PfScalars &S, uint32_t i)
+{
+    const int32_t v = a.idx[F.off + i];
+    const uint32_t e = static_cast<uint32_t>(-(v + 1));
+    uint32_t src = v >= 0 ? static_cast<uint32_t>(v)
+                          : (e < F.n ? __ldcg(a.srcs + F.off + e) : F.n);
+    if (src >= F.n) {
+        atomicOr(&S.err, DEV_ERR_INTERNAL);
+        src = 0;
+    }
+    return src;
+}
+
+// bootstrap body of the bearings-only model (prior at t == 0)
+template <bool First>
+__device__ __forceinline__ void bearings_one(const BearingsConst &c,
+    uint32_t seed, uint32_t i, uint32_t t, float z, int resampled,
+    float Mprev, float &x, float &y, float &vx, float &vy, float &lw, float &m,
+    float &s, float &s2, float &sx, float &sy, float &sw)
+{
+    float e[4];
+    bearings_normals(t, seed, i, e);
+    float lw_old = 0.0f;
+    if (First) {
+        bearings_prior(c, e, x, y, vx, vy);
+    } else {
+        lw_old = resampled ? 0.0f : lw - Mprev;
+        const float wo = resampled ? 1.0f : __expf(lw_old);
+        sx += wo * x;
+        sy += wo * y;
+        sw += wo;
+        bearings_step(c, e, x, y, vx, vy);
+    }
+    lw = lw_old + bearings_loglik(c, z, x, y);
+    lse_push(lw, m, s, s2);
+}
+
+// One global step of every running filter (bootstrap kinds).  A filter at
+// t < T moves and weights its particles; at t == T it only records the
+// weighted mean of its final particles.
+template <int kBlock, int kPPT, bool First, int Kind>
 __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
 {
     constexpr uint32_t kTile = kBlock * kPPT;
@@ -155,7 +333,6 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
     __shared__ double sh[5][kW];
     __shared__ float shmax[kW + 1];
     __shared__ bool is_last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint32_t f = a.tile_filter[tile];
         const BFilter F = a.flt[f];
@@ -166,8 +343,12 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
         const float Mprev = First ? 0.0f : static_cast<float>(S.M);
         float ox = 0.0f, oy = 0.0f;
         if (!mon) {
-            ox = static_cast<float>(a.obs[2 * (F.obs_off + t) + 0]);
-            oy = static_cast<float>(a.obs[2 * (F.obs_off + t) + 1]);
+            if (Kind == kKindCv) {
+                ox = static_cast<float>(a.obs[2 * (F.obs_off + t) + 0]);
+                oy = static_cast<float>(a.obs[2 * (F.obs_off + t) + 1]);
+            } else {
+                ox = static_cast<float>(a.obs[F.obs_off + t]);
+            }
         }
         float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
         const uint32_t i0 = (tile - F.tile0) * kTile + threadIdx.x * kPPT;
@@ -188,18 +369,8 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
                 for (int k = 0; k < kPPT; ++k) {
                     const uint32_t i = i0 + k;
                     if (i < F.n) {
-                        uint32_t src = i;
-                        if (gather) {
-                            const int32_t v = a.idx[F.off + i];
-                            const uint32_t e = static_cast<uint32_t>(-(v + 1));
-                            src = v >= 0 ? static_cast<uint32_t>(v)
-                                         : (e < F.n ? __ldcg(a.srcs + F.off + e)
-                                                    : F.n);
-                            if (src >= F.n) {
-                                atomicOr(&S.err, DEV_ERR_INTERNAL);
-                                src = 0;
-                            }
-                        }
+                        const uint32_t src =
+                            gather ? batch_source(a, F, S, i) : i;
                         X[k] = a.ax[F.off + src];
                         Y[k] = a.ay[F.off + src];
                         VX[k] = a.avx[F.off + src];
@@ -230,10 +401,16 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
         } else {
 #pragma unroll
             for (int k = 0; k < kPPT; ++k)
-                if (i0 + k < F.n)
-                    batch_one<First>(F.c, F.seed, i0 + k, t, ox, oy,
-                        resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k], m,
-                        s, s2, sx, sy, sw);
+                if (i0 + k < F.n) {
+                    if (Kind == kKindCv)
+                        batch_one<First>(F.c, F.seed, i0 + k, t, ox, oy,
+                            resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k],
+                            m, s, s2, sx, sy, sw);
+                    else
+                        bearings_one<First>(F.bc, F.seed, i0 + k, t, ox,
+                            resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k],
+                            m, s, s2, sx, sy, sw);
+                }
             const uint32_t g0 = F.off + i0;
             if (full) {
                 store_run<kPPT>(a.bx + g0, X);
@@ -253,123 +430,111 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
                     }
             }
         }
+        tile_finish<kBlock, First>(a, tile, F, S, t, mon, m, s, s2, sx, sy,
+            sw, shm, sh, shmax, is_last);
+        __syncthreads();
+    }
+}
 
-        // ---- tile record: FP32 within a warp, FP64 across warps
+constexpr int kLearnBlock = 128;                    // 4 warps
+constexpr uint32_t kLearnTile = kLearnBlock / 2;     // 16 particles a warp
+
+// One global step of the learned-proposal filters.  Each warp evaluates the
+// proposal network for 16 particles on the tensor cores; lanes 4g and
+// 4g + 1 then move particles g and g + 8 of the warp's 16.
+template <bool First>
+__global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
+    const BatchArgs a)
+{
+    constexpr int kW = kLearnBlock / 32;
+    __shared__ __align__(16) uint32_t sp[kPackedWords];
+    __shared__ float shm[kW];
+    __shared__ double sh[5][kW];
+    __shared__ float shmax[kW + 1];
+    __shared__ bool is_last;
+    const uint32_t t = *a.step;
+    const uint32_t ntiles = t <= a.tmax ? a.active[t] : 0u;
+    if (!First)
+        load_packed(sp, a.packed);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int g = lane >> 2, q = lane & 3;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t f = a.tile_filter[tile];
+        const BFilter F = a.flt[f];
+        const BearingsConst &c = F.bc;
+        PfScalars &S = a.st[f];
+        const bool mon = !First && t == F.T;
+        const int resampled = First ? 1 : S.resampled;
+        const bool gather = First ? false : (S.gather != 0);
+        const float Mprev = First ? 0.0f : static_cast<float>(S.M);
+        const float z = mon ? 0.0f : static_cast<float>(a.obs[F.obs_off + t]);
+        const uint32_t i = (tile - F.tile0) * kLearnTile + 16 * wid + g +
+            (q == 1 ? 8u : 0u);
+        const bool mine = q < 2 && i < F.n;
+        float x = 0, y = 0, vx = 0, vy = 0, lw = 0;
+        if (!First && mine) {
+            const uint32_t src = gather ? batch_source(a, F, S, i) : i;
+            x = a.ax[F.off + src];
+            y = a.ay[F.off + src];
+            vx = a.avx[F.off + src];
+            vy = a.avy[F.off + src];
+            lw = resampled ? 0.0f : a.lw[F.off + i];
+        }
+        float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
+        if (mon) {
+            if (mine) {
+                const float wo = resampled ? 1.0f : __expf(lw - Mprev);
+                sx += wo * x;
+                sy += wo * y;
+                sw += wo;
+            }
+        } else if (First) {
+            if (mine) {
+                float e[4];
+                bearings_normals(t, F.seed, i, e);
+                bearings_prior(c, e, x, y, vx, vy);
+                lw = bearings_loglik(c, z, x, y);
+                lse_push(lw, m, s, s2);
+            }
+        } else {
+            float fe[6];
+            bearings_features(c, x, y, vx, vy, sinf(z), cosf(z), fe);
+            uint32_t a0[4];
+            features_to_a(fe, a0);
+            float o[4];
+            mlp_forward_warp<false>(sp, a0, o);
+            float v[8];
+            out_to_owner(o, v);
+            if (mine) {
+                const float lw_old = resampled ? 0.0f : lw - Mprev;
+                const float wo = resampled ? 1.0f : __expf(lw_old);
+                sx += wo * x;
+                sy += wo * y;
+                sw += wo;
+                float e[4], nu[4];
+                bearings_normals(t, F.seed, i, e);
+                float lq = 0;
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
-            const float om = __shfl_xor_sync(0xFFFFFFFFu, m, d);
-            const float os = __shfl_xor_sync(0xFFFFFFFFu, s, d);
-            const float os2 = __shfl_xor_sync(0xFFFFFFFFu, s2, d);
-            sx += __shfl_xor_sync(0xFFFFFFFFu, sx, d);
-            sy += __shfl_xor_sync(0xFFFFFFFFu, sy, d);
-            sw += __shfl_xor_sync(0xFFFFFFFFu, sw, d);
-            lse_merge_f(m, s, s2, om, os, os2);
-        }
-        if (lane == 0) {
-            shm[wid] = m;
-            sh[0][wid] = s;
-            sh[1][wid] = s2;
-            sh[2][wid] = sx;
-            sh[3][wid] = sy;
-            sh[4][wid] = sw;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float mb = -INFINITY;
-            for (int w = 0; w < kW; ++w)
-                mb = fmaxf(mb, shm[w]);
-            MovePartial p = {0, 0, 0, mb, 0, 0};
-            for (int w = 0; w < kW; ++w) {
-                p.sx += sh[2][w];
-                p.sy += sh[3][w];
-                p.sw += sh[4][w];
-                if (shm[w] > -INFINITY) {
-                    const double fct = __expf(shm[w] - mb);
-                    p.s += sh[0][w] * fct;
-                    p.s2 += sh[1][w] * fct * fct;
+                for (int d = 0; d < 4; ++d) {
+                    const float l = fminf(fmaxf(v[4 + d], c.lmin), c.lmax);
+                    nu[d] = v[d] + __expf(0.5f * l) * e[d];
+                    lq += 0.5f * (e[d] * e[d] - nu[d] * nu[d]) + 0.5f * l;
                 }
-            }
-            a.part[tile] = p;
-            __threadfence();
-            is_last = atomicAdd(&S.done, 1u) == F.ntiles - 1;
-        }
-        __syncthreads();
-        if (is_last) {
-            // ---- the filter's last tile: combine its tile records
-            __threadfence();
-            float M = -INFINITY;
-            for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock)
-                M = fmaxf(M, static_cast<float>(a.part[F.tile0 + b].m));
-            M = block_reduce(M, OpMax(), -INFINITY, shmax);
-            double S1 = 0, S2 = 0, SX = 0, SY = 0, SW = 0;
-            for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock) {
-                const MovePartial p = a.part[F.tile0 + b];
-                SX += p.sx;
-                SY += p.sy;
-                SW += p.sw;
-                if (p.m > -INFINITY) {
-                    const double fct = __expf(static_cast<float>(p.m) - M);
-                    S1 += p.s * fct;
-                    S2 += p.s2 * fct * fct;
-                }
-            }
-#pragma unroll
-            for (int d = 16; d > 0; d >>= 1) {
-                S1 += __shfl_xor_sync(0xFFFFFFFFu, S1, d);
-                S2 += __shfl_xor_sync(0xFFFFFFFFu, S2, d);
-                SX += __shfl_xor_sync(0xFFFFFFFFu, SX, d);
-                SY += __shfl_xor_sync(0xFFFFFFFFu, SY, d);
-                SW += __shfl_xor_sync(0xFFFFFFFFu, SW, d);
-            }
-            if (lane == 0) {
-                sh[0][wid] = S1;
-                sh[1][wid] = S2;
-                sh[2][wid] = SX;
-                sh[3][wid] = SY;
-                sh[4][wid] = SW;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double T1 = 0, T2 = 0, TX = 0, TY = 0, TW = 0;
-                for (int w = 0; w < kW; ++w) {
-                    T1 += sh[0][w];
-                    T2 += sh[1][w];
-                    TX += sh[2][w];
-                    TY += sh[3][w];
-                    TW += sh[4][w];
-                }
-                if (mon) {
-                    a.h_mean[2 * (F.hist_off + F.T - 1) + 0] = TX / TW;
-                    a.h_mean[2 * (F.hist_off + F.T - 1) + 1] = TY / TW;
-                    S.resampled = 0; // finished: nothing left to resample
-                    S.gather = 0;
-                } else {
-                    const double prev_mass =
-                        First ? static_cast<double>(F.n) : TW;
-                    if (!First) {
-                        a.h_mean[2 * (F.hist_off + t - 1) + 0] = TX / TW;
-                        a.h_mean[2 * (F.hist_off + t - 1) + 1] = TY / TW;
-                    }
-                    const double ess = T1 * T1 / T2;
-                    const double M1 = static_cast<double>(M);
-                    S.logz += M1 + log(T1) - log(prev_mass);
-                    if (!(T1 > 0) || !(ess > 0))
-                        S.err |= DEV_ERR_NONFINITE;
-                    const int flag =
-                        ess < a.threshold * static_cast<double>(F.n) ? 1 : 0;
-                    a.h_ess[F.hist_off + t] = ess;
-                    a.h_logz[F.hist_off + t] = S.logz;
-                    a.h_res[F.hist_off + t] = flag;
-                    S.M = M1;
-                    S.S = T1;
-                    S.ess = ess;
-                    S.resampled = flag;
-                    S.gather = 0;
-                    S.step = t + 1;
-                }
-                S.done = 0;
+                bearings_step(c, nu, x, y, vx, vy);
+                lw = lw_old + bearings_loglik(c, z, x, y) + lq;
+                lse_push(lw, m, s, s2);
             }
         }
+        if (!mon && mine) {
+            const uint32_t gi = F.off + i;
+            a.bx[gi] = x;
+            a.by[gi] = y;
+            a.bvx[gi] = vx;
+            a.bvy[gi] = vy;
+            a.lw[gi] = lw;
+        }
+        tile_finish<kLearnBlock, First>(a, tile, F, S, t, mon, m, s, s2, sx,
+            sy, sw, shm, sh, shmax, is_last);
         __syncthreads();
     }
 }
@@ -639,6 +804,21 @@ __global__ void k_batch_simulate(const vsmc_cuda_cv_model *models,
         obs + 2 * obs_off[f]);
 }
 
+// Bearings simulation of one filter on one thread: the FP64 draws of
+// vsmc_cuda_bearings_simulate (CounterEngine(seed), NormalDistribution pairs,
+// one NormalDistribution(0, sigma_z) for the bearing noise).
+__global__ void k_batch_simulate_bearings(
+    const vsmc_cuda_bearings_model *models, const uint32_t *seeds,
+    const uint32_t *T, const uint32_t *obs_off, uint32_t nf, double *truth,
+    double *obs)
+{
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf)
+        return;
+    bearings_simulate_seq(seeds[f], T[f], models[f],
+        truth ? truth + 4 * obs_off[f] : nullptr, obs + obs_off[f]);
+}
+
 constexpr int kResBlock = 512;
 
 struct Shape {
@@ -648,60 +828,89 @@ constexpr Shape kShapes[] = {
     {1, 128}, {2, 128}, {4, 128}, {1, 256}, {2, 256}, {4, 256}};
 constexpr int kNumShapes = 6;
 
-template <int kBlock, int kPPT>
-static cudaError_t launch_step_t(bool first, int grid, const BatchArgs &a,
+template <int kBlock, int kPPT, int Kind>
+static cudaError_t launch_step_k(bool first, int grid, const BatchArgs &a,
     cudaStream_t st)
 {
     if (first)
-        k_batch_step<kBlock, kPPT, true><<<grid, kBlock, 0, st>>>(a);
+        k_batch_step<kBlock, kPPT, true, Kind><<<grid, kBlock, 0, st>>>(a);
     else
-        k_batch_step<kBlock, kPPT, false><<<grid, kBlock, 0, st>>>(a);
+        k_batch_step<kBlock, kPPT, false, Kind><<<grid, kBlock, 0, st>>>(a);
     return cudaGetLastError();
 }
 
-static cudaError_t launch_step(
-    Shape s, bool first, int grid, const BatchArgs &a, cudaStream_t st)
+template <int kBlock, int kPPT>
+static cudaError_t launch_step_t(int kind, bool first, int grid,
+    const BatchArgs &a, cudaStream_t st)
 {
-    if (s.block == 128) {
-        if (s.ppt == 1)
-            return launch_step_t<128, 1>(first, grid, a, st);
-        if (s.ppt == 2)
-            return launch_step_t<128, 2>(first, grid, a, st);
-        return launch_step_t<128, 4>(first, grid, a, st);
-    }
-    if (s.ppt == 1)
-        return launch_step_t<256, 1>(first, grid, a, st);
-    if (s.ppt == 2)
-        return launch_step_t<256, 2>(first, grid, a, st);
-    return launch_step_t<256, 4>(first, grid, a, st);
+    return kind == kKindCv
+        ? launch_step_k<kBlock, kPPT, kKindCv>(first, grid, a, st)
+        : launch_step_k<kBlock, kPPT, kKindBearings>(first, grid, a, st);
 }
 
-template <int kBlock, int kPPT>
-static int occupancy_t()
+static cudaError_t launch_step(int kind, Shape s, bool first, int grid,
+    const BatchArgs &a, cudaStream_t st)
+{
+    if (kind == kKindLearned) {
+        if (first)
+            k_batch_step_learned<true><<<grid, kLearnBlock, 0, st>>>(a);
+        else
+            k_batch_step_learned<false><<<grid, kLearnBlock, 0, st>>>(a);
+        return cudaGetLastError();
+    }
+    if (s.block == 128) {
+        if (s.ppt == 1)
+            return launch_step_t<128, 1>(kind, first, grid, a, st);
+        if (s.ppt == 2)
+            return launch_step_t<128, 2>(kind, first, grid, a, st);
+        return launch_step_t<128, 4>(kind, first, grid, a, st);
+    }
+    if (s.ppt == 1)
+        return launch_step_t<256, 1>(kind, first, grid, a, st);
+    if (s.ppt == 2)
+        return launch_step_t<256, 2>(kind, first, grid, a, st);
+    return launch_step_t<256, 4>(kind, first, grid, a, st);
+}
+
+template <typename K>
+static int occupancy_of(K kernel, int block)
 {
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ, k_batch_step<kBlock, kPPT, false>, kBlock, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, block, 0) !=
             cudaSuccess ||
         occ < 1)
         occ = 2;
     return occ;
 }
 
-static int occupancy(Shape s)
+template <int kBlock, int kPPT>
+static int occupancy_t(int kind)
 {
+    return kind == kKindCv
+        ? occupancy_of(k_batch_step<kBlock, kPPT, false, kKindCv>, kBlock)
+        : occupancy_of(
+              k_batch_step<kBlock, kPPT, false, kKindBearings>, kBlock);
+}
+
+static int occupancy(int kind, Shape s)
+{
+    if (kind == kKindLearned)
+        return occupancy_of(k_batch_step_learned<false>, kLearnBlock);
     if (s.block == 128)
-        return s.ppt == 1 ? occupancy_t<128, 1>()
-                          : (s.ppt == 2 ? occupancy_t<128, 2>()
-                                        : occupancy_t<128, 4>());
-    return s.ppt == 1 ? occupancy_t<256, 1>()
-                      : (s.ppt == 2 ? occupancy_t<256, 2>()
-                                    : occupancy_t<256, 4>());
+        return s.ppt == 1 ? occupancy_t<128, 1>(kind)
+                          : (s.ppt == 2 ? occupancy_t<128, 2>(kind)
+                                        : occupancy_t<128, 4>(kind));
+    return s.ppt == 1 ? occupancy_t<256, 1>(kind)
+                      : (s.ppt == 2 ? occupancy_t<256, 2>(kind)
+                                    : occupancy_t<256, 4>(kind));
 }
 
 } // namespace vsmc_cuda
 
 struct vsmc_cuda_batch {
+    int kind = kKindCv;
+    const uint32_t *packed = nullptr; // learned kind: proposal network
+    std::vector<vsmc_cuda_bearings_model> bmodels;
     uint32_t nf = 0;
     uint32_t tmax = 0;
     int scheme = VSMC_CUDA_STRATIFIED;
@@ -770,7 +979,9 @@ static void batch_free(vsmc_cuda_batch *b)
 // tile tables for a shape (host + device)
 static int batch_layout(vsmc_cuda_batch *b, Shape s)
 {
-    const uint32_t tile = static_cast<uint32_t>(s.ppt * s.block);
+    const uint32_t tile = b->kind == kKindLearned
+        ? kLearnTile
+        : static_cast<uint32_t>(s.ppt * s.block);
     b->tile_filter.clear();
     for (uint32_t k = 0; k < b->nf; ++k) {
         BFilter &F = b->flt[k];
@@ -832,6 +1043,7 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.h_logz = b->d_logz;
     a.h_res = b->d_res;
     a.step = b->d_step;
+    a.packed = b->packed;
     a.nfilters = b->nf;
     a.tmax = b->tmax;
     a.scheme = b->scheme;
@@ -850,7 +1062,7 @@ static int enqueue_run(
     VSMC_CUDA_CHECK_LAUNCH();
     for (int t = 0; t < nsteps; ++t) {
         const BatchArgs a = batch_args(b, obs, t & 1);
-        VSMC_CUDA_TRY(launch_step(b->shape, t == 0, grid, a, st));
+        VSMC_CUDA_TRY(launch_step(b->kind, b->shape, t == 0, grid, a, st));
         k_batch_resample<kResBlock><<<b->nf, kResBlock, 0, st>>>(a);
         VSMC_CUDA_CHECK_LAUNCH();
     }
@@ -877,27 +1089,37 @@ static int check_errors(vsmc_cuda_batch *b)
 
 extern "C" {
 
-int vsmc_cuda_batch_create(vsmc_cuda_batch **out, size_t nfilters,
-    const uint32_t *n, const uint32_t *T, const vsmc_cuda_cv_model *models,
-    const uint32_t *seeds, int scheme, double threshold, void *stream)
+} // extern "C"
+
+namespace vsmc_cuda
 {
-    if (out == nullptr || n == nullptr || T == nullptr || models == nullptr ||
-        seeds == nullptr || std::isnan(threshold) ||
+
+// Shared constructor of the three kinds: cv (position model) or bm
+// (bearings model) per filter; packed: the proposal network (learned kind).
+static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
+    const uint32_t *n, const uint32_t *T, const vsmc_cuda_cv_model *cv,
+    const vsmc_cuda_bearings_model *bm, const uint32_t *seeds,
+    const uint32_t *packed, int scheme, double threshold, void *stream)
+{
+    if (out == nullptr || n == nullptr || T == nullptr || seeds == nullptr ||
+        std::isnan(threshold) ||
         (scheme != VSMC_CUDA_STRATIFIED && scheme != VSMC_CUDA_SYSTEMATIC))
         return VSMC_CUDA_ERR_ARG;
     *out = nullptr;
     if (nfilters < 1 || nfilters > (size_t(1) << 24))
         return VSMC_CUDA_ERR_SIZE;
+    const uint32_t min_tile = kind == kKindLearned ? kLearnTile : 128u;
     size_t total = 0, totalT = 0, tiles = 0;
     uint32_t tmax = 0;
     for (size_t f = 0; f < nfilters; ++f) {
-        if (!valid_cv_model(&models[f]))
+        if (kind == kKindCv ? !valid_cv_model(&cv[f])
+                            : !valid_bearings_model(&bm[f]))
             return VSMC_CUDA_ERR_ARG;
         if (n[f] < 2 || n[f] > (1u << 30) || T[f] < 1 || T[f] > (1u << 24))
             return VSMC_CUDA_ERR_SIZE;
         total += (static_cast<size_t>(n[f]) + 3) / 4 * 4;
         totalT += T[f];
-        tiles += (n[f] + 127) / 128; // the smallest tile
+        tiles += (n[f] + min_tile - 1) / min_tile; // the smallest tile
         tmax = std::max(tmax, T[f]);
     }
     if (total >= (size_t(1) << 31) || totalT >= (size_t(1) << 31))
@@ -905,6 +1127,8 @@ int vsmc_cuda_batch_create(vsmc_cuda_batch **out, size_t nfilters,
     vsmc_cuda_batch *b = new (std::nothrow) vsmc_cuda_batch;
     if (b == nullptr)
         return VSMC_CUDA_ERR_ALLOC;
+    b->kind = kind;
+    b->packed = packed;
     b->nf = static_cast<uint32_t>(nfilters);
     b->tmax = tmax;
     b->scheme = scheme;
@@ -912,7 +1136,10 @@ int vsmc_cuda_batch_create(vsmc_cuda_batch **out, size_t nfilters,
     b->n.assign(n, n + nfilters);
     b->T.assign(T, T + nfilters);
     b->seeds.assign(seeds, seeds + nfilters);
-    b->models.assign(models, models + nfilters);
+    if (kind == kKindCv)
+        b->models.assign(cv, cv + nfilters);
+    else
+        b->bmodels.assign(bm, bm + nfilters);
     b->total_T = totalT;
     b->total_particles = total;
     b->max_tiles = tiles;
@@ -944,7 +1171,10 @@ int vsmc_cuda_batch_create(vsmc_cuda_batch **out, size_t nfilters,
         while ((size_t(1) << lg) < n[f])
             ++lg;
         F.shift = static_cast<uint32_t>(63 - lg);
-        F.c = make_cv_const<float>(models[f]);
+        if (kind == kKindCv)
+            F.c = make_cv_const<float>(cv[f]);
+        else
+            F.bc = make_bearings_const(bm[f]);
     }
     b->res_order.resize(nfilters);
     for (uint32_t k = 0; k < nfilters; ++k)
@@ -1006,6 +1236,31 @@ int vsmc_cuda_batch_create(vsmc_cuda_batch **out, size_t nfilters,
     return VSMC_CUDA_OK;
 }
 
+} // namespace vsmc_cuda
+
+extern "C" {
+
+int vsmc_cuda_batch_create(vsmc_cuda_batch **out, size_t nfilters,
+    const uint32_t *n, const uint32_t *T, const vsmc_cuda_cv_model *models,
+    const uint32_t *seeds, int scheme, double threshold, void *stream)
+{
+    if (models == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    return batch_create(out, kKindCv, nfilters, n, T, models, nullptr, seeds,
+        nullptr, scheme, threshold, stream);
+}
+
+int vsmc_cuda_batch_create_bearings(vsmc_cuda_batch **out, size_t nfilters,
+    const uint32_t *n, const uint32_t *T,
+    const vsmc_cuda_bearings_model *models, const uint32_t *seeds,
+    const uint32_t *packed, int scheme, double threshold, void *stream)
+{
+    if (models == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    return batch_create(out, packed ? kKindLearned : kKindBearings, nfilters,
+        n, T, nullptr, models, seeds, packed, scheme, threshold, stream);
+}
+
 int vsmc_cuda_batch_destroy(vsmc_cuda_batch *b)
 {
     if (b == nullptr)
@@ -1029,26 +1284,38 @@ int vsmc_cuda_batch_simulate(vsmc_cuda_batch *b, double *truth_dev,
 {
     if (b == nullptr || obs_dev == nullptr)
         return VSMC_CUDA_ERR_ARG;
-    vsmc_cuda_cv_model *dm = nullptr;
     uint32_t *dseed = nullptr, *dT = nullptr, *doff = nullptr;
     cudaStream_t st = b->stream;
     Scratch scratch(st);
-    dm = scratch.get<vsmc_cuda_cv_model>(b->nf);
+    void *dm = b->kind == kKindCv
+        ? static_cast<void *>(scratch.get<vsmc_cuda_cv_model>(b->nf))
+        : static_cast<void *>(scratch.get<vsmc_cuda_bearings_model>(b->nf));
     dseed = scratch.get<uint32_t>(b->nf);
     dT = scratch.get<uint32_t>(b->nf);
     doff = scratch.get<uint32_t>(b->nf);
     if (!dm || !dseed || !dT || !doff)
         return VSMC_CUDA_ERR_ALLOC;
-    VSMC_CUDA_TRY(cudaMemcpyAsync(dm, b->models.data(),
-        sizeof(vsmc_cuda_cv_model) * b->nf, cudaMemcpyHostToDevice, st));
+    if (b->kind == kKindCv)
+        VSMC_CUDA_TRY(cudaMemcpyAsync(dm, b->models.data(),
+            sizeof(vsmc_cuda_cv_model) * b->nf, cudaMemcpyHostToDevice, st));
+    else
+        VSMC_CUDA_TRY(cudaMemcpyAsync(dm, b->bmodels.data(),
+            sizeof(vsmc_cuda_bearings_model) * b->nf, cudaMemcpyHostToDevice,
+            st));
     VSMC_CUDA_TRY(cudaMemcpyAsync(dseed, b->seeds.data(),
         sizeof(uint32_t) * b->nf, cudaMemcpyHostToDevice, st));
     VSMC_CUDA_TRY(cudaMemcpyAsync(dT, b->T.data(), sizeof(uint32_t) * b->nf,
         cudaMemcpyHostToDevice, st));
     VSMC_CUDA_TRY(cudaMemcpyAsync(doff, b->obs_off.data(),
         sizeof(uint32_t) * b->nf, cudaMemcpyHostToDevice, st));
-    k_batch_simulate<<<(b->nf + 63) / 64, 64, 0, st>>>(
-        dm, dseed, dT, doff, b->nf, truth_dev, obs_dev);
+    if (b->kind == kKindCv)
+        k_batch_simulate<<<(b->nf + 63) / 64, 64, 0, st>>>(
+            static_cast<const vsmc_cuda_cv_model *>(dm), dseed, dT, doff,
+            b->nf, truth_dev, obs_dev);
+    else
+        k_batch_simulate_bearings<<<(b->nf + 63) / 64, 64, 0, st>>>(
+            static_cast<const vsmc_cuda_bearings_model *>(dm), dseed, dT,
+            doff, b->nf, truth_dev, obs_dev);
     VSMC_CUDA_CHECK_LAUNCH();
     VSMC_CUDA_TRY(cudaStreamSynchronize(st));
     return VSMC_CUDA_OK;
@@ -1066,7 +1333,7 @@ int vsmc_cuda_batch_run_device(vsmc_cuda_batch *b, const double *obs_dev)
             cudaGraphExecDestroy(b->graph);
             b->graph = nullptr;
         }
-        const int grid = num_sms() * occupancy(b->shape);
+        const int grid = num_sms() * occupancy(b->kind, b->shape);
         VSMC_CUDA_TRY(cudaStreamBeginCapture(
             b->stream, cudaStreamCaptureModeThreadLocal));
         const int rc = enqueue_run(b, obs_dev, nsteps, grid);
@@ -1120,8 +1387,10 @@ int vsmc_cuda_batch_run(vsmc_cuda_batch *b, const double *obs_host,
 {
     if (b == nullptr || obs_host == nullptr)
         return VSMC_CUDA_ERR_ARG;
+    const size_t obs_dim = b->kind == kKindCv ? 2 : 1;
     VSMC_CUDA_TRY(cudaMemcpyAsync(b->d_obs, obs_host,
-        sizeof(double) * 2 * b->total_T, cudaMemcpyHostToDevice, b->stream));
+        sizeof(double) * obs_dim * b->total_T, cudaMemcpyHostToDevice,
+        b->stream));
     const int rc = vsmc_cuda_batch_run_device(b, b->d_obs);
     if (rc != VSMC_CUDA_OK)
         return rc;
@@ -1131,7 +1400,7 @@ int vsmc_cuda_batch_run(vsmc_cuda_batch *b, const double *obs_host,
 
 int vsmc_cuda_batch_set_shape(vsmc_cuda_batch *b, int ppt, int block)
 {
-    if (b == nullptr)
+    if (b == nullptr || b->kind == kKindLearned)
         return VSMC_CUDA_ERR_ARG;
     for (int k = 0; k < kNumShapes; ++k)
         if (kShapes[k].ppt == ppt && kShapes[k].block == block)
@@ -1151,7 +1420,8 @@ int vsmc_cuda_batch_get_shape(vsmc_cuda_batch *b, int *ppt, int *block)
 int vsmc_cuda_batch_autotune(vsmc_cuda_batch *b, const double *obs_dev,
     int steps, float *ms_host)
 {
-    if (b == nullptr || obs_dev == nullptr || steps < 1)
+    if (b == nullptr || obs_dev == nullptr || steps < 1 ||
+        b->kind == kKindLearned)
         return VSMC_CUDA_ERR_ARG;
     const int nsteps = std::min(steps, static_cast<int>(b->tmax) + 1);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1167,7 +1437,7 @@ int vsmc_cuda_batch_autotune(vsmc_cuda_batch *b, const double *obs_dev,
         rc = batch_layout(b, kShapes[k]);
         if (rc != VSMC_CUDA_OK)
             break;
-        const int grid = num_sms() * occupancy(b->shape);
+        const int grid = num_sms() * occupancy(b->kind, b->shape);
         rc = enqueue_run(b, obs_dev, nsteps, grid); // warm-up
         if (rc != VSMC_CUDA_OK)
             break;
