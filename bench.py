@@ -394,6 +394,7 @@ def run_learned(args):
     import vsmc_gb300 as vc
     vc.lib()
     m = vc.bearings_model()
+    m.dt, m.q, m.sd_vel0 = args.bearings_dt, args.bearings_q, args.bearings_sdv
     T, R = 200, args.replicates
     obs = torch.zeros(T, dtype=torch.float64, device="cuda")
     truth = torch.zeros(4 * T, dtype=torch.float64, device="cuda")
@@ -420,8 +421,9 @@ def run_learned(args):
         res = np.zeros(T, np.int32)
         logz = np.zeros(T)
         t0 = time.perf_counter()
-        port.vo_bearings_pf_run(64, Nref, T, 123, 1, 0.5,
-                                ctypes.byref(binding.bearings_model()),
+        om = binding.bearings_model()
+        om.dt, om.q, om.sd_vel0 = m.dt, m.q, m.sd_vel0
+        port.vo_bearings_pf_run(64, Nref, T, 123, 1, 0.5, ctypes.byref(om),
                                 P(obs_np), None, 0, P(mean), P(ess), P(res),
                                 P(logz))
         ref_s = time.perf_counter() - t0
@@ -433,7 +435,7 @@ def run_learned(args):
 
     def measure(N, packed):
         b = vc.FilterBatch([N] * R, [T] * R, np.arange(R) + 1000,
-                           bearings=True, packed=packed,
+                           models=[m] * R, bearings=True, packed=packed,
                            stream=ctypes.c_void_p(stream.cuda_stream))
         for _ in range(args.warmup):
             b.run_device(obs_all.data_ptr())
@@ -482,6 +484,9 @@ def run_learned(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 network (fp32 accumulate), fp32 state",
         "data": "synthetic bearings-only track (seed 0), T=200",
+        "model": {"dt": m.dt, "q": m.q, "sigma_z": m.sigma_z,
+                  "start": [m.x0, m.y0], "sd_pos0": m.sd_pos0,
+                  "sd_vel0": m.sd_vel0},
         "config": {
             "workload": f"{R} filters x N={args.learned_particles} learned "
                         f"proposal vs bootstrap N in {args.boot_particles}",
@@ -523,6 +528,9 @@ def main():
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--ref-particles", type=int, default=1 << 18)
+    ap.add_argument("--bearings-dt", type=float, default=1.0)
+    ap.add_argument("--bearings-q", type=float, default=1.0)
+    ap.add_argument("--bearings-sdv", type=float, default=0.5)
     ap.add_argument("--filters", type=int, default=4096)
     ap.add_argument("--tune-steps", type=int, default=60)
     args = ap.parse_args()

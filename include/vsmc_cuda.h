@@ -465,6 +465,61 @@ int vsmc_cuda_batch_get_shape(vsmc_cuda_batch *batch, int *ppt, int *block);
 int vsmc_cuda_batch_autotune(vsmc_cuda_batch *batch, const double *obs_dev,
     int steps, float *ms_host);
 
+/* --------------------------------------------- genealogy and summary */
+
+/* Lineage over a history of resampling index rows (device, row-major
+ * [iters][N]: row k = each particle's parent among the particles before
+ * iteration k, the identity for an iteration without resampling).
+ * trace: out[id] = the ancestor at iteration `iter` of particle id of the
+ * last iteration -- ResampleIndex::index(id, iter) (resample/index.hpp:
+ * 117-129) for every id.  matrix: every line, layout 0 = [N][iters]
+ * (index_matrix<RowMajor>), 1 = [iters][N] (index_matrix<ColMajor>)
+ * (resample/index.hpp:131-201).  An index outside [0, N) gives
+ * VSMC_CUDA_ERR_ARG.  Synchronize. */
+int vsmc_cuda_resample_index_trace(size_t N, size_t iters, const int *rows,
+    size_t iter, int *out, void *stream);
+int vsmc_cuda_resample_index_matrix(size_t N, size_t iters, const int *rows,
+    int layout, int *out, void *stream);
+/* Sampler::print (core/sampler.hpp:646-689) for a sampler with naccept
+ * moves / MCMC steps and one monitor of nmon variables named mon_name.0,
+ * mon_name.1, ...: header "Size Resampled Accept.0 ... ESS <monitor>" and
+ * one row per iteration, every field followed by sep, doubles as the
+ * ostream default (6 significant digits).  Host arrays: resampled, ess (T),
+ * mon (T x nmon), accept (T x naccept; NULL = one column of N).  buf (cap
+ * bytes) gets the text, NUL-terminated; *len its length; VSMC_CUDA_ERR_SIZE
+ * if it does not fit (cap 0: length only). */
+int vsmc_cuda_sampler_print(size_t T, size_t N, const int *resampled,
+    const double *ess, size_t nmon, const char *mon_name, const double *mon,
+    size_t naccept, const size_t *accept, char sep, char *buf, size_t cap,
+    size_t *len);
+/* Precision-32 filters: record each step's resampling index row (the
+ * parents after resampling, or the identity) into a max_steps x n device
+ * array; rows_dev points at it (valid while the filter lives). */
+int vsmc_cuda_pf_record_genealogy(vsmc_cuda_pf *pf, int on);
+int vsmc_cuda_pf_genealogy(vsmc_cuda_pf *pf, const int **rows_dev);
+/* Resample-move (precision 32, before initialize): after every step t >= 1
+ * that resampled, `sweeps` random-walk Metropolis steps on each particle's
+ * acceleration innovation a (the RandomWalk / NormalMVProposal update of
+ * rng/random_walk.hpp:95-114, proposal a' = a + scale * N(0, I2), target
+ * N(a; 0, sigma_a^2 I2) g(y_t | x_t), x_t = F x_{t-1} + G a), the mcmc
+ * queue of Sampler::iterate (core/sampler.hpp:409-438, 746-754).  Steps
+ * that did not resample (weights not equal) are left unmoved.  sweeps 0
+ * turns it off.  accepts: the accepted steps per step (host, T). */
+int vsmc_cuda_pf_set_mcmc(vsmc_cuda_pf *pf, size_t sweeps, double scale);
+int vsmc_cuda_pf_mcmc_accepts(vsmc_cuda_pf *pf, size_t T, uint32_t *host);
+/* Kernel-level resample-move step: `sweeps` such moves at step t on
+ * caller-owned SoA state [4][n] after step t's move (particle i's
+ * innovation is that of parent[i], or of i when parent is NULL);
+ * accepted (device, 1 uint32) is incremented by the accepted steps. */
+int vsmc_cuda_cv_mcmc_f32(size_t n, size_t t, size_t sweeps, uint32_t seed,
+    const vsmc_cuda_cv_model *model, const double obs[2], double scale,
+    const int *parent, float *state, uint32_t *accepted, void *stream);
+/* The filter's first T steps as Sampler::print text (monitor "pos", the
+ * weighted position mean; Accept.0 = n for the move, Accept.1 = the
+ * MCMC accepts when resample-move is on). */
+int vsmc_cuda_pf_print(vsmc_cuda_pf *pf, size_t T, char sep, char *buf,
+    size_t cap, size_t *len);
+
 /* One move + log-likelihood step on caller-owned SoA state (kernel-level
  * parity entry point): t == 0 draws the prior, t > 0 propagates.  ll
  * receives the per-particle log-likelihood of obs (host, 2 doubles). */

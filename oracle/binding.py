@@ -88,6 +88,9 @@ PORT_PROTOTYPES = {
     "vo_mlp_forward": (None, [VP, SZ, VP, VP]),
     "vo_mlp_loss_grad": (None, [VP, SZ, VP, VP, VP, VP]),
     "vo_mlp_set_rounding": (None, [I32]),
+    "vo_resample_index_trace": (None, [SZ, SZ, VP, SZ, VP]),
+    "vo_cv_mcmc_f32": (None, [SZ, SZ, SZ, U32, _MP, VP, F64, VP, VP, VP]),
+    "vo_resample_index_matrix": (None, [SZ, SZ, VP, I32, VP]),
     "vo_bearings_pf_run": (I32, [I32, SZ, SZ, U32, I32, F64, _BMP, VP, VP,
                                  I32, VP, VP, VP, VP]),
     "vo_engine_run": (None, [I32, VP, VP, SZ, I32, SZ, F64, F64, VP, VP,
@@ -114,6 +117,9 @@ REF_PROTOTYPES = {
     "ref_weight_set": (F64, [SZ, VP, VP]),
     "ref_pf_run": (I32, [I32, SZ, SZ, U32, I32, F64, I32, F64, F64, F64, F64,
                          F64, F64, VP, VP, VP, VP, VP]),
+    "ref_pf_print": (SZ, [SZ, SZ, U32, I32, F64, F64, F64, F64, F64, F64,
+                          F64, VP, VP, VP, VP, VP, ctypes.c_char_p, SZ]),
+    "ref_resample_index": (None, [SZ, SZ, VP, I32, VP, VP]),
     "ref_pf_simulate": (None, [U32, SZ, F64, F64, F64, F64, F64, F64, VP,
                                VP]),
     "vsmc_resample_trans_u01_rep": (None, [I32, I32, VP, VP, VP]),

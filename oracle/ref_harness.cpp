@@ -26,12 +26,15 @@
 #include <vsmc/rng/normal_distribution.hpp>
 #include <vsmc/rng/student_t_distribution.hpp>
 #include <vsmc/rng/u01_sequence.hpp>
+#include <vsmc/resample/index.hpp>
 #include <vsmc/resample/resample.hpp>
 #include <vsmc/smp/backend_omp.hpp>
 
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <sstream>
+#include <string>
 #include <vector>
 
 namespace
@@ -336,7 +339,8 @@ class PFMean : public vsmc::MonitorEvalOMP<PFState<T>, PFMean<T>>
 template <typename T>
 int pf_run(std::size_t N, std::size_t T_, uint32_t seed, int scheme,
     double threshold, int native_rng, const ModelParam &p, const double *obs,
-    double *mean_out, double *ess_out, int *resampled_out, double *logz_out)
+    double *mean_out, double *ess_out, int *resampled_out, double *logz_out,
+    std::string *tsv = nullptr)
 {
     if (native_rng)
         vsmc::Seed::instance().set(seed);
@@ -371,6 +375,11 @@ int pf_run(std::size_t N, std::size_t T_, uint32_t seed, int scheme,
         mean_out[2 * t + 1] = mon.record(1, t);
         ess_out[t] = sampler.ess_history(t);
         resampled_out[t] = sampler.resampled_history(t) ? 1 : 0;
+    }
+    if (tsv) {
+        std::ostringstream os;
+        sampler.print(os);
+        *tsv = os.str();
     }
     return 0;
 }
@@ -587,6 +596,47 @@ int ref_pf_run(int precision, std::size_t N, std::size_t T, uint32_t seed,
             obs, mean_out, ess_out, resampled_out, logz_out);
     return pf_run<double>(N, T, seed, scheme, threshold, native_rng, p, obs,
         mean_out, ess_out, resampled_out, logz_out);
+}
+
+// Sampler::print (core/sampler.hpp:646-689) of an FP64 run of the filter
+// above; buf receives the text (truncated to cap - 1 bytes, NUL-terminated);
+// returns its full length.
+std::size_t ref_pf_print(std::size_t N, std::size_t T, uint32_t seed,
+    int scheme, double threshold, double dt, double sigma_a, double obs_scale,
+    double nu, double sd_pos0, double sd_vel0, const double *obs,
+    double *mean_out, double *ess_out, int *resampled_out, double *logz_out,
+    char *buf, std::size_t cap)
+{
+    ModelParam p = {dt, sigma_a, obs_scale, nu, sd_pos0, sd_vel0};
+    std::string tsv;
+    pf_run<double>(N, T, seed, scheme, threshold, 0, p, obs, mean_out,
+        ess_out, resampled_out, logz_out, &tsv);
+    if (cap > 0) {
+        const std::size_t k = tsv.size() < cap - 1 ? tsv.size() : cap - 1;
+        std::memcpy(buf, tsv.data(), k);
+        buf[k] = 0;
+    }
+    return tsv.size();
+}
+
+// ResampleIndex<int> fed `iters` index rows of N (row-major [iter][N]);
+// out: index_matrix<RowMajor> (layout 0) or <ColMajor> (layout 1)
+// (resample/index.hpp:127-201); trace: index(id, iter) for every id and iter
+// ([iter][N]).
+void ref_resample_index(std::size_t N, std::size_t iters, const int *rows,
+    int layout, int *out, int *trace)
+{
+    vsmc::ResampleIndex<int> ri(N);
+    ri.reset(); // the constructor leaves the iteration count unset
+    for (std::size_t i = 0; i != iters; ++i)
+        ri.push_back(rows + i * N);
+    vsmc::Vector<int> m = layout == 0
+        ? ri.index_matrix<vsmc::RowMajor>()
+        : ri.index_matrix<vsmc::ColMajor>();
+    std::memcpy(out, m.data(), sizeof(int) * N * iters);
+    for (std::size_t it = 0; it != iters; ++it)
+        for (std::size_t id = 0; id != N; ++id)
+            trace[it * N + id] = ri.index(id, it);
 }
 
 // Observation simulation: Philox4x32 engine seeded with `seed` (key {seed,0},

@@ -1755,3 +1755,107 @@ int vo_bearings_pf_run(int precision, size_t N, size_t T, uint32_t seed,
 #endif
     return 0;
 }
+
+/* =====================================================================
+ * ResampleIndex (resample/index.hpp:46-206): rows[k] holds each particle's
+ * parent before iteration k.  index(id, iter) follows rows back from the
+ * last iteration (index.hpp:117-129); index_matrix gives every line,
+ * row-major [N][iters] or column-major [iters][N] (index.hpp:131-201).
+ * ===================================================================== */
+void vo_resample_index_trace(
+    size_t N, size_t iters, const int *rows, size_t iter, int *out)
+{
+    for (size_t id = 0; id != N; ++id) {
+        size_t cur = iters - 1;
+        int idx = rows[cur * N + id];
+        while (cur != iter) {
+            --cur;
+            idx = rows[cur * N + (size_t)idx];
+        }
+        out[id] = idx;
+    }
+}
+
+void vo_resample_index_matrix(
+    size_t N, size_t iters, const int *rows, int layout, int *out)
+{
+    if (N * iters == 0)
+        return;
+    if (layout == 0) { /* row major: out[i * iters + k] */
+        for (size_t i = 0; i != N; ++i)
+            out[i * iters + iters - 1] = rows[(iters - 1) * N + i];
+        for (size_t k = iters - 1; k != 0; --k)
+            for (size_t i = 0; i != N; ++i)
+                out[i * iters + k - 1] =
+                    rows[(k - 1) * N + (size_t)out[i * iters + k]];
+    } else { /* column major: out[k * N + i] */
+        for (size_t i = 0; i != N; ++i)
+            out[(iters - 1) * N + i] = rows[(iters - 1) * N + i];
+        for (size_t k = iters - 1; k != 0; --k)
+            for (size_t i = 0; i != N; ++i)
+                out[(k - 1) * N + i] =
+                    rows[(k - 1) * N + (size_t)out[k * N + i]];
+    }
+}
+
+/* =====================================================================
+ * Resample-move step: random-walk Metropolis on a particle's acceleration
+ * innovation a (RandomWalk with an unbounded Normal proposal,
+ * rng/random_walk.hpp:95-114), target N(a; 0, sigma_a^2 I) g(y | x),
+ * x = F x' + G a, so a' = a + s e moves the state by G (a' - a).  Proposal
+ * and uniform: Philox4x32 block of counter {2 + k, i, 0, 0}, key {t, seed}
+ * (words 0, 1 -> Box-Muller pair, word 2 -> u in [0, 1)); particle i's
+ * current innovation is the pair its parent j drew at step t.
+ * ===================================================================== */
+void vo_cv_mcmc_f32(size_t N, size_t t, size_t sweeps, uint32_t seed,
+    const vo_model *m, const double obs[2], double scale, const int *parent,
+    float *state, uint32_t *accepted)
+{
+    const float dt = (float)m->dt, h = (float)(0.5 * m->dt * m->dt);
+    const float sa = (float)m->sigma_a;
+    const float inv_var = 1.0f / (sa * sa), s_rw = (float)scale;
+    uint32_t acc = 0;
+    for (size_t i = 0; i < N; ++i) {
+        const size_t j = parent ? (size_t)parent[i] : i;
+        vo_philox e;
+        vo_particle_engine(&e, t, seed, j);
+        float ax, ay;
+        vo_pair_f(&e, sa, &ax, &ay);
+        float x = state[i], y = state[N + i];
+        float vx = state[2 * N + i], vy = state[3 * N + i];
+        float lt = -0.5f * inv_var * (ax * ax + ay * ay) +
+            vo_ll_f32(m, obs, x, y);
+        for (size_t k = 0; k < sweeps; ++k) {
+            const uint32_t ctr[4] = {(uint32_t)(2 + k), (uint32_t)i, 0, 0};
+            const uint32_t key[2] = {(uint32_t)t, seed};
+            uint32_t w[4];
+            vo_philox4x32_block(ctr, key, w);
+            const float u1 = vo_u01_u32_f32(2, w[0]);
+            const float u2 = vo_u01_u32_f32(1, w[1]);
+            const float r = sqrtf(-2 * logf(u1));
+            const float th = VO_PI_2F * u2;
+            const float e1 = r * cosf(th), e2 = r * sinf(th);
+            const float bx = ax + s_rw * e1, by = ay + s_rw * e2;
+            const float dx = bx - ax, dy = by - ay;
+            const float nx = x + h * dx, ny = y + h * dy;
+            const float nvx = vx + dt * dx, nvy = vy + dt * dy;
+            const float lt2 = -0.5f * inv_var * (bx * bx + by * by) +
+                vo_ll_f32(m, obs, nx, ny);
+            if (logf(vo_u01_u32_f32(1, w[2])) < lt2 - lt) {
+                x = nx;
+                y = ny;
+                vx = nvx;
+                vy = nvy;
+                ax = bx;
+                ay = by;
+                lt = lt2;
+                ++acc;
+            }
+        }
+        state[i] = x;
+        state[N + i] = y;
+        state[2 * N + i] = vx;
+        state[3 * N + i] = vy;
+    }
+    *accepted += acc;
+}

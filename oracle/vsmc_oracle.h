@@ -164,6 +164,19 @@ int vo_bearings_pf_run(int precision, size_t N, size_t T, uint32_t seed,
     const float *params, int threads, double *mean_out, double *ess_out,
     int *resampled_out, double *logz_out);
 
+/* resample-move: `sweeps` random-walk Metropolis steps on each particle's
+ * acceleration innovation (parent: NULL = identity); *accepted += accepts */
+void vo_cv_mcmc_f32(size_t N, size_t t, size_t sweeps, uint32_t seed,
+    const vo_model *m, const double obs[2], double scale, const int *parent,
+    float *state, uint32_t *accepted);
+
+/* ResampleIndex::index for every id at `iter`, and index_matrix (layout 0
+ * row-major [N][iters], 1 column-major [iters][N]); rows: [iters][N] */
+void vo_resample_index_trace(
+    size_t N, size_t iters, const int *rows, size_t iter, int *out);
+void vo_resample_index_matrix(
+    size_t N, size_t iters, const int *rows, int layout, int *out);
+
 /* test helper: k scalar words, then one bulk / u01 / normal batch operation */
 void vo_engine_run(int kind, const uint64_t key[4], const uint64_t ctr[4],
     size_t k, int op, size_t n, double mean, double sd, void *out,

@@ -214,6 +214,44 @@ def pf_runs(R):
     return out
 
 
+def genealogy(R, rng):
+    """ResampleIndex (resample/index.hpp) traces and index matrices over
+    random index histories, and Sampler::print (core/sampler.hpp:646-689)
+    of a short FP64 filter run with its histories."""
+    out = {}
+    for si, (N, iters) in enumerate([(1, 1), (7, 1), (13, 5), (200, 17)]):
+        rows = np.zeros((iters, N), np.int32)
+        for it in range(iters):
+            if rng.random() < 0.3:
+                rows[it] = np.arange(N)  # a step without resampling
+            else:
+                rows[it] = np.sort(rng.integers(0, N, N))
+        out[f"rows{si}"] = rows
+        for layout in (0, 1):
+            m = np.zeros(N * iters, np.int32)
+            tr = np.zeros(N * iters, np.int32)
+            R.ref_resample_index(N, iters, P(rows), layout, P(m), P(tr))
+            out[f"matrix{si}_{layout}"] = m
+            out[f"trace{si}"] = tr
+    out["nsizes"] = np.array([4])
+    m = (0.1, 1.0, 0.5, 10.0, 2.0, 1.0)
+    T, N = 20, 1000
+    truth = np.zeros(4 * T)
+    obs = np.zeros(2 * T)
+    R.ref_pf_simulate(2, T, *m, P(truth), P(obs))
+    mean = np.zeros(2 * T)
+    ess = np.zeros(T)
+    res = np.zeros(T, np.int32)
+    logz = np.zeros(T)
+    buf = ctypes.create_string_buffer(1 << 16)
+    n = R.ref_pf_print(N, T, 7, 1, 0.5, *m, P(obs), P(mean), P(ess), P(res),
+                       P(logz), buf, len(buf))
+    assert n < len(buf)
+    out.update(tsv=np.frombuffer(buf.raw[:n], np.uint8), tsv_N=np.array([N]),
+               tsv_mean=mean.reshape(T, 2), tsv_ess=ess, tsv_res=res)
+    return out
+
+
 def main():
     if binding.build_ref() is None:
         sys.exit("reference tree not found: cannot generate the fixtures")
@@ -225,7 +263,8 @@ def main():
                      ("sequences", lambda: sequences(R)),
                      ("resample", lambda: resampling(R, rng)),
                      ("weight", lambda: weights(R, rng)),
-                     ("pf", lambda: pf_runs(R))):
+                     ("pf", lambda: pf_runs(R)),
+                     ("genealogy", lambda: genealogy(R, rng))):
         data = fn()
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **data)

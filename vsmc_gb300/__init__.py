@@ -156,6 +156,19 @@ PROTOTYPES = {
     "vsmc_cuda_batch_create_bearings": (
         I32, [ctypes.POINTER(VP), SZ, VP, VP, VP, VP, VP, I32, F64, VP]),
     "vsmc_cuda_batch_destroy": (I32, [VP]),
+    "vsmc_cuda_resample_index_trace": (I32, [SZ, SZ, VP, SZ, VP, VP]),
+    "vsmc_cuda_resample_index_matrix": (I32, [SZ, SZ, VP, I32, VP, VP]),
+    "vsmc_cuda_sampler_print": (I32, [SZ, SZ, VP, VP, SZ, ctypes.c_char_p,
+                                      VP, SZ, VP, ctypes.c_char, VP, SZ,
+                                      ctypes.POINTER(SZ)]),
+    "vsmc_cuda_pf_record_genealogy": (I32, [VP, I32]),
+    "vsmc_cuda_pf_set_mcmc": (I32, [VP, SZ, F64]),
+    "vsmc_cuda_pf_mcmc_accepts": (I32, [VP, SZ, VP]),
+    "vsmc_cuda_cv_mcmc_f32": (I32, [SZ, SZ, SZ, U32, _MODELP, VP, F64, VP, VP,
+                                    VP, VP]),
+    "vsmc_cuda_pf_genealogy": (I32, [VP, ctypes.POINTER(VP)]),
+    "vsmc_cuda_pf_print": (I32, [VP, SZ, ctypes.c_char, VP, SZ,
+                                 ctypes.POINTER(SZ)]),
     "vsmc_cuda_bearings_simulate": (I32, [U32, SZ, _BMODELP, VP, VP, VP]),
     "vsmc_cuda_mlp_sizes": (I32, [ctypes.POINTER(SZ), ctypes.POINTER(SZ)]),
     "vsmc_cuda_mlp_init": (I32, [U32, VP, VP]),
@@ -231,6 +244,30 @@ def check(status, where=""):
 def call(name, *args):
     """Call an entry point and raise VsmcCudaError on a non-zero status."""
     return check(getattr(lib(), name)(*args), name)
+
+
+def sampler_print(resampled, ess, mean, N, sep="\t", accept=None,
+                  mon_name="pos"):
+    """Sampler::print text from host histories (host-only code path)."""
+    import numpy as np
+    res = np.ascontiguousarray(resampled, dtype=np.int32)
+    es = np.ascontiguousarray(ess, dtype=np.float64)
+    mn = np.ascontiguousarray(mean, dtype=np.float64)
+    T = len(es)
+    nmon = mn.shape[1] if mn.ndim == 2 else 0
+    acc = None
+    nacc = 1
+    if accept is not None:
+        acc = np.ascontiguousarray(accept, dtype=np.uint64)
+        nacc = acc.shape[1] if acc.ndim == 2 else 1
+    n = SZ()
+    args = [T, N, res.ctypes.data, es.ctypes.data, nmon, mon_name.encode(),
+            mn.ctypes.data, nacc, acc.ctypes.data if acc is not None else None,
+            sep.encode()]
+    lib().vsmc_cuda_sampler_print(*args, None, 0, ctypes.byref(n))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    call("vsmc_cuda_sampler_print", *args, buf, len(buf), ctypes.byref(n))
+    return buf.value.decode()
 
 
 def rng(kind=PHILOX4X32, seed=0, key=None, ctr=None):
@@ -466,6 +503,33 @@ class ParticleFilter:
         call("vsmc_cuda_pf_history", self.handle, T, mean.ctypes.data,
              ess.ctypes.data, res.ctypes.data, logz.ctypes.data)
         return {"mean": mean, "ess": ess, "resampled": res, "logz": logz}
+
+    def set_mcmc(self, sweeps, scale):
+        call("vsmc_cuda_pf_set_mcmc", self.handle, sweeps, scale)
+
+    def mcmc_accepts(self, T):
+        import numpy as np
+        out = np.zeros(T, dtype=np.uint32)
+        call("vsmc_cuda_pf_mcmc_accepts", self.handle, T, out.ctypes.data)
+        return out
+
+    def record_genealogy(self, on=True):
+        call("vsmc_cuda_pf_record_genealogy", self.handle, 1 if on else 0)
+
+    def genealogy_ptr(self):
+        p = VP()
+        call("vsmc_cuda_pf_genealogy", self.handle, ctypes.byref(p))
+        return p.value
+
+    def print_tsv(self, T, sep="\t"):
+        """Sampler::print text of the first T steps."""
+        n = SZ()
+        lib().vsmc_cuda_pf_print(self.handle, T, sep.encode(), None, 0,
+                                 ctypes.byref(n))
+        buf = ctypes.create_string_buffer(n.value + 1)
+        call("vsmc_cuda_pf_print", self.handle, T, sep.encode(), buf,
+             len(buf), ctypes.byref(n))
+        return buf.value.decode()
 
     def state_ptrs(self):
         s, w = VP(), VP()

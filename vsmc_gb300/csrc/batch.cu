@@ -151,15 +151,17 @@ __device__ __forceinline__ void store_run(float *p, const float (&v)[kPPT])
     }
 }
 
-// The tile's record (FP32 within a warp, FP64 across warps) and, in the
-// block that finishes a filter's last tile, the filter's FP64 combination:
-// ESS, log-evidence increment, resampling decision and histories (or, at
-// t == T, the last weighted mean).  All threads of the block call it.
+// The record of `count` consecutive tiles of one filter done by this block
+// (FP32 within a warp, FP64 across warps), written at the first of them
+// (the others get empty records) and, in the block that completes the
+// filter's last tile, the filter's FP64 combination: ESS, log-evidence
+// increment, resampling decision and histories (or, at t == T, the last
+// weighted mean).  All threads of the block call it.
 template <int kBlock, bool First>
 __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
-    const BFilter &F, PfScalars &S, uint32_t t, bool mon, float m, float s,
-    float s2, float sx, float sy, float sw, float *shm, double (*sh)[kBlock / 32],
-    float *shmax, bool &is_last)
+    uint32_t count, const BFilter &F, PfScalars &S, uint32_t t, bool mon,
+    float m, float s, float s2, float sx, float sy, float sw, float *shm,
+    double (*sh)[kBlock / 32], float *shmax, bool &is_last)
 {
     constexpr int kW = kBlock / 32;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -198,8 +200,11 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
             }
         }
         a.part[tile] = p;
+        const MovePartial empty = {0, 0, 0, -INFINITY, 0, 0};
+        for (uint32_t k = 1; k < count; ++k)
+            a.part[tile + k] = empty;
         __threadfence();
-        is_last = atomicAdd(&S.done, 1u) == F.ntiles - 1;
+        is_last = atomicAdd(&S.done, count) == F.ntiles - count;
     }
     __syncthreads();
     if (!is_last)
@@ -319,9 +324,19 @@ __device__ __forceinline__ void bearings_one(const BearingsConst &c,
     lse_push(lw, m, s, s2);
 }
 
+// This block's contiguous run [lo, hi) of the step's active tiles.
+__device__ __forceinline__ void tile_run(
+    uint32_t ntiles, uint32_t &lo, uint32_t &hi)
+{
+    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+    lo = min(ntiles, blockIdx.x * per);
+    hi = min(ntiles, lo + per);
+}
+
 // One global step of every running filter (bootstrap kinds).  A filter at
 // t < T moves and weights its particles; at t == T it only records the
-// weighted mean of its final particles.
+// weighted mean of its final particles.  Each block takes a contiguous run
+// of tiles and records one reduction per filter it touches.
 template <int kBlock, int kPPT, bool First, int Kind>
 __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
 {
@@ -333,7 +348,11 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
     __shared__ double sh[5][kW];
     __shared__ float shmax[kW + 1];
     __shared__ bool is_last;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    uint32_t lo, hi;
+    tile_run(ntiles, lo, hi);
+    uint32_t seg = lo;
+    float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
+    for (uint32_t tile = lo; tile < hi; ++tile) {
         const uint32_t f = a.tile_filter[tile];
         const BFilter F = a.flt[f];
         PfScalars &S = a.st[f];
@@ -350,7 +369,6 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
                 ox = static_cast<float>(a.obs[F.obs_off + t]);
             }
         }
-        float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
         const uint32_t i0 = (tile - F.tile0) * kTile + threadIdx.x * kPPT;
         const bool full = i0 + kPPT <= F.n;
         float X[kPPT], Y[kPPT], VX[kPPT], VY[kPPT], LW[kPPT];
@@ -359,7 +377,15 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
             X[k] = Y[k] = VX[k] = VY[k] = LW[k] = 0.0f;
         if (!First) {
             const uint32_t g0 = F.off + i0;
-            if (!gather && full) {
+            // after a resample, a group whose slots all keep their own
+            // particle reads like an unresampled one
+            bool own = !gather;
+            if (gather && full && kPPT == 4) {
+                const int4 I = __ldcs(reinterpret_cast<const int4 *>(a.idx + g0));
+                const int b = static_cast<int>(i0);
+                own = I.x == b && I.y == b + 1 && I.z == b + 2 && I.w == b + 3;
+            }
+            if (own && full) {
                 load_run<kPPT>(a.ax + g0, X);
                 load_run<kPPT>(a.ay + g0, Y);
                 load_run<kPPT>(a.avx + g0, VX);
@@ -430,9 +456,15 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
                     }
             }
         }
-        tile_finish<kBlock, First>(a, tile, F, S, t, mon, m, s, s2, sx, sy,
-            sw, shm, sh, shmax, is_last);
-        __syncthreads();
+        // the filter's segment ends here: record it
+        if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
+            tile_finish<kBlock, First>(a, seg, tile + 1 - seg, F, S, t, mon,
+                m, s, s2, sx, sy, sw, shm, sh, shmax, is_last);
+            __syncthreads();
+            m = -INFINITY;
+            s = s2 = sx = sy = sw = 0;
+            seg = tile + 1;
+        }
     }
 }
 
@@ -458,7 +490,11 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         load_packed(sp, a.packed);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int g = lane >> 2, q = lane & 3;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    uint32_t lo, hi;
+    tile_run(ntiles, lo, hi);
+    uint32_t seg = lo;
+    float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
+    for (uint32_t tile = lo; tile < hi; ++tile) {
         const uint32_t f = a.tile_filter[tile];
         const BFilter F = a.flt[f];
         const BearingsConst &c = F.bc;
@@ -480,7 +516,6 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
             vy = a.avy[F.off + src];
             lw = resampled ? 0.0f : a.lw[F.off + i];
         }
-        float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
         if (mon) {
             if (mine) {
                 const float wo = resampled ? 1.0f : __expf(lw - Mprev);
@@ -533,9 +568,14 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
             a.bvy[gi] = vy;
             a.lw[gi] = lw;
         }
-        tile_finish<kLearnBlock, First>(a, tile, F, S, t, mon, m, s, s2, sx,
-            sy, sw, shm, sh, shmax, is_last);
-        __syncthreads();
+        if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
+            tile_finish<kLearnBlock, First>(a, seg, tile + 1 - seg, F, S, t,
+                mon, m, s, s2, sx, sy, sw, shm, sh, shmax, is_last);
+            __syncthreads();
+            m = -INFINITY;
+            s = s2 = sx = sy = sw = 0;
+            seg = tile + 1;
+        }
     }
 }
 
@@ -819,7 +859,7 @@ __global__ void k_batch_simulate_bearings(
         truth ? truth + 4 * obs_off[f] : nullptr, obs + obs_off[f]);
 }
 
-constexpr int kResBlock = 512;
+constexpr int kResBlock = 1024;
 
 struct Shape {
     int ppt, block;

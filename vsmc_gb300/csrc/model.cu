@@ -62,6 +62,35 @@ __global__ void k_cv_simulate(uint32_t seed, uint32_t T, double dt,
         truth, obs);
 }
 
+// Kernel-level resample-move steps (cv_mcmc_step) on caller-owned state.
+__global__ void __launch_bounds__(256) k_cv_mcmc(uint32_t n, uint32_t t,
+    uint32_t sweeps, uint32_t seed, CvConst<float> c, float ox, float oy,
+    float s_rw, float inv_var, const int *parent, float *sx, float *sy,
+    float *svx, float *svy, uint32_t *accepted)
+{
+    uint32_t acc = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const uint32_t j = parent ? static_cast<uint32_t>(parent[i]) : i;
+        float x = sx[i], y = sy[i], vx = svx[i], vy = svy[i];
+        float ax, ay;
+        cv_innovation(c, t, seed, j, ax, ay);
+        float lt =
+            -0.5f * inv_var * (ax * ax + ay * ay) + cv_loglik(c, ox, oy, x, y);
+        for (uint32_t k = 0; k < sweeps; ++k)
+            acc += cv_mcmc_step(
+                c, ox, oy, s_rw, inv_var, t, seed, i, k, x, y, vx, vy, ax, ay, lt);
+        sx[i] = x;
+        sy[i] = y;
+        svx[i] = vx;
+        svy[i] = vy;
+    }
+    __shared__ uint32_t sh[256 / 32 + 1];
+    acc = block_reduce(acc, OpAdd(), 0u, sh);
+    if (threadIdx.x == 0 && acc)
+        atomicAdd(accepted, acc);
+}
+
 template <typename T>
 static int cv_move_impl(size_t n, size_t t, uint32_t seed,
     const vsmc_cuda_cv_model *model, const double obs[2], T *state, T *ll,
@@ -100,6 +129,30 @@ int vsmc_cuda_cv_move_f32(size_t n, size_t t, uint32_t seed,
     float *ll, void *stream)
 {
     return cv_move_impl<float>(n, t, seed, model, obs, state, ll, stream);
+}
+
+int vsmc_cuda_cv_mcmc_f32(size_t n, size_t t, size_t sweeps, uint32_t seed,
+    const vsmc_cuda_cv_model *model, const double obs[2], double scale,
+    const int *parent, float *state, uint32_t *accepted, void *stream)
+{
+    if (!valid_cv_model(model) || obs == nullptr || accepted == nullptr ||
+        !(scale >= 0) || !(model->sigma_a > 0) || (state == nullptr && n))
+        return VSMC_CUDA_ERR_ARG;
+    if (n >= (size_t(1) << 31) || t < 1 || t > 0xFFFFFFFFull ||
+        sweeps > 1024)
+        return t < 1 ? VSMC_CUDA_ERR_ARG : VSMC_CUDA_ERR_SIZE;
+    if (n == 0 || sweeps == 0)
+        return VSMC_CUDA_OK;
+    const CvConst<float> c = make_cv_const<float>(*model);
+    const float sa = static_cast<float>(model->sigma_a);
+    k_cv_mcmc<<<grid_for(n, 256, 1, 8), 256, 0, as_stream(stream)>>>(
+        static_cast<uint32_t>(n), static_cast<uint32_t>(t),
+        static_cast<uint32_t>(sweeps), seed, c, static_cast<float>(obs[0]),
+        static_cast<float>(obs[1]), static_cast<float>(scale),
+        1.0f / (sa * sa), parent, state, state + n, state + 2 * n,
+        state + 3 * n, accepted);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
 }
 
 int vsmc_cuda_cv_simulate(uint32_t seed, size_t T,

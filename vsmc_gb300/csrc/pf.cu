@@ -13,6 +13,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <vector>
 
 using namespace vsmc_cuda;
 
@@ -98,15 +99,36 @@ static int launch_step32(vsmc_cuda_pf *pf, bool first)
     else
         k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
     launch_resample32(pf);
+    if (pf->record_gen)
+        k_pf32_record<<<grid_for(pf->n, kPfBlock, 4, 8), kPfBlock, 0,
+            pf->stream>>>(a, pf->gen);
+    if (pf->mcmc_sweeps > 0) {
+        // resample-move: the moved (or copied) state goes back to buffer
+        // cur, so the step's input buffer stays the current one
+        float *A = buf32(pf, pf->cur);
+        const size_t ld = pf->stride;
+        const float sa = static_cast<float>(pf->model.sigma_a);
+        k_pf32_mcmc<<<grid_for(pf->n, kPfBlock, 1, 8), kPfBlock, 0,
+            pf->stream>>>(a, A, A + ld, A + 2 * ld, A + 3 * ld,
+            pf->mcmc_sweeps, pf->mcmc_scale, 1.0f / (sa * sa), pf->h_acc);
+        k_pf32_clear_gather<<<1, 1, 0, pf->stream>>>(pf->sc);
+    }
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
+}
+
+// the buffer holding the state after a step
+static void advance_buffer(vsmc_cuda_pf *pf)
+{
+    if (pf->mcmc_sweeps == 0)
+        pf->cur = 1 - pf->cur;
 }
 
 static int launch_first32(vsmc_cuda_pf *pf)
 {
     const int rc = launch_step32(pf, true);
     if (rc == VSMC_CUDA_OK)
-        pf->cur = 1 - pf->cur;
+        advance_buffer(pf);
     return rc;
 }
 
@@ -115,7 +137,7 @@ static int step32(vsmc_cuda_pf *pf)
     if (!pf->use_graph) {
         const int rc = launch_step32(pf, false);
         if (rc == VSMC_CUDA_OK)
-            pf->cur = 1 - pf->cur;
+            advance_buffer(pf);
         return rc;
     }
     const int par = pf->cur;
@@ -132,7 +154,7 @@ static int step32(vsmc_cuda_pf *pf)
         VSMC_CUDA_TRY(cudaGraphInstantiate(&pf->graph_exec[par], g, 0));
     }
     VSMC_CUDA_TRY(cudaGraphLaunch(pf->graph_exec[par], pf->stream));
-    pf->cur = 1 - pf->cur;
+    advance_buffer(pf);
     return VSMC_CUDA_OK;
 }
 
@@ -203,7 +225,9 @@ static void free_all(vsmc_cuda_pf *pf)
         if (pf->graph[k])
             cudaGraphDestroy(pf->graph[k]);
     }
-    void *ptrs[] = {pf->state, pf->state2, pf->weight, pf->obs, pf->h_mean,
+    void *ptrs[] = {pf->h_acc, pf->gen, pf->state, pf->state2, pf->weight,
+        pf->obs,
+        pf->h_mean,
         pf->h_ess, pf->h_logz, pf->h_res, pf->sc, pf->part, pf->qpart,
         pf->epart, pf->cpart, pf->mpart, pf->rep, pf->idx, pf->marks,
         pf->empties};
@@ -464,6 +488,9 @@ static int pf_begin(vsmc_cuda_pf *pf)
     int rc = reset_scalars(pf);
     if (rc != VSMC_CUDA_OK)
         return rc;
+    if (pf->h_acc)
+        VSMC_CUDA_TRY(cudaMemsetAsync(pf->h_acc, 0,
+            sizeof(uint32_t) * pf->max_steps, pf->stream));
     pf->t = 0;
     pf->mean_pending = false;
     rc = pf->precision == 32 ? launch_first32(pf) : pf64_step(pf, true);
@@ -558,6 +585,102 @@ int vsmc_cuda_pf_history(vsmc_cuda_pf *pf, size_t T, double *mean_host,
         VSMC_CUDA_TRY(cudaMemcpyAsync(logz_host, pf->h_logz,
             T * sizeof(double), cudaMemcpyDeviceToHost, st));
     return sync_and_check(pf);
+}
+
+static void drop_graphs(vsmc_cuda_pf *pf)
+{
+    for (int k = 0; k < 2; ++k) {
+        if (pf->graph_exec[k])
+            cudaGraphExecDestroy(pf->graph_exec[k]);
+        if (pf->graph[k])
+            cudaGraphDestroy(pf->graph[k]);
+        pf->graph_exec[k] = nullptr;
+        pf->graph[k] = nullptr;
+    }
+}
+
+int vsmc_cuda_pf_record_genealogy(vsmc_cuda_pf *pf, int on)
+{
+    if (pf == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
+    if (on && pf->gen == nullptr) {
+        void *p = nullptr;
+        VSMC_CUDA_TRY(cudaMalloc(&p, sizeof(int32_t) * pf->n * pf->max_steps));
+        pf->gen = static_cast<int32_t *>(p);
+    }
+    if ((on != 0) != pf->record_gen)
+        drop_graphs(pf); // captured with or without the record kernel
+    pf->record_gen = on != 0;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_set_mcmc(vsmc_cuda_pf *pf, size_t sweeps, double scale)
+{
+    if (pf == nullptr || pf->precision != 32 || !(scale >= 0) ||
+        !(pf->model.sigma_a > 0) || pf->t != 0)
+        return VSMC_CUDA_ERR_ARG;
+    if (sweeps > 1024)
+        return VSMC_CUDA_ERR_SIZE;
+    if (sweeps > 0 && pf->h_acc == nullptr) {
+        void *p = nullptr;
+        VSMC_CUDA_TRY(cudaMalloc(&p, sizeof(uint32_t) * pf->max_steps));
+        pf->h_acc = static_cast<uint32_t *>(p);
+        VSMC_CUDA_TRY(cudaMemset(pf->h_acc, 0, sizeof(uint32_t) * pf->max_steps));
+    }
+    if (static_cast<uint32_t>(sweeps) != pf->mcmc_sweeps)
+        drop_graphs(pf);
+    pf->mcmc_sweeps = static_cast<uint32_t>(sweeps);
+    pf->mcmc_scale = static_cast<float>(scale);
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_mcmc_accepts(vsmc_cuda_pf *pf, size_t T, uint32_t *host)
+{
+    if (pf == nullptr || host == nullptr || pf->h_acc == nullptr ||
+        T > pf->max_steps)
+        return VSMC_CUDA_ERR_ARG;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(host, pf->h_acc, sizeof(uint32_t) * T,
+        cudaMemcpyDeviceToHost, pf->stream));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_genealogy(vsmc_cuda_pf *pf, const int **rows_dev)
+{
+    if (pf == nullptr || rows_dev == nullptr || pf->gen == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    *rows_dev = pf->gen;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_print(vsmc_cuda_pf *pf, size_t T, char sep, char *buf,
+    size_t cap, size_t *len)
+{
+    if (pf == nullptr || len == nullptr || T > pf->max_steps)
+        return VSMC_CUDA_ERR_ARG;
+    std::vector<double> mean(2 * T), ess(T), logz(T);
+    std::vector<int> res(T);
+    if (T > 0) {
+        const int rc = vsmc_cuda_pf_history(
+            pf, T, mean.data(), ess.data(), res.data(), logz.data());
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+    }
+    if (pf->mcmc_sweeps == 0)
+        return vsmc_cuda_sampler_print(T, pf->n, res.data(), ess.data(), 2,
+            "pos", mean.data(), 0, nullptr, sep, buf, cap, len);
+    // the move accepts every particle; the MCMC column is the accept count
+    std::vector<uint32_t> acc(T);
+    VSMC_CUDA_TRY(cudaMemcpyAsync(acc.data(), pf->h_acc,
+        sizeof(uint32_t) * T, cudaMemcpyDeviceToHost, pf->stream));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
+    std::vector<size_t> a2(2 * T);
+    for (size_t t = 0; t < T; ++t) {
+        a2[2 * t] = pf->n;
+        a2[2 * t + 1] = acc[t];
+    }
+    return vsmc_cuda_sampler_print(T, pf->n, res.data(), ess.data(), 2, "pos",
+        mean.data(), 2, a2.data(), sep, buf, cap, len);
 }
 
 int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,

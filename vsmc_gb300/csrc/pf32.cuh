@@ -824,6 +824,73 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_fill(const Rs32Args a)
         atomicOr(&a.sc->err, err);
 }
 
+// Genealogy row of the step just finished (t = step - 1): each particle's
+// parent among the step's particles before resampling, or itself when the
+// step did not resample.
+__global__ void __launch_bounds__(kPfBlock) k_pf32_record(
+    const Pf32Args a, int32_t *rows)
+{
+    const uint32_t t = a.sc->step - 1;
+    if (t >= a.max_steps)
+        return;
+    const bool res = a.sc->resampled != 0;
+    int32_t *row = rows + static_cast<size_t>(t) * a.n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += gridDim.x * blockDim.x) {
+        uint32_t src = res ? source_of(a.idx, a.srcs, a.idx[i]) : i;
+        if (src >= a.n) {
+            atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+            src = 0;
+        }
+        row[i] = static_cast<int32_t>(src);
+    }
+}
+
+// Resample-move: after a step that resampled (t >= 1), `sweeps` random-walk
+// Metropolis steps (cv_mcmc_step) on each particle's acceleration, on the
+// gathered state; the result goes to the other buffer (out).  Steps that
+// did not resample (weights not equal) copy the state through unchanged.
+// acc_hist[t] += the accepted steps.
+__global__ void __launch_bounds__(kPfBlock) k_pf32_mcmc(const Pf32Args a,
+    float *ox_, float *oy_, float *ovx, float *ovy, uint32_t sweeps,
+    float s_rw, float inv_var, uint32_t *acc_hist)
+{
+    const uint32_t t = a.sc->step - 1;
+    const bool gather = a.sc->gather != 0;
+    const bool move = a.sc->resampled != 0 && t >= 1;
+    const uint32_t to = t < a.max_steps ? t : a.max_steps - 1;
+    const float obx = static_cast<float>(a.obs[2 * to + 0]);
+    const float oby = static_cast<float>(a.obs[2 * to + 1]);
+    uint32_t acc = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += gridDim.x * blockDim.x) {
+        uint32_t src = gather ? source_of(a.idx, a.srcs, a.idx[i]) : i;
+        if (src >= a.n) {
+            atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+            src = 0;
+        }
+        // the step's output is in the b buffer
+        float x = a.bx[src], y = a.by[src], vx = a.bvx[src], vy = a.bvy[src];
+        if (move) {
+            float ax, ay;
+            cv_innovation(a.c, t, a.seed, src, ax, ay);
+            float lt = -0.5f * inv_var * (ax * ax + ay * ay) +
+                cv_loglik(a.c, obx, oby, x, y);
+            for (uint32_t k = 0; k < sweeps; ++k)
+                acc += cv_mcmc_step(a.c, obx, oby, s_rw, inv_var, t, a.seed, i,
+                    k, x, y, vx, vy, ax, ay, lt);
+        }
+        ox_[i] = x;
+        oy_[i] = y;
+        ovx[i] = vx;
+        ovy[i] = vy;
+    }
+    __shared__ uint32_t sh[kPfBlock / 32 + 1];
+    acc = block_reduce(acc, OpAdd(), 0u, sh);
+    if (threadIdx.x == 0 && acc && t < a.max_steps)
+        atomicAdd(acc_hist + t, acc);
+}
+
 // parent index of every slot from the encoded idx (reference layout)
 __global__ void __launch_bounds__(kPfBlock) k_rs32_decode(
     const Rs32Args a, int32_t *parent)

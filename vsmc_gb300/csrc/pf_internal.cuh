@@ -47,6 +47,11 @@ struct vsmc_cuda_pf {
     int32_t *rep = nullptr;
     int32_t *idx = nullptr;
     uint32_t *marks = nullptr, *empties = nullptr;
+    uint32_t mcmc_sweeps = 0; // FP32 resample-move: sweeps after resampling
+    float mcmc_scale = 0;
+    uint32_t *h_acc = nullptr; // accepted MCMC steps per step (max_steps)
+    int32_t *gen = nullptr; // FP32 genealogy rows (max_steps x n) or null
+    bool record_gen = false;
     cudaGraph_t graph[2] = {nullptr, nullptr};
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr}; // by buffer parity
 

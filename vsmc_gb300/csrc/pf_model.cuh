@@ -127,4 +127,52 @@ __device__ __forceinline__ void cv_move(const CvConst<double> &c, double ax,
     vy = __dadd_rn(vy, __dmul_rn(c.dt, ay));
 }
 
+// The acceleration innovation (2D) of particle j at step t >= 1: the pair
+// cv_move drew for it.
+__device__ __forceinline__ void cv_innovation(const CvConst<float> &c,
+    uint32_t t, uint32_t seed, uint32_t j, float &ax, float &ay)
+{
+    const u32x4 w = particle_block(t, seed, j);
+    float z1, z2;
+    normal_pair_f(w.x, w.y, z1, z2);
+    ax = c.sigma_a * z1;
+    ay = c.sigma_a * z2;
+}
+
+// One random-walk Metropolis step on a particle's acceleration innovation
+// a, the RandomWalk / NormalMVProposal update of rng/random_walk.hpp:95-114
+// with an unbounded Normal proposal (log q ratio 0): the state is
+// x_t = F x_{t-1} + G a, so a' = a + s e moves it by G (a' - a); the target
+// is N(a; 0, sigma_a^2 I) g(y | x_t) and the step accepts when
+// log u < lt' - lt with u in [0, 1).  Words: Philox4x32 key {t, seed},
+// counter {2 + k, i, 0, 0} (k the sweep, i the particle's slot): the first
+// two give the proposal pair, the third u.  lt holds the log target of the
+// current (x, a); returns 1 on acceptance.
+__device__ __forceinline__ int cv_mcmc_step(const CvConst<float> &c,
+    float ox, float oy, float s_rw, float inv_var, uint32_t t, uint32_t seed,
+    uint32_t i, uint32_t k, float &x, float &y, float &vx, float &vy,
+    float &ax, float &ay, float &lt)
+{
+    const u32x4 w = philox4x32_10(2u + k, i, 0u, 0u, t, seed);
+    float e1, e2;
+    normal_pair_f(w.x, w.y, e1, e2);
+    const float bx = ax + s_rw * e1, by = ay + s_rw * e2;
+    const float dx = bx - ax, dy = by - ay;
+    const float nx = x + c.h * dx, ny = y + c.h * dy;
+    const float nvx = vx + c.dt * dx, nvy = vy + c.dt * dy;
+    const float lt2 =
+        -0.5f * inv_var * (bx * bx + by * by) + cv_loglik(c, ox, oy, nx, ny);
+    if (logf(u01_co_f(w.z)) < lt2 - lt) {
+        x = nx;
+        y = ny;
+        vx = nvx;
+        vy = nvy;
+        ax = bx;
+        ay = by;
+        lt = lt2;
+        return 1;
+    }
+    return 0;
+}
+
 } // namespace vsmc_cuda
