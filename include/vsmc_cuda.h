@@ -373,8 +373,10 @@ int vsmc_cuda_bearings_simulate(uint32_t seed, size_t T,
     const vsmc_cuda_bearings_model *model, double *truth, double *obs,
     void *stream);
 
-/* The proposal network: inputs (x / 10, y / 10, vx, vy, sin z, cos z),
- * two hidden layers of 64 (GELU, tanh form), outputs (m, l): the mean and
+/* The proposal network: inputs from the previous state and the bearing --
+ * the predicted position p = (x + dt vx, y + dt vy) as p / (10 + |p|), the
+ * velocity as v / (1 + |v|), sin z, cos z -- two hidden layers of 64 (GELU,
+ * tanh form), outputs (m, l): the mean and
  * diagonal log-variance of the whitened transition noise nu (x = F x' + L nu,
  * L = chol(Q)).  Parameters: FP32, *nparams floats (W1[64][6], b1[64],
  * W2[64][64], b2[64], W3[8][64], b3[8]); the packed copy (BF16 operand
@@ -433,7 +435,7 @@ int vsmc_cuda_batch_create(vsmc_cuda_batch **batch, size_t nfilters,
  * (packed == NULL) or the learned proposal (packed: the packed proposal
  * network, device, kept by pointer for the batch's lifetime).  Observations
  * are one bearing per step (filter f's block starts at entry
- * T[0] + ... + T[f-1]).  The learned kind has a fixed kernel shape (16
+ * T[0] + ... + T[f-1]).  The learned kind has a fixed kernel shape (32
  * particles per warp; set_shape and autotune refuse it). */
 int vsmc_cuda_batch_create_bearings(vsmc_cuda_batch **batch, size_t nfilters,
     const uint32_t *n, const uint32_t *T,

@@ -1628,7 +1628,11 @@ void vo_bearings_move_f32(size_t N, size_t t, uint32_t seed,
         } else {
             float nu[4] = {ev[0], ev[1], ev[2], ev[3]};
             if (params) {
-                const float f[6] = {x * 0.1f, y * 0.1f, vx, vy, sz, cz};
+                /* predicted position and velocity on bounded scales */
+                const float px = x + dt * vx, py = y + dt * vy;
+                const float ip = 1.0f / (10.0f + sqrtf(px * px + py * py));
+                const float iv = 1.0f / (1.0f + sqrtf(vx * vx + vy * vy));
+                const float f[6] = {px * ip, py * ip, vx * iv, vy * iv, sz, cz};
                 vo_mlp_row r;
                 vo_mlp_row_forward(params, f, &r);
                 for (int d = 0; d < 4; ++d) {

@@ -193,8 +193,11 @@ def _samples(m, M, T, rng):
         xn[1] = x[1] + m.dt * x[3] + l11 * nu[2]
         xn[3] = x[3] + l21 * nu[2] + l22 * nu[3]
         z = np.arctan2(xn[1], xn[0]) + m.sigma_z * rng.normal(size=M)
-        feats.append(np.stack([x[0] / 10, x[1] / 10, x[2], x[3], np.sin(z),
-                               np.cos(z)], axis=1))
+        px, py = x[0] + m.dt * x[2], x[1] + m.dt * x[3]
+        ip = 1 / (10 + np.hypot(px, py))
+        iv = 1 / (1 + np.hypot(x[2], x[3]))
+        feats.append(np.stack([px * ip, py * ip, x[2] * iv, x[3] * iv,
+                               np.sin(z), np.cos(z)], axis=1))
         nus.append(nu.T)
         x = xn
     return (np.concatenate(feats).astype(np.float32),

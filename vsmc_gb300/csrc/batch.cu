@@ -468,12 +468,13 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
     }
 }
 
-constexpr int kLearnBlock = 128;                    // 4 warps
-constexpr uint32_t kLearnTile = kLearnBlock / 2;     // 16 particles a warp
+constexpr int kLearnBlock = 128;                // 4 warps
+constexpr uint32_t kLearnTile = kLearnBlock;     // 32 particles a warp
 
 // One global step of the learned-proposal filters.  Each warp evaluates the
-// proposal network for 16 particles on the tensor cores; lanes 4g and
-// 4g + 1 then move particles g and g + 8 of the warp's 16.
+// proposal network for 32 particles on the tensor cores (two 16-row tiles
+// sharing the weight loads); lane 4g + q then moves particle g + 8q of the
+// warp's 32.
 template <bool First>
 __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
     const BatchArgs a)
@@ -504,9 +505,9 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         const bool gather = First ? false : (S.gather != 0);
         const float Mprev = First ? 0.0f : static_cast<float>(S.M);
         const float z = mon ? 0.0f : static_cast<float>(a.obs[F.obs_off + t]);
-        const uint32_t i = (tile - F.tile0) * kLearnTile + 16 * wid + g +
-            (q == 1 ? 8u : 0u);
-        const bool mine = q < 2 && i < F.n;
+        const uint32_t i =
+            (tile - F.tile0) * kLearnTile + 32 * wid + g + 8 * q;
+        const bool mine = i < F.n;
         float x = 0, y = 0, vx = 0, vy = 0, lw = 0;
         if (!First && mine) {
             const uint32_t src = gather ? batch_source(a, F, S, i) : i;
@@ -534,12 +535,12 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         } else {
             float fe[6];
             bearings_features(c, x, y, vx, vy, sinf(z), cosf(z), fe);
-            uint32_t a0[4];
-            features_to_a(fe, a0);
-            float o[4];
-            mlp_forward_warp<false>(sp, a0, o);
+            uint32_t a0[4], b0[4];
+            features_to_a2(fe, a0, b0);
+            float oa[4], ob[4];
+            mlp_forward_warp2(sp, a0, b0, oa, ob);
             float v[8];
-            out_to_owner(o, v);
+            out_to_owner2(oa, ob, v);
             if (mine) {
                 const float lw_old = resampled ? 0.0f : lw - Mprev;
                 const float wo = resampled ? 1.0f : __expf(lw_old);

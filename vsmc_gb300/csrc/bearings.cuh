@@ -33,9 +33,8 @@ struct BearingsConst {
     float dt, l11, l21, l22; // transition Cholesky factor per axis
     float inv_sz, ll_c;      // 1 / sigma_z, -log(sigma_z sqrt(2 pi))
     float x0, y0, vx0, vy0, sd_pos0, sd_vel0;
-    float fscale; // network input scale for the positions
     float lmin, lmax; // log-variance clamp of the learned proposal
-    float pad;
+    float pad[2];
 };
 
 inline bool valid_bearings_model(const vsmc_cuda_bearings_model *m)
@@ -78,10 +77,9 @@ inline BearingsConst make_bearings_const(const vsmc_cuda_bearings_model &m)
     c.vy0 = static_cast<float>(m.vy0);
     c.sd_pos0 = static_cast<float>(m.sd_pos0);
     c.sd_vel0 = static_cast<float>(m.sd_vel0);
-    c.fscale = 0.1f;
     c.lmin = -12.0f;
     c.lmax = 4.0f;
-    c.pad = 0;
+    c.pad[0] = c.pad[1] = 0;
     return c;
 }
 
@@ -127,14 +125,21 @@ __device__ __forceinline__ float bearings_loglik(
     return c.ll_c - 0.5f * s * s;
 }
 
-// the network inputs of a particle at its previous state and the bearing
+// The network inputs of a particle at its previous state and the bearing:
+// the predicted position p = (x + dt vx, y + dt vy) as p / (10 + |p|) (its
+// direction, and its range on a saturating scale), the velocity as
+// v / (1 + |v|), and (sin z, cos z).  Bounded inputs keep the activations
+// in range however far the target drifts.
 __device__ __forceinline__ void bearings_features(const BearingsConst &c,
     float x, float y, float vx, float vy, float sz, float cz, float (&f)[6])
 {
-    f[0] = x * c.fscale;
-    f[1] = y * c.fscale;
-    f[2] = vx;
-    f[3] = vy;
+    const float px = x + c.dt * vx, py = y + c.dt * vy;
+    const float ip = 1.0f / (10.0f + sqrtf(px * px + py * py));
+    const float iv = 1.0f / (1.0f + sqrtf(vx * vx + vy * vy));
+    f[0] = px * ip;
+    f[1] = py * ip;
+    f[2] = vx * iv;
+    f[3] = vy * iv;
     f[4] = sz;
     f[5] = cz;
 }

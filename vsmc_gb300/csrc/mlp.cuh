@@ -194,6 +194,76 @@ __device__ __forceinline__ void mlp_forward_warp(const uint32_t *packed,
     }
 }
 
+// Forward pass of one warp over 32 rows as two 16-row tiles (a, b) that
+// share every weight fragment load.  Accumulator outputs oa, ob.
+__device__ __forceinline__ void mlp_forward_warp2(const uint32_t *packed,
+    const uint32_t (&a0)[4], const uint32_t (&b0)[4], float (&oa)[4],
+    float (&ob)[4])
+{
+    const int lane = threadIdx.x & 31;
+    const int tig = lane & 3;
+    const float *bias = reinterpret_cast<const float *>(packed + kPackedBias);
+    float ha[8][4], hb[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const float bl = bias[8 * nt + 2 * tig];
+        const float bh = bias[8 * nt + 2 * tig + 1];
+        ha[nt][0] = hb[nt][0] = bl;
+        ha[nt][1] = hb[nt][1] = bh;
+        ha[nt][2] = hb[nt][2] = bl;
+        ha[nt][3] = hb[nt][3] = bh;
+        const uint2 w = frag(packed, kF1, nt, lane);
+        mma_bf16(ha[nt], a0, w.x, w.y);
+        mma_bf16(hb[nt], b0, w.x, w.y);
+    }
+    uint32_t xa[4][4], xb[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int kt = nt >> 1, hi = nt & 1;
+        xa[kt][0 + 2 * hi] = pack_bf16(gelu_f(ha[nt][0]), gelu_f(ha[nt][1]));
+        xa[kt][1 + 2 * hi] = pack_bf16(gelu_f(ha[nt][2]), gelu_f(ha[nt][3]));
+        xb[kt][0 + 2 * hi] = pack_bf16(gelu_f(hb[nt][0]), gelu_f(hb[nt][1]));
+        xb[kt][1 + 2 * hi] = pack_bf16(gelu_f(hb[nt][2]), gelu_f(hb[nt][3]));
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const float bl = bias[kHid + 8 * nt + 2 * tig];
+        const float bh = bias[kHid + 8 * nt + 2 * tig + 1];
+        ha[nt][0] = hb[nt][0] = bl;
+        ha[nt][1] = hb[nt][1] = bh;
+        ha[nt][2] = hb[nt][2] = bl;
+        ha[nt][3] = hb[nt][3] = bh;
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            const uint2 w = frag(packed, kF2, kt * 8 + nt, lane);
+            mma_bf16(ha[nt], xa[kt], w.x, w.y);
+            mma_bf16(hb[nt], xb[kt], w.x, w.y);
+        }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int kt = nt >> 1, hi = nt & 1;
+        xa[kt][0 + 2 * hi] = pack_bf16(gelu_f(ha[nt][0]), gelu_f(ha[nt][1]));
+        xa[kt][1 + 2 * hi] = pack_bf16(gelu_f(ha[nt][2]), gelu_f(ha[nt][3]));
+        xb[kt][0 + 2 * hi] = pack_bf16(gelu_f(hb[nt][0]), gelu_f(hb[nt][1]));
+        xb[kt][1 + 2 * hi] = pack_bf16(gelu_f(hb[nt][2]), gelu_f(hb[nt][3]));
+    }
+    {
+        const float bl = bias[2 * kHid + 2 * tig];
+        const float bh = bias[2 * kHid + 2 * tig + 1];
+        oa[0] = ob[0] = bl;
+        oa[1] = ob[1] = bh;
+        oa[2] = ob[2] = bl;
+        oa[3] = ob[3] = bh;
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) {
+            const uint2 w = frag(packed, kF3, kt, lane);
+            mma_bf16(oa, xa[kt], w.x, w.y);
+            mma_bf16(ob, xb[kt], w.x, w.y);
+        }
+    }
+}
+
 // copy the packed parameters into shared memory (all threads of the block)
 __device__ __forceinline__ void load_packed(
     uint32_t *dst, const uint32_t *src)
@@ -281,6 +351,57 @@ __device__ __forceinline__ void owner8_to_a(
     a[1] = pack_bf16(r1lo, r1hi);
     a[2] = 0;
     a[3] = 0;
+}
+
+
+// 32-row plumbing: lane 4g + q owns row g + 8q of the warp's 32 (tile a
+// holds rows 0..15, tile b rows 16..31).
+__device__ __forceinline__ void features_to_a2(
+    const float (&f)[6], uint32_t (&a)[4], uint32_t (&b)[4])
+{
+    const int lane = threadIdx.x & 31;
+    const int t = lane & 3;
+    const int base = lane & ~3;
+    float v[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float x = __shfl_sync(0xFFFFFFFFu, f[2 * p], base + q);
+            const float y = __shfl_sync(0xFFFFFFFFu, f[2 * p + 1], base + q);
+            if (t == p) {
+                v[q][0] = x;
+                v[q][1] = y;
+            }
+        }
+    }
+    a[0] = pack_bf16(v[0][0], v[0][1]);
+    a[1] = pack_bf16(v[1][0], v[1][1]);
+    a[2] = a[3] = 0;
+    b[0] = pack_bf16(v[2][0], v[2][1]);
+    b[1] = pack_bf16(v[3][0], v[3][1]);
+    b[2] = b[3] = 0;
+}
+
+__device__ __forceinline__ void out_to_owner2(
+    const float (&oa)[4], const float (&ob)[4], float (&v)[8])
+{
+    const int lane = threadIdx.x & 31;
+    const int base = lane & ~3;
+    const int q = lane & 3;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float a0 = __shfl_sync(0xFFFFFFFFu, oa[0], base + j);
+        const float a1 = __shfl_sync(0xFFFFFFFFu, oa[1], base + j);
+        const float a2 = __shfl_sync(0xFFFFFFFFu, oa[2], base + j);
+        const float a3 = __shfl_sync(0xFFFFFFFFu, oa[3], base + j);
+        const float b0 = __shfl_sync(0xFFFFFFFFu, ob[0], base + j);
+        const float b1 = __shfl_sync(0xFFFFFFFFu, ob[1], base + j);
+        const float b2 = __shfl_sync(0xFFFFFFFFu, ob[2], base + j);
+        const float b3 = __shfl_sync(0xFFFFFFFFu, ob[3], base + j);
+        v[2 * j] = q == 0 ? a0 : (q == 1 ? a2 : (q == 2 ? b0 : b2));
+        v[2 * j + 1] = q == 0 ? a1 : (q == 1 ? a3 : (q == 2 ? b1 : b3));
+    }
 }
 
 } // namespace vsmc_cuda

@@ -154,10 +154,9 @@ __global__ void __launch_bounds__(128) k_bearings_move(uint32_t n, uint32_t t,
     const int wglobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int g = lane >> 2, q = lane & 3;
-    const bool owner = q < 2;
-    for (uint32_t p0 = 16u * wglobal; p0 < n; p0 += 16u * nwarps) {
-        const uint32_t i = p0 + g + (q == 1 ? 8u : 0u);
-        const bool mine = owner && i < n;
+    for (uint32_t p0 = 32u * wglobal; p0 < n; p0 += 32u * nwarps) {
+        const uint32_t i = p0 + g + 8u * q;
+        const bool mine = i < n;
         float x = 0, y = 0, vx = 0, vy = 0;
         if (mine) {
             x = sx[i];
@@ -167,12 +166,12 @@ __global__ void __launch_bounds__(128) k_bearings_move(uint32_t n, uint32_t t,
         }
         float f[6];
         bearings_features(c, x, y, vx, vy, sz, cz, f);
-        uint32_t a0[4];
-        features_to_a(f, a0);
-        float o[4];
-        mlp_forward_warp<false>(sp, a0, o);
+        uint32_t a0[4], b0[4];
+        features_to_a2(f, a0, b0);
+        float oa[4], ob[4];
+        mlp_forward_warp2(sp, a0, b0, oa, ob);
         float v[8];
-        out_to_owner(o, v);
+        out_to_owner2(oa, ob, v);
         if (mine) {
             float e[4], nu[4];
             bearings_normals(t, seed, i, e);
@@ -204,19 +203,19 @@ __global__ void __launch_bounds__(128) k_mlp_forward(
     const int wglobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int g = lane >> 2, q = lane & 3;
-    for (uint32_t p0 = 16u * wglobal; p0 < B; p0 += 16u * nwarps) {
-        const uint32_t i = p0 + g + (q == 1 ? 8u : 0u);
-        const bool mine = q < 2 && i < B;
+    for (uint32_t p0 = 32u * wglobal; p0 < B; p0 += 32u * nwarps) {
+        const uint32_t i = p0 + g + 8u * q;
+        const bool mine = i < B;
         float f[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k)
             f[k] = mine ? feat[6 * i + k] : 0.0f;
-        uint32_t a0[4];
-        features_to_a(f, a0);
-        float o[4];
-        mlp_forward_warp<false>(sp, a0, o);
+        uint32_t a0[4], b0[4];
+        features_to_a2(f, a0, b0);
+        float oa[4], ob[4];
+        mlp_forward_warp2(sp, a0, b0, oa, ob);
         float v[8];
-        out_to_owner(o, v);
+        out_to_owner2(oa, ob, v);
         if (mine)
 #pragma unroll
             for (int k = 0; k < 8; ++k)
@@ -629,7 +628,7 @@ int vsmc_cuda_mlp_forward(const uint32_t *packed, size_t B, const float *feat,
         return VSMC_CUDA_ERR_SIZE;
     if (B == 0)
         return VSMC_CUDA_OK;
-    const int grid = grid_for((B + 15) / 16 * 32, 128, 1, 8);
+    const int grid = grid_for((B + 31) / 32 * 32, 128, 1, 8);
     k_mlp_forward<<<grid, 128, 0, as_stream(stream)>>>(
         packed, static_cast<uint32_t>(B), feat, out);
     VSMC_CUDA_CHECK_LAUNCH();
@@ -670,7 +669,7 @@ int vsmc_cuda_bearings_move_f32(size_t n, size_t t, uint32_t seed,
     const uint32_t nn = static_cast<uint32_t>(n);
     cudaStream_t st = as_stream(stream);
     if (packed != nullptr && t > 0) {
-        const int grid = grid_for((n + 15) / 16 * 32, 128, 1, 8);
+        const int grid = grid_for((n + 31) / 32 * 32, 128, 1, 8);
         k_bearings_move<true><<<grid, 128, 0, st>>>(nn,
             static_cast<uint32_t>(t), seed, c, static_cast<float>(z), packed,
             state, state + n, state + 2 * n, state + 3 * n, lw_inc);
