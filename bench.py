@@ -625,13 +625,16 @@ def main():
     e2e_value = aggregate_rate(psteps * e2e_steps, world, e2e_max)
     peak, peak_kind = measured_peaks()
     achieved = BYTES_PER_PARTICLE_STEP * n / (kernel_ms / 1000.0) / 1e9
+    # DRAM bytes per launch from the step kernel's ncu capture (bytes per
+    # particle at N = 2^23, scaled to this launch's particles)
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic_pf32_step.json")
+    prof = os.path.join(ROOT, "profiles", "k_pf32_step_N2e23.md")
     if os.path.exists(prof):
+        import re
         with open(prof) as fh:
-            per_particle = json.load(fh).get("dram_bytes_per_particle")
-        if per_particle:
-            traffic = per_particle * n
+            mt = re.search(r"dram bytes per particle:\s*([0-9.]+)", fh.read())
+        if mt:
+            traffic = float(mt.group(1)) * n
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -161,7 +161,8 @@ template <int kBlock, bool First>
 __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
     uint32_t count, const BFilter &F, PfScalars &S, uint32_t t, bool mon,
     float m, float s, float s2, float sx, float sy, float sw, float *shm,
-    double (*sh)[kBlock / 32], float *shmax, bool &is_last)
+    float (*shw)[kBlock / 32], double (*sh)[kBlock / 32], float *shmax,
+    bool &is_last)
 {
     constexpr int kW = kBlock / 32;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -177,34 +178,39 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
     }
     if (lane == 0) {
         shm[wid] = m;
-        sh[0][wid] = s;
-        sh[1][wid] = s2;
-        sh[2][wid] = sx;
-        sh[3][wid] = sy;
-        sh[4][wid] = sw;
+        shw[0][wid] = s;
+        shw[1][wid] = s2;
+        shw[2][wid] = sx;
+        shw[3][wid] = sy;
+        shw[4][wid] = sw;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float mb = -INFINITY;
-        for (int w = 0; w < kW; ++w)
-            mb = fmaxf(mb, shm[w]);
-        MovePartial p = {0, 0, 0, mb, 0, 0};
-        for (int w = 0; w < kW; ++w) {
-            p.sx += sh[2][w];
-            p.sy += sh[3][w];
-            p.sw += sh[4][w];
-            if (shm[w] > -INFINITY) {
-                const double fct = __expf(shm[w] - mb);
-                p.s += sh[0][w] * fct;
-                p.s2 += sh[1][w] * fct * fct;
-            }
+    if (wid == 0) {
+        // warp 0 merges the warps' records in FP32
+        const bool in = lane < kW;
+        float wm = in ? shm[lane] : -INFINITY;
+        float ws = in ? shw[0][lane] : 0.0f, ws2 = in ? shw[1][lane] : 0.0f;
+        float wx = in ? shw[2][lane] : 0.0f, wy = in ? shw[3][lane] : 0.0f;
+        float ww = in ? shw[4][lane] : 0.0f;
+#pragma unroll
+        for (int d = kW / 2; d > 0; d >>= 1) {
+            const float om = __shfl_xor_sync(0xFFFFFFFFu, wm, d);
+            const float os = __shfl_xor_sync(0xFFFFFFFFu, ws, d);
+            const float os2 = __shfl_xor_sync(0xFFFFFFFFu, ws2, d);
+            wx += __shfl_xor_sync(0xFFFFFFFFu, wx, d);
+            wy += __shfl_xor_sync(0xFFFFFFFFu, wy, d);
+            ww += __shfl_xor_sync(0xFFFFFFFFu, ww, d);
+            lse_merge_f(wm, ws, ws2, om, os, os2);
         }
-        a.part[tile] = p;
-        const MovePartial empty = {0, 0, 0, -INFINITY, 0, 0};
-        for (uint32_t k = 1; k < count; ++k)
-            a.part[tile + k] = empty;
-        __threadfence();
-        is_last = atomicAdd(&S.done, count) == F.ntiles - count;
+        if (lane == 0) {
+            const MovePartial p = {wx, wy, ww, wm, ws, ws2};
+            a.part[tile] = p;
+            const MovePartial empty = {0, 0, 0, -INFINITY, 0, 0};
+            for (uint32_t k = 1; k < count; ++k)
+                a.part[tile + k] = empty;
+            __threadfence();
+            is_last = atomicAdd(&S.done, count) == F.ntiles - count;
+        }
     }
     __syncthreads();
     if (!is_last)
@@ -345,6 +351,7 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
     const uint32_t t = *a.step;
     const uint32_t ntiles = t <= a.tmax ? a.active[t] : 0u;
     __shared__ float shm[kW];
+    __shared__ float shw[5][kW];
     __shared__ double sh[5][kW];
     __shared__ float shmax[kW + 1];
     __shared__ bool is_last;
@@ -459,7 +466,7 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
         // the filter's segment ends here: record it
         if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
             tile_finish<kBlock, First>(a, seg, tile + 1 - seg, F, S, t, mon,
-                m, s, s2, sx, sy, sw, shm, sh, shmax, is_last);
+                m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
             __syncthreads();
             m = -INFINITY;
             s = s2 = sx = sy = sw = 0;
@@ -482,6 +489,7 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
     constexpr int kW = kLearnBlock / 32;
     __shared__ __align__(16) uint32_t sp[kPackedWords];
     __shared__ float shm[kW];
+    __shared__ float shw[5][kW];
     __shared__ double sh[5][kW];
     __shared__ float shmax[kW + 1];
     __shared__ bool is_last;
@@ -537,8 +545,24 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
             bearings_features(c, x, y, vx, vy, sinf(z), cosf(z), fe);
             uint32_t a0[4], b0[4];
             features_to_a2(fe, a0, b0);
+            // one 16-row tile at a time keeps one tile's activations live
             float oa[4], ob[4];
-            mlp_forward_warp2(sp, a0, b0, oa, ob);
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+                uint32_t in[4];
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    in[r] = h ? b0[r] : a0[r];
+                float o[4];
+                mlp_forward_warp<false>(sp, in, o);
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    if (h)
+                        ob[r] = o[r];
+                    else
+                        oa[r] = o[r];
+                }
+            }
             float v[8];
             out_to_owner2(oa, ob, v);
             if (mine) {
@@ -571,7 +595,7 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         }
         if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
             tile_finish<kLearnBlock, First>(a, seg, tile + 1 - seg, F, S, t,
-                mon, m, s, s2, sx, sy, sw, shm, sh, shmax, is_last);
+                mon, m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
             __syncthreads();
             m = -INFINITY;
             s = s2 = sx = sy = sw = 0;
@@ -609,7 +633,6 @@ __global__ void __launch_bounds__(kB) k_batch_resample(const BatchArgs a)
     __shared__ uint32_t sh32[kW + 1];
     __shared__ QR shqr[kW];
     __shared__ uint32_t lastF[kW];
-    __shared__ uint32_t carryF;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t err = 0;
 
@@ -647,9 +670,6 @@ __global__ void __launch_bounds__(kB) k_batch_resample(const BatchArgs a)
         carry.j = 1;
         carry.r = 0;
     }
-    if (threadIdx.x == 0)
-        carryF = 0;
-    __syncthreads();
     uint32_t empties = 0, copies = 0;
     for (uint32_t base = 0; base < n; base += kChunk) {
         const uint32_t i0 = base + threadIdx.x * 4;
@@ -684,13 +704,8 @@ __global__ void __launch_bounds__(kB) k_batch_resample(const BatchArgs a)
             else
                 Fv[k] = f_of(qr_add(st, loc[k], Q), sys, n, Q, sc, wc);
         }
-        uint32_t Fprev = __shfl_up_sync(0xFFFFFFFFu, Fv[3], 1);
-        if (lane == 31)
-            lastF[wid] = Fv[3];
-        __syncthreads();
-        if (lane == 0)
-            Fprev = wid == 0 ? carryF : lastF[wid - 1];
-        __syncthreads();
+        // F before this thread's first particle is F at its start position
+        uint32_t Fprev = i0 == 0 ? 0u : f_of(st, sys, n, Q, sc, wc);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int32_t r = static_cast<int32_t>(Fv[k] - Fprev);
@@ -701,10 +716,7 @@ __global__ void __launch_bounds__(kB) k_batch_resample(const BatchArgs a)
                 copies += static_cast<uint32_t>(r);
             }
         }
-        if (threadIdx.x == kB - 1)
-            carryF = Fv[3];
         carry = qr_add(carry, total, Q);
-        __syncthreads();
     }
     copies = block_reduce(copies, OpAdd(), 0u, sh32);
     const uint32_t nempty = block_reduce(empties, OpAdd(), 0u, sh32);

@@ -194,38 +194,44 @@ __global__ void __launch_bounds__(kPfBlock, 5) k_pf32_step(const Pf32Args a)
         sw += __shfl_xor_sync(0xFFFFFFFFu, sw, d);
         lse_merge_f(m, s, s2, om, os, os2);
     }
-    // ---- block and grid level: FP64 accumulation, FP32 rescale factors
-    __shared__ float shm[kPfBlock / 32];
-    __shared__ double sh[5][kPfBlock / 32];
+    // ---- block level in FP32 (warp 0 merges the warps' records), then one
+    // FP64 record per block
+    constexpr int kW = kPfBlock / 32;
+    __shared__ float shw[6][kW];
+    __shared__ double sh[5][kW];
     __shared__ bool is_last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) {
-        shm[wid] = m;
-        sh[0][wid] = s;
-        sh[1][wid] = s2;
-        sh[2][wid] = sx;
-        sh[3][wid] = sy;
-        sh[4][wid] = sw;
+        shw[0][wid] = m;
+        shw[1][wid] = s;
+        shw[2][wid] = s2;
+        shw[3][wid] = sx;
+        shw[4][wid] = sy;
+        shw[5][wid] = sw;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float mb = -INFINITY;
-        for (int w = 0; w < kPfBlock / 32; ++w)
-            mb = fmaxf(mb, shm[w]);
-        MovePartial p = {0, 0, 0, mb, 0, 0};
-        for (int w = 0; w < kPfBlock / 32; ++w) {
-            p.sx += sh[2][w];
-            p.sy += sh[3][w];
-            p.sw += sh[4][w];
-            if (shm[w] > -INFINITY) {
-                const double f = __expf(shm[w] - mb);
-                p.s += sh[0][w] * f;
-                p.s2 += sh[1][w] * f * f;
-            }
+    if (wid == 0) {
+        const bool in = lane < kW;
+        float wm = in ? shw[0][lane] : -INFINITY;
+        float ws = in ? shw[1][lane] : 0.0f, ws2 = in ? shw[2][lane] : 0.0f;
+        float wx = in ? shw[3][lane] : 0.0f, wy = in ? shw[4][lane] : 0.0f;
+        float ww = in ? shw[5][lane] : 0.0f;
+#pragma unroll
+        for (int d = kW / 2; d > 0; d >>= 1) {
+            const float om = __shfl_xor_sync(0xFFFFFFFFu, wm, d);
+            const float os = __shfl_xor_sync(0xFFFFFFFFu, ws, d);
+            const float os2 = __shfl_xor_sync(0xFFFFFFFFu, ws2, d);
+            wx += __shfl_xor_sync(0xFFFFFFFFu, wx, d);
+            wy += __shfl_xor_sync(0xFFFFFFFFu, wy, d);
+            ww += __shfl_xor_sync(0xFFFFFFFFu, ww, d);
+            lse_merge_f(wm, ws, ws2, om, os, os2);
         }
-        a.part[blockIdx.x] = p;
-        __threadfence();
-        is_last = atomicAdd(&a.sc->done, 1u) == gridDim.x - 1;
+        if (lane == 0) {
+            const MovePartial p = {wx, wy, ww, wm, ws, ws2};
+            a.part[blockIdx.x] = p;
+            __threadfence();
+            is_last = atomicAdd(&a.sc->done, 1u) == gridDim.x - 1;
+        }
     }
     __syncthreads();
     if (!is_last)
@@ -475,8 +481,6 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     __shared__ uint64_t shq[kPfBlock / 32 + 1];
     __shared__ QR shqr[kPfBlock / 32];
     __shared__ uint32_t she[kPfBlock / 32 + 1];
-    __shared__ uint32_t lastF[kPfBlock / 32];
-    __shared__ uint32_t carryF;
     __shared__ QR start0;
     uint64_t offset, Q;
     block_prefix_of_parts(a.qpart, blockIdx.x, gridDim.x, offset, Q, shq);
@@ -505,7 +509,6 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
             s.r = Q - (G - offset * static_cast<uint64_t>(n));
         }
         start0 = s;
-        carryF = lo == 0 ? 0u : f_of(s, sys, n, Q, sc, wc);
     }
     __syncthreads();
     QR carry = start0;
@@ -554,14 +557,9 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
             else
                 F[k] = 0;
         }
-        // F before this thread's first particle: the previous thread's last
-        uint32_t Fprev = __shfl_up_sync(0xFFFFFFFFu, F[3], 1);
-        if (lane == 31)
-            lastF[wid] = F[3];
-        __syncthreads();
-        if (lane == 0)
-            Fprev = wid == 0 ? carryF : lastF[wid - 1];
-        __syncthreads();
+        // F before this thread's first particle is F at the thread's start
+        // position (particle 0 has nothing before it)
+        uint32_t Fprev = i0 == 0 ? 0u : f_of(st, sys, n, Q, sc, wc);
         int32_t r[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -584,11 +582,7 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
                     copies += static_cast<uint32_t>(r[k]);
                 }
         }
-        // the next tile starts after the last particle of this one
-        if (threadIdx.x == blockDim.x - 1)
-            carryF = F[3];
         carry = qr_add(carry, tile_total, Q);
-        __syncthreads();
     }
     if (err)
         atomicOr(&a.sc->err, err);
