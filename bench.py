@@ -372,7 +372,9 @@ def run_batched(args):
                                   "40 B per particle-step"},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            "gpu_launches": (1 + 2 * (int(T.max()) + 1)) * args.steps,
+            # per run: the reset, then per global step the step kernel and
+            # the five resampling passes
+            "gpu_launches": (1 + 6 * (int(T.max()) + 1)) * args.steps,
         }
         line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
         print(json.dumps(line), flush=True)
@@ -646,7 +648,10 @@ def main():
                          "resampling as in the reference"}
 
     if rank == 0:
-        launches_per_run = 1 + 5 + 6 * (T - 1) + 1 + 1
+        # reset, T steps of 6 kernels (the fused step and 5 resampling
+        # kernels, which return at once on steps that do not resample),
+        # final mean
+        launches_per_run = 1 + 6 * T + 1
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,

@@ -3,9 +3,9 @@
 // Thousands of independent filters, each with its own particle count,
 // horizon, model constants and seed, advance together: per global step one
 // persistent kernel moves, weights and reduces the particles of every filter
-// still running, and one kernel resamples, one block per filter, the filters
-// whose ESS fell below the threshold.  A whole run (every step of the longest
-// horizon) is one CUDA graph.
+// still running, and five kernels resample the filters whose ESS fell below
+// the threshold, in equal chunks listed by the step kernel.  A whole run
+// (every step of the longest horizon) is one CUDA graph.
 //
 // Filter f behaves exactly as a single precision-32 filter (pf.cu) with seed
 // seeds[f]: the same particle streams (Philox4x32 key {step, seed}, counter
@@ -54,7 +54,7 @@ struct BFilter {
     uint32_t hist_off; // first history entry (caller's filter order)
     uint32_t seed;
     uint32_t shift;    // fixed-point K = 63 - ceil(log2 n)
-    uint32_t pad;
+    uint32_t rs_chunk; // resampling chunk: a multiple of 4096 particles
     union {
         CvConst<float> c;   // position / Student-t model
         BearingsConst bc;   // bearings-only model
@@ -71,7 +71,6 @@ struct BatchArgs {
     PfScalars *st;               // dynamic state, one per filter
     const uint32_t *tile_filter; // filter of each tile
     const uint32_t *active;      // [tmax + 1] tiles of the filters with T >= t
-    const uint32_t *res_order;   // filters by particle count, largest first
     const float *ax, *ay, *avx, *avy; // state in
     float *bx, *by, *bvx, *bvy;       // state out
     float *lw;
@@ -82,6 +81,13 @@ struct BatchArgs {
     double *h_mean, *h_ess, *h_logz;
     int *h_res;
     uint32_t *step; // global step counter
+    // resampling list of the step: rs_list[rpar * rs_cap + v] = {filter,
+    // chunk}, rs_count[rpar] entries; per-entry totals of the passes
+    uint2 *rs_list;
+    uint32_t *rs_count;
+    uint64_t *rs_q;
+    uint32_t *rs_e, *rs_c, *rs_m;
+    uint32_t rs_cap, rpar;
     const uint32_t *packed; // proposal network (learned kind)
     uint32_t nfilters, tmax;
     int scheme;
@@ -159,7 +165,8 @@ __device__ __forceinline__ void store_run(float *p, const float (&v)[kPPT])
 // weighted mean).  All threads of the block call it.
 template <int kBlock, bool First>
 __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
-    uint32_t count, const BFilter &F, PfScalars &S, uint32_t t, bool mon,
+    uint32_t count, uint32_t f, const BFilter &F, PfScalars &S, uint32_t t,
+    bool mon,
     float m, float s, float s2, float sx, float sy, float sw, float *shm,
     float (*shw)[kBlock / 32], double (*sh)[kBlock / 32], float *shmax,
     bool &is_last)
@@ -250,7 +257,9 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
         sh[4][wid] = SW;
     }
     __syncthreads();
+    __shared__ uint32_t rs_first; // first list entry of the filter's chunks
     if (threadIdx.x == 0) {
+        rs_first = ~0u;
         double T1 = 0, T2 = 0, TX = 0, TY = 0, TW = 0;
         for (int w = 0; w < kW; ++w) {
             T1 += sh[0][w];
@@ -286,8 +295,24 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
             S.resampled = flag;
             S.gather = 0;
             S.step = t + 1;
+            if (flag) {
+                const uint32_t nc = (F.n + F.rs_chunk - 1) / F.rs_chunk;
+                const uint32_t v = atomicAdd(a.rs_count + a.rpar, nc);
+                if (v + nc <= a.rs_cap)
+                    rs_first = v;
+                else
+                    S.err |= DEV_ERR_INTERNAL;
+            }
         }
         S.done = 0;
+    }
+    __syncthreads();
+    if (rs_first != ~0u) {
+        // list the filter's resampling chunks
+        uint2 *list = a.rs_list + static_cast<size_t>(a.rpar) * a.rs_cap;
+        const uint32_t nc = (F.n + F.rs_chunk - 1) / F.rs_chunk;
+        for (uint32_t j = threadIdx.x; j < nc; j += kBlock)
+            list[rs_first + j] = make_uint2(f, j);
     }
 }
 
@@ -344,7 +369,8 @@ __device__ __forceinline__ void tile_run(
 // weighted mean of its final particles.  Each block takes a contiguous run
 // of tiles and records one reduction per filter it touches.
 template <int kBlock, int kPPT, bool First, int Kind>
-__global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
+__global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
+    const BatchArgs a)
 {
     constexpr uint32_t kTile = kBlock * kPPT;
     constexpr int kW = kBlock / 32;
@@ -465,8 +491,8 @@ __global__ void __launch_bounds__(kBlock) k_batch_step(const BatchArgs a)
         }
         // the filter's segment ends here: record it
         if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
-            tile_finish<kBlock, First>(a, seg, tile + 1 - seg, F, S, t, mon,
-                m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
+            tile_finish<kBlock, First>(a, seg, tile + 1 - seg, f, F, S, t,
+                mon, m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
             __syncthreads();
             m = -INFINITY;
             s = s2 = sx = sy = sw = 0;
@@ -594,8 +620,8 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
             a.lw[gi] = lw;
         }
         if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
-            tile_finish<kLearnBlock, First>(a, seg, tile + 1 - seg, F, S, t,
-                mon, m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
+            tile_finish<kLearnBlock, First>(a, seg, tile + 1 - seg, f, F, S,
+                t, mon, m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
             __syncthreads();
             m = -INFINITY;
             s = s2 = sx = sy = sw = 0;
@@ -604,234 +630,448 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
     }
 }
 
-// Resampling of one filter by one block (kB threads, 4 particles each per
-// chunk): the fixed-point total, the counts, the slot assignment and the
-// empty-slot sources, as the single filter's k_rs32_* kernels do over the
-// whole grid.  The filter's arrays stay in L2 between the passes.
-template <int kB>
-__global__ void __launch_bounds__(kB) k_batch_resample(const BatchArgs a)
+// ---------------------------------------------------------------- resampling
+//
+// The filters that resample at a step are resampled together by five
+// kernels over the step's list of equal chunks: entry v of the list is chunk
+// k of filter f (its particles [k c, (k + 1) c) with c = F.rs_chunk), and
+// the chunks of a filter are consecutive entries, listed by the block that
+// finished the filter's step (tile_finish).  The five passes are the single
+// filter's k_rs32_qsum / count / assign / markmax / fill: a fixed-point
+// total per chunk, replication counts, slot assignment, the max of the marks
+// per chunk of surplus ranks, and the sources of the empty slots.  A chunk
+// takes its offsets from the per-chunk totals of the earlier chunks of its
+// filter (at most kMaxRsChunks, summed by every warp on its own).  Blocks
+// walk the list with a grid stride: the grids are fixed when a run is
+// captured, and filters that do not resample cost nothing.
+
+// one list entry, with its filter's sizes
+struct RsChunk {
+    uint32_t f, k;    // filter, chunk of the filter
+    uint32_t base;    // list entry of the filter's chunk 0
+    uint32_t nc;      // chunks of the filter
+    uint32_t n, off, shift;
+    uint32_t lo, hi;  // particles (or surplus ranks) of the chunk
+};
+
+__device__ __forceinline__ RsChunk rs_chunk_at(const BatchArgs &a, uint32_t v)
 {
-    constexpr int kW = kB / 32;
-    constexpr uint32_t kChunk = kB * 4;
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        atomicAdd(a.step, 1u); // every step kernel block has read it
-    if (blockIdx.x >= a.nfilters)
-        return;
-    const uint32_t f = a.res_order[blockIdx.x];
-    PfScalars &S = a.st[f];
-    if (!S.resampled)
-        return;
-    const BFilter F = a.flt[f];
-    const uint32_t n = F.n;
-    const float M = static_cast<float>(S.M);
-    const float *lw = a.lw + F.off;
-    int32_t *rep = a.rep + F.off;
-    int32_t *idx = a.idx + F.off;
-    uint32_t *marks = a.marks + F.off;
-    uint32_t *srcs = a.srcs + F.off;
-    __shared__ uint64_t sh64[kW + 1];
-    __shared__ uint32_t sh32[kW + 1];
-    __shared__ QR shqr[kW];
-    __shared__ uint32_t lastF[kW];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t err = 0;
+    const uint2 e =
+        __ldcg(a.rs_list + static_cast<size_t>(a.rpar) * a.rs_cap + v);
+    const BFilter &F = a.flt[e.x];
+    RsChunk c;
+    c.f = e.x;
+    c.k = e.y;
+    c.base = v - e.y;
+    c.n = F.n;
+    c.off = F.off;
+    c.shift = F.shift;
+    const uint32_t csz = F.rs_chunk;
+    c.nc = (c.n + csz - 1) / csz;
+    c.lo = min(c.n, c.k * csz);
+    c.hi = min(c.n, c.lo + csz);
+    return c;
+}
 
-    // ---- A: fixed-point total
-    uint64_t acc = 0;
-    for (uint32_t i0 = threadIdx.x * 4; i0 < n; i0 += kChunk) {
-        if (i0 + 3 < n) {
-            const float4 v = __ldcg(reinterpret_cast<const float4 *>(lw + i0));
-            acc += fixed_q(v.x, M, F.shift) + fixed_q(v.y, M, F.shift) +
-                fixed_q(v.z, M, F.shift) + fixed_q(v.w, M, F.shift);
-        } else {
-            for (uint32_t i = i0; i < n; ++i)
-                acc += fixed_q(lw[i], M, F.shift);
-        }
-    }
-    const uint64_t Q = block_reduce(acc, OpAdd(), uint64_t(0), sh64);
-    if (Q == 0) {
-        if (threadIdx.x == 0)
-            atomicOr(&S.err, DEV_ERR_NONFINITE);
-        return;
-    }
-    const PfScalars sc = S;
-    const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
-    const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
-    const float invQ = __frcp_rn(__ull2float_rn(Q));
-    WordCache wc;
-    wc.blk = ~0ull;
+// op over the per-chunk totals of the filter: of chunks j < k (before) and
+// of all its chunks (all); every lane of the calling warp gets both
+template <typename T, typename Op>
+__device__ __forceinline__ void chunk_totals(
+    const T *part, const RsChunk &c, Op op, T identity, T &before, T &all)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const T v = lane < c.nc ? __ldcg(part + c.base + lane) : identity;
+    before = warp_reduce(lane < c.k ? v : identity, op);
+    all = warp_reduce(v, op);
+}
 
-    // ---- B: counts.  Start: X = 0 * n - G.
-    QR carry;
-    if (sys && cp.G > 0) {
-        carry.j = 0;
-        carry.r = Q - cp.G;
-    } else {
-        carry.j = 1;
-        carry.r = 0;
+// pass 1: fixed-point total of each chunk (four tiles in flight per thread).
+// Block 0 also advances the step counter (every step kernel block has read
+// it) and empties the next step's list.
+__global__ void __launch_bounds__(kPfBlock) k_brs_qsum(const BatchArgs a)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(a.step, 1u);
+        a.rs_count[a.rpar ^ 1u] = 0;
     }
-    uint32_t empties = 0, copies = 0;
-    for (uint32_t base = 0; base < n; base += kChunk) {
-        const uint32_t i0 = base + threadIdx.x * 4;
-        uint64_t q[4];
-        if (i0 + 3 < n) {
-            const float4 v = __ldcg(reinterpret_cast<const float4 *>(lw + i0));
-            q[0] = fixed_q(v.x, M, F.shift);
-            q[1] = fixed_q(v.y, M, F.shift);
-            q[2] = fixed_q(v.z, M, F.shift);
-            q[3] = fixed_q(v.w, M, F.shift);
-        } else {
+    const uint32_t count = __ldcg(a.rs_count + a.rpar);
+    __shared__ uint64_t sh[kPfBlock / 32 + 1];
+    constexpr int kG = 4;
+    for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
+        const RsChunk c = rs_chunk_at(a, v);
+        const float M = static_cast<float>(a.st[c.f].M);
+        const float *lw = a.lw + c.off;
+        uint64_t acc = 0;
+        for (uint32_t base = c.lo; base < c.hi; base += kG * kPfTile) {
+            if (base + kG * kPfTile <= c.hi) {
+                float4 x[kG];
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                q[k] = i0 + k < n ? fixed_q(lw[i0 + k], M, F.shift) : 0;
-        }
-        QR loc[4];
-        QR ac = {0, 0};
+                for (int h = 0; h < kG; ++h)
+                    x[h] = __ldcg(reinterpret_cast<const float4 *>(
+                        lw + base + h * kPfTile + threadIdx.x * 4));
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            qr_push(ac, q[k], n, false, Q, invQ, cp, err);
-            loc[k] = ac;
-        }
-        QR total;
-        const QR ex = block_exclusive_qr<kB>(ac, Q, shqr, &total);
-        const QR st = qr_add(carry, ex, Q);
-        uint32_t Fv[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = i0 + k;
-            if (i + 1 >= n)
-                Fv[k] = n; // the last particle takes the rest
-            else
-                Fv[k] = f_of(qr_add(st, loc[k], Q), sys, n, Q, sc, wc);
-        }
-        // F before this thread's first particle is F at its start position
-        uint32_t Fprev = i0 == 0 ? 0u : f_of(st, sys, n, Q, sc, wc);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int32_t r = static_cast<int32_t>(Fv[k] - Fprev);
-            Fprev = Fv[k];
-            if (i0 + k < n) {
-                rep[i0 + k] = r;
-                empties += r == 0 ? 1u : 0u;
-                copies += static_cast<uint32_t>(r);
-            }
-        }
-        carry = qr_add(carry, total, Q);
-    }
-    copies = block_reduce(copies, OpAdd(), 0u, sh32);
-    const uint32_t nempty = block_reduce(empties, OpAdd(), 0u, sh32);
-    if (copies != n)
-        err |= DEV_ERR_INTERNAL;
-
-    // ---- C: slots.  idx[i] = i for a parent, -(e + 1) for the e-th empty
-    // slot; marks[first surplus rank of a parent with two or more copies] =
-    // parent + 1.
-    uint32_t coff = 0, eoff = 0;
-    for (uint32_t base = 0; base < n; base += kChunk) {
-        const uint32_t i0 = base + threadIdx.x * 4;
-        int32_t r[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            r[k] = i0 + k < n ? rep[i0 + k] : -1;
-        uint32_t tr = 0, te = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (r[k] >= 0) {
-                tr += static_cast<uint32_t>(r[k]);
-                te += r[k] == 0 ? 1u : 0u;
-            }
-        const uint64_t v = (static_cast<uint64_t>(tr) << 32) | te;
-        uint64_t tot;
-        const uint64_t incl =
-            block_inclusive_scan(v, OpAdd(), uint64_t(0), sh64, &tot);
-        const uint64_t exv = incl - v;
-        uint32_t c = coff + static_cast<uint32_t>(exv >> 32);
-        uint32_t e = eoff + static_cast<uint32_t>(exv & 0xFFFFFFFFu);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = i0 + k;
-            if (r[k] < 0)
-                continue;
-            if (r[k] == 0) {
-                idx[i] = -static_cast<int32_t>(e) - 1;
-                ++e;
+                for (int h = 0; h < kG; ++h)
+                    acc += fixed_q(x[h].x, M, c.shift) +
+                        fixed_q(x[h].y, M, c.shift) +
+                        fixed_q(x[h].z, M, c.shift) +
+                        fixed_q(x[h].w, M, c.shift);
             } else {
-                idx[i] = static_cast<int32_t>(i);
-                if (r[k] >= 2) {
-                    const uint32_t rank = c - (i - e);
-                    if (rank < n)
-                        marks[rank] = i + 1;
-                    else
-                        err |= DEV_ERR_INTERNAL;
+                for (int h = 0; h < kG; ++h) {
+                    const uint32_t i0 = base + h * kPfTile + threadIdx.x * 4;
+                    for (uint32_t i = i0; i < c.hi && i < i0 + 4; ++i)
+                        acc += fixed_q(lw[i], M, c.shift);
                 }
-                c += static_cast<uint32_t>(r[k]);
             }
         }
-        coff += static_cast<uint32_t>(tot >> 32);
-        eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
+        acc = block_reduce(acc, OpAdd(), uint64_t(0), sh);
+        if (threadIdx.x == 0)
+            a.rs_q[v] = acc;
     }
-    __syncthreads();
+}
 
-    // ---- D: the parent of surplus rank k is the running max of the marks
-    uint32_t run_carry = 0;
-    for (uint32_t base = 0; base < nempty; base += kChunk) {
-        const uint32_t k0 = base + threadIdx.x * 4;
-        uint32_t mk[4], run[4];
-        uint32_t tmax = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            mk[k] = k0 + k < nempty ? marks[k0 + k] : 0u;
-            tmax = max(tmax, mk[k]);
-            run[k] = tmax;
+// pass 2: replication counts from the fixed-point CDF; empty and copy
+// counts per chunk
+__global__ void __launch_bounds__(kPfBlock, 4) k_brs_count(const BatchArgs a)
+{
+    const uint32_t count = __ldcg(a.rs_count + a.rpar);
+    const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
+    __shared__ QR shqr[kPfBlock / 32];
+    __shared__ uint32_t she[kPfBlock / 32 + 1];
+    __shared__ QR start0;
+    for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
+        const RsChunk c = rs_chunk_at(a, v);
+        PfScalars &S = a.st[c.f];
+        uint64_t offset, Q;
+        chunk_totals(a.rs_q, c, OpAdd(), uint64_t(0), offset, Q);
+        if (Q == 0) { // the same for the whole block
+            if (c.k == 0 && threadIdx.x == 0)
+                atomicOr(&S.err, DEV_ERR_NONFINITE);
+            continue;
         }
-        uint32_t tot;
-        const uint32_t incl =
-            block_inclusive_scan(tmax, OpMax(), 0u, sh32, &tot);
-        uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
-        if (lane == 31)
-            lastF[wid] = incl;
-        __syncthreads();
-        if (lane == 0)
-            before = wid > 0 ? lastF[wid - 1] : 0u;
-        __syncthreads();
-        before = max(before, run_carry);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (k0 + k < nempty) {
-                const uint32_t rk = max(run[k], before);
-                if (rk == 0 || rk - 1 >= n)
-                    err |= DEV_ERR_INTERNAL;
-                srcs[k0 + k] = rk - 1;
-                if (mk[k])
-                    marks[k0 + k] = 0;
+        const PfScalars sc = S; // the engine before this resample
+        const float M = static_cast<float>(sc.M);
+        const uint32_t n = c.n;
+        const float *lw = a.lw + c.off;
+        int32_t *rep = a.rep + c.off;
+        const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
+        const float invQ = __frcp_rn(__ull2float_rn(Q));
+        WordCache wc;
+        wc.blk = ~0ull;
+        uint32_t err = 0;
+        if (threadIdx.x == 0) {
+            // the chunk's first CDF value, offset, by one 128-bit division
+            const uint64_t G = sys ? cp.G : 0;
+            long long j;
+            uint64_t r;
+            QR s;
+            if (cn_divmod(offset, G, cp, j, r, err)) {
+                s.j = static_cast<uint32_t>(j + 1);
+                s.r = r;
+            } else { // offset n < G < Q: X = -(G - offset n)
+                s.j = 0;
+                s.r = Q - (G - offset * static_cast<uint64_t>(n));
             }
+            start0 = s;
         }
-        run_carry = max(run_carry, tot);
-    }
-    __syncthreads();
-    if (err)
-        atomicOr(&S.err, err);
-    if (threadIdx.x == 0) {
-        S.nempty = nempty;
-        S.Q = Q;
-        S.gather = 1;
-        // the words U01SequenceSystematic / U01SequenceStratified consume
-        // (rng/u01_sequence.hpp:177-259, resample/transform.hpp:61-70)
-        if (sys) {
-            engine_advance(S, 1);
-        } else {
-            const uint32_t jf = n - static_cast<uint32_t>(rep[n - 1]);
-            engine_advance(S, jf < n ? jf + 1 : n);
+        __syncthreads();
+        QR carry = start0;
+        uint32_t empties = 0, copies = 0;
+        // the next tile's log-weights are loaded while this one is counted
+        float4 nxt = make_float4(0, 0, 0, 0);
+        if (c.lo + threadIdx.x * 4 + 3 < c.hi)
+            nxt = __ldcg(reinterpret_cast<const float4 *>(
+                lw + c.lo + threadIdx.x * 4));
+        for (uint32_t base = c.lo; base < c.hi; base += kPfTile) {
+            const uint32_t i0 = base + threadIdx.x * 4;
+            const float4 x = nxt;
+            if (i0 + kPfTile + 3 < c.hi)
+                nxt = __ldcg(
+                    reinterpret_cast<const float4 *>(lw + i0 + kPfTile));
+            uint64_t q[4];
+            if (i0 + 3 < c.hi) {
+                q[0] = fixed_q(x.x, M, c.shift);
+                q[1] = fixed_q(x.y, M, c.shift);
+                q[2] = fixed_q(x.z, M, c.shift);
+                q[3] = fixed_q(x.w, M, c.shift);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    q[k] = i0 + k < c.hi ? fixed_q(lw[i0 + k], M, c.shift) : 0;
+            }
+            // positions after each of this thread's particles, from its start
+            QR loc[4];
+            QR acc = {0, 0};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                qr_push(acc, q[k], n, false, Q, invQ, cp, err);
+                loc[k] = acc;
+            }
+            QR tile_total;
+            const QR ex = block_exclusive_qr(acc, Q, shqr, &tile_total);
+            const QR st = qr_add(carry, ex, Q);
+            uint32_t Fv[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t i = i0 + k;
+                if (i + 1 >= n)
+                    Fv[k] = n; // the last particle takes the rest
+                else if (i < c.hi)
+                    Fv[k] = f_of(qr_add(st, loc[k], Q), sys, n, Q, sc, wc);
+                else
+                    Fv[k] = 0;
+            }
+            // F before this thread's first particle is F at its start
+            // position (particle 0 has nothing before it)
+            uint32_t Fprev = i0 == 0 ? 0u : f_of(st, sys, n, Q, sc, wc);
+            int32_t r[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                r[k] = static_cast<int32_t>(Fv[k] - Fprev);
+                Fprev = Fv[k];
+            }
+            if (i0 + 3 < c.hi) {
+                *reinterpret_cast<int4 *>(rep + i0) =
+                    make_int4(r[0], r[1], r[2], r[3]);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    empties += r[k] == 0 ? 1u : 0u;
+                    copies += static_cast<uint32_t>(r[k]);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (i0 + k < c.hi) {
+                        rep[i0 + k] = r[k];
+                        empties += r[k] == 0 ? 1u : 0u;
+                        copies += static_cast<uint32_t>(r[k]);
+                    }
+            }
+            carry = qr_add(carry, tile_total, Q);
+        }
+        if (err)
+            atomicOr(&S.err, err);
+        empties = block_reduce(empties, OpAdd(), 0u, she);
+        copies = block_reduce(copies, OpAdd(), 0u, she);
+        if (threadIdx.x == 0) {
+            a.rs_e[v] = empties;
+            a.rs_c[v] = copies;
         }
     }
 }
 
+// pass 3: slot assignment.  With c copies and e empty slots before slot i,
+// the first surplus rank of i is c - (i - e); idx[i] = i for a parent,
+// -(e + 1) for the e-th empty slot; marks[first surplus rank of a parent
+// with two or more copies] = parent + 1.  Chunk 0 records the filter's
+// resample: Q, the empty count, the gather flag and the engine words the
+// scheme consumed.
+__global__ void __launch_bounds__(kPfBlock) k_brs_assign(const BatchArgs a)
+{
+    const uint32_t count = __ldcg(a.rs_count + a.rpar);
+    const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
+    __shared__ uint64_t sh64[kPfBlock / 32 + 1];
+    for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
+        const RsChunk c = rs_chunk_at(a, v);
+        PfScalars &S = a.st[c.f];
+        uint64_t qb, Q;
+        chunk_totals(a.rs_q, c, OpAdd(), uint64_t(0), qb, Q);
+        if (Q == 0) { // counted nothing: no resample
+            if (c.k == 0 && threadIdx.x == 0)
+                S.nempty = 0;
+            continue;
+        }
+        uint32_t eoff, etotal, coff, ctotal;
+        chunk_totals(a.rs_e, c, OpAdd(), 0u, eoff, etotal);
+        chunk_totals(a.rs_c, c, OpAdd(), 0u, coff, ctotal);
+        const int32_t *rep = a.rep + c.off;
+        int32_t *idx = a.idx + c.off;
+        uint32_t *marks = a.marks + c.off;
+        if (c.k == 0 && threadIdx.x == 0) {
+            S.Q = Q;
+            S.nempty = etotal;
+            S.gather = 1;
+            if (ctotal != c.n)
+                atomicOr(&S.err, DEV_ERR_INTERNAL);
+            // the words U01SequenceSystematic / U01SequenceStratified
+            // consume (rng/u01_sequence.hpp:177-259,
+            // resample/transform.hpp:61-70)
+            if (sys) {
+                engine_advance(S, 1);
+            } else {
+                const uint32_t jf =
+                    c.n - static_cast<uint32_t>(rep[c.n - 1]);
+                engine_advance(S, jf < c.n ? jf + 1 : c.n);
+            }
+        }
+        uint32_t err = 0;
+        int4 nxt = load_rep4(rep, c.lo + threadIdx.x * 4, c.hi);
+        for (uint32_t base = c.lo; base < c.hi; base += kPfTile) {
+            const uint32_t i0 = base + threadIdx.x * 4;
+            const int4 cur = nxt;
+            if (base + kPfTile < c.hi)
+                nxt = load_rep4(rep, i0 + kPfTile, c.hi);
+            const int32_t r[4] = {cur.x, cur.y, cur.z, cur.w};
+            uint32_t tr = 0, te = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (r[k] >= 0) {
+                    tr += static_cast<uint32_t>(r[k]);
+                    te += r[k] == 0 ? 1u : 0u;
+                }
+            const uint64_t w = (static_cast<uint64_t>(tr) << 32) | te;
+            uint64_t tot;
+            const uint64_t incl =
+                block_inclusive_scan(w, OpAdd(), uint64_t(0), sh64, &tot);
+            const uint64_t exv = incl - w;
+            uint32_t cc = coff + static_cast<uint32_t>(exv >> 32);
+            uint32_t e = eoff + static_cast<uint32_t>(exv & 0xFFFFFFFFu);
+            int32_t out[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t i = i0 + k;
+                if (r[k] == 0) {
+                    out[k] = -static_cast<int32_t>(e) - 1;
+                    ++e;
+                } else {
+                    out[k] = static_cast<int32_t>(i);
+                    if (r[k] >= 2) {
+                        const uint32_t rk = cc - (i - e);
+                        if (rk < c.n)
+                            marks[rk] = i + 1;
+                        else
+                            err |= DEV_ERR_INTERNAL;
+                    }
+                }
+                if (r[k] > 0)
+                    cc += static_cast<uint32_t>(r[k]);
+            }
+            if (i0 + 3 < c.hi) {
+                *reinterpret_cast<int4 *>(idx + i0) =
+                    make_int4(out[0], out[1], out[2], out[3]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (r[k] >= 0)
+                        idx[i0 + k] = out[k];
+            }
+            coff += static_cast<uint32_t>(tot >> 32);
+            eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
+        }
+        if (err)
+            atomicOr(&S.err, err);
+    }
+}
+
+// pass 4: max of the marks over each chunk's surplus ranks (ranks [lo, hi)
+// below the filter's empty count)
+__global__ void __launch_bounds__(kPfBlock) k_brs_markmax(const BatchArgs a)
+{
+    const uint32_t count = __ldcg(a.rs_count + a.rpar);
+    __shared__ uint32_t sh[kPfBlock / 32 + 1];
+    for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
+        const RsChunk c = rs_chunk_at(a, v);
+        const uint32_t K = min(a.st[c.f].nempty, c.n);
+        const uint32_t lo = min(K, c.lo), hi = min(K, c.hi);
+        const uint32_t *marks = a.marks + c.off;
+        uint32_t mx = 0;
+        constexpr uint32_t kStep = 4 * kPfBlock;
+        for (uint32_t k0 = lo + threadIdx.x * 4; k0 < hi; k0 += 2 * kStep) {
+            const uint4 x = load_marks4(marks, k0, hi);
+            const uint4 y = k0 + kStep < hi ? load_marks4(marks, k0 + kStep, hi)
+                                            : make_uint4(0, 0, 0, 0);
+            mx = max(mx, max(max(x.x, x.y), max(x.z, x.w)));
+            mx = max(mx, max(max(y.x, y.y), max(y.z, y.w)));
+        }
+        mx = block_reduce(mx, OpMax(), 0u, sh);
+        if (threadIdx.x == 0)
+            a.rs_m[v] = mx;
+    }
+}
+
+// pass 5: the running max of the marks is the parent of each surplus rank:
+// srcs[k] = that parent; the marks are cleared for the next resample
+__global__ void __launch_bounds__(kPfBlock) k_brs_fill(const BatchArgs a)
+{
+    const uint32_t count = __ldcg(a.rs_count + a.rpar);
+    __shared__ uint32_t sh[kPfBlock / 32 + 1];
+    __shared__ uint32_t shl[kPfBlock / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr uint32_t kStep = 4 * kPfBlock;
+    for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
+        const RsChunk c = rs_chunk_at(a, v);
+        PfScalars &S = a.st[c.f];
+        const uint32_t K = min(S.nempty, c.n);
+        const uint32_t lo = min(K, c.lo), hi = min(K, c.hi);
+        if (lo >= hi)
+            continue; // the same for the whole block
+        uint32_t carry, mall;
+        chunk_totals(a.rs_m, c, OpMax(), 0u, carry, mall);
+        uint32_t *marks = a.marks + c.off;
+        uint32_t *srcs = a.srcs + c.off;
+        uint32_t err = 0;
+        uint4 nxt = load_marks4(marks, lo + threadIdx.x * 4, hi);
+        for (uint32_t base = lo; base < hi; base += kStep) {
+            const uint32_t k0 = base + threadIdx.x * 4;
+            const uint4 cur = nxt;
+            if (base + kStep < hi)
+                nxt = load_marks4(marks, k0 + kStep, hi);
+            const uint32_t mk[4] = {cur.x, cur.y, cur.z, cur.w};
+            uint32_t run[4];
+            uint32_t tmax = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                tmax = max(tmax, mk[k]);
+                run[k] = tmax;
+            }
+            uint32_t tot;
+            const uint32_t incl =
+                block_inclusive_scan(tmax, OpMax(), 0u, sh, &tot);
+            // exclusive max: the previous lane's inclusive value, or the
+            // previous warp's total for lane 0
+            uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+            if (lane == 31)
+                shl[wid] = incl;
+            __syncthreads();
+            if (lane == 0)
+                before = wid > 0 ? shl[wid - 1] : 0u;
+            __syncthreads();
+            before = max(before, carry);
+            uint32_t out[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t rk = max(run[k], before);
+                if (k0 + k < hi && (rk == 0 || rk - 1 >= c.n))
+                    err |= DEV_ERR_INTERNAL;
+                out[k] = rk - 1;
+            }
+            if (k0 + 3 < hi) {
+                *reinterpret_cast<uint4 *>(srcs + k0) =
+                    make_uint4(out[0], out[1], out[2], out[3]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k0 + k < hi)
+                        srcs[k0 + k] = out[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (mk[k] && k0 + k < hi)
+                    marks[k0 + k] = 0;
+            carry = max(carry, tot);
+        }
+        if (err)
+            atomicOr(&S.err, err);
+    }
+}
+
 __global__ void k_batch_reset(PfScalars *st, const BFilter *flt, uint32_t nf,
-    uint32_t *step)
+    uint32_t *step, uint32_t *rs_count)
 {
     const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f == 0)
+    if (f == 0) {
         *step = 0;
+        rs_count[0] = rs_count[1] = 0;
+    }
     if (f >= nf)
         return;
     PfScalars z = {};
@@ -872,7 +1112,9 @@ __global__ void k_batch_simulate_bearings(
         truth ? truth + 4 * obs_off[f] : nullptr, obs + obs_off[f]);
 }
 
-constexpr int kResBlock = 1024;
+constexpr uint32_t kRsMinChunk = 4 * kPfTile; // resampling chunk: 4096 or more
+constexpr uint32_t kMaxRsChunks = 32;          // chunks of one filter, at most
+constexpr int kRsKernels = 5;
 
 struct Shape {
     int ppt, block;
@@ -978,7 +1220,8 @@ struct vsmc_cuda_batch {
     size_t total_T = 0;
     // internal order: horizon descending
     std::vector<uint32_t> order;     // internal -> caller
-    std::vector<uint32_t> res_order; // internal filters by n descending
+    uint32_t rs_cap = 0;            // resampling chunks of all filters
+    int rs_grid[kRsKernels] = {};   // persistent grids of the passes
     std::vector<BFilter> flt;        // internal order
     std::vector<uint32_t> tile_filter, active;
     size_t total_particles = 0; // with padding
@@ -987,7 +1230,11 @@ struct vsmc_cuda_batch {
     BFilter *d_flt = nullptr;
     PfScalars *d_st = nullptr;
     uint32_t *d_tile_filter = nullptr, *d_active = nullptr,
-             *d_res_order = nullptr, *d_step = nullptr;
+             *d_step = nullptr;
+    uint2 *d_rs_list = nullptr;
+    uint32_t *d_rs_count = nullptr;
+    uint64_t *d_rs_q = nullptr;
+    uint32_t *d_rs_e = nullptr, *d_rs_c = nullptr, *d_rs_m = nullptr;
     float *d_state[2] = {nullptr, nullptr};
     float *d_lw = nullptr;
     int32_t *d_rep = nullptr, *d_idx = nullptr;
@@ -1019,7 +1266,8 @@ static void batch_free(vsmc_cuda_batch *b)
     if (b->graph)
         cudaGraphExecDestroy(b->graph);
     void *ptrs[] = {b->d_flt, b->d_st, b->d_tile_filter, b->d_active,
-        b->d_res_order, b->d_step, b->d_state[0], b->d_state[1], b->d_lw,
+        b->d_step, b->d_rs_list, b->d_rs_count, b->d_rs_q, b->d_rs_e,
+        b->d_rs_c, b->d_rs_m, b->d_state[0], b->d_state[1], b->d_lw,
         b->d_rep, b->d_idx, b->d_marks, b->d_srcs, b->d_part, b->d_obs,
         b->d_mean, b->d_ess, b->d_logz, b->d_res};
     for (void *p : ptrs)
@@ -1075,7 +1323,6 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.st = b->d_st;
     a.tile_filter = b->d_tile_filter;
     a.active = b->d_active;
-    a.res_order = b->d_res_order;
     a.ax = A;
     a.ay = A + ld;
     a.avx = A + 2 * ld;
@@ -1096,6 +1343,14 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.h_logz = b->d_logz;
     a.h_res = b->d_res;
     a.step = b->d_step;
+    a.rs_list = b->d_rs_list;
+    a.rs_count = b->d_rs_count;
+    a.rs_q = b->d_rs_q;
+    a.rs_e = b->d_rs_e;
+    a.rs_c = b->d_rs_c;
+    a.rs_m = b->d_rs_m;
+    a.rs_cap = b->rs_cap;
+    a.rpar = static_cast<uint32_t>(cur); // step parity, as the state buffers
     a.packed = b->packed;
     a.nfilters = b->nf;
     a.tmax = b->tmax;
@@ -1111,12 +1366,18 @@ static int enqueue_run(
 {
     cudaStream_t st = b->stream;
     k_batch_reset<<<(b->nf + 255) / 256, 256, 0, st>>>(
-        b->d_st, b->d_flt, b->nf, b->d_step);
+        b->d_st, b->d_flt, b->nf, b->d_step, b->d_rs_count);
     VSMC_CUDA_CHECK_LAUNCH();
     for (int t = 0; t < nsteps; ++t) {
         const BatchArgs a = batch_args(b, obs, t & 1);
         VSMC_CUDA_TRY(launch_step(b->kind, b->shape, t == 0, grid, a, st));
-        k_batch_resample<kResBlock><<<b->nf, kResBlock, 0, st>>>(a);
+        // the filters that resample, in the chunks the step listed
+        const dim3 blk(kPfBlock);
+        k_brs_qsum<<<b->rs_grid[0], blk, 0, st>>>(a);
+        k_brs_count<<<b->rs_grid[1], blk, 0, st>>>(a);
+        k_brs_assign<<<b->rs_grid[2], blk, 0, st>>>(a);
+        k_brs_markmax<<<b->rs_grid[3], blk, 0, st>>>(a);
+        k_brs_fill<<<b->rs_grid[4], blk, 0, st>>>(a);
         VSMC_CUDA_CHECK_LAUNCH();
     }
     return VSMC_CUDA_OK;
@@ -1224,16 +1485,28 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
         while ((size_t(1) << lg) < n[f])
             ++lg;
         F.shift = static_cast<uint32_t>(63 - lg);
+        F.rs_chunk = kRsMinChunk;
+        while ((F.n + F.rs_chunk - 1) / F.rs_chunk > kMaxRsChunks)
+            F.rs_chunk *= 2;
+        b->rs_cap += (F.n + F.rs_chunk - 1) / F.rs_chunk;
         if (kind == kKindCv)
             F.c = make_cv_const<float>(cv[f]);
         else
             F.bc = make_bearings_const(bm[f]);
     }
-    b->res_order.resize(nfilters);
-    for (uint32_t k = 0; k < nfilters; ++k)
-        b->res_order[k] = k;
-    std::stable_sort(b->res_order.begin(), b->res_order.end(),
-        [&](uint32_t x, uint32_t y) { return b->flt[x].n > b->flt[y].n; });
+    // the resampling passes walk the step's list with one full wave of
+    // blocks each
+    {
+        const int sms = num_sms();
+        const int occ[kRsKernels] = {occupancy_of(k_brs_qsum, kPfBlock),
+            occupancy_of(k_brs_count, kPfBlock),
+            occupancy_of(k_brs_assign, kPfBlock),
+            occupancy_of(k_brs_markmax, kPfBlock),
+            occupancy_of(k_brs_fill, kPfBlock)};
+        for (int k = 0; k < kRsKernels; ++k)
+            b->rs_grid[k] = static_cast<int>(std::min<size_t>(
+                static_cast<size_t>(sms) * occ[k], b->rs_cap));
+    }
 
     b->stream = as_stream(stream);
     if (b->stream == nullptr) {
@@ -1258,7 +1531,12 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     B_TRY(balloc(&b->d_st, nfilters));
     B_TRY(balloc(&b->d_tile_filter, tiles));
     B_TRY(balloc(&b->d_active, tmax + 1));
-    B_TRY(balloc(&b->d_res_order, nfilters));
+    B_TRY(balloc(&b->d_rs_list, 2 * static_cast<size_t>(b->rs_cap)));
+    B_TRY(balloc(&b->d_rs_count, 2));
+    B_TRY(balloc(&b->d_rs_q, b->rs_cap));
+    B_TRY(balloc(&b->d_rs_e, b->rs_cap));
+    B_TRY(balloc(&b->d_rs_c, b->rs_cap));
+    B_TRY(balloc(&b->d_rs_m, b->rs_cap));
     B_TRY(balloc(&b->d_step, 1));
     B_TRY(balloc(&b->d_state[0], 4 * total));
     B_TRY(balloc(&b->d_state[1], 4 * total));
@@ -1277,10 +1555,6 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
         cudaSuccess)
         B_TRY(VSMC_CUDA_ERR_CUDA);
     if (cudaMemsetAsync(b->d_mean, 0, sizeof(double) * 2 * totalT,
-            b->stream) != cudaSuccess)
-        B_TRY(VSMC_CUDA_ERR_CUDA);
-    if (cudaMemcpyAsync(b->d_res_order, b->res_order.data(),
-            sizeof(uint32_t) * nfilters, cudaMemcpyHostToDevice,
             b->stream) != cudaSuccess)
         B_TRY(VSMC_CUDA_ERR_CUDA);
     B_TRY(batch_layout(b, b->shape));

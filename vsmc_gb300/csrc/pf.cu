@@ -90,21 +90,25 @@ static void launch_resample32(vsmc_cuda_pf *pf)
     k_rs32_fill<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
 }
 
-// the kernels of one FP32 step (reads buffer cur, writes the other)
-static int launch_step32(vsmc_cuda_pf *pf, bool first)
+// the fused step kernel of one FP32 step (reads buffer cur, writes the
+// other)
+static void launch_step_kernel32(
+    vsmc_cuda_pf *pf, bool first, const Pf32Args &a)
 {
-    const Pf32Args a = make_args32(pf);
     if (first)
         k_pf32_step<true><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
     else
         k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
-    launch_resample32(pf);
+}
+
+// the kernels that follow resampling every step: genealogy row, and the
+// resample-move sweeps (whose output goes back to buffer cur)
+static void launch_post32(vsmc_cuda_pf *pf, const Pf32Args &a)
+{
     if (pf->record_gen)
         k_pf32_record<<<grid_for(pf->n, kPfBlock, 4, 8), kPfBlock, 0,
             pf->stream>>>(a, pf->gen);
     if (pf->mcmc_sweeps > 0) {
-        // resample-move: the moved (or copied) state goes back to buffer
-        // cur, so the step's input buffer stays the current one
         float *A = buf32(pf, pf->cur);
         const size_t ld = pf->stride;
         const float sa = static_cast<float>(pf->model.sigma_a);
@@ -113,6 +117,15 @@ static int launch_step32(vsmc_cuda_pf *pf, bool first)
             pf->mcmc_sweeps, pf->mcmc_scale, 1.0f / (sa * sa), pf->h_acc);
         k_pf32_clear_gather<<<1, 1, 0, pf->stream>>>(pf->sc);
     }
+}
+
+// the kernels of one FP32 step, launched on the stream
+static int launch_step32(vsmc_cuda_pf *pf, bool first)
+{
+    const Pf32Args a = make_args32(pf);
+    launch_step_kernel32(pf, first, a);
+    launch_resample32(pf);
+    launch_post32(pf, a);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
 }
@@ -147,8 +160,11 @@ static int step32(vsmc_cuda_pf *pf)
         const int rc = launch_step32(pf, false);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(pf->stream, &g);
-        if (rc != VSMC_CUDA_OK)
+        if (rc != VSMC_CUDA_OK) {
+            if (g)
+                cudaGraphDestroy(g);
             return rc;
+        }
         VSMC_CUDA_TRY(e);
         pf->graph[par] = g;
         VSMC_CUDA_TRY(cudaGraphInstantiate(&pf->graph_exec[par], g, 0));

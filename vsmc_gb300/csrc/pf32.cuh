@@ -594,20 +594,6 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     }
 }
 
-// counts of slots i0..i0+3 below hi (-1 past hi)
-__device__ __forceinline__ int4 load_rep4(
-    const int32_t *rep, uint32_t i0, uint32_t hi)
-{
-    if (i0 + 3 < hi)
-        return __ldcg(reinterpret_cast<const int4 *>(rep + i0));
-    int4 v;
-    v.x = i0 + 0 < hi ? rep[i0 + 0] : -1;
-    v.y = i0 + 1 < hi ? rep[i0 + 1] : -1;
-    v.z = i0 + 2 < hi ? rep[i0 + 2] : -1;
-    v.w = i0 + 3 < hi ? rep[i0 + 3] : -1;
-    return v;
-}
-
 // Slot assignment.  With c = copies before slot i and e = empty slots before
 // i, the first surplus rank of i is c - (i - e) (every non-empty slot before
 // i keeps one of its copies).  idx[i] = i for a parent (it keeps its slot),
@@ -709,20 +695,6 @@ __device__ __forceinline__ void rank_range(
         lo = K;
     if (hi > K)
         hi = K;
-}
-
-// marks k0..k0+3 below hi (0 past hi); k0 is a multiple of 4
-__device__ __forceinline__ uint4 load_marks4(
-    const uint32_t *marks, uint32_t k0, uint32_t hi)
-{
-    if (k0 + 3 < hi)
-        return __ldcg(reinterpret_cast<const uint4 *>(marks + k0));
-    uint4 v;
-    v.x = k0 + 0 < hi ? __ldcg(marks + k0 + 0) : 0u;
-    v.y = k0 + 1 < hi ? __ldcg(marks + k0 + 1) : 0u;
-    v.z = k0 + 2 < hi ? __ldcg(marks + k0 + 2) : 0u;
-    v.w = k0 + 3 < hi ? __ldcg(marks + k0 + 3) : 0u;
-    return v;
 }
 
 // per-block max of the marks over the block's share of the surplus ranks

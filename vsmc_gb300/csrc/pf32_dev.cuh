@@ -226,6 +226,11 @@ __device__ __forceinline__ QR qr_add(const QR &a, const QR &b, uint64_t Q)
 __device__ __forceinline__ void qr_reduce(
     uint64_t &r, uint32_t &j, uint64_t Q, float invQ, uint32_t &err)
 {
+    // the common case: r < 2Q (at most one more multiple)
+    if (r < Q)
+        return;
+    r -= Q;
+    ++j;
     int guard = 0;
     while (r >= Q) {
         const float est = fmaf(__uint2float_rz(static_cast<uint32_t>(r >> 32)),
@@ -350,6 +355,34 @@ __device__ __forceinline__ QR block_exclusive_qr(
     *total = sh[nw - 1];
     __syncthreads();
     return ex;
+}
+
+// counts of slots i0..i0+3 below hi (-1 past hi)
+__device__ __forceinline__ int4 load_rep4(
+    const int32_t *rep, uint32_t i0, uint32_t hi)
+{
+    if (i0 + 3 < hi)
+        return __ldcg(reinterpret_cast<const int4 *>(rep + i0));
+    int4 v;
+    v.x = i0 + 0 < hi ? rep[i0 + 0] : -1;
+    v.y = i0 + 1 < hi ? rep[i0 + 1] : -1;
+    v.z = i0 + 2 < hi ? rep[i0 + 2] : -1;
+    v.w = i0 + 3 < hi ? rep[i0 + 3] : -1;
+    return v;
+}
+
+// marks k0..k0+3 below hi (0 past hi); k0 is a multiple of 4
+__device__ __forceinline__ uint4 load_marks4(
+    const uint32_t *marks, uint32_t k0, uint32_t hi)
+{
+    if (k0 + 3 < hi)
+        return __ldcg(reinterpret_cast<const uint4 *>(marks + k0));
+    uint4 v;
+    v.x = k0 + 0 < hi ? __ldcg(marks + k0 + 0) : 0u;
+    v.y = k0 + 1 < hi ? __ldcg(marks + k0 + 1) : 0u;
+    v.z = k0 + 2 < hi ? __ldcg(marks + k0 + 2) : 0u;
+    v.w = k0 + 3 < hi ? __ldcg(marks + k0 + 3) : 0u;
+    return v;
 }
 
 } // namespace vsmc_cuda
