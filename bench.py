@@ -384,6 +384,145 @@ def run_batched(args):
     return 0
 
 
+def run_micro(args):
+    """RNG and resampling microbenchmarks (the 2^30-word RNG and N = 2^24
+    resampling workload): every call goes through the public C ABI, output
+    in HBM; each item is timed over `steps` calls with CUDA events after
+    `warmup` calls.  Headline: raw Philox4x32-10 words/s."""
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    import vsmc_gb300 as vc
+    vc.lib()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    nw = 1 << args.rng_log2
+    buf = torch.empty(8 * nw, dtype=torch.uint8, device="cuda")
+    peak, peak_kind = measured_peaks()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps / 1000.0
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    items = {}
+    # (name, engine kind, entry point, extra args, output bytes per value)
+    rng_items = [
+        ("philox4x32_u32", vc.PHILOX4X32, "vsmc_cuda_rng_rand", (), 4),
+        ("threefry4x64_u64", vc.THREEFRY4X64, "vsmc_cuda_rng_rand", (), 8),
+        ("u01_f64", vc.PHILOX4X32, "vsmc_cuda_rng_u01", (), 8),
+        ("u01_f32", vc.PHILOX4X32, "vsmc_cuda_rng_u01_f32", (), 4),
+        ("normal_f64", vc.PHILOX4X32, "vsmc_cuda_rng_normal",
+         (ctypes.c_double(0.0), ctypes.c_double(1.0)), 8),
+        ("normal_f32", vc.PHILOX4X32, "vsmc_cuda_rng_normal_f32",
+         (ctypes.c_float(0.0), ctypes.c_float(1.0)), 4),
+    ]
+    for name, kind, fn, extra, vb in rng_items:
+        r = vc.rng(kind, seed=1)
+        sec = timed(lambda: vc.call(fn, ctypes.byref(r), nw, buf.data_ptr(),
+                                    *extra, sptr))
+        items[name] = {"values": nw, "seconds": sec, "values_per_s": nw / sec,
+                       "GB_per_s": vb * nw / sec / 1e9,
+                       "frac_hbm": vb * nw / sec / 1e9 / peak}
+    # resampling: normalised FP64 weights from log w ~ N(0, 3^2)
+    n = 1 << args.rs_log2
+    lw = np.random.default_rng(7).normal(0.0, 3.0, n)
+    w = np.exp(lw - lw.max())
+    w /= w.sum()
+    w_dev = torch.from_numpy(w).cuda()
+    rep = torch.empty(n, dtype=torch.int32, device="cuda")
+    names = ["multinomial", "stratified", "systematic", "residual",
+             "residual_stratified", "residual_systematic"]
+    for scheme, name in enumerate(names):
+        r = vc.rng(vc.PHILOX4X32, seed=1)
+        sec = timed(lambda: vc.call("vsmc_cuda_resample", n, n,
+                                    ctypes.byref(r), w_dev.data_ptr(),
+                                    rep.data_ptr(), scheme, sptr))
+        items["resample_" + name] = {
+            "particles": n, "seconds": sec, "particles_per_s": n / sec,
+            "GB_per_s": 12 * n / sec / 1e9,
+            "frac_hbm": 12 * n / sec / 1e9 / peak}
+    clocks.stop()
+    # end to end: Philox words into pinned host memory through the C ABI
+    host = torch.empty(4 * nw, dtype=torch.uint8, pin_memory=True)
+    r = vc.rng(vc.PHILOX4X32, seed=1)
+
+    def e2e_call():
+        vc.call("vsmc_cuda_rng_rand", ctypes.byref(r), nw, buf.data_ptr(),
+                sptr)
+        host.copy_(buf[:4 * nw], non_blocking=True)
+
+    e2e_s = timed(e2e_call)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import binding
+        port = binding.port()
+        ns = 1 << 24
+        out = np.zeros(ns, np.uint32)
+        key = (ctypes.c_uint32 * 2)(1, 0)
+        ctr = (ctypes.c_uint32 * 4)(0, 0, 0, 0)
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 3.0:
+            port.vo_philox4x32_words(key, ctr, ns, out.ctypes.data, 1)
+            reps += 1
+        dt = time.perf_counter() - t0
+        cpu = {"value": ns * reps / dt, "unit": "words/s", "cores": 1,
+               "kind": "port",
+               "sample": f"{reps} x 2^24 Philox4x32-10 words, bulk path, "
+                         "oracle restatement, one core"}
+        nr = 1 << 22
+        wr = w[:nr] / w[:nr].sum()
+        repc = np.zeros(nr, np.int32)
+        nxt = (ctypes.c_uint32 * 4)()
+        t0 = time.perf_counter()
+        port.vo_resample_words(1, nr, nr, key, ctr, wr.ctypes.data,
+                               repc.ctypes.data, nxt)
+        dt = time.perf_counter() - t0
+        cpu["resample_stratified_particles_per_s"] = nr / dt
+    ph = items["philox4x32_u32"]
+    line = {
+        "metric": "words/sec (Philox4x32-10 raw u32 through the engine's "
+                  "bulk path)",
+        "value": ph["values_per_s"], "unit": "words/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * ph["seconds"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (counter-based streams; weights from a seeded "
+                "N(0, 3^2) log-weight draw)",
+        "config": {"workload": f"RNG 2^{args.rng_log2} values per call; "
+                               f"resampling N = 2^{args.rs_log2}, all six "
+                               "schemes, FP64 weights",
+                   "l2": "outputs 4-8 GiB >> L2; no flush",
+                   "items": items},
+        "e2e": {"value": nw / e2e_s, "unit": "words/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4 * nw},
+        "roofline": {"bound": "hbm", "achieved": ph["GB_per_s"],
+                     "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+                     "frac": ph["frac_hbm"],
+                     "scope": "4 B written per word; the generator is "
+                              "integer-pipe work (ncu pipe counters in "
+                              "profiles)"},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_learned(args):
     """Learned proposal vs bootstrap on the bearings-only model: R filters
     (independent seeds) on one simulated observation sequence; log-evidence
@@ -453,12 +592,19 @@ def run_learned(args):
         out = b.history()
         b.close()
         logz = np.array([o["logz"][-1] for o in out])
+        # variance of the cumulative log-evidence over the R filters, by step
+        lz_all = np.stack([o["logz"] for o in out])
+        var_at = {str(t): float(lz_all[:, t].var())
+                  for t in (0, 10, 30, 50, 100, T - 1)}
+        ess_at = {str(t): float(np.mean([o["ess"][t] for o in out]) / N)
+                  for t in (0, 10, 30, 50, 100, T - 1)}
         means = np.stack([o["mean"] for o in out])  # R x T x 2
         err = None
         if ref_mean is not None:
             err = float(np.sqrt(np.mean((means.mean(axis=0) - ref_mean) ** 2)))
         return {"N": N, "ms": ms, "rate": N * T * R / (ms / 1000.0),
                 "logz_sd": float(logz.std()), "logz_mean": float(logz.mean()),
+                "logz_var_by_step": var_at, "ess_frac_by_step": ess_at,
                 "mean_rmse_vs_ref": err}
 
     clocks = ClockSampler(local)
@@ -520,7 +666,7 @@ def main():
     ap.add_argument("--T", type=int, default=T_STEPS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="single",
-                    choices=["single", "batched", "learned"])
+                    choices=["single", "batched", "learned", "micro"])
     ap.add_argument("--replicates", type=int, default=1024)
     ap.add_argument("--learned-particles", type=int, default=1 << 12)
     ap.add_argument("--boot-particles", type=int, nargs="+",
@@ -534,6 +680,8 @@ def main():
     ap.add_argument("--bearings-q", type=float, default=1.0)
     ap.add_argument("--bearings-sdv", type=float, default=0.5)
     ap.add_argument("--filters", type=int, default=4096)
+    ap.add_argument("--rng-log2", type=int, default=30)
+    ap.add_argument("--rs-log2", type=int, default=24)
     ap.add_argument("--tune-steps", type=int, default=60)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -543,6 +691,8 @@ def main():
         return run_batched(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "micro":
+        return run_micro(args)
 
     import torch
     rank, world, local = dist_setup(args.gpus)

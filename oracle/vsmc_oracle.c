@@ -1469,6 +1469,25 @@ static double vo_gelu(double x, double *grad)
     return x * s;
 }
 
+/* GELU of a pre-activation as the filter kernels evaluate it (mlp.cuh,
+ * gelu2_bf16): the FP32 pre-activation rounded to BF16, then
+ * 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) with every product and
+ * fused multiply-add rounded to BF16.  The device takes tanh from the
+ * hardware approximation; here it is tanhf rounded to BF16, so the two
+ * can differ by a BF16 unit in the last place. */
+static double vo_gelu_bf16(double pre)
+{
+    const float c0 = vo_bf16(0.7978845608028654f);
+    const float c1 = vo_bf16(0.0356774081363001f);
+    const float x = vo_bf16((float)pre);
+    const float x2 = vo_bf16(x * x);
+    const float t = vo_bf16(fmaf(x2, c1, c0));
+    const float u = vo_bf16(x * t);
+    const float th = vo_bf16(tanhf(u));
+    const float h = vo_bf16(x * 0.5f);
+    return vo_bf16(fmaf(h, th, h));
+}
+
 #define VO_IN 6
 #define VO_HID 64
 #define VO_OUT 8
@@ -1499,9 +1518,14 @@ static float p_w3(const float *p, int d, int j)
     return p[VO_W3 + d * VO_HID + j];
 }
 
-/* one row of the forward pass: BF16 weights and activations, FP64 sums */
-static void vo_mlp_row_forward(const float *p, const float *f, vo_mlp_row *r)
+/* one row of the forward pass: BF16 weights and activations, FP64 sums;
+ * filter = 1: the hidden activations as the filter kernels form them
+ * (vo_gelu_bf16, device rounding mode only), else GELU in FP64 rounded to
+ * BF16 as the training and parity kernels form them */
+static void vo_mlp_row_forward(
+    const float *p, const float *f, vo_mlp_row *r, int filter)
 {
+    const int fast = filter && vo_mlp_device_rounding;
     for (int k = 0; k < VO_IN; ++k)
         r->a0[k] = vo_bf16d(f[k]);
     for (int j = 0; j < VO_HID; ++j) {
@@ -1509,14 +1533,16 @@ static void vo_mlp_row_forward(const float *p, const float *f, vo_mlp_row *r)
         for (int k = 0; k < VO_IN; ++k)
             s += vo_bf16d(p[VO_W1 + j * VO_IN + k]) * r->a0[k];
         r->pre1[j] = s + p[VO_B1 + j];
-        r->a1[j] = vo_bf16d(vo_gelu(r->pre1[j], NULL));
+        r->a1[j] = fast ? vo_gelu_bf16(r->pre1[j])
+                        : vo_bf16d(vo_gelu(r->pre1[j], NULL));
     }
     for (int j = 0; j < VO_HID; ++j) {
         double s = 0;
         for (int k = 0; k < VO_HID; ++k)
             s += vo_bf16d(p[VO_W2 + j * VO_HID + k]) * r->a1[k];
         r->pre2[j] = s + p[VO_B2 + j];
-        r->a2[j] = vo_bf16d(vo_gelu(r->pre2[j], NULL));
+        r->a2[j] = fast ? vo_gelu_bf16(r->pre2[j])
+                        : vo_bf16d(vo_gelu(r->pre2[j], NULL));
     }
     for (int d = 0; d < VO_OUT; ++d) {
         double s = 0;
@@ -1532,7 +1558,7 @@ void vo_mlp_forward(const float *params, size_t B, const float *feat,
     _Pragma("omp parallel for schedule(static)")
     for (size_t i = 0; i < B; ++i) {
         vo_mlp_row r;
-        vo_mlp_row_forward(params, feat + 6 * i, &r);
+        vo_mlp_row_forward(params, feat + 6 * i, &r, 0);
         for (int d = 0; d < VO_OUT; ++d)
             out[8 * i + d] = (float)r.out[d];
     }
@@ -1549,7 +1575,7 @@ void vo_mlp_loss_grad(const float *params, size_t B, const float *feat,
     const double inv_b = 1.0 / (double)B;
     for (size_t i = 0; i < B; ++i) {
         vo_mlp_row r;
-        vo_mlp_row_forward(params, feat + 6 * i, &r);
+        vo_mlp_row_forward(params, feat + 6 * i, &r, 0);
         double dout[VO_OUT];
         for (int d = 0; d < 4; ++d) {
             const double res = nu[4 * i + d] - r.out[d];
@@ -1634,7 +1660,7 @@ void vo_bearings_move_f32(size_t N, size_t t, uint32_t seed,
                 const float iv = 1.0f / (1.0f + sqrtf(vx * vx + vy * vy));
                 const float f[6] = {px * ip, py * ip, vx * iv, vy * iv, sz, cz};
                 vo_mlp_row r;
-                vo_mlp_row_forward(params, f, &r);
+                vo_mlp_row_forward(params, f, &r, 1);
                 for (int d = 0; d < 4; ++d) {
                     float l = (float)r.out[4 + d];
                     l = l < -12.0f ? -12.0f : (l > 4.0f ? 4.0f : l);

@@ -61,6 +61,13 @@ struct BFilter {
     };
 };
 
+// A block's record of the tiles of one filter: FP32 sums, as the block
+// forms them (the single filter widens the same values to FP64).
+struct TileRecord {
+    float sx, sy, sw; // previous-step monitor sums
+    float m, s, s2;   // new log-weights: max, sum exp, sum exp^2
+};
+
 // filter kinds
 constexpr int kKindCv = 0;       // CV + Student-t positions, bootstrap
 constexpr int kKindBearings = 1; // bearings-only, bootstrap
@@ -76,8 +83,8 @@ struct BatchArgs {
     float *lw;
     int32_t *rep, *idx;
     uint32_t *marks, *srcs;
-    MovePartial *part; // per tile
-    const double *obs;
+    TileRecord *part; // per tile
+    const float *obs; // the observations in FP32 (converted once per run)
     double *h_mean, *h_ess, *h_logz;
     int *h_res;
     uint32_t *step; // global step counter
@@ -166,10 +173,8 @@ __device__ __forceinline__ void store_run(float *p, const float (&v)[kPPT])
 template <int kBlock, bool First>
 __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
     uint32_t count, uint32_t f, const BFilter &F, PfScalars &S, uint32_t t,
-    bool mon,
-    float m, float s, float s2, float sx, float sy, float sw, float *shm,
-    float (*shw)[kBlock / 32], double (*sh)[kBlock / 32], float *shmax,
-    bool &is_last)
+    bool mon, float m, float s, float s2, float sx, float sy, float sw,
+    float *shm, float (*shw)[kBlock / 32], bool &is_last)
 {
     constexpr int kW = kBlock / 32;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -210,9 +215,9 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
             lse_merge_f(wm, ws, ws2, om, os, os2);
         }
         if (lane == 0) {
-            const MovePartial p = {wx, wy, ww, wm, ws, ws2};
+            const TileRecord p = {wx, wy, ww, wm, ws, ws2};
             a.part[tile] = p;
-            const MovePartial empty = {0, 0, 0, -INFINITY, 0, 0};
+            const TileRecord empty = {0, 0, 0, -INFINITY, 0, 0};
             for (uint32_t k = 1; k < count; ++k)
                 a.part[tile + k] = empty;
             __threadfence();
@@ -222,52 +227,33 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
     __syncthreads();
     if (!is_last)
         return;
-    // ---- the filter's last tile: combine its tile records
+    // ---- the filter's last tile: warp 0 combines its tile records in FP64
     __threadfence();
+    if (wid != 0)
+        return;
     float M = -INFINITY;
-    for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock)
-        M = fmaxf(M, static_cast<float>(a.part[F.tile0 + b].m));
-    M = block_reduce(M, OpMax(), -INFINITY, shmax);
-    double S1 = 0, S2 = 0, SX = 0, SY = 0, SW = 0;
-    for (uint32_t b = threadIdx.x; b < F.ntiles; b += kBlock) {
-        const MovePartial p = a.part[F.tile0 + b];
-        SX += p.sx;
-        SY += p.sy;
-        SW += p.sw;
+    for (uint32_t b = lane; b < F.ntiles; b += 32)
+        M = fmaxf(M, __ldcg(&a.part[F.tile0 + b].m));
+    M = warp_reduce(M, OpMax());
+    double T1 = 0, T2 = 0, TX = 0, TY = 0, TW = 0;
+    for (uint32_t b = lane; b < F.ntiles; b += 32) {
+        const TileRecord p = a.part[F.tile0 + b];
+        TX += p.sx;
+        TY += p.sy;
+        TW += p.sw;
         if (p.m > -INFINITY) {
-            const double fct = __expf(static_cast<float>(p.m) - M);
-            S1 += p.s * fct;
-            S2 += p.s2 * fct * fct;
+            const double fct = __expf(p.m - M);
+            T1 += p.s * fct;
+            T2 += p.s2 * fct * fct;
         }
     }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        S1 += __shfl_xor_sync(0xFFFFFFFFu, S1, d);
-        S2 += __shfl_xor_sync(0xFFFFFFFFu, S2, d);
-        SX += __shfl_xor_sync(0xFFFFFFFFu, SX, d);
-        SY += __shfl_xor_sync(0xFFFFFFFFu, SY, d);
-        SW += __shfl_xor_sync(0xFFFFFFFFu, SW, d);
-    }
-    __syncthreads();
+    T1 = warp_reduce(T1, OpAdd());
+    T2 = warp_reduce(T2, OpAdd());
+    TX = warp_reduce(TX, OpAdd());
+    TY = warp_reduce(TY, OpAdd());
+    TW = warp_reduce(TW, OpAdd());
+    uint32_t rs_first = ~0u; // first list entry of the filter's chunks
     if (lane == 0) {
-        sh[0][wid] = S1;
-        sh[1][wid] = S2;
-        sh[2][wid] = SX;
-        sh[3][wid] = SY;
-        sh[4][wid] = SW;
-    }
-    __syncthreads();
-    __shared__ uint32_t rs_first; // first list entry of the filter's chunks
-    if (threadIdx.x == 0) {
-        rs_first = ~0u;
-        double T1 = 0, T2 = 0, TX = 0, TY = 0, TW = 0;
-        for (int w = 0; w < kW; ++w) {
-            T1 += sh[0][w];
-            T2 += sh[1][w];
-            TX += sh[2][w];
-            TY += sh[3][w];
-            TW += sh[4][w];
-        }
         if (mon) {
             a.h_mean[2 * (F.hist_off + F.T - 1) + 0] = TX / TW;
             a.h_mean[2 * (F.hist_off + F.T - 1) + 1] = TY / TW;
@@ -290,6 +276,7 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
             a.h_logz[F.hist_off + t] = S.logz;
             a.h_res[F.hist_off + t] = flag;
             S.M = M1;
+            S.Mf = M;
             S.S = T1;
             S.ess = ess;
             S.resampled = flag;
@@ -306,12 +293,12 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
         }
         S.done = 0;
     }
-    __syncthreads();
+    rs_first = __shfl_sync(0xFFFFFFFFu, rs_first, 0);
     if (rs_first != ~0u) {
         // list the filter's resampling chunks
         uint2 *list = a.rs_list + static_cast<size_t>(a.rpar) * a.rs_cap;
         const uint32_t nc = (F.n + F.rs_chunk - 1) / F.rs_chunk;
-        for (uint32_t j = threadIdx.x; j < nc; j += kBlock)
+        for (uint32_t j = lane; j < nc; j += 32)
             list[rs_first + j] = make_uint2(f, j);
     }
 }
@@ -378,8 +365,6 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
     const uint32_t ntiles = t <= a.tmax ? a.active[t] : 0u;
     __shared__ float shm[kW];
     __shared__ float shw[5][kW];
-    __shared__ double sh[5][kW];
-    __shared__ float shmax[kW + 1];
     __shared__ bool is_last;
     uint32_t lo, hi;
     tile_run(ntiles, lo, hi);
@@ -392,14 +377,14 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
         const bool mon = !First && t == F.T;
         const int resampled = First ? 1 : S.resampled;
         const bool gather = First ? false : (S.gather != 0);
-        const float Mprev = First ? 0.0f : static_cast<float>(S.M);
+        const float Mprev = First ? 0.0f : S.Mf;
         float ox = 0.0f, oy = 0.0f;
         if (!mon) {
             if (Kind == kKindCv) {
-                ox = static_cast<float>(a.obs[2 * (F.obs_off + t) + 0]);
-                oy = static_cast<float>(a.obs[2 * (F.obs_off + t) + 1]);
+                ox = a.obs[2 * (F.obs_off + t) + 0];
+                oy = a.obs[2 * (F.obs_off + t) + 1];
             } else {
-                ox = static_cast<float>(a.obs[F.obs_off + t]);
+                ox = a.obs[F.obs_off + t];
             }
         }
         const uint32_t i0 = (tile - F.tile0) * kTile + threadIdx.x * kPPT;
@@ -492,7 +477,7 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
         // the filter's segment ends here: record it
         if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
             tile_finish<kBlock, First>(a, seg, tile + 1 - seg, f, F, S, t,
-                mon, m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
+                mon, m, s, s2, sx, sy, sw, shm, shw, is_last);
             __syncthreads();
             m = -INFINITY;
             s = s2 = sx = sy = sw = 0;
@@ -516,8 +501,6 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
     __shared__ __align__(16) uint32_t sp[kPackedWords];
     __shared__ float shm[kW];
     __shared__ float shw[5][kW];
-    __shared__ double sh[5][kW];
-    __shared__ float shmax[kW + 1];
     __shared__ bool is_last;
     const uint32_t t = *a.step;
     const uint32_t ntiles = t <= a.tmax ? a.active[t] : 0u;
@@ -537,8 +520,8 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         const bool mon = !First && t == F.T;
         const int resampled = First ? 1 : S.resampled;
         const bool gather = First ? false : (S.gather != 0);
-        const float Mprev = First ? 0.0f : static_cast<float>(S.M);
-        const float z = mon ? 0.0f : static_cast<float>(a.obs[F.obs_off + t]);
+        const float Mprev = First ? 0.0f : S.Mf;
+        const float z = mon ? 0.0f : a.obs[F.obs_off + t];
         const uint32_t i =
             (tile - F.tile0) * kLearnTile + 32 * wid + g + 8 * q;
         const bool mine = i < F.n;
@@ -580,7 +563,7 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
                 for (int r = 0; r < 4; ++r)
                     in[r] = h ? b0[r] : a0[r];
                 float o[4];
-                mlp_forward_warp<false>(sp, in, o);
+                mlp_forward_warp<false, true>(sp, in, o);
 #pragma unroll
                 for (int r = 0; r < 4; ++r) {
                     if (h)
@@ -621,7 +604,7 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         }
         if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
             tile_finish<kLearnBlock, First>(a, seg, tile + 1 - seg, f, F, S,
-                t, mon, m, s, s2, sx, sy, sw, shm, shw, sh, shmax, is_last);
+                t, mon, m, s, s2, sx, sy, sw, shm, shw, is_last);
             __syncthreads();
             m = -INFINITY;
             s = s2 = sx = sy = sw = 0;
@@ -699,7 +682,7 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_qsum(const BatchArgs a)
     constexpr int kG = 4;
     for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
         const RsChunk c = rs_chunk_at(a, v);
-        const float M = static_cast<float>(a.st[c.f].M);
+        const float M = a.st[c.f].Mf;
         const float *lw = a.lw + c.off;
         uint64_t acc = 0;
         for (uint32_t base = c.lo; base < c.hi; base += kG * kPfTile) {
@@ -731,7 +714,7 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_qsum(const BatchArgs a)
 
 // pass 2: replication counts from the fixed-point CDF; empty and copy
 // counts per chunk
-__global__ void __launch_bounds__(kPfBlock, 4) k_brs_count(const BatchArgs a)
+__global__ void __launch_bounds__(kPfBlock) k_brs_count(const BatchArgs a)
 {
     const uint32_t count = __ldcg(a.rs_count + a.rpar);
     const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
@@ -749,7 +732,7 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_brs_count(const BatchArgs a)
             continue;
         }
         const PfScalars sc = S; // the engine before this resample
-        const float M = static_cast<float>(sc.M);
+        const float M = sc.Mf;
         const uint32_t n = c.n;
         const float *lw = a.lw + c.off;
         int32_t *rep = a.rep + c.off;
@@ -1064,6 +1047,14 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_fill(const BatchArgs a)
     }
 }
 
+// the run's observations in FP32, as the step kernels use them
+__global__ void k_obs_f32(const double *obs, float *out, uint32_t count)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += gridDim.x * blockDim.x)
+        out[i] = static_cast<float>(obs[i]);
+}
+
 __global__ void k_batch_reset(PfScalars *st, const BFilter *flt, uint32_t nf,
     uint32_t *step, uint32_t *rs_count)
 {
@@ -1239,7 +1230,8 @@ struct vsmc_cuda_batch {
     float *d_lw = nullptr;
     int32_t *d_rep = nullptr, *d_idx = nullptr;
     uint32_t *d_marks = nullptr, *d_srcs = nullptr;
-    MovePartial *d_part = nullptr;
+    TileRecord *d_part = nullptr;
+    float *d_obsf = nullptr; // the run's observations in FP32
     double *d_obs = nullptr;
     double *d_mean = nullptr, *d_ess = nullptr, *d_logz = nullptr;
     int *d_res = nullptr;
@@ -1268,7 +1260,7 @@ static void batch_free(vsmc_cuda_batch *b)
     void *ptrs[] = {b->d_flt, b->d_st, b->d_tile_filter, b->d_active,
         b->d_step, b->d_rs_list, b->d_rs_count, b->d_rs_q, b->d_rs_e,
         b->d_rs_c, b->d_rs_m, b->d_state[0], b->d_state[1], b->d_lw,
-        b->d_rep, b->d_idx, b->d_marks, b->d_srcs, b->d_part, b->d_obs,
+        b->d_rep, b->d_idx, b->d_marks, b->d_srcs, b->d_part, b->d_obs, b->d_obsf,
         b->d_mean, b->d_ess, b->d_logz, b->d_res};
     for (void *p : ptrs)
         if (p)
@@ -1337,7 +1329,7 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.marks = b->d_marks;
     a.srcs = b->d_srcs;
     a.part = b->d_part;
-    a.obs = obs;
+    a.obs = b->d_obsf;
     a.h_mean = b->d_mean;
     a.h_ess = b->d_ess;
     a.h_logz = b->d_logz;
@@ -1365,6 +1357,10 @@ static int enqueue_run(
     vsmc_cuda_batch *b, const double *obs, int nsteps, int grid)
 {
     cudaStream_t st = b->stream;
+    const uint32_t nobs = static_cast<uint32_t>(
+        (b->kind == kKindCv ? 2 : 1) * b->total_T);
+    k_obs_f32<<<grid_for(nobs, 256, 1, 4), 256, 0, st>>>(obs, b->d_obsf, nobs);
+    VSMC_CUDA_CHECK_LAUNCH();
     k_batch_reset<<<(b->nf + 255) / 256, 256, 0, st>>>(
         b->d_st, b->d_flt, b->nf, b->d_step, b->d_rs_count);
     VSMC_CUDA_CHECK_LAUNCH();
@@ -1547,6 +1543,7 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     B_TRY(balloc(&b->d_srcs, total));
     B_TRY(balloc(&b->d_part, tiles));
     B_TRY(balloc(&b->d_obs, 2 * totalT));
+    B_TRY(balloc(&b->d_obsf, 2 * totalT));
     B_TRY(balloc(&b->d_mean, 2 * totalT));
     B_TRY(balloc(&b->d_ess, totalT));
     B_TRY(balloc(&b->d_logz, totalT));

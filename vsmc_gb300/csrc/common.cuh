@@ -110,10 +110,13 @@ __device__ __forceinline__ u32x4 philox4x32_10(
             k0 += 0x9E3779B9u;
             k1 += 0xBB67AE85u;
         }
-        const uint32_t hi_a = __umulhi(0xCD9E8D57u, c2);
-        const uint32_t lo_a = 0xCD9E8D57u * c2;
-        const uint32_t hi_b = __umulhi(0xD2511F53u, c0);
-        const uint32_t lo_b = 0xD2511F53u * c0;
+        // each 32 x 32 product once, as one widening multiply
+        const uint64_t pa = static_cast<uint64_t>(c2) * 0xCD9E8D57u;
+        const uint64_t pb = static_cast<uint64_t>(c0) * 0xD2511F53u;
+        const uint32_t hi_a = static_cast<uint32_t>(pa >> 32);
+        const uint32_t lo_a = static_cast<uint32_t>(pa);
+        const uint32_t hi_b = static_cast<uint32_t>(pb >> 32);
+        const uint32_t lo_b = static_cast<uint32_t>(pb);
         const uint32_t n0 = hi_a ^ k0 ^ c1;
         const uint32_t n2 = hi_b ^ k1 ^ c3;
         c0 = n0;

@@ -18,6 +18,8 @@
 
 #include <cuda_bf16.h>
 
+#include <cstring>
+
 namespace vsmc_cuda
 {
 
@@ -73,6 +75,41 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<const uint32_t *>(&v);
 }
 
+// GELU (tanh form) of two pre-activations in packed BF16 arithmetic, the
+// way the filters evaluate the network: x rounded to BF16, then
+// 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) with BF16 multiplies and
+// the hardware tanh approximation (tanh.approx.bf16x2, sm_90 and later).
+// One SFU operation per pair instead of two per value; the result is the
+// BF16 operand the next layer takes.  Training keeps gelu_f in FP32.
+__device__ __forceinline__ uint32_t gelu2_bf16(float lo, float hi)
+{
+    const __nv_bfloat162 x = __floats2bfloat162_rn(lo, hi);
+    const __nv_bfloat162 c0 = __float2bfloat162_rn(0.7978845608028654f);
+    const __nv_bfloat162 c1 = __float2bfloat162_rn(0.0356774081363001f);
+    const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
+    const __nv_bfloat162 u = __hmul2(x, __hfma2(__hmul2(x, x), c1, c0));
+    uint32_t ub, tb;
+    memcpy(&ub, &u, 4);
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(tb) : "r"(ub));
+    __nv_bfloat162 t;
+    memcpy(&t, &tb, 4);
+    const __nv_bfloat162 h = __hmul2(x, half);
+    const __nv_bfloat162 r = __hfma2(h, t, h);
+    uint32_t out;
+    memcpy(&out, &r, 4);
+    return out;
+}
+
+// the BF16 operand pair GELU(lo), GELU(hi): packed BF16 (Fast) or FP32
+template <bool Fast>
+__device__ __forceinline__ uint32_t gelu_pair(float lo, float hi)
+{
+    if constexpr (Fast)
+        return gelu2_bf16(lo, hi);
+    else
+        return pack_bf16(gelu_f(lo), gelu_f(hi));
+}
+
 __device__ __forceinline__ float bf16_round(float x)
 {
     return __bfloat162float(__float2bfloat16_rn(x));
@@ -104,7 +141,7 @@ __device__ __forceinline__ uint2 frag(
 // the hidden pre-activations (accumulator fragments of 8 n-tiles) and the
 // BF16 operand fragments of the hidden activations are kept for the
 // backward pass.  packed: the packed parameters (shared memory).
-template <bool Keep>
+template <bool Keep, bool Fast = false>
 __device__ __forceinline__ void mlp_forward_warp(const uint32_t *packed,
     const uint32_t (&a0)[4], float (&out)[4], float (*pre1)[4] = nullptr,
     float (*pre2)[4] = nullptr, uint32_t (*act1)[4] = nullptr,
@@ -135,8 +172,8 @@ __device__ __forceinline__ void mlp_forward_warp(const uint32_t *packed,
                 pre1[nt][r] = h[nt][r];
         }
         const int kt = nt >> 1, hi = nt & 1;
-        a[kt][0 + 2 * hi] = pack_bf16(gelu_f(h[nt][0]), gelu_f(h[nt][1]));
-        a[kt][1 + 2 * hi] = pack_bf16(gelu_f(h[nt][2]), gelu_f(h[nt][3]));
+        a[kt][0 + 2 * hi] = gelu_pair<Fast>(h[nt][0], h[nt][1]);
+        a[kt][1 + 2 * hi] = gelu_pair<Fast>(h[nt][2], h[nt][3]);
     }
     if (Keep) {
 #pragma unroll
@@ -168,8 +205,8 @@ __device__ __forceinline__ void mlp_forward_warp(const uint32_t *packed,
                 pre2[nt][r] = h[nt][r];
         }
         const int kt = nt >> 1, hi = nt & 1;
-        a[kt][0 + 2 * hi] = pack_bf16(gelu_f(h[nt][0]), gelu_f(h[nt][1]));
-        a[kt][1 + 2 * hi] = pack_bf16(gelu_f(h[nt][2]), gelu_f(h[nt][3]));
+        a[kt][0 + 2 * hi] = gelu_pair<Fast>(h[nt][0], h[nt][1]);
+        a[kt][1 + 2 * hi] = gelu_pair<Fast>(h[nt][2], h[nt][3]);
     }
     if (Keep) {
 #pragma unroll
@@ -196,6 +233,7 @@ __device__ __forceinline__ void mlp_forward_warp(const uint32_t *packed,
 
 // Forward pass of one warp over 32 rows as two 16-row tiles (a, b) that
 // share every weight fragment load.  Accumulator outputs oa, ob.
+template <bool Fast = false>
 __device__ __forceinline__ void mlp_forward_warp2(const uint32_t *packed,
     const uint32_t (&a0)[4], const uint32_t (&b0)[4], float (&oa)[4],
     float (&ob)[4])
@@ -220,10 +258,10 @@ __device__ __forceinline__ void mlp_forward_warp2(const uint32_t *packed,
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
         const int kt = nt >> 1, hi = nt & 1;
-        xa[kt][0 + 2 * hi] = pack_bf16(gelu_f(ha[nt][0]), gelu_f(ha[nt][1]));
-        xa[kt][1 + 2 * hi] = pack_bf16(gelu_f(ha[nt][2]), gelu_f(ha[nt][3]));
-        xb[kt][0 + 2 * hi] = pack_bf16(gelu_f(hb[nt][0]), gelu_f(hb[nt][1]));
-        xb[kt][1 + 2 * hi] = pack_bf16(gelu_f(hb[nt][2]), gelu_f(hb[nt][3]));
+        xa[kt][0 + 2 * hi] = gelu_pair<Fast>(ha[nt][0], ha[nt][1]);
+        xa[kt][1 + 2 * hi] = gelu_pair<Fast>(ha[nt][2], ha[nt][3]);
+        xb[kt][0 + 2 * hi] = gelu_pair<Fast>(hb[nt][0], hb[nt][1]);
+        xb[kt][1 + 2 * hi] = gelu_pair<Fast>(hb[nt][2], hb[nt][3]);
     }
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
@@ -243,10 +281,10 @@ __device__ __forceinline__ void mlp_forward_warp2(const uint32_t *packed,
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
         const int kt = nt >> 1, hi = nt & 1;
-        xa[kt][0 + 2 * hi] = pack_bf16(gelu_f(ha[nt][0]), gelu_f(ha[nt][1]));
-        xa[kt][1 + 2 * hi] = pack_bf16(gelu_f(ha[nt][2]), gelu_f(ha[nt][3]));
-        xb[kt][0 + 2 * hi] = pack_bf16(gelu_f(hb[nt][0]), gelu_f(hb[nt][1]));
-        xb[kt][1 + 2 * hi] = pack_bf16(gelu_f(hb[nt][2]), gelu_f(hb[nt][3]));
+        xa[kt][0 + 2 * hi] = gelu_pair<Fast>(ha[nt][0], ha[nt][1]);
+        xa[kt][1 + 2 * hi] = gelu_pair<Fast>(ha[nt][2], ha[nt][3]);
+        xb[kt][0 + 2 * hi] = gelu_pair<Fast>(hb[nt][0], hb[nt][1]);
+        xb[kt][1 + 2 * hi] = gelu_pair<Fast>(hb[nt][2], hb[nt][3]);
     }
     {
         const float bl = bias[2 * kHid + 2 * tig];

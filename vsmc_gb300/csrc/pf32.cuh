@@ -513,7 +513,6 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     __syncthreads();
     QR carry = start0;
     uint32_t empties = 0, copies = 0;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     // the next tile's log-weights are loaded while this one is counted
     float4 nxt = make_float4(0, 0, 0, 0);
     if (!checked && lo + threadIdx.x * 4 + 3 < hi)

@@ -32,6 +32,7 @@ struct PfScalars {
     uint32_t rindex;     // resampling engine: next word index in gen(rctr)
     uint32_t rkey[2];
     uint32_t rctr[4];
+    float Mf; // M as a float (the batched filters' kernels read it per tile)
 };
 
 // The state lives in two SoA buffers; a step reads one (A) and writes the

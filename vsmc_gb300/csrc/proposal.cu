@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(128) k_bearings_move(uint32_t n, uint32_t t,
         uint32_t a0[4], b0[4];
         features_to_a2(f, a0, b0);
         float oa[4], ob[4];
-        mlp_forward_warp2(sp, a0, b0, oa, ob);
+        mlp_forward_warp2<true>(sp, a0, b0, oa, ob);
         float v[8];
         out_to_owner2(oa, ob, v);
         if (mine) {

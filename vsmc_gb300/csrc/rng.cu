@@ -66,6 +66,28 @@ __global__ void __launch_bounds__(256) k_threefry_blocks(uint64_t k0,
 // Output element types the plan kernel can write.
 enum class Emit { Word, U01D, U01F };
 
+// The four outputs of one block at o[0..3]: one 16-byte streaming store per
+// 16 bytes when o is 16-byte aligned, else element stores.
+template <Emit E, typename Gen, typename Out>
+__device__ __forceinline__ void emit4(Out *o, const typename Gen::block_t &blk)
+{
+    Out v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        emit<E>(v, i, Gen::word(blk, i));
+    if ((reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+        uint4 u[sizeof(Out) / 4];
+        memcpy(u, v, sizeof(v));
+#pragma unroll
+        for (int h = 0; h < static_cast<int>(sizeof(Out) / 4); ++h)
+            __stcs(reinterpret_cast<uint4 *>(o) + h, u[h]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            o[i] = v[i];
+    }
+}
+
 // Writes stream positions [p_begin, p_end) of `plan` to out[p - p_begin].
 template <typename Gen, Emit E, typename Out>
 __global__ void __launch_bounds__(256) k_plan_stream(Gen gen, StreamPlan plan,
@@ -88,6 +110,10 @@ __global__ void __launch_bounds__(256) k_plan_stream(Gen gen, StreamPlan plan,
     for (uint64_t j = j0 + tid; j < j1; j += stride) {
         const typename Gen::block_t blk = gen.block(plan, j);
         const uint64_t p0 = plan.head + 4 * j;
+        if (p0 >= p_begin && p0 + 4 <= p_end) { // an interior block
+            emit4<E, Gen>(out + (p0 - p_begin), blk);
+            continue;
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const uint64_t p = p0 + i;

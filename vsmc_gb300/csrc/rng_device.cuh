@@ -28,7 +28,8 @@ struct StreamPlan {
     uint32_t head;        // words taken from the current block gen(C0)
     uint32_t periodic_x4; // periodic part: 1 = 256 bulk blocks per call,
                           //                0 = 255 bulk + 1 scalar per call
-    uint32_t pad;
+    uint32_t simple;      // no block's low counter limb reaches all ones:
+                          // block j's counter is c0 + j + 1, no carry
     uint64_t first_last;  // first block of the final (or only) call
     uint64_t nb_last;     // bulk blocks in the final call
     uint64_t n_total;     // words in the whole plan
@@ -121,6 +122,12 @@ inline void plan_finish(StreamPlan &p)
     p.head = static_cast<uint32_t>(
         p.n_total < 4 - p.x ? p.n_total : 4 - p.x);
     p.total_blocks = p.n_total > p.head ? (p.n_total - p.head + 3) / 4 : 0;
+    // low limbs c0 + 1 .. c0 + total_blocks all below 0xFFFFFFFF (for
+    // either engine): no carry and no extra carry of the bulk path
+    p.simple = p.total_blocks <= 0xFFFFFFFEull &&
+            p.c0[0] <= 0xFFFFFFFEull - p.total_blocks
+        ? 1u
+        : 0u;
 }
 
 // One CounterEngine::operator()(n, r) call.
@@ -204,7 +211,14 @@ struct PhiloxGen {
     __device__ block_t block(const StreamPlan &p, uint64_t j) const
     {
         uint32_t c[4];
-        plan_counter32(p, j, c);
+        if (p.simple) {
+            c[0] = static_cast<uint32_t>(p.c0[0] + 1 + j);
+            c[1] = static_cast<uint32_t>(p.c0[1]);
+            c[2] = static_cast<uint32_t>(p.c0[2]);
+            c[3] = static_cast<uint32_t>(p.c0[3]);
+        } else {
+            plan_counter32(p, j, c);
+        }
         return philox4x32_10(c[0], c[1], c[2], c[3], k0, k1);
     }
 
@@ -234,7 +248,14 @@ struct ThreefryGen {
     __device__ block_t block(const StreamPlan &p, uint64_t j) const
     {
         uint64_t c[4];
-        plan_counter64(p, j, c);
+        if (p.simple) {
+            c[0] = p.c0[0] + 1 + j;
+            c[1] = p.c0[1];
+            c[2] = p.c0[2];
+            c[3] = p.c0[3];
+        } else {
+            plan_counter64(p, j, c);
+        }
         return threefry4x64_20({c[0], c[1], c[2], c[3]}, k[0], k[1], k[2], k[3]);
     }
 
