@@ -372,9 +372,9 @@ def run_batched(args):
                                   "40 B per particle-step"},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            # per run: the reset, then per global step the step kernel and
-            # the five resampling passes
-            "gpu_launches": (1 + 6 * (int(T.max()) + 1)) * args.steps,
+            # per run: the observation conversion and the reset, then per
+            # global step the step kernel and the five resampling passes
+            "gpu_launches": (2 + 6 * (int(T.max()) + 1)) * args.steps,
         }
         line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
         print(json.dumps(line), flush=True)
