@@ -714,13 +714,15 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_qsum(const BatchArgs a)
 
 // pass 2: replication counts from the fixed-point CDF; empty and copy
 // counts per chunk
-__global__ void __launch_bounds__(kPfBlock) k_brs_count(const BatchArgs a)
+__global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
 {
     const uint32_t count = __ldcg(a.rs_count + a.rpar);
     const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
     __shared__ QR shqr[kPfBlock / 32];
     __shared__ uint32_t she[kPfBlock / 32 + 1];
     __shared__ QR start0;
+    __shared__ uint4 wbuf[2 * kPfBlock];        // stratified words of a tile
+    __shared__ uint32_t wsh[2 * (kPfBlock / 32)];
     for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
         const RsChunk c = rs_chunk_at(a, v);
         PfScalars &S = a.st[c.f];
@@ -738,8 +740,6 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_count(const BatchArgs a)
         int32_t *rep = a.rep + c.off;
         const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
         const float invQ = __frcp_rn(__ull2float_rn(Q));
-        WordCache wc;
-        wc.blk = ~0ull;
         uint32_t err = 0;
         if (threadIdx.x == 0) {
             // the chunk's first CDF value, offset, by one 128-bit division
@@ -792,6 +792,13 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_count(const BatchArgs a)
             QR tile_total;
             const QR ex = block_exclusive_qr(acc, Q, shqr, &tile_total);
             const QR st = qr_add(carry, ex, Q);
+            WordBuf wv = {wbuf, 0, 0};
+            if (!sys) {
+                uint32_t wlo, whi;
+                words_span(st, qr_add(st, loc[3], Q), n, sc, wlo, whi);
+                wv = fill_words<kPfBlock>(
+                    sc, wlo, whi, wbuf, 2 * kPfBlock, wsh);
+            }
             uint32_t Fv[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -799,13 +806,13 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_count(const BatchArgs a)
                 if (i + 1 >= n)
                     Fv[k] = n; // the last particle takes the rest
                 else if (i < c.hi)
-                    Fv[k] = f_of(qr_add(st, loc[k], Q), sys, n, Q, sc, wc);
+                    Fv[k] = f_of_buf(qr_add(st, loc[k], Q), sys, n, Q, sc, wv);
                 else
                     Fv[k] = 0;
             }
             // F before this thread's first particle is F at its start
             // position (particle 0 has nothing before it)
-            uint32_t Fprev = i0 == 0 ? 0u : f_of(st, sys, n, Q, sc, wc);
+            uint32_t Fprev = i0 == 0 ? 0u : f_of_buf(st, sys, n, Q, sc, wv);
             int32_t r[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {

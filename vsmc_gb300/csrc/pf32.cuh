@@ -471,7 +471,7 @@ __device__ __forceinline__ void block_prefix_of_parts(
 
 // Replication counts from the fixed-point CDF; per-block empty and copy
 // counts.
-__global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
+__global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
 {
     if (!a.sc->resampled)
         return;
@@ -482,6 +482,8 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     __shared__ QR shqr[kPfBlock / 32];
     __shared__ uint32_t she[kPfBlock / 32 + 1];
     __shared__ QR start0;
+    __shared__ uint4 wbuf[2 * kPfBlock];        // stratified words of a tile
+    __shared__ uint32_t wsh[2 * (kPfBlock / 32)];
     uint64_t offset, Q;
     block_prefix_of_parts(a.qpart, blockIdx.x, gridDim.x, offset, Q, shq);
     if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -492,8 +494,6 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
     const uint32_t n = a.n;
     const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
     const float invQ = __frcp_rn(__ull2float_rn(Q));
-    WordCache wc;
-    wc.blk = ~0ull;
     uint32_t err = 0;
     if (threadIdx.x == 0) {
         // the block's first CDF value, offset, by one 128-bit division
@@ -545,6 +545,12 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
         QR tile_total;
         const QR ex = block_exclusive_qr(acc, Q, shqr, &tile_total);
         const QR st = qr_add(carry, ex, Q);
+        WordBuf wv = {wbuf, 0, 0};
+        if (!sys) {
+            uint32_t wlo, whi;
+            words_span(st, qr_add(st, loc[3], Q), n, sc, wlo, whi);
+            wv = fill_words<kPfBlock>(sc, wlo, whi, wbuf, 2 * kPfBlock, wsh);
+        }
         uint32_t F[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -552,13 +558,13 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_count(const Rs32Args a)
             if (i + 1 >= n)
                 F[k] = n; // the last particle takes the rest
             else if (i < hi)
-                F[k] = f_of(qr_add(st, loc[k], Q), sys, n, Q, sc, wc);
+                F[k] = f_of_buf(qr_add(st, loc[k], Q), sys, n, Q, sc, wv);
             else
                 F[k] = 0;
         }
         // F before this thread's first particle is F at the thread's start
         // position (particle 0 has nothing before it)
-        uint32_t Fprev = i0 == 0 ? 0u : f_of(st, sys, n, Q, sc, wc);
+        uint32_t Fprev = i0 == 0 ? 0u : f_of_buf(st, sys, n, Q, sc, wv);
         int32_t r[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {

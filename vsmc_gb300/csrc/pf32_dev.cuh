@@ -275,31 +275,45 @@ __device__ __forceinline__ void qr_push(QR &acc, uint64_t q, uint32_t n,
     qr_reduce(acc.r, acc.j, Q, invQ, err);
 }
 
-// word k of the resampling engine's stream, caching the last Philox block
-struct WordCache {
-    uint64_t blk;
-    u32x4 w;
+// Stratified counting needs, for each CDF position X = (j - 1) Q + r, the
+// engine word of uniform j - 1.  A tile's positions are nondecreasing, so
+// the words it needs lie in one range of the engine stream; the block
+// generates that range's Philox blocks once into shared memory (one or two
+// per thread) instead of each thread generating the blocks its own
+// positions fall in.  Block b of the stream is at wb[b - b0] for
+// b0 <= b < b0 + nb; a block beyond the buffer (a tile whose positions
+// span more than it) is generated where it is needed.
+struct WordBuf {
+    const uint4 *wb;
+    uint32_t b0, nb;
 };
 
-__device__ __forceinline__ uint32_t cached_word(
-    const PfScalars &sc, uint64_t k, WordCache &c)
+// block b of the engine stream, for the rare word outside the buffer (not
+// inlined: it stays off the register budget of the common path)
+static __device__ __noinline__ uint4 engine_block_at(
+    const PfScalars &sc, uint32_t b)
 {
-    const uint64_t pos = static_cast<uint64_t>(sc.rindex) + k;
-    const uint64_t b = pos >> 2;
-    if (b != c.blk) {
-        uint32_t ctr[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
-        ctr32_add(ctr, b);
-        c.w = philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], sc.rkey[0],
-            sc.rkey[1]);
-        c.blk = b;
-    }
-    const uint32_t i = static_cast<uint32_t>(pos & 3);
-    return i == 0 ? c.w.x : (i == 1 ? c.w.y : (i == 2 ? c.w.z : c.w.w));
+    uint32_t c[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
+    ctr32_add(c, b);
+    const u32x4 p =
+        philox4x32_10(c[0], c[1], c[2], c[3], sc.rkey[0], sc.rkey[1]);
+    return make_uint4(p.x, p.y, p.z, p.w);
 }
 
-// F from a position (see QR)
-__device__ __forceinline__ uint32_t f_of(const QR &x, bool sys, uint32_t n,
-    uint64_t Q, const PfScalars &sc, WordCache &wc)
+// word `pos` (rindex + j) of the engine stream
+__device__ __forceinline__ uint32_t buf_word(
+    const PfScalars &sc, uint32_t pos, const WordBuf &w)
+{
+    const uint32_t b = pos >> 2;
+    const uint32_t d = b - w.b0;
+    const uint4 v = d < w.nb ? w.wb[d] : engine_block_at(sc, b);
+    const uint32_t r = pos & 3u;
+    return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w));
+}
+
+// F from a position (see QR), the stratified words from the tile's buffer
+__device__ __forceinline__ uint32_t f_of_buf(const QR &x, bool sys,
+    uint32_t n, uint64_t Q, const PfScalars &sc, const WordBuf &w)
 {
     if (sys)
         return x.j < n ? x.j : n;
@@ -308,7 +322,67 @@ __device__ __forceinline__ uint32_t f_of(const QR &x, bool sys, uint32_t n,
     const uint32_t j0 = x.j - 1;
     if (j0 >= n)
         return n;
-    return j0 + (ceil_aq(cached_word(sc, j0, wc), Q) <= x.r ? 1u : 0u);
+    return j0 + (ceil_aq(buf_word(sc, sc.rindex + j0, w), Q) <= x.r ? 1u
+                                                                     : 0u);
+}
+
+// The engine words [wlo, whi] (empty when wlo > whi) a thread may need:
+// from its start position st to the position after its last particle,
+// last = st + loc (a superset of what f_of_buf reads).
+__device__ __forceinline__ void words_span(const QR &st, const QR &last,
+    uint32_t n, const PfScalars &sc, uint32_t &wlo, uint32_t &whi)
+{
+    const uint32_t jl = st.j >= 1 ? st.j - 1 : 0;
+    const uint32_t jh = (last.j < n ? last.j : n);
+    if (jh == 0 || jl > jh - 1) {
+        wlo = 0xFFFFFFFFu;
+        whi = 0;
+    } else {
+        wlo = sc.rindex + jl;
+        whi = sc.rindex + (jh - 1);
+    }
+}
+
+// Generates the Philox blocks covering every thread's [wlo, whi] into wb
+// (cap blocks) and returns the buffer view.  sh holds 2 * kBlock / 32
+// entries.  Call with the whole block; it has two barriers.
+template <int kBlock>
+__device__ __forceinline__ WordBuf fill_words(const PfScalars &sc,
+    uint32_t wlo, uint32_t whi, uint4 *wb, uint32_t cap, uint32_t *sh)
+{
+    constexpr int kW = kBlock / 32;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t lo = __reduce_min_sync(0xFFFFFFFFu, wlo);
+    const uint32_t hi = __reduce_max_sync(0xFFFFFFFFu, whi);
+    if (lane == 0) {
+        sh[wid] = lo;
+        sh[kW + wid] = hi;
+    }
+    __syncthreads();
+    uint32_t blo = 0xFFFFFFFFu, bhi = 0;
+#pragma unroll
+    for (int k = 0; k < kW; ++k) {
+        blo = min(blo, sh[k]);
+        bhi = max(bhi, sh[kW + k]);
+    }
+    WordBuf w;
+    w.wb = wb;
+    w.b0 = 0;
+    w.nb = 0;
+    if (blo <= bhi) {
+        w.b0 = blo >> 2;
+        const uint32_t nb = (bhi >> 2) - w.b0 + 1;
+        w.nb = nb < cap ? nb : cap;
+        for (uint32_t d = threadIdx.x; d < w.nb; d += kBlock) {
+            uint32_t c[4] = {sc.rctr[0], sc.rctr[1], sc.rctr[2], sc.rctr[3]};
+            ctr32_add(c, w.b0 + d);
+            const u32x4 p =
+                philox4x32_10(c[0], c[1], c[2], c[3], sc.rkey[0], sc.rkey[1]);
+            wb[d] = make_uint4(p.x, p.y, p.z, p.w);
+        }
+    }
+    __syncthreads();
+    return w;
 }
 
 // Block-wide exclusive scan of positions over kBlock threads; *total gets
