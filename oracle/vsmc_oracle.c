@@ -1654,19 +1654,36 @@ void vo_bearings_move_f32(size_t N, size_t t, uint32_t seed,
         } else {
             float nu[4] = {ev[0], ev[1], ev[2], ev[3]};
             if (params) {
-                /* predicted position and velocity on bounded scales */
+                /* inputs in the bearing frame of z: the predicted position
+                 * along it on a saturating range scale, across it in
+                 * units of sigma_z r (softly held below 8, scaled by 1/8),
+                 * the velocity's along / across parts on a bounded scale,
+                 * sin z and cos z */
                 const float px = x + dt * vx, py = y + dt * vy;
-                const float ip = 1.0f / (10.0f + sqrtf(px * px + py * py));
+                const float rng = sqrtf(px * px + py * py);
+                const float pa = cz * px + sz * py;
+                const float pb = cz * py - sz * px;
+                const float e = pb * inv_sz / (rng > 1e-6f ? rng : 1e-6f);
+                const float eb = e / sqrtf(1.0f + 0.015625f * e * e);
                 const float iv = 1.0f / (1.0f + sqrtf(vx * vx + vy * vy));
-                const float f[6] = {px * ip, py * ip, vx * iv, vy * iv, sz, cz};
+                const float f[6] = {pa / (10.0f + rng), 0.125f * eb,
+                    (cz * vx + sz * vy) * iv, (cz * vy - sz * vx) * iv, sz,
+                    cz};
                 vo_mlp_row r;
                 vo_mlp_row_forward(params, f, &r, 1);
+                /* the draw nu' = (a1, a2, b1, b2) in the bearing frame,
+                 * then rotated pairwise to the axes */
+                float fr[4];
                 for (int d = 0; d < 4; ++d) {
                     float l = (float)r.out[4 + d];
                     l = l < -12.0f ? -12.0f : (l > 4.0f ? 4.0f : l);
-                    nu[d] = (float)r.out[d] + expf(0.5f * l) * ev[d];
-                    lq += 0.5f * (ev[d] * ev[d] - nu[d] * nu[d]) + 0.5f * l;
+                    fr[d] = (float)r.out[d] + expf(0.5f * l) * ev[d];
+                    lq += 0.5f * (ev[d] * ev[d] - fr[d] * fr[d]) + 0.5f * l;
                 }
+                nu[0] = cz * fr[0] - sz * fr[2];
+                nu[2] = sz * fr[0] + cz * fr[2];
+                nu[1] = cz * fr[1] - sz * fr[3];
+                nu[3] = sz * fr[1] + cz * fr[3];
             }
             const float dx = l11 * nu[0], dvx = l21 * nu[0] + l22 * nu[1];
             const float dy = l11 * nu[2], dvy = l21 * nu[2] + l22 * nu[3];

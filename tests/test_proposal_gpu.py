@@ -195,7 +195,8 @@ def test_bearings_batch_tracks_oracle(vc, port, learned):
 
 
 def _samples(m, M, T, rng):
-    """(features of x_{t-1} and z_t, nu_t) from M simulated tracks."""
+    """(features of x_{t-1} and z_t, nu_t) from M simulated tracks, both in
+    the bearing frame of z_t (the inputs and targets the trainer forms)."""
     l11 = np.sqrt(m.q * m.dt ** 3 / 3)
     l21 = m.q * m.dt ** 2 / 2 / l11
     l22 = np.sqrt(m.q * m.dt - l21 ** 2)
@@ -212,12 +213,20 @@ def _samples(m, M, T, rng):
         xn[1] = x[1] + m.dt * x[3] + l11 * nu[2]
         xn[3] = x[3] + l21 * nu[2] + l22 * nu[3]
         z = np.arctan2(xn[1], xn[0]) + m.sigma_z * rng.normal(size=M)
+        sz, cz = np.sin(z), np.cos(z)
         px, py = x[0] + m.dt * x[2], x[1] + m.dt * x[3]
-        ip = 1 / (10 + np.hypot(px, py))
+        r = np.hypot(px, py)
+        e = (cz * py - sz * px) / (m.sigma_z * np.maximum(r, 1e-6))
         iv = 1 / (1 + np.hypot(x[2], x[3]))
-        feats.append(np.stack([px * ip, py * ip, x[2] * iv, x[3] * iv,
-                               np.sin(z), np.cos(z)], axis=1))
-        nus.append(nu.T)
+        feats.append(np.stack([(cz * px + sz * py) / (10 + r),
+                               0.125 * e / np.sqrt(1 + e * e / 64),
+                               (cz * x[2] + sz * x[3]) * iv,
+                               (cz * x[3] - sz * x[2]) * iv, sz, cz], axis=1))
+        # the noise pairs (x1, y1), (x2, y2) rotated into the frame:
+        # (along, along, across, across)
+        nus.append(np.stack([cz * nu[0] + sz * nu[2], cz * nu[1] + sz * nu[3],
+                             cz * nu[2] - sz * nu[0], cz * nu[3] - sz * nu[1]],
+                            axis=1))
         x = xn
     return (np.concatenate(feats).astype(np.float32),
             np.concatenate(nus).astype(np.float32))

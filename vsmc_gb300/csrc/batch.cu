@@ -550,8 +550,9 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
                 lse_push(lw, m, s, s2);
             }
         } else {
+            const float sz = sinf(z), cz = cosf(z);
             float fe[6];
-            bearings_features(c, x, y, vx, vy, sinf(z), cosf(z), fe);
+            bearings_features(c, x, y, vx, vy, sz, cz, fe);
             uint32_t a0[4], b0[4];
             features_to_a2(fe, a0, b0);
             // one 16-row tile at a time keeps one tile's activations live
@@ -580,15 +581,16 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
                 sx += wo * x;
                 sy += wo * y;
                 sw += wo;
-                float e[4], nu[4];
+                float e[4], fr[4], nu[4];
                 bearings_normals(t, F.seed, i, e);
                 float lq = 0;
 #pragma unroll
                 for (int d = 0; d < 4; ++d) {
                     const float l = fminf(fmaxf(v[4 + d], c.lmin), c.lmax);
-                    nu[d] = v[d] + __expf(0.5f * l) * e[d];
-                    lq += 0.5f * (e[d] * e[d] - nu[d] * nu[d]) + 0.5f * l;
+                    fr[d] = v[d] + __expf(0.5f * l) * e[d];
+                    lq += 0.5f * (e[d] * e[d] - fr[d] * fr[d]) + 0.5f * l;
                 }
+                frame_to_axes(sz, cz, fr, nu); // the draw, bearing frame
                 bearings_step(c, nu, x, y, vx, vy);
                 lw = lw_old + bearings_loglik(c, z, x, y) + lq;
                 lse_push(lw, m, s, s2);

@@ -10,10 +10,11 @@
 //
 // Proposals work in the transition's whitened coordinates nu = (nu_x1,
 // nu_x2, nu_y1, nu_y2): the bootstrap draws nu ~ N(0, I); the learned
-// proposal draws nu ~ N(m, diag(exp(l))) with (m, l) from the network, and
-// the state follows as x = F x' + L nu.  The weight increment is
-//   log g(z | x) + log N(nu; 0, I) - log N(nu; m, diag(exp(l)))
-// (the Jacobian of nu -> x is the same in both densities and cancels).
+// proposal draws nu' ~ N(m, diag(exp(l))) in the bearing frame of z (see
+// frame_to_axes) with (m, l) from the network, rotates it to nu, and the
+// state follows as x = F x' + L nu.  The weight increment is
+//   log g(z | x) + log N(nu'; 0, I) - log N(nu'; m, diag(exp(l)))
+// (the Jacobian of nu' -> x is the same in both densities and cancels).
 //
 // No reference counterpart: the reference's pf example is the Student-t
 // position model (example/pf/include/pf.hpp); this model and the learned
@@ -125,21 +126,53 @@ __device__ __forceinline__ float bearings_loglik(
     return c.ll_c - 0.5f * s * s;
 }
 
-// The network inputs of a particle at its previous state and the bearing:
-// the predicted position p = (x + dt vx, y + dt vy) as p / (10 + |p|) (its
-// direction, and its range on a saturating scale), the velocity as
-// v / (1 + |v|), and (sin z, cos z).  Bounded inputs keep the activations
-// in range however far the target drifts.
+// The bearing frame of an observation z: along = (cos z, sin z), across =
+// (-sin z, cos z).  The whitened transition noise nu = (x1, x2, y1, y2)
+// (position and velocity parts per axis) rotates pairwise into
+// nu' = (a1, a2, b1, b2), the along and across parts of the position pair
+// (x1, y1) and of the velocity pair (x2, y2).  The rotation is orthogonal,
+// so N(nu; 0, I) = N(nu'; 0, I) with Jacobian 1; the factor L is the same on
+// both axes, so the position noise across the bearing is l11 b1 alone.  The
+// proposal's mean and diagonal log-variance live in this frame.
+__device__ __forceinline__ void frame_to_axes(
+    float sz, float cz, const float (&v)[4], float (&nu)[4])
+{
+    nu[0] = cz * v[0] - sz * v[2];
+    nu[2] = sz * v[0] + cz * v[2];
+    nu[1] = cz * v[1] - sz * v[3];
+    nu[3] = sz * v[1] + cz * v[3];
+}
+
+__device__ __forceinline__ void axes_to_frame(
+    float sz, float cz, const float (&nu)[4], float (&v)[4])
+{
+    v[0] = cz * nu[0] + sz * nu[2];
+    v[2] = cz * nu[2] - sz * nu[0];
+    v[1] = cz * nu[1] + sz * nu[3];
+    v[3] = cz * nu[3] - sz * nu[1];
+}
+
+// The network inputs of a particle at its previous state and the bearing z,
+// in the bearing frame.  With the predicted position p = (x + dt vx,
+// y + dt vy) and r = |p|: p along the bearing on a saturating range scale,
+// p_a / (10 + r); p across it in units of the bearing's resolution,
+// e = p_b / (sigma_z r), held below 8 by e / sqrt(1 + (e / 8)^2) and scaled
+// by 1/8; the velocity's along and across parts as v / (1 + |v|); and
+// (sin z, cos z).  Every input is bounded whatever the state.
 __device__ __forceinline__ void bearings_features(const BearingsConst &c,
     float x, float y, float vx, float vy, float sz, float cz, float (&f)[6])
 {
     const float px = x + c.dt * vx, py = y + c.dt * vy;
-    const float ip = 1.0f / (10.0f + sqrtf(px * px + py * py));
+    const float r = sqrtf(px * px + py * py);
+    const float pa = cz * px + sz * py;
+    const float pb = cz * py - sz * px;
+    const float e = pb * c.inv_sz / fmaxf(r, 1e-6f);
+    const float eb = e / sqrtf(1.0f + 0.015625f * e * e);
     const float iv = 1.0f / (1.0f + sqrtf(vx * vx + vy * vy));
-    f[0] = px * ip;
-    f[1] = py * ip;
-    f[2] = vx * iv;
-    f[3] = vy * iv;
+    f[0] = pa / (10.0f + r);
+    f[1] = 0.125f * eb;
+    f[2] = (cz * vx + sz * vy) * iv;
+    f[3] = (cz * vy - sz * vx) * iv;
     f[4] = sz;
     f[5] = cz;
 }

@@ -173,15 +173,16 @@ __global__ void __launch_bounds__(128) k_bearings_move(uint32_t n, uint32_t t,
         float v[8];
         out_to_owner2(oa, ob, v);
         if (mine) {
-            float e[4], nu[4];
+            float e[4], fr[4], nu[4];
             bearings_normals(t, seed, i, e);
             float lq = 0;
 #pragma unroll
             for (int d = 0; d < 4; ++d) {
                 const float l = fminf(fmaxf(v[4 + d], c.lmin), c.lmax);
-                nu[d] = v[d] + __expf(0.5f * l) * e[d];
-                lq += 0.5f * (e[d] * e[d] - nu[d] * nu[d]) + 0.5f * l;
+                fr[d] = v[d] + __expf(0.5f * l) * e[d];
+                lq += 0.5f * (e[d] * e[d] - fr[d] * fr[d]) + 0.5f * l;
             }
+            frame_to_axes(sz, cz, fr, nu); // the draw, bearing frame
             bearings_step(c, nu, x, y, vx, vy);
             sx[i] = x;
             sy[i] = y;
@@ -513,15 +514,17 @@ __global__ void k_traj_step(uint32_t M, uint32_t t, uint32_t seed,
             float zn1, zn2;
             normal_pair_f(w2.x, w2.y, zn1, zn2);
             const float z = atan2f(y, x) + sigma_z * zn1;
-            float f[6];
-            bearings_features(c, px, py, pvx, pvy, sinf(z), cosf(z), f);
+            const float sz = sinf(z), cz = cosf(z);
+            float f[6], fr[4];
+            bearings_features(c, px, py, pvx, pvy, sz, cz, f);
+            axes_to_frame(sz, cz, e, fr); // the target, bearing frame
             const size_t row = static_cast<size_t>(t - 1) * M + i;
 #pragma unroll
             for (int k = 0; k < 6; ++k)
                 feat[6 * row + k] = f[k];
 #pragma unroll
             for (int d = 0; d < 4; ++d)
-                nu_out[4 * row + d] = e[d];
+                nu_out[4 * row + d] = fr[d];
         }
         tx[i] = x;
         ty[i] = y;
