@@ -673,7 +673,7 @@ def main():
                     default=[1 << 12, 1 << 14, 1 << 16])
     ap.add_argument("--train-traj", type=int, default=1 << 20)
     ap.add_argument("--train-batch", type=int, default=1 << 16)
-    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--train-steps", type=int, default=10000)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--ref-particles", type=int, default=1 << 18)
     ap.add_argument("--bearings-dt", type=float, default=1.0)

@@ -373,12 +373,16 @@ int vsmc_cuda_bearings_simulate(uint32_t seed, size_t T,
     const vsmc_cuda_bearings_model *model, double *truth, double *obs,
     void *stream);
 
-/* The proposal network: inputs from the previous state and the bearing --
- * the predicted position p = (x + dt vx, y + dt vy) as p / (10 + |p|), the
- * velocity as v / (1 + |v|), sin z, cos z -- two hidden layers of 64 (GELU,
- * tanh form), outputs (m, l): the mean and
- * diagonal log-variance of the whitened transition noise nu (x = F x' + L nu,
- * L = chol(Q)).  Parameters: FP32, *nparams floats (W1[64][6], b1[64],
+/* The proposal network: inputs from the previous state and the bearing z,
+ * in the bearing frame (along = (cos z, sin z), across = (-sin z, cos z)):
+ * with the predicted position p = (x + dt vx, y + dt vy) and r = |p|,
+ * p_along / (10 + r); e / sqrt(1 + (e / 8)^2) / 8 with e = p_across /
+ * (sigma_z r); the velocity's along and across parts over (1 + |v|); sin z;
+ * cos z.  Two hidden layers of 64 (GELU, tanh form); outputs (m, l): the
+ * mean and diagonal log-variance of the whitened transition noise in the
+ * bearing frame, nu' = (along, along, across, across) of the position and
+ * velocity noise pairs (x = F x' + L nu, L = chol(Q), nu the pairs rotated
+ * back).  Parameters: FP32, *nparams floats (W1[64][6], b1[64],
  * W2[64][64], b2[64], W3[8][64], b3[8]); the packed copy (BF16 operand
  * fragments + FP32 biases, *npacked 32-bit words) is what the kernels read. */
 int vsmc_cuda_mlp_sizes(size_t *nparams, size_t *npacked);
@@ -396,7 +400,7 @@ int vsmc_cuda_mlp_loss_grad(const uint32_t *packed, size_t B,
     void *stream);
 /* Train params in place with Adam (lr): ntraj trajectories simulated from
  * the model (seed) for T steps give ntraj * (T - 1) stored (x_{t-1}, z_t,
- * nu_t) samples; then `steps` Adam steps on minibatches of `batch` samples
+ * nu_t) samples (inputs and noise in the bearing frame of z_t); then `steps` Adam steps on minibatches of `batch` samples
  * drawn uniformly with replacement.  loss_host (may be NULL) receives the
  * mean loss of each minibatch (`steps` values).  Synchronizes. */
 int vsmc_cuda_mlp_train(const vsmc_cuda_bearings_model *model, uint32_t seed,
@@ -404,9 +408,9 @@ int vsmc_cuda_mlp_train(const vsmc_cuda_bearings_model *model, uint32_t seed,
     float *params, double *loss_host, void *stream);
 /* One FP32 move + weight increment on caller-owned SoA state [4][n]: t == 0
  * draws the prior; t > 0 draws nu ~ N(0, I) (packed == NULL, bootstrap) or
- * nu ~ N(m, diag(exp(l))) from the network (packed != NULL).  lw_inc gets
- * log g(z | x) (+ log N(nu; 0, I) - log N(nu; m, exp(l)) for the learned
- * proposal).  Particle streams: Philox4x32 key {t, seed}, counter
+ * nu' ~ N(m, diag(exp(l))) from the network in the bearing frame of z,
+ * rotated to nu (packed != NULL).  lw_inc gets log g(z | x)
+ * (+ log N(nu'; 0, I) - log N(nu'; m, exp(l)) for the learned proposal).  Particle streams: Philox4x32 key {t, seed}, counter
  * {0, i, 0, 0}, pre-incremented, two Box-Muller pairs. */
 int vsmc_cuda_bearings_move_f32(size_t n, size_t t, uint32_t seed,
     const vsmc_cuda_bearings_model *model, double z, const uint32_t *packed,
