@@ -85,6 +85,7 @@ struct BatchArgs {
     uint32_t *marks, *srcs;
     TileRecord *part; // per tile
     const float *obs; // the observations in FP32 (converted once per run)
+    const float2 *obs_sc; // bearings kinds: (sin z, cos z) of each bearing
     double *h_mean, *h_ess, *h_logz;
     int *h_res;
     uint32_t *step; // global step counter
@@ -550,7 +551,8 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
                 lse_push(lw, m, s, s2);
             }
         } else {
-            const float sz = sinf(z), cz = cosf(z);
+            const float2 scz = a.obs_sc[F.obs_off + t];
+            const float sz = scz.x, cz = scz.y;
             float fe[6];
             bearings_features(c, x, y, vx, vy, sz, cz, fe);
             uint32_t a0[4], b0[4];
@@ -1056,12 +1058,18 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_fill(const BatchArgs a)
     }
 }
 
-// the run's observations in FP32, as the step kernels use them
-__global__ void k_obs_f32(const double *obs, float *out, uint32_t count)
+// the run's observations in FP32, as the step kernels use them, and for
+// the bearings kinds (sc != null) the sine and cosine of each FP32 bearing
+__global__ void k_obs_f32(
+    const double *obs, float *out, float2 *sc, uint32_t count)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count;
-         i += gridDim.x * blockDim.x)
-        out[i] = static_cast<float>(obs[i]);
+         i += gridDim.x * blockDim.x) {
+        const float z = static_cast<float>(obs[i]);
+        out[i] = z;
+        if (sc)
+            sc[i] = make_float2(sinf(z), cosf(z));
+    }
 }
 
 __global__ void k_batch_reset(PfScalars *st, const BFilter *flt, uint32_t nf,
@@ -1241,6 +1249,7 @@ struct vsmc_cuda_batch {
     uint32_t *d_marks = nullptr, *d_srcs = nullptr;
     TileRecord *d_part = nullptr;
     float *d_obsf = nullptr; // the run's observations in FP32
+    float2 *d_obs_sc = nullptr; // bearings kinds: sin, cos of each bearing
     double *d_obs = nullptr;
     double *d_mean = nullptr, *d_ess = nullptr, *d_logz = nullptr;
     int *d_res = nullptr;
@@ -1269,7 +1278,7 @@ static void batch_free(vsmc_cuda_batch *b)
     void *ptrs[] = {b->d_flt, b->d_st, b->d_tile_filter, b->d_active,
         b->d_step, b->d_rs_list, b->d_rs_count, b->d_rs_q, b->d_rs_e,
         b->d_rs_c, b->d_rs_m, b->d_state[0], b->d_state[1], b->d_lw,
-        b->d_rep, b->d_idx, b->d_marks, b->d_srcs, b->d_part, b->d_obs, b->d_obsf,
+        b->d_rep, b->d_idx, b->d_marks, b->d_srcs, b->d_part, b->d_obs, b->d_obsf, b->d_obs_sc,
         b->d_mean, b->d_ess, b->d_logz, b->d_res};
     for (void *p : ptrs)
         if (p)
@@ -1339,6 +1348,7 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.srcs = b->d_srcs;
     a.part = b->d_part;
     a.obs = b->d_obsf;
+    a.obs_sc = b->d_obs_sc;
     a.h_mean = b->d_mean;
     a.h_ess = b->d_ess;
     a.h_logz = b->d_logz;
@@ -1368,7 +1378,8 @@ static int enqueue_run(
     cudaStream_t st = b->stream;
     const uint32_t nobs = static_cast<uint32_t>(
         (b->kind == kKindCv ? 2 : 1) * b->total_T);
-    k_obs_f32<<<grid_for(nobs, 256, 1, 4), 256, 0, st>>>(obs, b->d_obsf, nobs);
+    k_obs_f32<<<grid_for(nobs, 256, 1, 4), 256, 0, st>>>(obs, b->d_obsf,
+        b->kind == kKindCv ? nullptr : b->d_obs_sc, nobs);
     VSMC_CUDA_CHECK_LAUNCH();
     k_batch_reset<<<(b->nf + 255) / 256, 256, 0, st>>>(
         b->d_st, b->d_flt, b->nf, b->d_step, b->d_rs_count);
@@ -1553,6 +1564,8 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     B_TRY(balloc(&b->d_part, tiles));
     B_TRY(balloc(&b->d_obs, 2 * totalT));
     B_TRY(balloc(&b->d_obsf, 2 * totalT));
+    if (kind != kKindCv)
+        B_TRY(balloc(&b->d_obs_sc, totalT));
     B_TRY(balloc(&b->d_mean, 2 * totalT));
     B_TRY(balloc(&b->d_ess, totalT));
     B_TRY(balloc(&b->d_logz, totalT));

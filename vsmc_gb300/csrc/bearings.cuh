@@ -158,7 +158,9 @@ __device__ __forceinline__ void axes_to_frame(
 // p_a / (10 + r); p across it in units of the bearing's resolution,
 // e = p_b / (sigma_z r), held below 8 by e / sqrt(1 + (e / 8)^2) and scaled
 // by 1/8; the velocity's along and across parts as v / (1 + |v|); and
-// (sin z, cos z).  Every input is bounded whatever the state.
+// (sin z, cos z).  Every input is bounded whatever the state.  The inputs
+// are rounded to BF16 for the network, so the quotients use the fast
+// division and reciprocal square root.
 __device__ __forceinline__ void bearings_features(const BearingsConst &c,
     float x, float y, float vx, float vy, float sz, float cz, float (&f)[6])
 {
@@ -166,10 +168,10 @@ __device__ __forceinline__ void bearings_features(const BearingsConst &c,
     const float r = sqrtf(px * px + py * py);
     const float pa = cz * px + sz * py;
     const float pb = cz * py - sz * px;
-    const float e = pb * c.inv_sz / fmaxf(r, 1e-6f);
-    const float eb = e / sqrtf(1.0f + 0.015625f * e * e);
-    const float iv = 1.0f / (1.0f + sqrtf(vx * vx + vy * vy));
-    f[0] = pa / (10.0f + r);
+    const float e = __fdividef(pb * c.inv_sz, fmaxf(r, 1e-6f));
+    const float eb = e * rsqrtf(1.0f + 0.015625f * e * e);
+    const float iv = __fdividef(1.0f, 1.0f + sqrtf(vx * vx + vy * vy));
+    f[0] = __fdividef(pa, 10.0f + r);
     f[1] = 0.125f * eb;
     f[2] = (cz * vx + sz * vy) * iv;
     f[3] = (cz * vy - sz * vx) * iv;
