@@ -13,6 +13,7 @@
 #include "seqsum.cuh"
 #include "resample_internal.cuh"
 
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -90,10 +91,135 @@ __device__ __forceinline__ size_t lower_count(
     return lo;
 }
 
-__global__ void k_counts(size_t m, size_t n, const double *cdf,
-    const double *pm, uint32_t *F)
+// Order-preserving integer key of a double, so the running maximum of the
+// uniforms and the counting compare integers (GB300's FP64 rate is a small
+// fraction of its integer rate): keys order as the doubles do, -0 equals +0,
+// and a NaN uniform sits above everything, as the two-pointer test
+// `u <= accw` is false for it.
+__device__ __forceinline__ long long okey(double u)
 {
-    GRID_LOOP(i, m - 1) F[i] = static_cast<uint32_t>(upper_count(pm, n, cdf[i]));
+    const long long b = __double_as_longlong(u);
+    const unsigned long long a =
+        static_cast<unsigned long long>(b) & 0x7FFFFFFFFFFFFFFFull;
+    if (a == 0)
+        return 0; // +0 and -0
+    if (a > 0x7FF0000000000000ull)
+        return LLONG_MAX; // NaN
+    return b >= 0 ? b : (b ^ LLONG_MAX);
+}
+
+// the key a CDF value is compared with: a NaN CDF value counts no uniform
+__device__ __forceinline__ long long okey_cdf(double x)
+{
+    const unsigned long long a =
+        static_cast<unsigned long long>(__double_as_longlong(x)) &
+        0x7FFFFFFFFFFFFFFFull;
+    return a > 0x7FF0000000000000ull ? LLONG_MIN : okey(x);
+}
+
+struct LoadOKey {
+    const double *u;
+    __device__ long long operator()(size_t i) const { return okey(u[i]); }
+};
+
+struct StoreK {
+    long long *p;
+    __device__ void operator()(size_t i, long long v) const { p[i] = v; }
+};
+
+struct OpMaxK {
+    __device__ __forceinline__ long long operator()(long long a,
+        long long b) const
+    {
+        return a < b ? b : a;
+    }
+};
+
+// The first index j >= lo with pmk_j > x (hi if none), given that every
+// j < lo has pmk_j <= x and pmk_hi > x or hi == n.
+__device__ __forceinline__ size_t first_above(
+    const long long *pmk, size_t lo, size_t hi, long long x)
+{
+    while (lo < hi) {
+        const size_t mid = lo + (hi - lo) / 2;
+        if (pmk[mid] <= x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// #{j < n : pmk_j <= x} by exponential search from a guess g <= n.
+__device__ __forceinline__ size_t count_from(
+    const long long *pmk, size_t n, long long x, size_t g)
+{
+    size_t lo, hi;
+    size_t step = 1;
+    if (g < n && pmk[g] <= x) { // the answer is above g
+        lo = g + 1;
+        hi = n;
+        while (lo < n) {
+            const size_t probe = lo + step - 1;
+            if (probe >= n)
+                break;
+            if (pmk[probe] > x) {
+                hi = probe;
+                break;
+            }
+            lo = probe + 1;
+            step <<= 1;
+        }
+    } else { // the answer is at most g
+        lo = 0;
+        hi = g;
+        while (step <= hi) {
+            const size_t probe = hi - step;
+            if (pmk[probe] <= x) {
+                lo = probe + 1;
+                break;
+            }
+            hi = probe;
+            step <<= 1;
+        }
+    }
+    return first_above(pmk, lo, hi, x);
+}
+
+// floor(c n) for c in [0, 1) from the bits of c (integer operations; only a
+// starting guess, so the low bits of c are dropped); n for c >= 1, 0 for a
+// negative c
+__device__ __forceinline__ size_t guess_cn(double c, size_t n)
+{
+    const unsigned long long b =
+        static_cast<unsigned long long>(__double_as_longlong(c));
+    if (b >> 63)
+        return 0;
+    const int e = static_cast<int>(b >> 52) - 1023;
+    if (e >= 0)
+        return n;
+    const int sh = 31 - e; // c n = (mant >> 21) n 2^(e - 31)
+    if (sh >= 64)
+        return 0;
+    const unsigned long long m32 = ((b & ((1ull << 52) - 1)) | (1ull << 52)) >> 21;
+    const unsigned long long g = (m32 * static_cast<unsigned long long>(n)) >> sh;
+    return g < n ? static_cast<size_t>(g) : n;
+}
+
+// F[i] = #{j < n : pmk_j <= key(cdf_i)} for i < m - 1, both sequences
+// non-decreasing.  Every scheme spreads its uniforms over [0, 1), so the
+// answer is near n cdf_i: an exponential search from that guess needs a few
+// loads, and consecutive lanes touch neighbouring addresses.  A weight that
+// takes many copies costs a logarithmic number of loads.
+__global__ void __launch_bounds__(kB) k_counts(size_t m, size_t n,
+    const double *cdf, const long long *pmk, uint32_t *F)
+{
+    GRID_LOOP(i, m - 1)
+    {
+        const double c = cdf[i];
+        F[i] = static_cast<uint32_t>(
+            count_from(pmk, n, okey_cdf(c), guess_cn(c, n)));
+    }
 }
 
 __global__ void k_rep_from_counts(size_t m, size_t n, const uint32_t *F,
@@ -135,15 +261,30 @@ __device__ __forceinline__ uint32_t stream_word(const EngineState &e, size_t k)
     return i == 0 ? b.x : (i == 1 ? b.y : (i == 2 ? b.z : b.w));
 }
 
-// U01SequenceStratified: u_j = U_j * delta + j * delta
+// U01SequenceStratified: u_j = U_j * delta + j * delta.  Word j is at
+// stream position index + j; one Philox block gives the four words of
+// positions 4b .. 4b + 3.
 __global__ void k_stratified_seq(EngineState e, size_t n, double *u)
 {
     const double delta = 1.0 / static_cast<double>(n);
-    GRID_LOOP(j, n)
+    const uint64_t first = e.index;
+    const uint64_t nblk = (first + n + 3) / 4;
+    GRID_LOOP(b, nblk)
     {
-        const double U = u01_co_d(stream_word(e, j));
-        u[j] = __dadd_rn(__dmul_rn(U, delta),
-            __dmul_rn(static_cast<double>(j), delta));
+        uint32_t c[4] = {e.c[0], e.c[1], e.c[2], e.c[3]};
+        ctr32_add(c, b);
+        const u32x4 w = philox4x32_10(c[0], c[1], c[2], c[3], e.k0, e.k1);
+        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t pos = 4 * static_cast<uint64_t>(b) + k;
+            if (pos < first || pos - first >= n)
+                continue;
+            const size_t j = static_cast<size_t>(pos - first);
+            const double U = u01_co_d(ws[k]);
+            u[j] = __dadd_rn(__dmul_rn(U, delta),
+                __dmul_rn(static_cast<double>(j), delta));
+        }
     }
 }
 
@@ -499,18 +640,18 @@ int u01_rep_device(size_t m, size_t n, const double *w, const double *u,
         return VSMC_CUDA_OK;
     }
     double *cdf = scratch.get<double>(m - 1);
-    double *pm = scratch.get<double>(n);
-    double *pp = scratch.get<double>(scan_parts(n));
+    long long *pmk = scratch.get<long long>(n);
+    long long *pp = scratch.get<long long>(scan_parts(n));
     uint32_t *F = scratch.get<uint32_t>(m);
-    if (!cdf || !pm || !pp || !F)
+    if (!cdf || !pmk || !pp || !F)
         return VSMC_CUDA_ERR_ALLOC;
     int rc = seqsum_device(m - 1, w, cdf, nullptr, err, scratch, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    rc = device_scan(n, LoadKey{u}, StoreD{pm}, OpMaxD(), -static_cast<double>(INFINITY), pp, st);
+    rc = device_scan(n, LoadOKey{u}, StoreK{pmk}, OpMaxK(), LLONG_MIN, pp, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    k_counts<<<grid1(m), kB, 0, st>>>(m, n, cdf, pm, F);
+    k_counts<<<grid1(m), kB, 0, st>>>(m, n, cdf, pmk, F);
     k_rep_from_counts<<<grid1(m), kB, 0, st>>>(m, n, F, rep, integ);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;

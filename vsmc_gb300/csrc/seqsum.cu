@@ -16,6 +16,14 @@
 // with real IEEE additions.  The binade of every running sum is taken from an
 // approximate parallel prefix P with the margin 2^-19 relative, far above
 // both |P - exact| and |sequential - exact| <= (n - 1) 2^-53 (n < 2^31).
+//
+// The classification works on the doubles' bit patterns with integer
+// operations (GB300's FP64 rate is a small fraction of its integer rate),
+// and runs once per element inside the scan that counts breakpoints; the
+// later passes read breakpoints and increments back from the scan's output.
+// Between breakpoints every running sum lies in one binade, so
+// s_i = s_b + (r_b+1 + ... + r_i) u is the bit pattern of s_b plus that
+// integer.
 #include "common.cuh"
 #include "scan.cuh"
 #include "seqsum.cuh"
@@ -41,14 +49,21 @@ struct OpRF {
     }
 };
 
-constexpr double kMargin = 0x1p-19;
+// The margin tests on the fraction field f (units of 2^-52) of P, for
+// m = 2^-19:
+//   P (1 - m) >= 2^e       holds when f >= 2^33 + 2^14 + 1 (> 2^52 m / (1 - m))
+//   P (1 + m) <  2^(e + 1) holds when f <  2^52 - 2^34     (< 2^52 (1 - m) / (1 + m))
+constexpr uint64_t kFracMask = (1ull << 52) - 1;
+constexpr uint64_t kFracLo = (1ull << 33) + (1ull << 14) + 1;
+constexpr uint64_t kFracHi = (1ull << 52) - (1ull << 34);
+constexpr uint32_t kExpMin = 1023 - 1000; // running sums below 2^-1000 are breakpoints
 
 // exact power of two (ldexp scales without rounding)
 __device__ __forceinline__ double pow2(int k) { return ldexp(1.0, k); }
 
-__device__ __forceinline__ int binade(double v)
+__device__ __forceinline__ uint64_t dbits(double v)
 {
-    return static_cast<int>((__double_as_longlong(v) >> 52) & 0x7FF) - 1023;
+    return static_cast<uint64_t>(__double_as_longlong(v));
 }
 
 // classification of element i from the approximate prefix P
@@ -62,30 +77,48 @@ __device__ __forceinline__ Class classify(size_t i, const double *x,
     const double *P, uint32_t *err, bool allow_inf)
 {
     Class c = {false, 0, 0};
-    const double xi = x[i];
-    if (!(xi >= 0.0) || (isinf(xi) && !allow_inf)) {
+    const uint64_t xb = dbits(x[i]);
+    const uint32_t xe = static_cast<uint32_t>(xb >> 52) & 0x7FFu;
+    const uint64_t xf = xb & kFracMask;
+    // x >= 0 fails for NaN and for negatives other than -0
+    const bool bad = (xe == 0x7FFu && xf != 0) || ((xb >> 63) && (xb << 1));
+    const bool inf = xe == 0x7FFu && xf == 0;
+    if (bad || (inf && !allow_inf)) {
         if (err)
             atomicOr(err, DEV_ERR_NONFINITE);
         return c;
     }
-    if (isinf(xi))
+    if (inf || i == 0)
         return c;
-    if (i == 0)
+    const uint64_t pa = dbits(P[i - 1]);
+    const uint64_t pb = dbits(P[i]);
+    const uint32_t ea = static_cast<uint32_t>(pa >> 52); // sign bit included
+    if (ea < kExpMin || ea > 2046u || (pa & kFracMask) < kFracLo)
         return c;
-    const double lo = P[i - 1] * (1.0 - kMargin);
-    const double hi = P[i] * (1.0 + kMargin);
-    if (!(lo >= 0x1p-1000) || !isfinite(hi))
+    if (static_cast<uint32_t>(pb >> 52) != ea || (pb & kFracMask) >= kFracHi)
         return c;
-    const int e = binade(lo);
-    if (binade(hi) != e)
-        return c;
-    const double y = ldexp(xi, 52 - e); // exact
-    const double fl = floor(y);
-    if (y - fl == 0.5) // tie: rounding depends on the running sum's parity
-        return c;
+    const int e = static_cast<int>(ea) - 1023;
+    // x = mant 2^q; x / 2^(e-52) = mant / 2^k with k = e - 52 - q
+    const uint64_t mant = xe ? (xf | (1ull << 52)) : xf;
+    const int q = (xe ? static_cast<int>(xe) : 1) - 1075;
+    const int k = e - 52 - q;
+    uint64_t r;
+    if (k < 0) {
+        return c; // x above the running sum's binade: left to the fix-up
+    } else if (k == 0) {
+        r = mant;
+    } else if (k >= 64) {
+        r = 0; // mant < 2^53 <= 2^(k-1): below half a unit, no tie
+    } else {
+        const uint64_t rem = mant & ((1ull << k) - 1);
+        const uint64_t half = 1ull << (k - 1);
+        if (rem == half) // tie: rounding depends on the running sum's parity
+            return c;
+        r = (mant >> k) + (rem > half ? 1u : 0u);
+    }
     c.regular = true;
     c.e = e;
-    c.r = static_cast<uint64_t>(rint(y));
+    c.r = r;
     return c;
 }
 
@@ -102,10 +135,11 @@ struct StoreD {
 struct LoadRF {
     const double *x;
     const double *P;
+    uint32_t *err;
     bool allow_inf;
     __device__ RF operator()(size_t i) const
     {
-        const Class c = classify(i, x, P, nullptr, allow_inf);
+        const Class c = classify(i, x, P, err, allow_inf);
         return {c.regular ? c.r : 0ull, c.regular ? 0u : 1u, 0u};
     }
 };
@@ -115,18 +149,19 @@ struct StoreRF {
     __device__ void operator()(size_t i, RF v) const { p[i] = v; }
 };
 
-// breakpoint records, in order
-__global__ void __launch_bounds__(256) k_breakpoints(size_t n,
-    const double *x, const double *P, const RF *C, uint32_t *bidx,
-    uint64_t *bcr, uint32_t *err, bool allow_inf)
+// breakpoint records, in order: element i is a breakpoint when the scan's
+// breakpoint count steps at i
+__global__ void __launch_bounds__(256) k_breakpoints(
+    size_t n, const RF *C, uint32_t *bidx, uint64_t *bcr)
 {
     for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
          i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const Class c = classify(i, x, P, err, allow_inf);
-        if (!c.regular) {
-            const uint32_t k = C[i].f - 1;
+        const RF ci = C[i];
+        const uint32_t fprev = i ? C[i - 1].f : 0u;
+        if (ci.f != fprev) {
+            const uint32_t k = ci.f - 1;
             bidx[k] = static_cast<uint32_t>(i);
-            bcr[k] = C[i].r; // r_i = 0, so also the count through i - 1
+            bcr[k] = ci.r; // r_i = 0, so also the count through i - 1
         }
     }
 }
@@ -196,23 +231,26 @@ __global__ void __launch_bounds__(256) k_fixup(size_t n, const double *x,
     }
 }
 
-__global__ void __launch_bounds__(256) k_prefix_out(size_t n, const double *x,
-    const double *P, const RF *C, const uint64_t *bcr, const double *sb,
-    double *out, uint32_t *err, bool allow_inf)
+// s_i from its breakpoint: the breakpoint's own sum, or that sum's bit
+// pattern plus the integer increments since (one binade, one ulp grid)
+__global__ void __launch_bounds__(256) k_prefix_out(size_t n, const RF *C,
+    const uint64_t *bcr, const double *sb, double *out, uint32_t *err)
 {
     for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
          i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const Class c = classify(i, x, P, nullptr, allow_inf);
-        const uint32_t k = C[i].f - 1;
+        const RF ci = C[i];
+        const uint32_t fprev = i ? C[i - 1].f : 0u;
+        const uint32_t k = ci.f - 1;
         double s;
-        if (!c.regular) {
+        if (ci.f != fprev) {
             s = sb[k];
         } else {
-            s = sb[k] + static_cast<double>(C[i].r - bcr[k]) *
-                    pow2(c.e - 52);
-            const double lo = pow2(c.e);
-            if (!(s >= lo && s < 2.0 * lo))
+            const uint64_t b = dbits(sb[k]);
+            const uint64_t v = b + (ci.r - bcr[k]);
+            // the sum must stay in the breakpoint's binade (sign included)
+            if ((v >> 52) != (b >> 52))
                 atomicOr(err, DEV_ERR_BOUND);
+            s = __longlong_as_double(static_cast<long long>(v));
         }
         out[i] = s;
     }
@@ -243,17 +281,16 @@ int seqsum_device(size_t n, const double *x, double *prefix, double *total,
     int rc = device_scan(n, LoadX{x}, StoreD{P}, OpAdd(), 0.0, pd, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    rc = device_scan(
-        n, LoadRF{x, P, allow_inf}, StoreRF{C}, OpRF(), RF{0, 0, 0}, pr, st);
+    rc = device_scan(n, LoadRF{x, P, err, allow_inf}, StoreRF{C}, OpRF(),
+        RF{0, 0, 0}, pr, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
     const int grid = grid_for(n, 256, 4, 8);
-    k_breakpoints<<<grid, 256, 0, st>>>(n, x, P, C, bidx, bcr, err, allow_inf);
+    k_breakpoints<<<grid, 256, 0, st>>>(n, C, bidx, bcr);
     k_fixup<<<1, 256, 0, st>>>(
         n, x, P, C, bidx, bcr, sb, total, err, allow_inf);
     if (prefix)
-        k_prefix_out<<<grid, 256, 0, st>>>(
-            n, x, P, C, bcr, sb, prefix, err, allow_inf);
+        k_prefix_out<<<grid, 256, 0, st>>>(n, C, bcr, sb, prefix, err);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
 }
