@@ -429,7 +429,15 @@ def run_micro(args):
         ("normal_f32", vc.PHILOX4X32, "vsmc_cuda_rng_normal_f32",
          (ctypes.c_float(0.0), ctypes.c_float(1.0)), 4),
     ]
+    wanted = set(args.items.split(",")) if args.items else None
+
+    def keep(name):
+        # the headline item always runs
+        return wanted is None or name in wanted or name == "philox4x32_u32"
+
     for name, kind, fn, extra, vb in rng_items:
+        if not keep(name):
+            continue
         r = vc.rng(kind, seed=1)
         sec = timed(lambda: vc.call(fn, ctypes.byref(r), nw, buf.data_ptr(),
                                     *extra, sptr))
@@ -446,6 +454,8 @@ def run_micro(args):
     names = ["multinomial", "stratified", "systematic", "residual",
              "residual_stratified", "residual_systematic"]
     for scheme, name in enumerate(names):
+        if not keep("resample_" + name):
+            continue
         r = vc.rng(vc.PHILOX4X32, seed=1)
         sec = timed(lambda: vc.call("vsmc_cuda_resample", n, n,
                                     ctypes.byref(r), w_dev.data_ptr(),
@@ -682,6 +692,9 @@ def main():
     ap.add_argument("--filters", type=int, default=4096)
     ap.add_argument("--rng-log2", type=int, default=30)
     ap.add_argument("--rs-log2", type=int, default=24)
+    ap.add_argument("--items", default="",
+                    help="micro workload: comma-separated item names to run "
+                         "(default all; philox4x32_u32 always runs)")
     ap.add_argument("--tune-steps", type=int, default=60)
     args = ap.parse_args()
     if args.impl == "reference":
