@@ -369,9 +369,10 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
     __shared__ bool is_last;
     uint32_t lo, hi;
     tile_run(ntiles, lo, hi);
-    uint32_t seg = lo;
-    float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
-    for (uint32_t tile = lo; tile < hi; ++tile) {
+    // the run is cut into segments of one filter each; a segment reads its
+    // filter's description and state once, then streams its tiles
+    uint32_t tile = lo;
+    while (tile < hi) {
         const uint32_t f = a.tile_filter[tile];
         const BFilter F = a.flt[f];
         PfScalars &S = a.st[f];
@@ -388,102 +389,107 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
                 ox = a.obs[F.obs_off + t];
             }
         }
-        const uint32_t i0 = (tile - F.tile0) * kTile + threadIdx.x * kPPT;
-        const bool full = i0 + kPPT <= F.n;
-        float X[kPPT], Y[kPPT], VX[kPPT], VY[kPPT], LW[kPPT];
+        const uint32_t seg = tile;
+        uint32_t end = min(hi, F.tile0 + F.ntiles);
+        if (end <= tile) { // a tile table that disagrees with the filters
+            if (threadIdx.x == 0)
+                atomicOr(&S.err, DEV_ERR_INTERNAL);
+            end = tile + 1;
+        }
+        float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
+        for (; tile < end; ++tile) {
+            const uint32_t i0 = (tile - F.tile0) * kTile + threadIdx.x * kPPT;
+            const bool full = i0 + kPPT <= F.n;
+            float X[kPPT], Y[kPPT], VX[kPPT], VY[kPPT], LW[kPPT];
 #pragma unroll
-        for (int k = 0; k < kPPT; ++k)
-            X[k] = Y[k] = VX[k] = VY[k] = LW[k] = 0.0f;
-        if (!First) {
-            const uint32_t g0 = F.off + i0;
-            // after a resample, a group whose slots all keep their own
-            // particle reads like an unresampled one
-            bool own = !gather;
-            if (gather && full && kPPT == 4) {
-                const int4 I = __ldcs(reinterpret_cast<const int4 *>(a.idx + g0));
-                const int b = static_cast<int>(i0);
-                own = I.x == b && I.y == b + 1 && I.z == b + 2 && I.w == b + 3;
-            }
-            if (own && full) {
-                load_run<kPPT>(a.ax + g0, X);
-                load_run<kPPT>(a.ay + g0, Y);
-                load_run<kPPT>(a.avx + g0, VX);
-                load_run<kPPT>(a.avy + g0, VY);
-            } else {
+            for (int k = 0; k < kPPT; ++k)
+                X[k] = Y[k] = VX[k] = VY[k] = LW[k] = 0.0f;
+            if (!First) {
+                const uint32_t g0 = F.off + i0;
+                // after a resample, a group whose slots all keep their own
+                // particle reads like an unresampled one
+                bool own = !gather;
+                if (gather && full && kPPT == 4) {
+                    const int4 I = __ldcs(reinterpret_cast<const int4 *>(a.idx + g0));
+                    const int b = static_cast<int>(i0);
+                    own = I.x == b && I.y == b + 1 && I.z == b + 2 && I.w == b + 3;
+                }
+                if (own && full) {
+                    load_run<kPPT>(a.ax + g0, X);
+                    load_run<kPPT>(a.ay + g0, Y);
+                    load_run<kPPT>(a.avx + g0, VX);
+                    load_run<kPPT>(a.avy + g0, VY);
+                } else {
 #pragma unroll
-                for (int k = 0; k < kPPT; ++k) {
-                    const uint32_t i = i0 + k;
-                    if (i < F.n) {
-                        const uint32_t src =
-                            gather ? batch_source(a, F, S, i) : i;
-                        X[k] = a.ax[F.off + src];
-                        Y[k] = a.ay[F.off + src];
-                        VX[k] = a.avx[F.off + src];
-                        VY[k] = a.avy[F.off + src];
+                    for (int k = 0; k < kPPT; ++k) {
+                        const uint32_t i = i0 + k;
+                        if (i < F.n) {
+                            const uint32_t src =
+                                gather ? batch_source(a, F, S, i) : i;
+                            X[k] = a.ax[F.off + src];
+                            Y[k] = a.ay[F.off + src];
+                            VX[k] = a.avx[F.off + src];
+                            VY[k] = a.avy[F.off + src];
+                        }
+                    }
+                }
+                if (!resampled) {
+                    if (full) {
+                        load_run<kPPT>(a.lw + g0, LW);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < kPPT; ++k)
+                            if (i0 + k < F.n)
+                                LW[k] = a.lw[g0 + k];
                     }
                 }
             }
-            if (!resampled) {
-                if (full) {
-                    load_run<kPPT>(a.lw + g0, LW);
-                } else {
+            if (mon) {
 #pragma unroll
-                    for (int k = 0; k < kPPT; ++k)
-                        if (i0 + k < F.n)
-                            LW[k] = a.lw[g0 + k];
-                }
-            }
-        }
-        if (mon) {
-#pragma unroll
-            for (int k = 0; k < kPPT; ++k)
-                if (i0 + k < F.n) {
-                    const float wo = resampled ? 1.0f : __expf(LW[k] - Mprev);
-                    sx += wo * X[k];
-                    sy += wo * Y[k];
-                    sw += wo;
-                }
-        } else {
-#pragma unroll
-            for (int k = 0; k < kPPT; ++k)
-                if (i0 + k < F.n) {
-                    if (Kind == kKindCv)
-                        batch_one<First>(F.c, F.seed, i0 + k, t, ox, oy,
-                            resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k],
-                            m, s, s2, sx, sy, sw);
-                    else
-                        bearings_one<First>(F.bc, F.seed, i0 + k, t, ox,
-                            resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k],
-                            m, s, s2, sx, sy, sw);
-                }
-            const uint32_t g0 = F.off + i0;
-            if (full) {
-                store_run<kPPT>(a.bx + g0, X);
-                store_run<kPPT>(a.by + g0, Y);
-                store_run<kPPT>(a.bvx + g0, VX);
-                store_run<kPPT>(a.bvy + g0, VY);
-                store_run<kPPT>(a.lw + g0, LW);
+                for (int k = 0; k < kPPT; ++k)
+                    if (i0 + k < F.n) {
+                        const float wo = resampled ? 1.0f : __expf(LW[k] - Mprev);
+                        sx += wo * X[k];
+                        sy += wo * Y[k];
+                        sw += wo;
+                    }
             } else {
 #pragma unroll
                 for (int k = 0; k < kPPT; ++k)
                     if (i0 + k < F.n) {
-                        a.bx[g0 + k] = X[k];
-                        a.by[g0 + k] = Y[k];
-                        a.bvx[g0 + k] = VX[k];
-                        a.bvy[g0 + k] = VY[k];
-                        a.lw[g0 + k] = LW[k];
+                        if (Kind == kKindCv)
+                            batch_one<First>(F.c, F.seed, i0 + k, t, ox, oy,
+                                resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k],
+                                m, s, s2, sx, sy, sw);
+                        else
+                            bearings_one<First>(F.bc, F.seed, i0 + k, t, ox,
+                                resampled, Mprev, X[k], Y[k], VX[k], VY[k], LW[k],
+                                m, s, s2, sx, sy, sw);
                     }
+                const uint32_t g0 = F.off + i0;
+                if (full) {
+                    store_run<kPPT>(a.bx + g0, X);
+                    store_run<kPPT>(a.by + g0, Y);
+                    store_run<kPPT>(a.bvx + g0, VX);
+                    store_run<kPPT>(a.bvy + g0, VY);
+                    store_run<kPPT>(a.lw + g0, LW);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kPPT; ++k)
+                        if (i0 + k < F.n) {
+                            a.bx[g0 + k] = X[k];
+                            a.by[g0 + k] = Y[k];
+                            a.bvx[g0 + k] = VX[k];
+                            a.bvy[g0 + k] = VY[k];
+                            a.lw[g0 + k] = LW[k];
+                        }
+                }
             }
         }
         // the filter's segment ends here: record it
-        if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
-            tile_finish<kBlock, First>(a, seg, tile + 1 - seg, f, F, S, t,
-                mon, m, s, s2, sx, sy, sw, shm, shw, is_last);
-            __syncthreads();
-            m = -INFINITY;
-            s = s2 = sx = sy = sw = 0;
-            seg = tile + 1;
-        }
+        tile_finish<kBlock, First>(a, seg, end - seg, f, F, S, t, mon, m, s,
+            s2, sx, sy, sw, shm, shw, is_last);
+        __syncthreads();
     }
 }
 
