@@ -93,6 +93,7 @@ struct BatchArgs {
     // chunk}, rs_count[rpar] entries; per-entry totals of the passes
     uint2 *rs_list;
     uint32_t *rs_count;
+    uint32_t *work; // step kernel's tile counters, by step parity
     uint64_t *rs_q;
     uint32_t *rs_e, *rs_c, *rs_m;
     uint32_t rs_cap, rpar;
@@ -362,13 +363,31 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
 {
     constexpr uint32_t kTile = kBlock * kPPT;
     constexpr int kW = kBlock / 32;
+    // tiles a block takes at a time: 1024 particles (one tile at the default
+    // 4 x 256 shape, whose per-tile FP32 records then group the particles
+    // as the single filter's blocks do)
+    constexpr uint32_t kGrab = kTile >= 1024 ? 1u : 1024u / kTile;
     const uint32_t t = *a.step;
     const uint32_t ntiles = t <= a.tmax ? a.active[t] : 0u;
     __shared__ float shm[kW];
     __shared__ float shw[5][kW];
     __shared__ bool is_last;
-    uint32_t lo, hi;
-    tile_run(ntiles, lo, hi);
+    __shared__ uint32_t grab;
+    // the next step's counter was last used by the previous step's launch
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        a.work[(t + 1) & 1u] = 0;
+    // Blocks take runs of kGrab tiles from a counter until none is left, so
+    // a block whose tiles are slower (gathered reads after a resample, many
+    // small filters) takes fewer of them.
+    for (;;) {
+    if (threadIdx.x == 0)
+        grab = atomicAdd(a.work + (t & 1u), kGrab);
+    __syncthreads();
+    const uint32_t lo = grab;
+    __syncthreads();
+    if (lo >= ntiles)
+        break;
+    const uint32_t hi = min(ntiles, lo + kGrab);
     // the run is cut into segments of one filter each; a segment reads its
     // filter's description and state once, then streams its tiles
     uint32_t tile = lo;
@@ -490,6 +509,7 @@ __global__ void __launch_bounds__(kBlock, 1280 / kBlock) k_batch_step(
         tile_finish<kBlock, First>(a, seg, end - seg, f, F, S, t, mon, m, s,
             s2, sx, sy, sw, shm, shw, is_last);
         __syncthreads();
+    }
     }
 }
 
@@ -1084,7 +1104,8 @@ __global__ void k_batch_reset(PfScalars *st, const BFilter *flt, uint32_t nf,
     const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f == 0) {
         *step = 0;
-        rs_count[0] = rs_count[1] = 0;
+        // list counts, then the step kernel's tile counters
+        rs_count[0] = rs_count[1] = rs_count[2] = rs_count[3] = 0;
     }
     if (f >= nf)
         return;
@@ -1362,6 +1383,7 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.step = b->d_step;
     a.rs_list = b->d_rs_list;
     a.rs_count = b->d_rs_count;
+    a.work = b->d_rs_count + 2;
     a.rs_q = b->d_rs_q;
     a.rs_e = b->d_rs_e;
     a.rs_c = b->d_rs_c;
@@ -1554,7 +1576,7 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     B_TRY(balloc(&b->d_tile_filter, tiles));
     B_TRY(balloc(&b->d_active, tmax + 1));
     B_TRY(balloc(&b->d_rs_list, 2 * static_cast<size_t>(b->rs_cap)));
-    B_TRY(balloc(&b->d_rs_count, 2));
+    B_TRY(balloc(&b->d_rs_count, 4));
     B_TRY(balloc(&b->d_rs_q, b->rs_cap));
     B_TRY(balloc(&b->d_rs_e, b->rs_cap));
     B_TRY(balloc(&b->d_rs_c, b->rs_cap));
