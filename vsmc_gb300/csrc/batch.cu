@@ -344,15 +344,6 @@ __device__ __forceinline__ void bearings_one(const BearingsConst &c,
     lse_push(lw, m, s, s2);
 }
 
-// This block's contiguous run [lo, hi) of the step's active tiles.
-__device__ __forceinline__ void tile_run(
-    uint32_t ntiles, uint32_t &lo, uint32_t &hi)
-{
-    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
-    lo = min(ntiles, blockIdx.x * per);
-    hi = min(ntiles, lo + per);
-}
-
 // One global step of every running filter (bootstrap kinds).  A filter at
 // t < T moves and weights its particles; at t == T it only records the
 // weighted mean of its final particles.  Each block takes a contiguous run
@@ -535,11 +526,24 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         load_packed(sp, a.packed);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int g = lane >> 2, q = lane & 3;
-    uint32_t lo, hi;
-    tile_run(ntiles, lo, hi);
-    uint32_t seg = lo;
-    float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
-    for (uint32_t tile = lo; tile < hi; ++tile) {
+    // tiles a block takes at a time (1024 particles), from a per-step
+    // counter; the next step's counter was last used by the previous step
+    constexpr uint32_t kGrab = 1024u / kLearnTile;
+    __shared__ uint32_t grab;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        a.work[(t + 1) & 1u] = 0;
+    for (;;) {
+    if (threadIdx.x == 0)
+        grab = atomicAdd(a.work + (t & 1u), kGrab);
+    __syncthreads();
+    const uint32_t lo = grab;
+    __syncthreads();
+    if (lo >= ntiles)
+        break;
+    const uint32_t hi = min(ntiles, lo + kGrab);
+    // one segment per filter: its description and state are read once
+    uint32_t tile = lo;
+    while (tile < hi) {
         const uint32_t f = a.tile_filter[tile];
         const BFilter F = a.flt[f];
         const BearingsConst &c = F.bc;
@@ -549,97 +553,103 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
         const bool gather = First ? false : (S.gather != 0);
         const float Mprev = First ? 0.0f : S.Mf;
         const float z = mon ? 0.0f : a.obs[F.obs_off + t];
-        const uint32_t i =
-            (tile - F.tile0) * kLearnTile + 32 * wid + g + 8 * q;
-        const bool mine = i < F.n;
-        float x = 0, y = 0, vx = 0, vy = 0, lw = 0;
-        if (!First && mine) {
-            const uint32_t src = gather ? batch_source(a, F, S, i) : i;
-            x = a.ax[F.off + src];
-            y = a.ay[F.off + src];
-            vx = a.avx[F.off + src];
-            vy = a.avy[F.off + src];
-            lw = resampled ? 0.0f : a.lw[F.off + i];
+        const uint32_t seg = tile;
+        uint32_t end = min(hi, F.tile0 + F.ntiles);
+        if (end <= tile) { // a tile table that disagrees with the filters
+            if (threadIdx.x == 0)
+                atomicOr(&S.err, DEV_ERR_INTERNAL);
+            end = tile + 1;
         }
-        if (mon) {
-            if (mine) {
-                const float wo = resampled ? 1.0f : __expf(lw - Mprev);
-                sx += wo * x;
-                sy += wo * y;
-                sw += wo;
+        float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
+        for (; tile < end; ++tile) {
+            const uint32_t i =
+                (tile - F.tile0) * kLearnTile + 32 * wid + g + 8 * q;
+            const bool mine = i < F.n;
+            float x = 0, y = 0, vx = 0, vy = 0, lw = 0;
+            if (!First && mine) {
+                const uint32_t src = gather ? batch_source(a, F, S, i) : i;
+                x = a.ax[F.off + src];
+                y = a.ay[F.off + src];
+                vx = a.avx[F.off + src];
+                vy = a.avy[F.off + src];
+                lw = resampled ? 0.0f : a.lw[F.off + i];
             }
-        } else if (First) {
-            if (mine) {
-                float e[4];
-                bearings_normals(t, F.seed, i, e);
-                bearings_prior(c, e, x, y, vx, vy);
-                lw = bearings_loglik(c, z, x, y);
-                lse_push(lw, m, s, s2);
-            }
-        } else {
-            const float2 scz = a.obs_sc[F.obs_off + t];
-            const float sz = scz.x, cz = scz.y;
-            float fe[6];
-            bearings_features(c, x, y, vx, vy, sz, cz, fe);
-            uint32_t a0[4], b0[4];
-            features_to_a2(fe, a0, b0);
-            // one 16-row tile at a time keeps one tile's activations live
-            float oa[4], ob[4];
+            if (mon) {
+                if (mine) {
+                    const float wo = resampled ? 1.0f : __expf(lw - Mprev);
+                    sx += wo * x;
+                    sy += wo * y;
+                    sw += wo;
+                }
+            } else if (First) {
+                if (mine) {
+                    float e[4];
+                    bearings_normals(t, F.seed, i, e);
+                    bearings_prior(c, e, x, y, vx, vy);
+                    lw = bearings_loglik(c, z, x, y);
+                    lse_push(lw, m, s, s2);
+                }
+            } else {
+                const float2 scz = a.obs_sc[F.obs_off + t];
+                const float sz = scz.x, cz = scz.y;
+                float fe[6];
+                bearings_features(c, x, y, vx, vy, sz, cz, fe);
+                uint32_t a0[4], b0[4];
+                features_to_a2(fe, a0, b0);
+                // one 16-row tile at a time keeps one tile's activations live
+                float oa[4], ob[4];
 #pragma unroll 1
-            for (int h = 0; h < 2; ++h) {
-                uint32_t in[4];
+                for (int h = 0; h < 2; ++h) {
+                    uint32_t in[4];
 #pragma unroll
-                for (int r = 0; r < 4; ++r)
-                    in[r] = h ? b0[r] : a0[r];
-                float o[4];
-                mlp_forward_warp<false, true>(sp, in, o);
+                    for (int r = 0; r < 4; ++r)
+                        in[r] = h ? b0[r] : a0[r];
+                    float o[4];
+                    mlp_forward_warp<false, true>(sp, in, o);
 #pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    if (h)
-                        ob[r] = o[r];
-                    else
-                        oa[r] = o[r];
+                    for (int r = 0; r < 4; ++r) {
+                        if (h)
+                            ob[r] = o[r];
+                        else
+                            oa[r] = o[r];
+                    }
+                }
+                float v[8];
+                out_to_owner2(oa, ob, v);
+                if (mine) {
+                    const float lw_old = resampled ? 0.0f : lw - Mprev;
+                    const float wo = resampled ? 1.0f : __expf(lw_old);
+                    sx += wo * x;
+                    sy += wo * y;
+                    sw += wo;
+                    float e[4], fr[4], nu[4];
+                    bearings_normals(t, F.seed, i, e);
+                    float lq = 0;
+#pragma unroll
+                    for (int d = 0; d < 4; ++d) {
+                        const float l = fminf(fmaxf(v[4 + d], c.lmin), c.lmax);
+                        fr[d] = v[d] + __expf(0.5f * l) * e[d];
+                        lq += 0.5f * (e[d] * e[d] - fr[d] * fr[d]) + 0.5f * l;
+                    }
+                    frame_to_axes(sz, cz, fr, nu); // the draw, bearing frame
+                    bearings_step(c, nu, x, y, vx, vy);
+                    lw = lw_old + bearings_loglik(c, z, x, y) + lq;
+                    lse_push(lw, m, s, s2);
                 }
             }
-            float v[8];
-            out_to_owner2(oa, ob, v);
-            if (mine) {
-                const float lw_old = resampled ? 0.0f : lw - Mprev;
-                const float wo = resampled ? 1.0f : __expf(lw_old);
-                sx += wo * x;
-                sy += wo * y;
-                sw += wo;
-                float e[4], fr[4], nu[4];
-                bearings_normals(t, F.seed, i, e);
-                float lq = 0;
-#pragma unroll
-                for (int d = 0; d < 4; ++d) {
-                    const float l = fminf(fmaxf(v[4 + d], c.lmin), c.lmax);
-                    fr[d] = v[d] + __expf(0.5f * l) * e[d];
-                    lq += 0.5f * (e[d] * e[d] - fr[d] * fr[d]) + 0.5f * l;
-                }
-                frame_to_axes(sz, cz, fr, nu); // the draw, bearing frame
-                bearings_step(c, nu, x, y, vx, vy);
-                lw = lw_old + bearings_loglik(c, z, x, y) + lq;
-                lse_push(lw, m, s, s2);
+            if (!mon && mine) {
+                const uint32_t gi = F.off + i;
+                a.bx[gi] = x;
+                a.by[gi] = y;
+                a.bvx[gi] = vx;
+                a.bvy[gi] = vy;
+                a.lw[gi] = lw;
             }
         }
-        if (!mon && mine) {
-            const uint32_t gi = F.off + i;
-            a.bx[gi] = x;
-            a.by[gi] = y;
-            a.bvx[gi] = vx;
-            a.bvy[gi] = vy;
-            a.lw[gi] = lw;
-        }
-        if (tile + 1 == hi || a.tile_filter[tile + 1] != f) {
-            tile_finish<kLearnBlock, First>(a, seg, tile + 1 - seg, f, F, S,
-                t, mon, m, s, s2, sx, sy, sw, shm, shw, is_last);
-            __syncthreads();
-            m = -INFINITY;
-            s = s2 = sx = sy = sw = 0;
-            seg = tile + 1;
-        }
+        tile_finish<kLearnBlock, First>(a, seg, end - seg, f, F, S, t, mon, m,
+            s, s2, sx, sy, sw, shm, shw, is_last);
+        __syncthreads();
+    }
     }
 }
 
