@@ -120,7 +120,7 @@ __device__ __forceinline__ void load_group(const Pf32Args &a, uint32_t i0,
 }
 
 template <bool First>
-__global__ void __launch_bounds__(kPfBlock, 5) k_pf32_step(const Pf32Args a)
+__global__ void __launch_bounds__(kPfBlock, 4) k_pf32_step(const Pf32Args a)
 {
     const uint32_t t = a.sc->step;
     const int resampled = First ? 1 : a.sc->resampled;
