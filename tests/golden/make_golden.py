@@ -195,19 +195,25 @@ def pf_runs(R):
             out[f"{tag}_ess"] = ess
             out[f"{tag}_res"] = res
             out[f"{tag}_logz"] = logz
-    # the reference's own per-particle engines: config 1 over 64 seeds
+    # the reference's own per-particle engines: config 1 over 64 runs.
+    # Seed::get() steps the global seed by one per engine (rng/seed.hpp:
+    # 118-176), so the N particle engines of a run started at seed s take
+    # s + 1 .. s + N: runs started one apart would share N - 1 of their
+    # particles.  The runs start N + 64 apart, so no engine is shared.
     N = 1 << 14
+    seeds = np.arange(64, dtype=np.uint32) * np.uint32(N + 64)
     logz_end = np.zeros(64)
     mean_all = np.zeros((64, T, 2))
-    for seed in range(64):
+    for k, seed in enumerate(seeds):
         mean = np.zeros(2 * T)
         ess = np.zeros(T)
         res = np.zeros(T, np.int32)
         logz = np.zeros(T)
-        R.ref_pf_run(64, N, T, seed, 1, 0.5, 1, *m, P(obs), P(mean), P(ess),
-                     P(res), P(logz))
-        logz_end[seed] = logz[-1]
-        mean_all[seed] = mean.reshape(T, 2)
+        R.ref_pf_run(64, N, T, int(seed), 1, 0.5, 1, *m, P(obs), P(mean),
+                     P(ess), P(res), P(logz))
+        logz_end[k] = logz[-1]
+        mean_all[k] = mean.reshape(T, 2)
+    out["native64_seeds"] = seeds
     out["native64_logz"] = logz_end
     out["native64_mean_avg"] = mean_all.mean(axis=0)
     out["native64_mean_sd"] = mean_all.std(axis=0, ddof=1)
@@ -252,7 +258,7 @@ def genealogy(R, rng):
     return out
 
 
-def main():
+def main(only=None):
     if binding.build_ref() is None:
         sys.exit("reference tree not found: cannot generate the fixtures")
     R = binding.ref()
@@ -265,6 +271,11 @@ def main():
                      ("weight", lambda: weights(R, rng)),
                      ("pf", lambda: pf_runs(R)),
                      ("genealogy", lambda: genealogy(R, rng))):
+        if only and name not in only:
+            # keep the draws of the shared generator in their order
+            if name in ("u01", "resample", "weight", "genealogy"):
+                fn()
+            continue
         data = fn()
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **data)
@@ -272,4 +283,5 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    # optional arguments: the fixture names to write (default all)
+    main(set(sys.argv[1:]) or None)
