@@ -552,14 +552,21 @@ def run_learned(args):
     vc.call("vsmc_cuda_bearings_simulate", 0, T, ctypes.byref(m),
             truth.data_ptr(), obs.data_ptr(), None)
     obs_np = obs.cpu().numpy()
-    # ---- training on simulated trajectories
+    # ---- training on simulated trajectories plus rows from the particle
+    # clouds of bootstrap filters run on simulated tracks
     prop = vc.Proposal(seed=1)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    rows = None
+    if args.cloud_tracks > 0:
+        rows = vc.cloud_rows(m, 12, args.cloud_tracks, args.cloud_particles,
+                             T, args.cloud_candidates)
     losses = prop.train(m, seed=11, ntraj=args.train_traj, T=T,
                         batch=args.train_batch, steps=args.train_steps,
-                        lr=args.lr)
+                        lr=args.lr, rows=rows)
     train_s = time.perf_counter() - t0
+    cloud_rows_n = 0 if rows is None else int(rows[1].shape[0])
+    del rows
     # ---- reference posterior mean (FP64 oracle bootstrap, host cores)
     ref_mean = None
     if not args.no_cpu_baseline:
@@ -649,6 +656,10 @@ def run_learned(args):
             "workload": f"{R} filters x N={args.learned_particles} learned "
                         f"proposal vs bootstrap N in {args.boot_particles}",
             "train": {"trajectories": args.train_traj, "steps": T,
+                      "cloud_tracks": args.cloud_tracks,
+                      "cloud_particles": args.cloud_particles,
+                      "cloud_candidates": args.cloud_candidates,
+                      "cloud_rows": cloud_rows_n,
                       "batch": args.train_batch, "lr": args.lr,
                       "adam_steps": len(losses), "seconds": train_s,
                       "loss_first": float(losses[:50].mean()),
@@ -684,6 +695,11 @@ def main():
     ap.add_argument("--train-traj", type=int, default=1 << 20)
     ap.add_argument("--train-batch", type=int, default=1 << 16)
     ap.add_argument("--train-steps", type=int, default=10000)
+    ap.add_argument("--cloud-tracks", type=int, default=1024,
+                    help="learned workload: bootstrap-filter tracks whose "
+                         "particle clouds add training rows (0: none)")
+    ap.add_argument("--cloud-particles", type=int, default=256)
+    ap.add_argument("--cloud-candidates", type=int, default=256)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--ref-particles", type=int, default=1 << 18)
     ap.add_argument("--bearings-dt", type=float, default=1.0)

@@ -406,6 +406,27 @@ int vsmc_cuda_mlp_loss_grad(const uint32_t *packed, size_t B,
 int vsmc_cuda_mlp_train(const vsmc_cuda_bearings_model *model, uint32_t seed,
     size_t ntraj, size_t T, size_t batch, size_t steps, double lr,
     float *params, double *loss_host, void *stream);
+/* Training rows from the particle clouds of a bootstrap filter, one block
+ * per track: ntracks tracks simulated from the model, each filtered by P
+ * particles (a multiple of 32, at most 1024) for T steps (2 <= T <= 1024),
+ * resampled every step.  At step t >= 1 each particle x' of the cloud
+ * approximating p(x_{t-1} | z_{0:t-1}) gives a row: its inputs for z_t
+ * (feat, 6 floats) and a noise chosen among K draws of N(0, I) with
+ * probability proportional to g(z_t | F x' + L nu) (nu, 4 floats, bearing
+ * frame) -- a sampling-importance-resampling draw toward the locally
+ * optimal proposal the loss targets.  ntracks * P * (T - 1) rows (device).
+ * No reference counterpart. */
+int vsmc_cuda_mlp_cloud_rows(const vsmc_cuda_bearings_model *model,
+    uint32_t seed, size_t ntracks, size_t P, size_t T, size_t K, float *feat,
+    float *nu, void *stream);
+/* vsmc_cuda_mlp_train with nx extra rows (device xfeat[nx][6], xnu[nx][4],
+ * for instance from vsmc_cuda_mlp_cloud_rows): minibatch rows are drawn
+ * uniformly over the simulated samples and the extra rows together.
+ * Synchronizes.  No reference counterpart. */
+int vsmc_cuda_mlp_train_rows(const vsmc_cuda_bearings_model *model,
+    uint32_t seed, size_t ntraj, size_t T, const float *xfeat,
+    const float *xnu, size_t nx, size_t batch, size_t steps, double lr,
+    float *params, double *loss_host, void *stream);
 /* One FP32 move + weight increment on caller-owned SoA state [4][n]: t == 0
  * draws the prior; t > 0 draws nu ~ N(0, I) (packed == NULL, bootstrap) or
  * nu' ~ N(m, diag(exp(l))) from the network in the bearing frame of z,

@@ -266,3 +266,65 @@ def test_training_lowers_loss_and_log_evidence_spread(vc, port):
         b.close()
         sds[name] = float(np.std([o["logz"][-1] for o in out]))
     assert sds["learned"] < 0.8 * sds["bootstrap"], sds
+
+
+def _informative_model(vc, sigma_z=None):
+    m = vc.bearings_model()
+    m.dt, m.q, m.sd_vel0 = 1.0, 1.0, 0.5
+    if sigma_z is not None:
+        m.sigma_z = sigma_z
+    return m
+
+
+def test_cloud_rows_flat_likelihood_and_determinism(vc):
+    """With a bearing that says nothing (sigma_z = 50 rad) every candidate
+    weighs the same, so the chosen noise is N(0, I) in the bearing frame;
+    the rows are a function of the seed; every input is bounded."""
+    m = _informative_model(vc, sigma_z=50.0)
+    feat, nu = vc.cloud_rows(m, 3, 8, 64, 12, 8)
+    feat2, nu2 = vc.cloud_rows(m, 3, 8, 64, 12, 8)
+    assert feat.shape == (8 * 64 * 11, 6) and nu.shape == (8 * 64 * 11, 4)
+    assert bool((feat == feat2).all()) and bool((nu == nu2).all())
+    f, n = host(feat), host(nu)
+    assert np.isfinite(f).all() and np.isfinite(n).all()
+    assert np.abs(f[:, :4]).max() <= 1.0
+    np.testing.assert_allclose(f[:, 4] ** 2 + f[:, 5] ** 2, 1.0, atol=1e-5)
+    se = 1 / np.sqrt(len(n))
+    assert np.abs(n.mean(axis=0)).max() < 5 * se, n.mean(axis=0)
+    assert np.abs(n.var(axis=0) - 1).max() < 5 * np.sqrt(2) * se, n.var(0)
+
+
+def test_cloud_rows_pick_noise_toward_the_bearing(vc):
+    """With an informative bearing the chosen across-bearing position noise
+    pulls the predicted position back toward the observed bearing: it is
+    anti-correlated with the predicted lateral offset (input 1), and the
+    along-bearing noise is not."""
+    m = _informative_model(vc)
+    feat, nu = vc.cloud_rows(m, 5, 64, 256, 60, 64)
+    f, n = host(feat), host(nu)
+    eb = 8 * f[:, 1]
+    e = eb / np.sqrt(np.maximum(1 - eb * eb / 64, 1e-6))
+    sel = np.abs(e) < 6
+    assert np.corrcoef(n[sel, 2], e[sel])[0, 1] < -0.3
+    assert abs(np.corrcoef(n[sel, 0], e[sel])[0, 1]) < 0.05
+
+
+def test_cloud_rows_teach_the_filter_inputs(vc):
+    """Trained on simulated trajectories alone, the network meets the
+    filter's own inputs (particles off the observed bearing) rarely; with
+    the particle-cloud rows added its loss on held-out cloud rows (other
+    tracks, other seed) is clearly lower."""
+    import torch
+    m = _informative_model(vc)
+    T = 40
+    rows = vc.cloud_rows(m, 12, 256, 128, T, 128)
+    hf, hn = vc.cloud_rows(m, 77, 32, 128, T, 128)
+    idx = torch.arange(0, hf.shape[0], 7, device="cuda")
+    hf, hn = hf[idx].contiguous(), hn[idx].contiguous()
+    out = {}
+    for name, extra in (("trajectories", None), ("with clouds", rows)):
+        prop = vc.Proposal(seed=1)
+        prop.train(m, seed=11, ntraj=1 << 15, T=T, batch=1 << 12, steps=800,
+                   lr=3e-3, rows=extra)
+        out[name] = prop.loss(hf.data_ptr(), hn.data_ptr(), hf.shape[0])
+    assert out["with clouds"] < out["trajectories"] - 0.1, out

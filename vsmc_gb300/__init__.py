@@ -177,6 +177,10 @@ PROTOTYPES = {
     "vsmc_cuda_mlp_loss_grad": (I32, [VP, SZ, VP, VP, VP, VP, VP]),
     "vsmc_cuda_mlp_train": (I32, [_BMODELP, U32, SZ, SZ, SZ, SZ, F64, VP,
                                   VP, VP]),
+    "vsmc_cuda_mlp_cloud_rows": (I32, [_BMODELP, U32, SZ, SZ, SZ, SZ, VP, VP,
+                                       VP]),
+    "vsmc_cuda_mlp_train_rows": (I32, [_BMODELP, U32, SZ, SZ, VP, VP, SZ, SZ,
+                                       SZ, F64, VP, VP, VP]),
     "vsmc_cuda_bearings_move_f32": (I32, [SZ, SZ, U32, _BMODELP, F64, VP, VP,
                                           VP, VP]),
     "vsmc_cuda_batch_stream": (I32, [VP, ctypes.POINTER(VP)]),
@@ -426,13 +430,22 @@ class Proposal:
              self.packed.data_ptr(), None)
         torch.cuda.synchronize()
 
-    def train(self, model, seed, ntraj, T, batch, steps, lr):
-        """Adam on simulated trajectories; returns the minibatch losses."""
+    def train(self, model, seed, ntraj, T, batch, steps, lr, rows=None):
+        """Adam on simulated trajectories, plus the extra training rows
+        `rows` = (feat, nu) device tensors if given (for instance
+        cloud_rows()); returns the minibatch losses."""
         import numpy as np
         losses = np.zeros(steps)
-        call("vsmc_cuda_mlp_train", ctypes.byref(model), seed, ntraj, T,
-             batch, steps, lr, self.params.data_ptr(), losses.ctypes.data,
-             None)
+        if rows is None:
+            call("vsmc_cuda_mlp_train", ctypes.byref(model), seed, ntraj, T,
+                 batch, steps, lr, self.params.data_ptr(),
+                 losses.ctypes.data, None)
+        else:
+            feat, nu = rows
+            call("vsmc_cuda_mlp_train_rows", ctypes.byref(model), seed,
+                 ntraj, T, feat.data_ptr(), nu.data_ptr(), nu.shape[0],
+                 batch, steps, lr, self.params.data_ptr(),
+                 losses.ctypes.data, None)
         self.pack()
         return losses
 
@@ -536,3 +549,17 @@ class ParticleFilter:
         call("vsmc_cuda_pf_state", self.handle, ctypes.byref(s),
              ctypes.byref(w))
         return s.value, w.value
+
+
+def cloud_rows(model, seed, ntracks, particles, T, candidates):
+    """Training rows from bootstrap-filter particle clouds
+    (vsmc_cuda_mlp_cloud_rows): device tensors feat [rows, 6], nu [rows, 4]
+    with rows = ntracks * particles * (T - 1)."""
+    import torch
+    rows = ntracks * particles * (T - 1)
+    feat = torch.empty((rows, 6), dtype=torch.float32, device="cuda")
+    nu = torch.empty((rows, 4), dtype=torch.float32, device="cuda")
+    call("vsmc_cuda_mlp_cloud_rows", ctypes.byref(model), seed, ntracks,
+         particles, T, candidates, feat.data_ptr(), nu.data_ptr(), None)
+    torch.cuda.synchronize()
+    return feat, nu

@@ -533,22 +533,172 @@ __global__ void k_traj_step(uint32_t M, uint32_t t, uint32_t seed,
     }
 }
 
+// Training rows from the particle clouds of a bootstrap filter.  Block k
+// simulates track k of the model (FP32; Philox4x32 key {t, seed}, counter
+// {4, k, 0, 0} for the transition noise and {5, k, 0, 0} for the bearing
+// noise) and runs a bootstrap filter of P = blockDim.x particles on its
+// bearings, resampling every step (stratified, one uniform per particle).
+// At step t >= 1 the cloud before the move is the filter's particle
+// approximation of p(x_{t-1} | z_{0:t-1}); each of its particles x' gives
+// one row: its network inputs for z_t, and a noise nu* chosen among K draws
+// nu_k ~ N(0, I) with probability proportional to g(z_t | F x' + L nu_k)
+// (sampling-importance-resampling toward the locally optimal proposal
+// p(nu | x', z_t), the minimiser of the training loss), in the bearing frame.
+// The K weights are combined in one pass: candidate k replaces the choice
+// with probability w_k / (w_0 + ... + w_k).  Row ((k (T - 1)) + t - 1) P + j.
+// Particle j's streams: key {t, seed}, counters {6, k P + j, kk, 0} (the
+// candidates), {7, ...} (the replacement uniforms), {8, k P + j, 0, 0} (the
+// move), {9, ...} (the resampling uniform), {10, ...} (the prior at t = 0).
+constexpr int kCloudMaxP = 1024;
+constexpr int kCloudMaxT = 1024;
+
+__global__ void __launch_bounds__(kCloudMaxP) k_cloud_rows(BearingsConst c,
+    float sigma_z, uint32_t seed, uint32_t T, uint32_t K, float *feat,
+    float *nu_out)
+{
+    __shared__ float zs[kCloudMaxT];
+    __shared__ float cx[kCloudMaxP], cy[kCloudMaxP], cvx[kCloudMaxP],
+        cvy[kCloudMaxP];
+    __shared__ float mx[kCloudMaxP], my[kCloudMaxP], mvx[kCloudMaxP],
+        mvy[kCloudMaxP];
+    __shared__ float cdf[kCloudMaxP];
+    __shared__ float red[kCloudMaxP / 32 + 1];
+    const uint32_t k = blockIdx.x, j = threadIdx.x, P = blockDim.x;
+    const uint32_t pid = k * P + j;
+    if (j == 0) { // the track and its bearings, one thread
+        float e[4];
+        const u32x4 w0 = philox4x32_10(4u, k, 0u, 0u, 0u, seed);
+        normal_pair_f(w0.x, w0.y, e[0], e[1]);
+        normal_pair_f(w0.z, w0.w, e[2], e[3]);
+        float x, y, vx, vy;
+        bearings_prior(c, e, x, y, vx, vy);
+        for (uint32_t t = 0; t < T; ++t) {
+            if (t > 0) {
+                const u32x4 w = philox4x32_10(4u, k, 0u, 0u, t, seed);
+                normal_pair_f(w.x, w.y, e[0], e[1]);
+                normal_pair_f(w.z, w.w, e[2], e[3]);
+                bearings_step(c, e, x, y, vx, vy);
+            }
+            const u32x4 w2 = philox4x32_10(5u, k, 0u, 0u, t, seed);
+            float zn1, zn2;
+            normal_pair_f(w2.x, w2.y, zn1, zn2);
+            zs[t] = atan2f(y, x) + sigma_z * zn1;
+        }
+    }
+    __syncthreads();
+    // prior cloud, weighted by z_0 below
+    float x, y, vx, vy;
+    {
+        float e[4];
+        const u32x4 w = philox4x32_10(10u, pid, 0u, 0u, 0u, seed);
+        normal_pair_f(w.x, w.y, e[0], e[1]);
+        normal_pair_f(w.z, w.w, e[2], e[3]);
+        bearings_prior(c, e, x, y, vx, vy);
+    }
+    for (uint32_t t = 0; t < T; ++t) {
+        const float z = zs[t];
+        if (t > 0) {
+            const float sz = sinf(z), cz = cosf(z);
+            const size_t row =
+                (static_cast<size_t>(k) * (T - 1) + (t - 1)) * P + j;
+            float f[6];
+            bearings_features(c, x, y, vx, vy, sz, cz, f);
+#pragma unroll
+            for (int d = 0; d < 6; ++d)
+                feat[6 * row + d] = f[d];
+            // one pass over the K candidates
+            float m = -INFINITY, sum = 0.0f;
+            float pick[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (uint32_t kk = 0; kk < K; ++kk) {
+                const u32x4 w = philox4x32_10(6u, pid, kk, 0u, t, seed);
+                float e[4];
+                normal_pair_f(w.x, w.y, e[0], e[1]);
+                normal_pair_f(w.z, w.w, e[2], e[3]);
+                float px = x, py = y, pvx = vx, pvy = vy;
+                bearings_step(c, e, px, py, pvx, pvy);
+                const float l = bearings_loglik(c, z, px, py);
+                if (l > m) {
+                    sum = sum * __expf(m - l) + 1.0f;
+                    m = l;
+                } else {
+                    sum += __expf(l - m);
+                }
+                const u32x4 a = philox4x32_10(7u, pid, kk, 0u, t, seed);
+                if (u01_co_f(a.x) * sum < __expf(l - m)) {
+#pragma unroll
+                    for (int d = 0; d < 4; ++d)
+                        pick[d] = e[d];
+                }
+            }
+            float fr[4];
+            axes_to_frame(sz, cz, pick, fr);
+#pragma unroll
+            for (int d = 0; d < 4; ++d)
+                nu_out[4 * row + d] = fr[d];
+            // the bootstrap move
+            float e[4];
+            const u32x4 w = philox4x32_10(8u, pid, 0u, 0u, t, seed);
+            normal_pair_f(w.x, w.y, e[0], e[1]);
+            normal_pair_f(w.z, w.w, e[2], e[3]);
+            bearings_step(c, e, x, y, vx, vy);
+        }
+        // weight by z_t and resample (stratified over the block's CDF)
+        const float lw = bearings_loglik(c, z, x, y);
+        mx[j] = x;
+        my[j] = y;
+        mvx[j] = vx;
+        mvy[j] = vy;
+        const float M = block_reduce(lw, OpMax(), -INFINITY, red);
+        float total;
+        const float incl =
+            block_inclusive_scan(__expf(lw - M), OpAdd(), 0.0f, red, &total);
+        cdf[j] = incl;
+        __syncthreads();
+        const u32x4 w = philox4x32_10(9u, pid, 0u, 0u, t, seed);
+        const float u =
+            (static_cast<float>(j) + u01_co_f(w.x)) / static_cast<float>(P) *
+            total;
+        uint32_t lo = 0, hi = P - 1; // the first slot with cdf > u
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (cdf[mid] > u)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        x = mx[lo];
+        y = my[lo];
+        vx = mvx[lo];
+        vy = mvy[lo];
+        __syncthreads();
+    }
+}
+
 // A minibatch of `batch` rows drawn uniformly with replacement from the
 // `total` stored samples (Philox4x32 key {step, seed}, counter
 // {3, row, 0, 0}; index = floor(word * total / 2^32)).
-__global__ void k_minibatch(uint64_t total, uint32_t batch, uint32_t step,
-    uint32_t seed, const float *feat, const float *nu, float *mf, float *mn)
+// Rows at index total and above come from the extra rows (xfeat, xnu).
+__global__ void k_minibatch(uint64_t total, uint64_t nx, uint32_t batch,
+    uint32_t step, uint32_t seed, const float *feat, const float *nu,
+    const float *xfeat, const float *xnu, float *mf, float *mn)
 {
+    const uint64_t all = total + nx;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < batch;
          r += gridDim.x * blockDim.x) {
         const u32x4 w = philox4x32_10(3u, r, 0u, 0u, step, seed);
-        const uint64_t j = (static_cast<uint64_t>(w.x) * total) >> 32;
+        uint64_t j = (static_cast<uint64_t>(w.x) * all) >> 32;
+        const float *fs = feat, *ns = nu;
+        if (j >= total) {
+            j -= total;
+            fs = xfeat;
+            ns = xnu;
+        }
 #pragma unroll
         for (int k = 0; k < 6; ++k)
-            mf[6 * r + k] = feat[6 * j + k];
+            mf[6 * r + k] = fs[6 * j + k];
 #pragma unroll
         for (int d = 0; d < 4; ++d)
-            mn[4 * r + d] = nu[4 * j + d];
+            mn[4 * r + d] = ns[4 * j + d];
     }
 }
 
@@ -720,8 +870,40 @@ int vsmc_cuda_mlp_train(const vsmc_cuda_bearings_model *model, uint32_t seed,
     size_t ntraj, size_t T, size_t batch, size_t steps, double lr,
     float *params, double *loss_host, void *stream)
 {
-    if (!valid_bearings_model(model) || params == nullptr || !(lr > 0))
+    return vsmc_cuda_mlp_train_rows(model, seed, ntraj, T, nullptr, nullptr,
+        0, batch, steps, lr, params, loss_host, stream);
+}
+
+int vsmc_cuda_mlp_cloud_rows(const vsmc_cuda_bearings_model *model,
+    uint32_t seed, size_t ntracks, size_t P, size_t T, size_t K, float *feat,
+    float *nu, void *stream)
+{
+    if (!valid_bearings_model(model) || feat == nullptr || nu == nullptr)
         return VSMC_CUDA_ERR_ARG;
+    if (ntracks < 1 || ntracks > 0x7FFFFFFFull || P < 32 || P % 32 != 0 ||
+        P > static_cast<size_t>(kCloudMaxP) || T < 2 ||
+        T > static_cast<size_t>(kCloudMaxT) || K < 1 || K > 0xFFFFFFFFull ||
+        ntracks * P > 0xFFFFFFFFull)
+        return VSMC_CUDA_ERR_SIZE;
+    cudaStream_t st = as_stream(stream);
+    k_cloud_rows<<<static_cast<unsigned>(ntracks), static_cast<unsigned>(P),
+        0, st>>>(make_bearings_const(*model),
+        static_cast<float>(model->sigma_z), seed, static_cast<uint32_t>(T),
+        static_cast<uint32_t>(K), feat, nu);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_mlp_train_rows(const vsmc_cuda_bearings_model *model,
+    uint32_t seed, size_t ntraj, size_t T, const float *xfeat,
+    const float *xnu, size_t nx, size_t batch, size_t steps, double lr,
+    float *params, double *loss_host, void *stream)
+{
+    if (!valid_bearings_model(model) || params == nullptr || !(lr > 0) ||
+        (nx > 0 && (xfeat == nullptr || xnu == nullptr)))
+        return VSMC_CUDA_ERR_ARG;
+    if (nx >= (size_t(1) << 32))
+        return VSMC_CUDA_ERR_SIZE;
     if (ntraj < 1 || ntraj >= (size_t(1) << 28) || T < 2 ||
         T > 0xFFFFFFFFull || batch < 16 || batch >= (size_t(1) << 24) ||
         steps < 1 || steps > 0xFFFFFFFFull ||
@@ -762,9 +944,9 @@ int vsmc_cuda_mlp_train(const vsmc_cuda_bearings_model *model, uint32_t seed,
     double p1 = 1, p2 = 1;
     const int mgrid = grid_for(batch, 256, 1, 8);
     for (size_t k = 0; k < steps; ++k) {
-        k_minibatch<<<mgrid, 256, 0, st>>>(total,
+        k_minibatch<<<mgrid, 256, 0, st>>>(total, nx,
             static_cast<uint32_t>(batch), static_cast<uint32_t>(k), seed, feat,
-            nu, mf, mn);
+            nu, xfeat, xnu, mf, mn);
         k_mlp_pack<<<(kPackedWords + 255) / 256, 256, 0, st>>>(params, packed);
         const int rc = enqueue_grad(packed, static_cast<uint32_t>(batch), mf,
             mn, part, grad, losses + k, st);
