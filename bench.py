@@ -55,6 +55,18 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_sustained():
+    """Dense BF16 TFLOP/s of a seconds-long cuBLAS loop (the peak for a
+    kernel timed inside a long run)."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        if "bf16_tflops_sustained" in d:
+            return float(d["bf16_tflops_sustained"]), "measured"
+    return 1700.0, "fallback"
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
@@ -629,6 +641,37 @@ def run_learned(args):
     learned = measure(args.learned_particles, prop.packed.data_ptr())
     boot = [measure(N, None) for N in args.boot_particles]
     clocks.stop()
+    # end to end: the learned filters through the C ABI, host observations
+    # in and histories out every run
+    NL = args.learned_particles
+    b = vc.FilterBatch([NL] * R, [T] * R, np.arange(R) + 1000,
+                       models=[m] * R, bearings=True,
+                       packed=prop.packed.data_ptr(),
+                       stream=ctypes.c_void_p(stream.cuda_stream))
+    obs_h = torch.from_numpy(np.tile(obs_np, R)).pin_memory()
+    hist_h = {k: torch.empty(R * T * w, dtype=dt, pin_memory=True)
+              for k, w, dt in (("mean", 2, torch.float64),
+                               ("ess", 1, torch.float64),
+                               ("res", 1, torch.int32),
+                               ("logz", 1, torch.float64))}
+    L = vc.lib()
+
+    def e2e_run():
+        vc.check(L.vsmc_cuda_batch_run(
+            b.handle, obs_h.data_ptr(), hist_h["mean"].data_ptr(),
+            hist_h["ess"].data_ptr(), hist_h["res"].data_ptr(),
+            hist_h["logz"].data_ptr()), "vsmc_cuda_batch_run")
+
+    e2e_run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(2, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_run()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    b.close()
+    h2d = obs_h.numel() * 8
+    d2h = sum(v.numel() * v.element_size() for v in hist_h.values())
     # bootstrap N at the learned filter's log-evidence SD (log-log fit)
     lx = np.log([b["N"] for b in boot])
     ly = np.log([b["logz_sd"] for b in boot])
@@ -641,6 +684,11 @@ def run_learned(args):
     if n_eq > boot[-1]["N"]:
         ms_eq = boot[-1]["ms"] * n_eq / boot[-1]["N"]
     value = n_eq * T * R / (learned["ms"] / 1000.0)
+    # the network's FLOPs per learned particle-step (t >= 1), unpadded:
+    # 2 (6 x 64 + 64 x 64 + 64 x 8)
+    flops = 2.0 * (6 * 64 + 64 * 64 + 64 * 8) * NL * (T - 1) * R
+    achieved = flops / (learned["ms"] / 1000.0) / 1e12
+    tpeak, tpeak_kind = measured_bf16_sustained()
     line = {
         "metric": "particle-steps/sec at fixed log-evidence SD "
                   "(learned proposal, bootstrap-equivalent)",
@@ -670,7 +718,20 @@ def run_learned(args):
             "speedup_at_equal_sd": ms_eq / learned["ms"],
             "reference": {"particles": args.ref_particles, "fp64": True,
                           "seconds": ref_s} if ref_mean is not None else None,
+            "l2": "state 2 x 4 x 4 B x 2^22 particles = 128 MiB per learned "
+                  "run's buffers, about L2; the network is in shared memory",
         },
+        "e2e": {"value": n_eq * T * R / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "tensor", "achieved": achieved,
+                     "peak": tpeak, "unit": "TFLOP/s",
+                     "frac": achieved / tpeak, "peak_source": tpeak_kind,
+                     "scope": "proposal network FLOPs of the learned run "
+                              "over its wall time; the step kernel is "
+                              "bound by the activations' ALU/SFU work and "
+                              "latency, not the tensor pipe",
+                     "traffic": None},
+        "gpu_launches": (2 + 6 * (T + 1)) * args.steps,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
