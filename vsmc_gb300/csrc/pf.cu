@@ -84,7 +84,7 @@ static void launch_resample32(vsmc_cuda_pf *pf)
     const Rs32Args r = make_rs_args32(pf);
     cudaStream_t st = pf->stream;
     k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    k_rs32_count<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    launch_rs32_count(pf->grid_rs, st, r);
     k_rs32_assign<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     k_rs32_markmax<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     k_rs32_fill<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
@@ -442,7 +442,7 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
         static_cast<uint32_t>(rng->ctr[1]), static_cast<uint32_t>(rng->ctr[2]),
         static_cast<uint32_t>(rng->ctr[3]), rng->index);
     k_rs32_qsum<<<grid, kPfBlock, 0, st>>>(r);
-    k_rs32_count<<<grid, kPfBlock, 0, st>>>(r);
+    launch_rs32_count(grid, st, r);
     k_rs32_assign<<<grid, kPfBlock, 0, st>>>(r);
     k_rs32_markmax<<<grid, kPfBlock, 0, st>>>(r);
     k_rs32_fill<<<grid, kPfBlock, 0, st>>>(r);
@@ -841,7 +841,7 @@ extern "C" int vsmc_cuda_resample_fixed_noalloc(size_t n, const uint64_t *q,
         static_cast<uint32_t>(rng->ctr[3]), rng->index);
     const int g = static_cast<int>(grid);
     k_rs32_qsum<<<g, kPfBlock, 0, st>>>(r);
-    k_rs32_count<<<g, kPfBlock, 0, st>>>(r);
+    launch_rs32_count(g, st, r);
     k_rs32_assign<<<g, kPfBlock, 0, st>>>(r);
     k_rs32_markmax<<<g, kPfBlock, 0, st>>>(r);
     k_rs32_fill<<<g, kPfBlock, 0, st>>>(r);

@@ -471,6 +471,7 @@ __device__ __forceinline__ void block_prefix_of_parts(
 
 // Replication counts from the fixed-point CDF; per-block empty and copy
 // counts.
+template <bool Sys>
 __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
 {
     if (!a.sc->resampled)
@@ -489,7 +490,7 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
     if (blockIdx.x == 0 && threadIdx.x == 0)
         a.sc->Q = Q;
     const PfScalars sc = *a.sc;
-    const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
+    constexpr bool sys = Sys; // the scheme (a.scheme) picked the instance
     const bool checked = a.q != nullptr;
     const uint32_t n = a.n;
     const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
@@ -597,6 +598,15 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
         a.epart[blockIdx.x] = empties;
         a.cpart[blockIdx.x] = copies;
     }
+}
+
+// the counting kernel of the scheme (systematic or stratified)
+inline void launch_rs32_count(int grid, cudaStream_t st, const Rs32Args &a)
+{
+    if (a.scheme == VSMC_CUDA_SYSTEMATIC)
+        k_rs32_count<true><<<grid, kPfBlock, 0, st>>>(a);
+    else
+        k_rs32_count<false><<<grid, kPfBlock, 0, st>>>(a);
 }
 
 // Slot assignment.  With c = copies before slot i and e = empty slots before
