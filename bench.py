@@ -399,8 +399,8 @@ def run_batched(args):
 def run_micro(args):
     """RNG and resampling microbenchmarks (the 2^30-word RNG and N = 2^24
     resampling workload): every call goes through the public C ABI, output
-    in HBM; each item is timed over `steps` calls with CUDA events after
-    `warmup` calls.  Headline: raw Philox4x32-10 words/s."""
+    in HBM; each item is the median of `steps` calls, each timed with CUDA
+    events, after `warmup` calls.  Headline: raw Philox4x32-10 words/s."""
     import torch
     rank, world, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
@@ -414,17 +414,21 @@ def run_micro(args):
     peak, peak_kind = measured_peaks()
 
     def timed(fn):
+        """Median over `steps` calls, each between its own CUDA events (the
+        resampling calls synchronize with the host, so one slow host-side
+        call would otherwise weigh on the mean)."""
         for _ in range(args.warmup):
             fn()
         torch.cuda.synchronize()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(args.steps):
+        ev = [(torch.cuda.Event(enable_timing=True),
+               torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        for e0, e1 in ev:
+            e0.record(stream)
             fn()
-        ev1.record(stream)
+            e1.record(stream)
         torch.cuda.synchronize()
-        return ev0.elapsed_time(ev1) / args.steps / 1000.0
+        return float(np.median([e0.elapsed_time(e1) for e0, e1 in ev])) / 1000.0
 
     clocks = ClockSampler(local)
     clocks.start()
