@@ -326,3 +326,22 @@ def test_monitor_mean(vc):
             out.data_ptr(), None)
     np.testing.assert_allclose(host(out)[:2], s.astype(np.float32)[:2] @ W,
                                rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("scheme", range(6))
+@pytest.mark.parametrize("bad", ["nan", "negative"])
+def test_schemes_reject_invalid_weights(vc, scheme, bad):
+    """A NaN or negative weight is reported (VSMC_CUDA_ERR_NONFINITE) by
+    every scheme, and the host engine is left where it was; the reference
+    leaves such input undefined (internal/assert.hpp:42-62)."""
+    import torch
+    m = n = 1000
+    w = np.full(m, 1.0 / m)
+    w[417] = np.nan if bad == "nan" else -1.0 / m
+    r = vc.rng(vc.PHILOX4X32, key=[3, 4], ctr=[5, 0, 0, 0])
+    before = [int(v) for v in r.ctr], r.index
+    rep = torch.zeros(m, dtype=torch.int32, device="cuda")
+    rc = vc.lib().vsmc_cuda_resample(m, n, ctypes.byref(r), dev(w).data_ptr(),
+                                     rep.data_ptr(), scheme, None)
+    assert rc == vc.ERR_NONFINITE
+    assert ([int(v) for v in r.ctr], r.index) == before

@@ -334,14 +334,23 @@ __global__ void k_systematic_terms(size_t n, double u01, double *t)
 
 // --------------------------------------------------------------- residual
 
-__global__ void k_residual_split(
-    size_t m, size_t n, const double *w, double *resid, int *integ)
+// A NaN, infinite or negative weight is reported and split as zero, so the
+// integer parts stay a valid count.
+__global__ void k_residual_split(size_t m, size_t n, const double *w,
+    double *resid, int *integ, uint32_t *err)
 {
     const double coeff = static_cast<double>(n);
     GRID_LOOP(i, m)
     {
-        const double x = __dmul_rn(coeff, w[i]);
-        const double ip = trunc(x);
+        const double wi = w[i];
+        if (!(wi >= 0.0) || isinf(wi)) {
+            atomicOr(err, DEV_ERR_NONFINITE);
+            resid[i] = 0.0;
+            integ[i] = 0;
+            continue;
+        }
+        const double x = __dmul_rn(coeff, wi);
+        const double ip = trunc(fmin(x, 2147483647.0));
         resid[i] = x - ip; // modf: exact
         integ[i] = static_cast<int>(ip);
     }
@@ -722,7 +731,7 @@ int residual_device(size_t m, size_t n, const double *w, double *resid,
         *R_host = n;
         return VSMC_CUDA_OK;
     }
-    k_residual_split<<<grid1(m), kB, 0, st>>>(m, n, w, resid, integ);
+    k_residual_split<<<grid1(m), kB, 0, st>>>(m, n, w, resid, integ, err);
     VSMC_CUDA_CHECK_LAUNCH();
     double *total = scratch.get<double>(1);
     int *isum = scratch.get<int>(1);
@@ -739,9 +748,17 @@ int residual_device(size_t m, size_t n, const double *w, double *resid,
     if (rc != VSMC_CUDA_OK)
         return rc;
     int R = 0;
+    uint32_t e = 0;
     VSMC_CUDA_TRY(cudaMemcpyAsync(
         &R, ipref + (m - 1), sizeof(int), cudaMemcpyDeviceToHost, st));
+    VSMC_CUDA_TRY(
+        cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, st));
     VSMC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (e & DEV_ERR_NONFINITE)
+        return VSMC_CUDA_ERR_NONFINITE;
+    // normalised weights give integer parts summing to at most n
+    if (R < 0 || static_cast<size_t>(R) > n)
+        return VSMC_CUDA_ERR_ARG;
     *R_host = n - static_cast<size_t>(R);
     return VSMC_CUDA_OK;
 }
