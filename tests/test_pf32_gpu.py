@@ -167,3 +167,23 @@ def test_pf32_reproducible_and_graph_equal(vc, port):
     for o in outs[1:]:
         for k in ("mean", "ess", "resampled", "logz"):
             assert np.array_equal(o[k], outs[0][k]), k
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 1000, 4097])
+def test_pf32_filter_small_and_ragged_sizes(vc, port, n):
+    """Particle counts below one 4-particle group, below one tile and just
+    above a tile: the run completes with finite histories, every ESS lies in
+    [1, n], and step 0 (same streams, no resampling yet) matches the
+    oracle's FP32 filter up to FP32 rounding."""
+    T = 20
+    obs, _ = _obs(port, T, seed=6)
+    pf = vc.ParticleFilter(n, 32, 1, 0.5, seed=2, max_steps=T)
+    g = pf.run(obs)
+    pf.close()
+    for k in ("mean", "ess", "logz"):
+        assert np.isfinite(g[k]).all(), k
+    assert (g["ess"] >= 1 - 1e-6).all() and (g["ess"] <= n + 1e-6).all()
+    o = _oracle_pf(port, 32, n, T, 2, 1, obs)
+    assert abs(g["ess"][0] - o["ess"][0]) / o["ess"][0] < 1e-4
+    assert abs(g["logz"][0] - o["logz"][0]) < 1e-4
+    assert g["resampled"][0] == o["resampled"][0]
