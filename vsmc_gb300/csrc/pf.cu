@@ -177,7 +177,7 @@ static int step32(vsmc_cuda_pf *pf)
 static int final_mean32(vsmc_cuda_pf *pf)
 {
     const Pf32Args a = make_args32(pf);
-    const int grid = grid_for(pf->n, kPfBlock, 8, 2);
+    const int grid = grid_for(pf->n, kPfBlock, 16, 8);
     k_pf32_final_mean<<<grid, kPfBlock, 0, pf->stream>>>(
         a, static_cast<uint32_t>(pf->t - 1));
     VSMC_CUDA_CHECK_LAUNCH();

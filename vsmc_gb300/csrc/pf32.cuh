@@ -317,18 +317,46 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_final_mean(
     const int resampled = a.sc->resampled;
     const bool gather = a.sc->gather != 0;
     const float M = static_cast<float>(a.sc->M);
-    double sx = 0, sy = 0, sw = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
-         i += gridDim.x * blockDim.x) {
+    const uint32_t n = a.n;
+    // FP32 within a thread and a warp, FP64 across warps and blocks, as
+    // the step kernel forms the monitor sums; four particles per thread
+    // step (float4 rows when nothing is gathered)
+    float sx = 0, sy = 0, sw = 0;
+    auto add = [&](uint32_t i, float x, float y) {
+        const float w = resampled ? 1.0f : __expf(a.lw[i] - M);
+        sx += w * x;
+        sy += w * y;
+        sw += w;
+    };
+    const uint32_t ngroups = n / 4;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups;
+         g += gridDim.x * blockDim.x) {
+        const uint32_t i0 = 4 * g;
+        if (!gather) {
+            const float4 X = ld4(a.ax, i0), Y = ld4(a.ay, i0);
+            add(i0 + 0, X.x, Y.x);
+            add(i0 + 1, X.y, Y.y);
+            add(i0 + 2, X.z, Y.z);
+            add(i0 + 3, X.w, Y.w);
+        } else {
+            for (uint32_t i = i0; i < i0 + 4; ++i) {
+                uint32_t src = source_of(a.idx, a.srcs, a.idx[i]);
+                if (src >= n) {
+                    atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+                    src = 0;
+                }
+                add(i, a.ax[src], a.ay[src]);
+            }
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x < n - 4 * ngroups) { // the last 1-3
+        const uint32_t i = 4 * ngroups + threadIdx.x;
         uint32_t src = gather ? source_of(a.idx, a.srcs, a.idx[i]) : i;
-        if (src >= a.n) {
+        if (src >= n) {
             atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
             src = 0;
         }
-        const float w = resampled ? 1.0f : __expf(a.lw[i] - M);
-        sx += w * a.ax[src];
-        sy += w * a.ay[src];
-        sw += w;
+        add(i, a.ax[src], a.ay[src]);
     }
     __shared__ double sh[3][kPfBlock / 32];
     __shared__ bool is_last;
