@@ -187,3 +187,26 @@ def test_pf32_filter_small_and_ragged_sizes(vc, port, n):
     assert abs(g["ess"][0] - o["ess"][0]) / o["ess"][0] < 1e-4
     assert abs(g["logz"][0] - o["logz"][0]) < 1e-4
     assert g["resampled"][0] == o["resampled"][0]
+
+
+def test_pf32_filter_at_2_to_28_particles(vc, port):
+    """N = 2^28 (about 14 GB of state, weights and resampling arrays): the
+    32-bit particle indices, the 35-bit fixed-point CDF and the 128-bit
+    position arithmetic at scale.  The run must agree with an N = 2^20 run
+    of the same model and observations within Monte Carlo error (the
+    smaller run's error dominates), and resample at step 0 like it."""
+    T = 4
+    obs, _ = _obs(port, T, seed=9)
+    out = {}
+    for lg in (20, 28):
+        pf = vc.ParticleFilter(1 << lg, 32, 2, 0.5, seed=4, max_steps=T)
+        out[lg] = pf.run(obs)
+        pf.close()
+    big, small = out[28], out[20]
+    for k in ("mean", "ess", "logz"):
+        assert np.isfinite(big[k]).all(), k
+    assert big["resampled"][0] == small["resampled"][0] == 1
+    np.testing.assert_allclose(big["ess"][0] / 2 ** 28,
+                               small["ess"][0] / 2 ** 20, rtol=0.02)
+    assert np.abs(big["logz"] - small["logz"]).max() < 0.05
+    assert np.abs(big["mean"] - small["mean"]).max() < 0.05
