@@ -204,7 +204,7 @@ static int materialize32(vsmc_cuda_pf *pf)
 
 __global__ void k_reset_scalars(PfScalars *sc, uint32_t seed)
 {
-    PfScalars z;
+    PfScalars z = {};
     z.M = 0;
     z.S = 0;
     z.logz = 0;
