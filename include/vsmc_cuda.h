@@ -115,7 +115,9 @@ int vsmc_cuda_rng_normal_f32(vsmc_cuda_rng *rng, size_t n, float *r,
  * per_stream variates into r[s * per_stream + k] exactly as successive
  * calls of NormalDistribution<double>(mean, sd) (rng/normal_distribution.hpp:
  * 199-216) or StudentTDistribution<double>(df) (rng/student_t_distribution.hpp:
- * 78-91, gamma by rng/gamma_distribution.hpp:132-216) on that engine. */
+ * 78-91, gamma by rng/gamma_distribution.hpp:132-216) on that engine.
+ * The gamma rejection loops stop after 65536 tries (each accepts with
+ * probability above 1/2); a variate that reaches the bound is NaN. */
 int vsmc_cuda_normal_streams(int kind, const uint64_t key[4], size_t nstreams,
     size_t per_stream, double mean, double stddev, double *r, void *stream);
 int vsmc_cuda_student_t_streams(int kind, const uint64_t key[4],
@@ -236,8 +238,14 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
  *     array's address and may load the library's device code: make it
  *     before any stream capture;
  *   - all callers on a device share the array, so calls whose work overlaps
- *     in time (other streams, other host threads) race and give wrong
- *     results: order them on one stream;
+ *     in time race and give wrong results.  Serialize the calls on the host:
+ *     one call at a time per device (each call synchronizes its stream
+ *     before returning, so one host thread calling in turn is safe; several
+ *     host threads need a lock of their own, even on one stream, since each
+ *     call queues several launches that could interleave);
+ *   - the array's address is looked up once per device for the life of the
+ *     process: a device reset (cudaDeviceReset) between calls is not
+ *     supported;
  *   - synchronizes the stream.
  * No reference counterpart (the reference allocates nothing on a device). */
 #define VSMC_CUDA_RESAMPLE_FIXED_NOALLOC_MAX_N (1u << 18)

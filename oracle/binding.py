@@ -149,10 +149,24 @@ def build_port():
     return PORT
 
 
+# Where this recipe reads the reference tree: VSMC_REF_ROOT, else the
+# read-only checkout of the build container.  The GPU host has neither.
+_REF_CHECKOUT = "/root/reference"
+
+
+def ref_root():
+    """The reference source tree (VSMC_REF_ROOT or the build container's
+    checkout), or None where it is absent."""
+    root = os.environ.get("VSMC_REF_ROOT") or _REF_CHECKOUT
+    if os.path.isdir(os.path.join(root, "include", "vsmc")):
+        return root
+    return None
+
+
 def build_ref():
     """Build the reference library if the reference tree is present."""
-    root = os.environ.get("VSMC_REF_ROOT", "/root/reference")
-    if not os.path.isdir(os.path.join(root, "include", "vsmc")):
+    root = ref_root()
+    if root is None:
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={root}"],
                    check=True)

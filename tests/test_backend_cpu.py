@@ -8,10 +8,12 @@ import pytest
 
 from conftest import ROOT
 
-REF = os.environ.get("VSMC_REF_ROOT", "/root/reference")
+from oracle.binding import ref_root
+
+REF = ref_root()
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include", "vsmc")),
+@pytest.mark.skipif(REF is None,
                     reason="reference headers not present on this host")
 def test_backend_header_builds_against_reference_sampler(tmp_path):
     from vsmc_gb300 import build

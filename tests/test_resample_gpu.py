@@ -345,3 +345,24 @@ def test_schemes_reject_invalid_weights(vc, scheme, bad):
                                      rep.data_ptr(), scheme, None)
     assert rc == vc.ERR_NONFINITE
     assert ([int(v) for v in r.ctr], r.index) == before
+
+
+@pytest.mark.parametrize("case", ["wraps_to_zero", "wraps_into_range"])
+def test_residual_split_rejects_integer_parts_past_2_to_31(vc, case):
+    """Unnormalized weights whose integer parts n * w_i add up past 2^31:
+    the total is formed in 64 bits, so a 32-bit wrap back into [0, n]
+    cannot pass as a valid draw; the split reports VSMC_CUDA_ERR_ARG."""
+    import torch
+    n = 4
+    if case == "wraps_to_zero":
+        w = np.full(4, 2.0**28)          # 4 * 2^30 = 2^32 = 0 mod 2^32
+    else:
+        w = np.array([2.0**28] * 4 + [0.5])  # 2^32 + 2 = 2 mod 2^32
+    m = len(w)
+    resid = torch.zeros(m, dtype=torch.float64, device="cuda")
+    integ = torch.zeros(m, dtype=torch.int32, device="cuda")
+    R = ctypes.c_size_t(0)
+    rc = vc.lib().vsmc_cuda_resample_trans_residual(
+        m, n, dev(w).data_ptr(), resid.data_ptr(), integ.data_ptr(),
+        ctypes.byref(R), None)
+    assert rc == vc.ERR_ARG

@@ -738,8 +738,13 @@ int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
 //     array's address with cudaGetSymbolAddress, which may load the
 //     library's device code; make that first call before any stream capture.
 //   * The array is shared by all callers on a device: two calls whose work
-//     overlaps in time (different streams, or different host threads) race
-//     on it and give wrong results.  Order them on one stream.
+//     overlaps in time race on it and give wrong results.  Callers serialize
+//     on the host, one call at a time per device.  Each call synchronizes
+//     its stream before returning, so one host thread calling in turn is
+//     safe; several host threads need a lock of their own even on one
+//     stream, since a call queues several launches.
+//   * The address is looked up once per device and kept for the life of the
+//     process; a device reset between calls is not supported.
 //   * The slot marks must be zero when counting starts; each call clears them
 //     with cudaMemsetAsync on its stream (no allocation).  Everything else
 //     in the array is fully written before it is read.

@@ -440,6 +440,23 @@ struct StoreI {
     __device__ void operator()(size_t i, int32_t v) const { p[i] = v; }
 };
 
+// int entries widened to 64 bits (sums of up to 2^31 counts of up to 2^31)
+struct LoadIW {
+    const int *p;
+    __device__ long long operator()(size_t i) const { return p[i]; }
+};
+
+// keeps only the last value of a scan (the total)
+struct StoreLastW {
+    long long *p;
+    size_t last;
+    __device__ void operator()(size_t i, long long v) const
+    {
+        if (i == last)
+            *p = v;
+    }
+};
+
 __global__ void k_index_square(size_t n, const int *rep, const I2 *incl,
     const int *src_of_rank, size_t nrank, int *idx, uint32_t *err)
 {
@@ -734,30 +751,32 @@ int residual_device(size_t m, size_t n, const double *w, double *resid,
     k_residual_split<<<grid1(m), kB, 0, st>>>(m, n, w, resid, integ, err);
     VSMC_CUDA_CHECK_LAUNCH();
     double *total = scratch.get<double>(1);
-    int *isum = scratch.get<int>(1);
-    int *pp = scratch.get<int>(scan_parts(m));
-    int *ipref = scratch.get<int>(m);
-    if (!total || !isum || !pp || !ipref)
+    long long *isum = scratch.get<long long>(1);
+    long long *pp = scratch.get<long long>(scan_parts(m));
+    if (!total || !isum || !pp)
         return VSMC_CUDA_ERR_ALLOC;
     int rc = seqsum_device(m, resid, nullptr, total, err, scratch, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
     k_scale<<<grid1(m), kB, 0, st>>>(m, total, resid);
     VSMC_CUDA_CHECK_LAUNCH();
-    rc = device_scan(m, LoadI{integ}, StoreI{ipref}, OpAdd(), 0, pp, st);
+    // the integer parts summed in 64 bits: unnormalized weights can push
+    // the sum past 2^31, and a wrapped 32-bit sum could land back in [0, n]
+    rc = device_scan(m, LoadIW{integ}, StoreLastW{isum, m - 1}, OpAdd(),
+        0LL, pp, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    int R = 0;
+    long long R = 0;
     uint32_t e = 0;
     VSMC_CUDA_TRY(cudaMemcpyAsync(
-        &R, ipref + (m - 1), sizeof(int), cudaMemcpyDeviceToHost, st));
+        &R, isum, sizeof(R), cudaMemcpyDeviceToHost, st));
     VSMC_CUDA_TRY(
         cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, st));
     VSMC_CUDA_TRY(cudaStreamSynchronize(st));
     if (e & DEV_ERR_NONFINITE)
         return VSMC_CUDA_ERR_NONFINITE;
     // normalised weights give integer parts summing to at most n
-    if (R < 0 || static_cast<size_t>(R) > n)
+    if (R < 0 || static_cast<unsigned long long>(R) > n)
         return VSMC_CUDA_ERR_ARG;
     *R_host = n - static_cast<size_t>(R);
     return VSMC_CUDA_OK;

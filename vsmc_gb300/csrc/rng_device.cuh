@@ -19,6 +19,8 @@
 
 #include "common.cuh"
 
+#include <math_constants.h>
+
 namespace vsmc_cuda
 {
 
@@ -459,9 +461,17 @@ struct NormalScalar {
 // StudentTDistribution<double>: normal first, then chi-squared = Gamma(df/2,
 // 2) by the reference's four gamma algorithms
 // (student_t_distribution.hpp:78-91, gamma_distribution.hpp:57-216).
+//
+// Every rejection loop accepts with probability above 1/2 per try for any
+// alpha, so a variate needing kGammaMaxTries tries means a broken engine or
+// argument: the loop then stops, the variate is NaN and `err` gets
+// DEV_ERR_BOUND.
+constexpr int kGammaMaxTries = 1 << 16;
+
 struct StudentTScalar {
     double df, alpha, d, c;
     int alg; // 0 T (alpha < 0.6), 1 W (alpha < 1), 2 N (alpha > 1), 3 E
+    uint32_t err = 0;
     NormalScalar<double> normal;
 
     __device__ explicit StudentTScalar(double nu)
@@ -487,9 +497,10 @@ struct StudentTScalar {
     template <typename Eng>
     __device__ double gamma(Eng &eng)
     {
-        double r = 0;
+        double r = CUDART_NAN;
+        int tries = 0;
         if (alg == 0) {
-            for (;;) {
+            for (; tries < kGammaMaxTries; ++tries) {
                 double u = eng.u01d();
                 double e = -log(eng.u01d());
                 if (u > d) {
@@ -504,22 +515,31 @@ struct StudentTScalar {
                 }
             }
         } else if (alg == 1) {
-            double u, e, x;
-            do {
-                u = -log(eng.u01d());
-                e = -log(eng.u01d());
-                x = exp(__dmul_rn(c, log(u)));
-            } while (__dadd_rn(u, e) < __dadd_rn(d, x));
-            r = x;
+            for (; tries < kGammaMaxTries; ++tries) {
+                const double u = -log(eng.u01d());
+                const double e = -log(eng.u01d());
+                const double x = exp(__dmul_rn(c, log(u)));
+                if (!(__dadd_rn(u, e) < __dadd_rn(d, x))) {
+                    r = x;
+                    break;
+                }
+            }
         } else if (alg == 2) {
             NormalScalar<double> rnorm(0, 1);
-            for (;;) {
+            for (; tries < kGammaMaxTries; ++tries) {
                 const double u = eng.u01d();
-                double w, v;
-                do {
+                double w = 0, v = 0;
+                bool pos = false;
+                for (; tries < kGammaMaxTries; ++tries) {
                     w = rnorm(eng);
                     v = __dadd_rn(1.0, __dmul_rn(c, w));
-                } while (v <= 0);
+                    if (!(v <= 0)) {
+                        pos = true;
+                        break;
+                    }
+                }
+                if (!pos)
+                    break;
                 v = __dmul_rn(__dmul_rn(v, v), v);
                 const double w2 = __dmul_rn(w, w);
                 double e = __dadd_rn(1.0, -__dmul_rn(__dmul_rn(0.0331, w2), w2));
@@ -537,6 +557,8 @@ struct StudentTScalar {
         } else {
             r = -log(eng.u01d());
         }
+        if (tries >= kGammaMaxTries)
+            err |= DEV_ERR_BOUND;
         return __dmul_rn(2.0, r);
     }
 
