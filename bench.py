@@ -742,6 +742,120 @@ def run_learned(args):
     return 0
 
 
+def build_sampler_program(ref, out_dir):
+    """nvcc build of tests/cpp/sampler_cuda.cu (vSMC's Sampler<T> on the
+    fused FP32 backend, include/vsmc_cuda_sampler.cuh) against the reference
+    tree `ref`; returns the binary's path."""
+    from vsmc_gb300 import build
+    lib = build.build()
+    libdir = os.path.dirname(lib)
+    exe = os.path.join(out_dir, "sampler_cuda")
+    cmd = [os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc"), "-std=c++17",
+           "-O3", "-gencode", "arch=compute_103a,code=sm_103a",
+           "-I", os.path.join(ref, "include"),
+           "-I", os.path.join(ROOT, "tests", "cpp", "shim"),
+           "-I", os.path.join(ROOT, "include"),
+           "-DVSMC_RNG_TYPE=::vsmc::Philox4x32", "-DVSMC_HAS_MKL=0",
+           "-DVSMC_HAS_TBB=0", "-Xcompiler", "-w"]
+    if os.uname().machine == "aarch64":
+        cmd += ["-DVSMC_UTILITY_SIMD_HPP", "-DVSMC_HAS_SSE2=0",
+                "-DVSMC_HAS_AVX2=0", "-DVSMC_HAS_AES_NI=0",
+                "-DVSMC_HAS_RDRAND=0"]
+    cmd += [os.path.join(ROOT, "tests", "cpp", "sampler_cuda.cu"), "-o", exe,
+            "-L", libdir, "-lvsmc_cuda", f"-Xlinker=-rpath={libdir}"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def run_sampler(args):
+    """The large single filter driven by the reference's own Sampler<T>
+    (initialize + iterate, Particle::resample, Monitor::eval) on the fused
+    FP32 backend, with the model a user device functor: the plugin API a
+    vSMC user switches to.  Each bench step is one whole run, timed on the
+    host clock around initialize + T - 1 iterates (the Sampler API waits for
+    every step's ESS, so the device work is inside it).  Needs the
+    reference's headers (VSMC_REF_ROOT) to compile the program."""
+    import tempfile
+    import torch
+    ref = os.environ.get("VSMC_REF_ROOT")
+    if not ref or not os.path.isdir(os.path.join(ref, "include", "vsmc")):
+        print(json.dumps({"metric": METRIC + " through vsmc::Sampler<T>",
+                          "unavailable": "needs the reference's headers "
+                                         "(VSMC_REF_ROOT) to compile the "
+                                         "Sampler<T> program"}))
+        return 0
+    import vsmc_gb300 as vc
+    vc.lib()
+    n, T = args.n, args.T
+    work = tempfile.mkdtemp(prefix="vsmc_sampler_")
+    exe = build_sampler_program(ref, work)
+    obs_dev = simulate_obs(vc, T, seed=0)
+    obs = obs_dev.view(T, 2).cpu().numpy()
+    obs_path = os.path.join(work, "obs.bin")
+    out_path = os.path.join(work, "out.bin")
+    np.ascontiguousarray(obs, dtype=np.float64).tofile(obs_path)
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    runs = args.warmup + args.steps
+    r = subprocess.run([exe, str(n), str(T), "1", str(SCHEME),
+                        repr(THRESHOLD), "1", obs_path, out_path, str(runs)],
+                       capture_output=True, text=True, check=True)
+    clocks.stop()
+    ms_runs = json.loads(r.stdout.strip().splitlines()[-1])["ms"]
+    timed = ms_runs[args.warmup:]
+    v = np.fromfile(out_path, dtype=np.float64)
+    resampled = int(v[3 * T:4 * T].sum())
+    # the library's own device-resident run in this process, same workload
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    pf = vc.ParticleFilter(n, 32, SCHEME, THRESHOLD, seed=1, max_steps=T,
+                           stream=ctypes.c_void_p(stream.cuda_stream))
+    for _ in range(args.warmup):
+        pf.run_device(T, obs_dev.data_ptr())
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        pf.run_device(T, obs_dev.data_ptr())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    lib_ms = ev0.elapsed_time(ev1) / args.steps
+    pf.close()
+    psteps = float(n) * T
+    ms = float(np.sum(timed))
+    value = psteps * args.steps / (ms / 1000.0)
+    line = {
+        "metric": METRIC + " through vsmc::Sampler<T>", "value": value,
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (observations simulated from the model, seed 0)",
+        "config": {
+            "workload": "large single bootstrap filter through the reference's "
+                        "Sampler<StateCUDA<4, float>> with InitializeCUDA / "
+                        "MoveCUDA of a user device model and MonitorMeanCUDA",
+            "particles": n, "steps_T": T, "scheme": "systematic",
+            "threshold": THRESHOLD,
+            "device_threshold": "the Sampler's (resampling queued right "
+                                "after each step)",
+            "timing": "host clock around initialize + iterate per run",
+            "resampled_steps_last_run": resampled,
+            "ms_per_run_each": timed,
+        },
+        "library_run_ms": lib_ms,
+        "sampler_over_library_time": (ms / args.steps) / lib_ms,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": (8 * 8 + 8) * T},
+        "clocks": clocks.summary(),
+        "gpu_launches": (1 + 6 * T) * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -752,7 +866,8 @@ def main():
     ap.add_argument("--T", type=int, default=T_STEPS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="single",
-                    choices=["single", "batched", "learned", "micro"])
+                    choices=["single", "batched", "learned", "micro",
+                             "sampler"])
     ap.add_argument("--replicates", type=int, default=1024)
     ap.add_argument("--learned-particles", type=int, default=1 << 12)
     ap.add_argument("--boot-particles", type=int, nargs="+",
@@ -787,6 +902,8 @@ def main():
         return run_learned(args)
     if args.workload == "micro":
         return run_micro(args)
+    if args.workload == "sampler":
+        return run_sampler(args)
 
     import torch
     rank, world, local = dist_setup(args.gpus)

@@ -360,6 +360,81 @@ int vsmc_cuda_pf_use_graph(vsmc_cuda_pf *pf, int on);
  * (smp/backend_omp.hpp:93-105, core/weight.hpp:168-173). */
 int vsmc_cuda_pf_launch_step_kernel(vsmc_cuda_pf *pf);
 
+/* ------------------------------------------- filters of user models */
+
+/* A precision-32 filter whose move and log-likelihood come from the caller's
+ * device model (vsmc_cuda_filter.cuh): dim state components (1..8, SoA rows
+ * of ((n + 255) / 256) * 256 floats), the weighted mean of the first
+ * monitor_dim (0..4, <= dim) recorded every step, scheme stratified or
+ * systematic on the exact integer CDF.  threshold >= 0: the step kernel
+ * flags a resample when ESS < threshold * n and vsmc_cuda_pf_step_commit
+ * runs it; threshold < 0: the host decides (vsmc_cuda_pf_resample_now), as
+ * Particle::resample does under Sampler<T> (core/particle.hpp:170-197).
+ * Replaces Sampler<T>(N, scheme, threshold) (core/sampler.hpp:107-114)
+ * with a state matrix StateMatrix<ColMajor, dim, float>
+ * (core/state_matrix.hpp:320-364) and a user move
+ * (smp/backend_base.hpp:243-363). */
+int vsmc_cuda_pf_create_model(vsmc_cuda_pf **pf, size_t n, size_t dim,
+    size_t monitor_dim, int scheme, double threshold, uint32_t seed,
+    size_t max_steps, void *stream);
+
+/* Buffers of a precision-32 filter's next step, for a step kernel of the
+ * caller's model (vsmc_cuda::pf_step_launch in vsmc_cuda_filter.cuh). */
+typedef struct {
+    const float *state_in;   /* dim rows of `stride` floats: before the step */
+    float *state_out;        /* dim rows: after the step */
+    float *log_weight;       /* n FP32 log-weights (updated in place) */
+    const int32_t *index;    /* slot encoding of the last resample */
+    const uint32_t *sources; /* parents of the empty slots */
+    void *partials;          /* max_grid per-block records */
+    void *scalars;           /* the filter's device scalars */
+    double *hist_mean;       /* max_steps x monitor_dim */
+    double *hist_ess, *hist_logz;
+    int *hist_resampled;
+    size_t n, stride, dim, monitor_dim, max_steps, max_grid;
+    size_t step;             /* index of the step (0 = initialize) */
+    uint32_t seed;
+    double threshold;        /* the device's resampling threshold (< 0: never) */
+    void *stream;            /* the filter's stream */
+} vsmc_cuda_pf_step_desc;
+
+/* The first call after creation or vsmc_cuda_pf_reset (step 0) also resets
+ * the filter's device scalars on its stream. */
+int vsmc_cuda_pf_step_desc_get(vsmc_cuda_pf *pf, vsmc_cuda_pf_step_desc *d);
+/* Back to step 0 (Sampler::initialize, core/sampler.hpp:443-455) for a
+ * filter of vsmc_cuda_pf_create_model. */
+int vsmc_cuda_pf_reset(vsmc_cuda_pf *pf);
+/* After the step kernel was launched on the descriptor's stream: the
+ * resampling passes (threshold >= 0; they return at once unless the step
+ * flagged a resample), then the buffers swap and the step index advances. */
+int vsmc_cuda_pf_step_commit(vsmc_cuda_pf *pf);
+/* Resample the current particles now (precision 32): the host decided
+ * ESS < threshold * N.  Particle::resample -> StateCUDA::copy(N, nullptr)
+ * (core/particle.hpp:186-192); the weights become equal, and the monitor
+ * mean becomes that of the resampled particles. */
+int vsmc_cuda_pf_resample_now(vsmc_cuda_pf *pf);
+/* Weight::set_equal (core/weight.hpp:99-103) on a precision-32 filter. */
+int vsmc_cuda_pf_set_equal(vsmc_cuda_pf *pf);
+/* Weight::set_log (add = 0) / Weight::add_log (add = 1)
+ * (core/weight.hpp:145-149, 168-173) on a precision-32 filter from n device
+ * doubles; ESS, the monitor sums' weights and (add) the log-evidence follow. */
+int vsmc_cuda_pf_weight_log(vsmc_cuda_pf *pf, const double *lw_dev, int add);
+
+/* Host view of the filter scalars after the work queued so far
+ * (synchronizes the filter's stream). */
+typedef struct {
+    double ess;           /* ESS of the current weights */
+    double log_evidence;  /* cumulative log-evidence */
+    double max_log_weight;
+    double sum_weight;    /* sum exp(lw - max_log_weight) */
+    double mean[4];       /* monitor: weighted mean of the first components */
+    size_t step;          /* steps taken */
+    int resampled;        /* the current weights are equal after a resample */
+    int monitor_dim;
+} vsmc_cuda_pf_status;
+
+int vsmc_cuda_pf_get_status(vsmc_cuda_pf *pf, vsmc_cuda_pf_status *out);
+
 /* ------------------------------------- bearings-only model, proposal */
 
 /* Bearings-only tracking: state (x, y, vx, vy); constant velocity with

@@ -1,9 +1,11 @@
 // vsmc_cuda_backend.hpp - CUDA backend classes for vSMC's Sampler<T>.
 //
 // The CUDA sibling of the reference's smp/backend_{seq,omp,tbb}.hpp for the
-// particle-filter path, built on the C ABI of libvsmc_cuda (vsmc_cuda.h):
+// particle-filter path, built on the C ABI of libvsmc_cuda (vsmc_cuda.h).
+// This header holds the FP64 classes, which keep the reference's arithmetic
+// step for step (normalized double weights, the exact resampling schemes):
 //
-//   StateCUDA<Dim, T>     particle state on the device (SoA, StateMatrix
+//   StateCUDA<Dim, double> particle state on the device (SoA, StateMatrix
 //                         <ColMajor, Dim, T> layout, core/state_matrix.hpp:
 //                         320-364); resampling runs in copy(N, nullptr)
 //   WeightCUDA            the Weight class (core/weight.hpp:67-230) on the
@@ -19,7 +21,11 @@
 //                         weighted mean on the device (core/monitor.hpp:
 //                         242-268)
 //
-// Usage (the pf example with the CUDA backend):
+// StateCUDA<Dim, float> -- the fused FP32 filter with a user device model
+// (InitializeCUDA<Model> / MoveCUDA<Model>) -- is in vsmc_cuda_sampler.cuh,
+// which needs nvcc.
+//
+// Usage (the pf example with the FP64 CUDA backend):
 //
 //   using State = vsmc::cuda::StateCUDA<4, double>;
 //   vsmc::Sampler<State> sampler(N, vsmc::Stratified, 0.5);
@@ -248,11 +254,14 @@ class WeightCUDA
 
 // Particle state on the device: Dim rows of N values (StateMatrix<ColMajor,
 // Dim, T> layout).  state(id, pos) reads a host copy downloaded on request.
+// This is the FP64 state; StateCUDA<Dim, float> (vsmc_cuda_sampler.cuh) is
+// the fused FP32 filter.
 template <std::size_t Dim, typename T>
 class StateCUDA
 {
-    static_assert(sizeof(T) == 4 || sizeof(T) == 8,
-        "StateCUDA holds float or double");
+    static_assert(sizeof(T) == 8,
+        "StateCUDA<Dim, double> here; StateCUDA<Dim, float> is the fused "
+        "FP32 filter of vsmc_cuda_sampler.cuh (compile with nvcc)");
 
     public:
     using size_type = std::size_t;
@@ -334,14 +343,9 @@ class StateCUDA
 
     void copy_device(size_type N)
     {
-        int rc;
-        if (sizeof(T) == 4)
-            rc = vsmc_cuda_state_copy_f32(N, Dim, idx_.get(),
-                reinterpret_cast<float *>(data_.get()), nullptr);
-        else
-            rc = vsmc_cuda_state_copy_f64(N, Dim, idx_.get(),
-                reinterpret_cast<double *>(data_.get()), nullptr);
-        check(rc, "vsmc_cuda_state_copy");
+        check(vsmc_cuda_state_copy_f64(N, Dim, idx_.get(),
+                  reinterpret_cast<double *>(data_.get()), nullptr),
+            "vsmc_cuda_state_copy");
     }
 
     size_type N_;
@@ -360,6 +364,9 @@ template <std::size_t Dim, typename T>
 class InitializeCV
 {
     static_assert(Dim == 4, "the constant-velocity model has 4 components");
+    static_assert(sizeof(T) == 8,
+        "FP64 only; the FP32 filter takes InitializeCUDA<Model> / "
+        "MoveCUDA<Model> (vsmc_cuda_sampler.cuh)");
 
     public:
     InitializeCV(const vsmc_cuda_cv_model &model, std::uint32_t seed,
@@ -382,23 +389,10 @@ class InitializeCV
     protected:
     void loglik(std::size_t t, StateCUDA<Dim, T> &s, std::size_t N)
     {
-        int rc;
-        if (sizeof(T) == 4) {
-            DeviceArray<float> llf(N);
-            rc = vsmc_cuda_cv_move_f32(N, t, seed_, &model_, obs_.data() + 2 * t,
-                reinterpret_cast<float *>(s.device_data()), llf.get(), nullptr);
-            check(rc, "vsmc_cuda_cv_move_f32");
-            std::vector<float> h(N);
-            llf.download(h.data(), N);
-            std::vector<double> d(h.begin(), h.end());
-            ll_.upload(d.data(), N);
-        } else {
-            rc = vsmc_cuda_cv_move_f64(N, t, seed_, &model_,
-                obs_.data() + 2 * t,
-                reinterpret_cast<double *>(s.device_data()), ll_.get(),
-                nullptr);
-            check(rc, "vsmc_cuda_cv_move_f64");
-        }
+        check(vsmc_cuda_cv_move_f64(N, t, seed_, &model_, obs_.data() + 2 * t,
+                  reinterpret_cast<double *>(s.device_data()), ll_.get(),
+                  nullptr),
+            "vsmc_cuda_cv_move_f64");
     }
 
     vsmc_cuda_cv_model model_;
@@ -437,18 +431,11 @@ class MonitorMeanCUDA
     {
         const std::size_t N = particle.size();
         out_.resize(dim);
-        int rc;
-        if (sizeof(T) == 4)
-            rc = vsmc_cuda_monitor_mean_f32(N, dim,
-                reinterpret_cast<const float *>(
-                    particle.value().device_data()),
-                particle.weight().device_data(), out_.get(), nullptr);
-        else
-            rc = vsmc_cuda_monitor_mean_f64(N, dim,
-                reinterpret_cast<const double *>(
-                    particle.value().device_data()),
-                particle.weight().device_data(), out_.get(), nullptr);
-        check(rc, "vsmc_cuda_monitor_mean");
+        check(vsmc_cuda_monitor_mean_f64(N, dim,
+                  reinterpret_cast<const double *>(
+                      particle.value().device_data()),
+                  particle.weight().device_data(), out_.get(), nullptr),
+            "vsmc_cuda_monitor_mean");
         out_.download(r, dim);
     }
 

@@ -1,5 +1,6 @@
-/* Minimal CBLAS stand-in used only to compile the reference headers as the
- * oracle (test infrastructure).  No system CBLAS exists on either machine.
+/* Minimal CBLAS stand-in for compiling the reference's headers: the oracle's
+ * reference build (oracle/Makefile) and the Sampler<T> programs of
+ * tests/cpp.  No system CBLAS exists on either machine.
  *
  * Only the two routines on the particle-filter path are defined, with the
  * plain sequential summation order a reference BLAS would use:

@@ -22,13 +22,12 @@ def test_backend_header_builds_against_reference_sampler(tmp_path):
     out = tmp_path / "backend_demo"
     cmd = ["g++", "-std=c++14", "-O1", "-w",
            "-I", os.path.join(REF, "include"),
-           "-I", os.path.join(ROOT, "oracle", "shim"),
+           "-I", os.path.join(ROOT, "tests", "cpp", "shim"),
            "-I", os.path.join(ROOT, "include"),
            "-I", os.path.join(cuda, "include"),
            "-DVSMC_RNG_TYPE=::vsmc::Philox4x32", "-DVSMC_HAS_MKL=0",
            "-DVSMC_HAS_TBB=0",
            os.path.join(ROOT, "tests", "cpp", "backend_demo.cpp"),
-           os.path.join(ROOT, "oracle", "shim", "stubs.c"),
            "-o", str(out), "-L", os.path.dirname(lib), "-lvsmc_cuda",
            "-L", os.path.join(cuda, "lib64"), "-lcudart",
            f"-Wl,-rpath,{os.path.dirname(lib)}"]

@@ -221,3 +221,20 @@ def test_port_vs_reference_random(port):
             port.vo_resample_words(scheme, M, N, P(k2), P(c4), P(w), P(b),
                                    P(nb))
             assert np.array_equal(a, b) and np.array_equal(na, nb)
+
+
+def test_numpy_philox_restatement_matches_oracle(port):
+    """The tests' vectorized Philox4x32-10 (conftest.philox4x32_10, used for
+    float64 restatements of the FP32 kernels) against the oracle's engine:
+    word k of an engine at counter {0, i, 0, 0} is block {1 + k // 4, i}."""
+    from conftest import P, philox4x32_10
+    key = np.array([7, 99], np.uint32)
+    for i in (0, 12345, 0xFFFFFFFF):
+        ctr = np.array([0, i, 0, 0], np.uint32)
+        want = np.zeros(8, np.uint32)
+        port.vo_philox4x32_words(P(key), P(ctr), 8, P(want), 0)
+        got = []
+        for b in (1, 2):
+            got += [int(g[0]) for g in philox4x32_10([[b], [i], [0], [0]],
+                                                     7, 99)]
+        assert got == [int(w) for w in want]

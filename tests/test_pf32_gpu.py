@@ -5,7 +5,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import P, dev, host
+from conftest import P, dev, host, normal_pair_f64, particle_words
 
 pytestmark = pytest.mark.gpu
 
@@ -46,32 +46,60 @@ def test_cv_move_f32_matches_oracle(vc, port, t, n):
     np.testing.assert_allclose(got_l, l_ref, rtol=1e-5, atol=1e-4)
 
 
+def _cv_f64(m, t, seed, state, obs):
+    """The model's move and log-likelihood in float64 on the FP32 kernel's
+    own inputs: its FP32 state, its Philox words (key {t, seed}, counter
+    {1, i, 0, 0}) and its 24-bit uniforms (the FP32 Box-Muller's (0, 1]
+    radius and [0, 1) angle).  The full Student-t density of both
+    coordinates (example/pf/include/pf.hpp:81-93 with its constants)."""
+    from math import lgamma
+    n = state.shape[1]
+    w0, w1, w2, w3 = particle_words(t, seed, n)
+    x = state.astype(np.float64)
+    if t == 0:
+        z1, z2 = normal_pair_f64(w0, w1)
+        z3, z4 = normal_pair_f64(w2, w3)
+        x = np.stack([m.sd_pos0 * z1, m.sd_pos0 * z2, m.sd_vel0 * z3,
+                      m.sd_vel0 * z4])
+    else:
+        z1, z2 = normal_pair_f64(w0, w1)
+        ax, ay = m.sigma_a * z1, m.sigma_a * z2
+        h = 0.5 * m.dt * m.dt
+        x = np.stack([x[0] + m.dt * x[2] + h * ax, x[1] + m.dt * x[3] + h * ay,
+                      x[2] + m.dt * ax, x[3] + m.dt * ay])
+    nu, s = m.nu, m.obs_scale
+    c = lgamma(0.5 * (nu + 1)) - lgamma(0.5 * nu) - 0.5 * np.log(nu * np.pi) \
+        - np.log(s)
+    qx = ((obs[0] - x[0]) / s) ** 2 / nu
+    qy = ((obs[1] - x[1]) / s) ** 2 / nu
+    ll = 2 * c - 0.5 * (nu + 1) * (np.log1p(qx) + np.log1p(qy))
+    return x, ll
+
+
 @pytest.mark.parametrize("t", [0, 1, 50])
-def test_cv_move_f32_vs_fp64_reference(vc, port, t):
-    """FP32 kernel against the FP64 computation on identical inputs."""
-    n = 2048
+def test_cv_move_f32_vs_fp64_on_same_uniforms(vc, t):
+    """The FP32 move and log-likelihood kernel against the FP64 evaluation of
+    the same model on identical inputs (same state, words and uniforms):
+    every element of the moved state and of the log-likelihood within 1e-5
+    relative (1e-5 absolute below magnitude 1), over 2^20 particles, so the
+    rare radius uniforms next to 1 are among them."""
+    n, seed = 1 << 20, 9
     rng = np.random.default_rng(t)
-    state64 = rng.normal(0, 2, (4, n))
-    state32 = state64.astype(np.float32)
+    state32 = rng.normal(0, 2, (4, n)).astype(np.float32)
     obs = np.array([1.5, 0.25])
     ds = dev(state32.copy())
     ll = dev(np.zeros(n, np.float32))
     m = _model(vc)
-    vc.call("vsmc_cuda_cv_move_f32", n, t, 9, ctypes.byref(m), P(obs),
+    vc.call("vsmc_cuda_cv_move_f32", n, t, seed, ctypes.byref(m), P(obs),
             ds.data_ptr(), ll.data_ptr(), None)
-    s_ref = state32.astype(np.float64)
-    l_ref = np.zeros(n)
-    om = _omodel()
-    if t == 0:
-        port.vo_pf_init_f64(n, 9, ctypes.byref(om), P(obs), P(s_ref), P(l_ref))
-    else:
-        port.vo_pf_move_f64(n, t, 9, ctypes.byref(om), P(obs), P(s_ref),
-                            P(l_ref))
-    # the FP32 radius uniform is (0,1] with 24 bits, the FP64 one [0,1) with
-    # 32 bits: compare the move only where both draw the same radius
+    x64, l64 = _cv_f64(m, t, seed, state32, obs)
     got = host(ds).astype(np.float64)
-    err = np.abs(got - s_ref) / np.maximum(1.0, np.abs(s_ref))
-    assert np.quantile(err, 0.99) < 1e-5
+    err = np.abs(got - x64) / np.maximum(1.0, np.abs(x64))
+    assert err.max() < 1e-5, (err.max(), np.unravel_index(err.argmax(),
+                                                          err.shape))
+    gl = host(ll).astype(np.float64)
+    el = np.abs(gl - l64) / np.maximum(1.0, np.abs(l64))
+    assert el.max() < 1e-5, (el.max(), el.argmax())
 
 
 @pytest.mark.parametrize("t", [0, 1, 99])

@@ -88,6 +88,30 @@ def default_model():
     return CvModel(0.1, 1.0, 0.5, 10.0, 2.0, 1.0)
 
 
+class PfStepDesc(ctypes.Structure):
+    """vsmc_cuda_pf_step_desc: the buffers of a filter's next step."""
+    _fields_ = [("state_in", ctypes.c_void_p), ("state_out", ctypes.c_void_p),
+                ("log_weight", ctypes.c_void_p), ("index", ctypes.c_void_p),
+                ("sources", ctypes.c_void_p), ("partials", ctypes.c_void_p),
+                ("scalars", ctypes.c_void_p), ("hist_mean", ctypes.c_void_p),
+                ("hist_ess", ctypes.c_void_p), ("hist_logz", ctypes.c_void_p),
+                ("hist_resampled", ctypes.c_void_p),
+                ("n", ctypes.c_size_t), ("stride", ctypes.c_size_t),
+                ("dim", ctypes.c_size_t), ("monitor_dim", ctypes.c_size_t),
+                ("max_steps", ctypes.c_size_t), ("max_grid", ctypes.c_size_t),
+                ("step", ctypes.c_size_t), ("seed", ctypes.c_uint32),
+                ("threshold", ctypes.c_double), ("stream", ctypes.c_void_p)]
+
+
+class PfStatus(ctypes.Structure):
+    """vsmc_cuda_pf_status: host view of a filter's device scalars."""
+    _fields_ = [("ess", ctypes.c_double), ("log_evidence", ctypes.c_double),
+                ("max_log_weight", ctypes.c_double),
+                ("sum_weight", ctypes.c_double),
+                ("mean", ctypes.c_double * 4), ("step", ctypes.c_size_t),
+                ("resampled", ctypes.c_int), ("monitor_dim", ctypes.c_int)]
+
+
 _RNGP = ctypes.POINTER(Rng)
 _MODELP = ctypes.POINTER(CvModel)
 _BMODELP = ctypes.POINTER(BearingsModel)
@@ -151,6 +175,15 @@ PROTOTYPES = {
     "vsmc_cuda_pf_stream": (I32, [VP, ctypes.POINTER(VP)]),
     "vsmc_cuda_pf_use_graph": (I32, [VP, I32]),
     "vsmc_cuda_pf_launch_step_kernel": (I32, [VP]),
+    "vsmc_cuda_pf_create_model": (
+        I32, [ctypes.POINTER(VP), SZ, SZ, SZ, I32, F64, U32, SZ, VP]),
+    "vsmc_cuda_pf_step_desc_get": (I32, [VP, ctypes.POINTER(PfStepDesc)]),
+    "vsmc_cuda_pf_step_commit": (I32, [VP]),
+    "vsmc_cuda_pf_reset": (I32, [VP]),
+    "vsmc_cuda_pf_resample_now": (I32, [VP]),
+    "vsmc_cuda_pf_set_equal": (I32, [VP]),
+    "vsmc_cuda_pf_weight_log": (I32, [VP, VP, I32]),
+    "vsmc_cuda_pf_get_status": (I32, [VP, ctypes.POINTER(PfStatus)]),
     "vsmc_cuda_batch_create": (
         I32, [ctypes.POINTER(VP), SZ, VP, VP, VP, VP, I32, F64, VP]),
     "vsmc_cuda_batch_create_bearings": (

@@ -262,7 +262,10 @@ __device__ __forceinline__ void tile_finish(const BatchArgs &a, uint32_t tile,
             S.resampled = 0; // finished: nothing left to resample
             S.gather = 0;
         } else {
-            const double prev_mass = First ? static_cast<double>(F.n) : TW;
+            // the previous weights' mass: their own normalizer (the
+            // single filter's step kernel uses the same one)
+            const double prev_mass =
+                First || S.resampled ? static_cast<double>(F.n) : S.S;
             if (!First) {
                 a.h_mean[2 * (F.hist_off + t - 1) + 0] = TX / TW;
                 a.h_mean[2 * (F.hist_off + t - 1) + 1] = TY / TW;

@@ -12,6 +12,8 @@
 #include <vector>
 
 #include "../../include/vsmc_cuda.h"
+#include "../../include/vsmc_cuda_device.cuh"
+#include "../../include/vsmc_cuda_filter.cuh"
 
 namespace vsmc_cuda
 {
@@ -34,12 +36,7 @@ void set_last_cuda_error(cudaError_t e);
 
 inline cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
 
-// Device-side error word bits (written with atomicOr, read by the host).
-enum : unsigned {
-    DEV_ERR_NONFINITE = 1u,  // NaN / inf / negative weight where forbidden
-    DEV_ERR_BOUND = 2u,      // an exactness bound was violated
-    DEV_ERR_INTERNAL = 4u,   // an index left its range
-};
+// The device-side error word bits DEV_ERR_* come from vsmc_cuda_filter.cuh.
 
 // ------------------------------------------------------- counter arithmetic
 
@@ -90,42 +87,9 @@ __host__ __device__ inline void ctr64_carry1(uint64_t c[4])
 
 // ------------------------------------------------------------- generators
 
-struct u32x4 {
-    uint32_t x, y, z, w;
-};
-
 struct u64x4 {
     uint64_t x, y, z, w;
 };
-
-// Philox4x32-10 on one counter block (no pre-increment).  Ten rounds; the
-// key is bumped by the Weyl constants before rounds 2..10.
-__device__ __forceinline__ u32x4 philox4x32_10(
-    uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
-    uint32_t k1)
-{
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        if (r > 0) {
-            k0 += 0x9E3779B9u;
-            k1 += 0xBB67AE85u;
-        }
-        // each 32 x 32 product once, as one widening multiply
-        const uint64_t pa = static_cast<uint64_t>(c2) * 0xCD9E8D57u;
-        const uint64_t pb = static_cast<uint64_t>(c0) * 0xD2511F53u;
-        const uint32_t hi_a = static_cast<uint32_t>(pa >> 32);
-        const uint32_t lo_a = static_cast<uint32_t>(pa);
-        const uint32_t hi_b = static_cast<uint32_t>(pb >> 32);
-        const uint32_t lo_b = static_cast<uint32_t>(pb);
-        const uint32_t n0 = hi_a ^ k0 ^ c1;
-        const uint32_t n2 = hi_b ^ k1 ^ c3;
-        c0 = n0;
-        c1 = lo_a;
-        c2 = n2;
-        c3 = lo_b;
-    }
-    return {c0, c1, c2, c3};
-}
 
 __device__ __forceinline__ uint64_t rotl64(uint64_t x, int r)
 {
@@ -167,39 +131,8 @@ __device__ __forceinline__ u64x4 threefry4x64_20(
     return {s0, s1, s2, s3};
 }
 
-// ---------------------------------------------------------------- u01
-// Integer -> real maps of the reference (rng/u01.hpp:126-172).  Every scale
-// is an exact power of two, so these are exact on any IEEE machine.
-
-// [0,1) from 32 bits in double: u * 2^-32
-__host__ __device__ __forceinline__ double u01_co_d(uint32_t u)
-{
-    return static_cast<double>(u) * 0x1p-32;
-}
-// [0,1) from 32 bits in float: (u >> 8) * 2^-24
-__host__ __device__ __forceinline__ float u01_co_f(uint32_t u)
-{
-    return static_cast<float>(u >> 8) * 0x1p-24f;
-}
-// (0,1] from 32 bits in float: (u >> 8) * 2^-24 + 2^-24
-__host__ __device__ __forceinline__ float u01_oc_f(uint32_t u)
-{
-    return static_cast<float>(u >> 8) * 0x1p-24f + 0x1p-24f;
-}
-// [0,1) from 64 bits in double: (u >> 11) * 2^-53
-__host__ __device__ __forceinline__ double u01_co_d64(uint64_t u)
-{
-    return static_cast<double>(u >> 11) * 0x1p-53;
-}
-// [0,1) from 64 bits in float: (u >> 40) * 2^-24
-__host__ __device__ __forceinline__ float u01_co_f64(uint64_t u)
-{
-    return static_cast<float>(u >> 40) * 0x1p-24f;
-}
-
-// 2*pi as the reference's const_pi_2 (math/constants.hpp:66)
-constexpr double kPi2 = 6.283185307179586476925286766559005768394;
-constexpr float kPi2f = 6.283185307179586476925286766559005768394f;
+// u32x4, philox4x32_10, the u01 maps, kPi2 and normal_pair_f come from
+// vsmc_cuda_device.cuh.
 
 // ------------------------------------------------------------ block scans
 

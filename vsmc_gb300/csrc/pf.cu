@@ -25,40 +25,70 @@ static float *buf32(vsmc_cuda_pf *pf, int which)
     return static_cast<float *>(which == 0 ? pf->state : pf->state2);
 }
 
-// A = the current state buffer, B = the other one
-static Pf32Args make_args32(vsmc_cuda_pf *pf)
+// Descriptor of the next step: it reads buffer cur and writes the other.
+static void step_desc(vsmc_cuda_pf *pf, vsmc_cuda_pf_step_desc *d)
 {
-    Pf32Args a = {};
-    const float *A = buf32(pf, pf->cur);
-    float *B = buf32(pf, 1 - pf->cur);
-    const size_t ld = pf->stride;
-    a.ax = A;
-    a.ay = A + ld;
-    a.avx = A + 2 * ld;
-    a.avy = A + 3 * ld;
-    a.bx = B;
-    a.by = B + ld;
-    a.bvx = B + 2 * ld;
-    a.bvy = B + 3 * ld;
+    *d = vsmc_cuda_pf_step_desc{};
+    d->state_in = buf32(pf, pf->cur);
+    d->state_out = buf32(pf, 1 - pf->cur);
+    d->log_weight = static_cast<float *>(pf->weight);
+    d->index = pf->idx;
+    d->sources = pf->empties;
+    d->partials = pf->part;
+    d->scalars = pf->sc;
+    d->hist_mean = pf->h_mean;
+    d->hist_ess = pf->h_ess;
+    d->hist_logz = pf->h_logz;
+    d->hist_resampled = pf->h_res;
+    d->n = pf->n;
+    d->stride = pf->stride;
+    d->dim = pf->dim;
+    d->monitor_dim = pf->mon_dim;
+    d->max_steps = pf->max_steps;
+    d->max_grid = pf->max_grid;
+    d->step = pf->t;
+    d->seed = pf->seed;
+    d->threshold = pf->threshold;
+    d->stream = pf->stream;
+}
+
+// Kernel arguments of the library's per-step kernels (genealogy record,
+// resample-move, materialize) with explicit input and output buffers.
+static PfStepArgs step_args(vsmc_cuda_pf *pf, const float *in, float *out)
+{
+    PfStepArgs a = {};
+    a.in = in;
+    a.out = out;
     a.lw = static_cast<float *>(pf->weight);
     a.idx = pf->idx;
     a.srcs = pf->empties;
-    a.n = static_cast<uint32_t>(pf->n);
-    a.seed = pf->seed;
-    a.max_steps = static_cast<uint32_t>(pf->max_steps);
-    a.threshold = pf->threshold;
-    a.c = make_cv_const<float>(pf->model);
-    a.obs = pf->obs;
     a.part = pf->part;
     a.sc = pf->sc;
     a.h_mean = pf->h_mean;
     a.h_ess = pf->h_ess;
     a.h_logz = pf->h_logz;
     a.h_res = pf->h_res;
+    a.stride = pf->stride;
+    a.n = static_cast<uint32_t>(pf->n);
+    a.seed = pf->seed;
+    a.max_steps = static_cast<uint32_t>(pf->max_steps);
+    a.threshold = pf->threshold;
     return a;
 }
 
-static Rs32Args make_rs_args32(vsmc_cuda_pf *pf)
+static CvModel cv_model(vsmc_cuda_pf *pf)
+{
+    CvModel m;
+    m.c = make_cv_const<float>(pf->model);
+    m.obs = pf->obs;
+    m.max_steps = static_cast<uint32_t>(pf->max_steps);
+    return m;
+}
+
+// Resampling arguments; mon_state is the state the resample draws from
+// (the last step's output), whose resampled mean becomes the monitor.
+static Rs32Args make_rs_args32(
+    vsmc_cuda_pf *pf, const float *mon_state, int force)
 {
     Rs32Args r = {};
     r.lw = static_cast<const float *>(pf->weight);
@@ -67,6 +97,7 @@ static Rs32Args make_rs_args32(vsmc_cuda_pf *pf)
     r.shift = pf->shift;
     r.chunk = pf->chunk_rs;
     r.scheme = pf->scheme;
+    r.force = force;
     r.qpart = pf->qpart;
     r.epart = pf->epart;
     r.cpart = pf->cpart;
@@ -76,12 +107,20 @@ static Rs32Args make_rs_args32(vsmc_cuda_pf *pf)
     r.marks = pf->marks;
     r.srcs = pf->empties;
     r.sc = pf->sc;
+    r.mon_state = mon_state;
+    r.stride = pf->stride;
+    r.mon_dim = static_cast<uint32_t>(pf->mon_dim);
+    r.max_steps = static_cast<uint32_t>(pf->max_steps);
+    r.mon_part = pf->part;
+    r.h_mean = pf->h_mean;
+    r.h_res = pf->h_res;
     return r;
 }
 
-static void launch_resample32(vsmc_cuda_pf *pf)
+static void launch_resample32(
+    vsmc_cuda_pf *pf, const float *mon_state, int force)
 {
-    const Rs32Args r = make_rs_args32(pf);
+    const Rs32Args r = make_rs_args32(pf, mon_state, force);
     cudaStream_t st = pf->stream;
     k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     launch_rs32_count(pf->grid_rs, st, r);
@@ -90,42 +129,46 @@ static void launch_resample32(vsmc_cuda_pf *pf)
     k_rs32_fill<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
 }
 
-// the fused step kernel of one FP32 step (reads buffer cur, writes the
+// the fused step kernel of the built-in model (reads buffer cur, writes the
 // other)
-static void launch_step_kernel32(
-    vsmc_cuda_pf *pf, bool first, const Pf32Args &a)
+static int launch_step_kernel32(vsmc_cuda_pf *pf, bool first)
 {
-    if (first)
-        k_pf32_step<true><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
-    else
-        k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
+    vsmc_cuda_pf_step_desc d;
+    step_desc(pf, &d);
+    d.step = first ? 0 : (pf->t > 0 ? pf->t : 1);
+    const int rc = pf_step_launch(d, cv_model(pf));
+    if (rc == VSMC_CUDA_ERR_CUDA)
+        set_last_cuda_error(cudaGetLastError());
+    return rc;
 }
 
 // the kernels that follow resampling every step: genealogy row, and the
 // resample-move sweeps (whose output goes back to buffer cur)
-static void launch_post32(vsmc_cuda_pf *pf, const Pf32Args &a)
+static void launch_post32(vsmc_cuda_pf *pf)
 {
+    const PfStepArgs a =
+        step_args(pf, buf32(pf, 1 - pf->cur), buf32(pf, pf->cur));
     if (pf->record_gen)
         k_pf32_record<<<grid_for(pf->n, kPfBlock, 4, 8), kPfBlock, 0,
             pf->stream>>>(a, pf->gen);
     if (pf->mcmc_sweeps > 0) {
-        float *A = buf32(pf, pf->cur);
-        const size_t ld = pf->stride;
         const float sa = static_cast<float>(pf->model.sigma_a);
         k_pf32_mcmc<<<grid_for(pf->n, kPfBlock, 1, 8), kPfBlock, 0,
-            pf->stream>>>(a, A, A + ld, A + 2 * ld, A + 3 * ld,
+            pf->stream>>>(a, make_cv_const<float>(pf->model), pf->obs,
             pf->mcmc_sweeps, pf->mcmc_scale, 1.0f / (sa * sa), pf->h_acc);
         k_pf32_clear_gather<<<1, 1, 0, pf->stream>>>(pf->sc);
     }
 }
 
-// the kernels of one FP32 step, launched on the stream
+// the kernels of one FP32 step of the built-in model, launched on the
+// stream
 static int launch_step32(vsmc_cuda_pf *pf, bool first)
 {
-    const Pf32Args a = make_args32(pf);
-    launch_step_kernel32(pf, first, a);
-    launch_resample32(pf);
-    launch_post32(pf, a);
+    const int rc = launch_step_kernel32(pf, first);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    launch_resample32(pf, buf32(pf, 1 - pf->cur), 0);
+    launch_post32(pf);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
 }
@@ -174,16 +217,6 @@ static int step32(vsmc_cuda_pf *pf)
     return VSMC_CUDA_OK;
 }
 
-static int final_mean32(vsmc_cuda_pf *pf)
-{
-    const Pf32Args a = make_args32(pf);
-    const int grid = grid_for(pf->n, kPfBlock, 16, 8);
-    k_pf32_final_mean<<<grid, kPfBlock, 0, pf->stream>>>(
-        a, static_cast<uint32_t>(pf->t - 1));
-    VSMC_CUDA_CHECK_LAUNCH();
-    return VSMC_CUDA_OK;
-}
-
 // apply a pending resampling gather to the stored state (host-side views)
 static int materialize32(vsmc_cuda_pf *pf)
 {
@@ -193,9 +226,10 @@ static int materialize32(vsmc_cuda_pf *pf)
     VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
     if (!gather)
         return VSMC_CUDA_OK;
-    const Pf32Args a = make_args32(pf);
+    const PfStepArgs a =
+        step_args(pf, buf32(pf, pf->cur), buf32(pf, 1 - pf->cur));
     k_pf32_materialize<<<grid_for(pf->n, kPfBlock, 4, 8), kPfBlock, 0,
-        pf->stream>>>(a);
+        pf->stream>>>(a, static_cast<uint32_t>(pf->dim));
     k_pf32_clear_gather<<<1, 1, 0, pf->stream>>>(pf->sc);
     VSMC_CUDA_CHECK_LAUNCH();
     pf->cur = 1 - pf->cur;
@@ -205,16 +239,7 @@ static int materialize32(vsmc_cuda_pf *pf)
 __global__ void k_reset_scalars(PfScalars *sc, uint32_t seed)
 {
     PfScalars z = {};
-    z.M = 0;
-    z.S = 0;
-    z.logz = 0;
-    z.ess = 0;
-    z.Q = 0;
-    z.step = 0;
     z.resampled = 1;
-    z.done = 0;
-    z.err = 0;
-    z.nempty = 0;
     z.rindex = 4;
     // resampling engine: key {0, seed}, counter {0, 0, 1, 0}
     z.rkey[0] = 0;
@@ -231,6 +256,127 @@ static int reset_scalars(vsmc_cuda_pf *pf)
     k_reset_scalars<<<1, 1, 0, pf->stream>>>(pf->sc, pf->seed);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
+}
+
+// Weight::set_equal: every weight equal, the stored log-weights stale
+__global__ void k_pf32_set_equal(PfScalars *sc, uint32_t n)
+{
+    sc->resampled = 1;
+    sc->M = 0;
+    sc->Mf = 0;
+    sc->S = static_cast<double>(n);
+    sc->ess = static_cast<double>(n);
+}
+
+// Equal weights written out (lw = 0, max 0), for a resample the host asks
+// for while the weights are equal; the state keeps any pending gather.
+__global__ void __launch_bounds__(kPfBlock) k_pf32_lw_zero(
+    float *lw, uint32_t n, PfScalars *sc)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x)
+        lw[i] = 0.0f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->resampled = 0;
+        sc->M = 0;
+        sc->Mf = 0;
+        sc->S = static_cast<double>(n);
+        sc->ess = static_cast<double>(n);
+    }
+}
+
+// Weight::set_log / add_log from n doubles (v): lw = v (+ the current
+// lw - M unless the weights are equal), then the step kernel's reduction:
+// (max, sum exp, sum exp^2) and the monitor's weighted sums over the
+// current particles (read through a pending gather); the last block sets
+// M, S, ESS, the monitor mean and, for add, the log-evidence increment.
+__global__ void __launch_bounds__(kPfBlock) k_pf32_weight_log(
+    const PfStepArgs a, const double *v, int add, uint32_t mon_dim)
+{
+    const bool equal = a.sc->resampled != 0;
+    const bool gather = a.sc->gather != 0;
+    const float Mprev = static_cast<float>(a.sc->M);
+    LseMon<kMaxMonitorDim> acc = lse_empty<kMaxMonitorDim>();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += gridDim.x * blockDim.x) {
+        float l = static_cast<float>(v[i]);
+        if (add && !equal)
+            l += a.lw[i] - Mprev;
+        a.lw[i] = l;
+        uint32_t src = gather ? pf_source(a.srcs, a.idx[i]) : i;
+        if (src >= a.n) {
+            atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+            src = 0;
+        }
+        float x[kMaxMonitorDim];
+#pragma unroll
+        for (int d = 0; d < kMaxMonitorDim; ++d)
+            x[d] = static_cast<uint32_t>(d) < mon_dim
+                ? a.in[d * a.stride + src]
+                : 0.0f;
+        acc.push(l, x);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+        acc.merge(acc.shfl_xor(d));
+    constexpr int kW = kPfBlock / 32;
+    __shared__ LseMon<kMaxMonitorDim> shw[kW];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        shw[wid] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        LseMon<kMaxMonitorDim> w = shw[0];
+        for (int k = 1; k < kW; ++k)
+            w.merge(shw[k]);
+        PfPartial p;
+        p.m = w.m;
+        p.s = w.s;
+        p.s2 = w.s2;
+#pragma unroll
+        for (int d = 0; d < kMaxMonitorDim; ++d)
+            p.mon[d] = w.mon[d];
+        a.part[blockIdx.x] = p;
+        __threadfence();
+        is_last = atomicAdd(&a.sc->done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!is_last || threadIdx.x != 0)
+        return;
+    __threadfence();
+    double M = -INFINITY;
+    for (uint32_t b = 0; b < gridDim.x; ++b)
+        M = fmax(M, __ldcg(&a.part[b].m));
+    double S = 0, S2 = 0, MON[kMaxMonitorDim] = {};
+    for (uint32_t b = 0; b < gridDim.x; ++b) {
+        const double pm = __ldcg(&a.part[b].m);
+        if (!(pm > -INFINITY))
+            continue;
+        const double f = exp(pm - M);
+        S += __ldcg(&a.part[b].s) * f;
+        S2 += __ldcg(&a.part[b].s2) * f * f;
+#pragma unroll
+        for (int d = 0; d < kMaxMonitorDim; ++d)
+            MON[d] += __ldcg(&a.part[b].mon[d]) * f;
+    }
+    PfScalars &sc = *a.sc;
+    if (!(S > 0))
+        sc.err |= DEV_ERR_NONFINITE;
+    if (add) {
+        const double prev_mass = equal ? static_cast<double>(a.n) : sc.S;
+        sc.logz += M + log(S) - log(prev_mass);
+    }
+#pragma unroll
+    for (int d = 0; d < kMaxMonitorDim; ++d)
+        if (static_cast<uint32_t>(d) < mon_dim)
+            sc.mean[d] = MON[d] / S;
+    sc.M = M;
+    sc.Mf = static_cast<float>(M);
+    sc.S = S;
+    sc.ess = S * S / S2;
+    sc.resampled = 0;
+    sc.done = 0;
 }
 
 static void free_all(vsmc_cuda_pf *pf)
@@ -279,17 +425,13 @@ static int sync_and_check(vsmc_cuda_pf *pf)
     return VSMC_CUDA_OK;
 }
 
-} // namespace vsmc_cuda
-
-extern "C" {
-
-int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
-    int scheme, double threshold, uint32_t seed,
-    const vsmc_cuda_cv_model *model, size_t max_steps, void *stream)
+// Shared constructor of the built-in (model != null) and the user-model
+// filters.
+static int pf_create(vsmc_cuda_pf **out, size_t n, size_t dim,
+    size_t mon_dim, int precision, int scheme, double threshold,
+    uint32_t seed, const vsmc_cuda_cv_model *model, size_t max_steps,
+    void *stream)
 {
-    if (out == nullptr || !valid_cv_model(model) ||
-        (precision != 32 && precision != 64) || std::isnan(threshold))
-        return VSMC_CUDA_ERR_ARG;
     *out = nullptr;
     if (n < 1 || n >= (size_t(1) << 31) || max_steps < 1 ||
         max_steps > (size_t(1) << 31))
@@ -304,11 +446,15 @@ int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
         return VSMC_CUDA_ERR_ALLOC;
     pf->n = n;
     pf->stride = (n + 255) / 256 * 256;
+    pf->dim = dim;
+    pf->mon_dim = mon_dim;
+    pf->custom = model == nullptr;
     pf->precision = precision;
     pf->scheme = scheme;
     pf->threshold = threshold;
     pf->seed = seed;
-    pf->model = *model;
+    if (model)
+        pf->model = *model;
     pf->max_steps = max_steps;
     pf->stream = as_stream(stream);
     if (pf->stream == nullptr) {
@@ -331,24 +477,25 @@ int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
             return rc;                                                        \
         }                                                                     \
     } while (0)
-    PF_TRY(dalloc(reinterpret_cast<char **>(&pf->state), esz * 4 * pf->stride));
-    PF_TRY(dalloc(reinterpret_cast<char **>(&pf->weight), esz * n));
-    PF_TRY(dalloc(&pf->obs, 2 * max_steps));
-    PF_TRY(dalloc(&pf->h_mean, 2 * max_steps));
+    PF_TRY(dalloc(reinterpret_cast<char **>(&pf->state),
+        esz * dim * pf->stride));
+    PF_TRY(dalloc(reinterpret_cast<char **>(&pf->weight), esz * pf->stride));
+    if (model)
+        PF_TRY(dalloc(&pf->obs, 2 * max_steps));
+    PF_TRY(dalloc(&pf->h_mean, (mon_dim ? mon_dim : 1) * max_steps));
     PF_TRY(dalloc(&pf->h_ess, max_steps));
     PF_TRY(dalloc(&pf->h_logz, max_steps));
     PF_TRY(dalloc(&pf->h_res, max_steps));
     PF_TRY(dalloc(&pf->sc, 1));
     if (precision == 32) {
-        int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &occ, k_pf32_step<false>, kPfBlock, 0) != cudaSuccess ||
-            occ < 1)
-            occ = 4;
-        const size_t ntiles = (n + kPfTile - 1) / kPfTile;
-        size_t g = static_cast<size_t>(num_sms()) * static_cast<size_t>(occ);
-        pf->grid_step = static_cast<int>(ntiles < g ? ntiles : g);
-        size_t grs = static_cast<size_t>(num_sms()) * 4;
+        if (model) {
+            // looked up here, outside any stream capture of a step
+            pf_step_occupancy<CvModel, true>();
+            pf_step_occupancy<CvModel, false>();
+        }
+        const size_t sms = static_cast<size_t>(num_sms());
+        pf->max_grid = sms * 16;
+        size_t grs = sms * 4;
         size_t chunk = (n + grs - 1) / grs;
         chunk = (chunk + kPfTile - 1) / kPfTile * kPfTile;
         pf->chunk_rs = static_cast<uint32_t>(chunk);
@@ -357,13 +504,13 @@ int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
         while ((size_t(1) << lg) < n)
             ++lg;
         pf->shift = static_cast<uint32_t>(63 - lg);
-        PF_TRY(dalloc(&pf->part, pf->grid_step > 1024 ? pf->grid_step : 1024));
+        PF_TRY(dalloc(&pf->part, pf->max_grid));
         PF_TRY(dalloc(&pf->qpart, pf->grid_rs));
         PF_TRY(dalloc(&pf->epart, pf->grid_rs));
         PF_TRY(dalloc(&pf->cpart, pf->grid_rs));
         PF_TRY(dalloc(&pf->mpart, pf->grid_rs));
         PF_TRY(dalloc(reinterpret_cast<char **>(&pf->state2),
-            esz * 4 * pf->stride));
+            esz * dim * pf->stride));
         PF_TRY(dalloc(&pf->rep, n + 4));
         PF_TRY(dalloc(&pf->idx, pf->stride));
         PF_TRY(dalloc(&pf->marks, n));
@@ -380,6 +527,34 @@ int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
     return VSMC_CUDA_OK;
 }
 
+} // namespace vsmc_cuda
+
+extern "C" {
+
+int vsmc_cuda_pf_create(vsmc_cuda_pf **out, size_t n, int precision,
+    int scheme, double threshold, uint32_t seed,
+    const vsmc_cuda_cv_model *model, size_t max_steps, void *stream)
+{
+    if (out == nullptr || !valid_cv_model(model) ||
+        (precision != 32 && precision != 64) || std::isnan(threshold))
+        return VSMC_CUDA_ERR_ARG;
+    return pf_create(out, n, 4, 2, precision, scheme, threshold, seed, model,
+        max_steps, stream);
+}
+
+int vsmc_cuda_pf_create_model(vsmc_cuda_pf **out, size_t n, size_t dim,
+    size_t monitor_dim, int scheme, double threshold, uint32_t seed,
+    size_t max_steps, void *stream)
+{
+    if (out == nullptr || std::isnan(threshold) || dim < 1 ||
+        dim > static_cast<size_t>(kMaxFilterDim) ||
+        monitor_dim > static_cast<size_t>(kMaxMonitorDim) ||
+        monitor_dim > dim)
+        return VSMC_CUDA_ERR_ARG;
+    return pf_create(out, n, dim, monitor_dim, 32, scheme, threshold, seed,
+        nullptr, max_steps, stream);
+}
+
 int vsmc_cuda_pf_destroy(vsmc_cuda_pf *pf)
 {
     if (pf == nullptr)
@@ -392,14 +567,120 @@ int vsmc_cuda_pf_destroy(vsmc_cuda_pf *pf)
 
 int vsmc_cuda_pf_launch_step_kernel(vsmc_cuda_pf *pf)
 {
-    if (pf == nullptr || pf->precision != 32 || pf->t == 0)
+    if (pf == nullptr || pf->precision != 32 || pf->custom || pf->t == 0)
         return VSMC_CUDA_ERR_ARG;
-    const Pf32Args a = make_args32(pf);
-    k_pf32_step<false><<<pf->grid_step, kPfBlock, 0, pf->stream>>>(a);
-    VSMC_CUDA_CHECK_LAUNCH();
+    const int rc = launch_step_kernel32(pf, false);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
     pf->cur = 1 - pf->cur;
     ++pf->t;
-    pf->mean_pending = true;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_step_desc_get(vsmc_cuda_pf *pf, vsmc_cuda_pf_step_desc *d)
+{
+    if (pf == nullptr || d == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
+    if (pf->t >= (size_t(1) << 32) - 1)
+        return VSMC_CUDA_ERR_SIZE;
+    if (pf->t == 0) {
+        const int rc = reset_scalars(pf);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+    }
+    step_desc(pf, d);
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_step_commit(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
+    pf->cur = 1 - pf->cur;
+    if (pf->threshold >= 0)
+        launch_resample32(pf, buf32(pf, pf->cur), 0);
+    VSMC_CUDA_CHECK_LAUNCH();
+    ++pf->t;
+    pf->host_equal = false;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_reset(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr || pf->precision != 32 || !pf->custom)
+        return VSMC_CUDA_ERR_ARG;
+    pf->t = 0;
+    pf->host_equal = false;
+    return reset_scalars(pf);
+}
+
+int vsmc_cuda_pf_resample_now(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr || pf->precision != 32 || pf->t == 0)
+        return VSMC_CUDA_ERR_ARG;
+    if (pf->host_equal) {
+        // equal weights: resample on them, not on the stale log-weights
+        k_pf32_lw_zero<<<grid_for(pf->n, kPfBlock, 4, 4), kPfBlock, 0,
+            pf->stream>>>(static_cast<float *>(pf->weight),
+            static_cast<uint32_t>(pf->n), pf->sc);
+    }
+    launch_resample32(pf, buf32(pf, pf->cur), 1);
+    VSMC_CUDA_CHECK_LAUNCH();
+    pf->host_equal = true;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_set_equal(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
+    if (pf->host_equal)
+        return VSMC_CUDA_OK;
+    k_pf32_set_equal<<<1, 1, 0, pf->stream>>>(
+        pf->sc, static_cast<uint32_t>(pf->n));
+    VSMC_CUDA_CHECK_LAUNCH();
+    pf->host_equal = true;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_weight_log(vsmc_cuda_pf *pf, const double *lw_dev, int add)
+{
+    if (pf == nullptr || lw_dev == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
+    const PfStepArgs a =
+        step_args(pf, buf32(pf, pf->cur), buf32(pf, 1 - pf->cur));
+    int grid = grid_for(pf->n, kPfBlock, 4, 4);
+    if (static_cast<size_t>(grid) > pf->max_grid)
+        grid = static_cast<int>(pf->max_grid);
+    k_pf32_weight_log<<<grid, kPfBlock, 0, pf->stream>>>(
+        a, lw_dev, add != 0, static_cast<uint32_t>(pf->mon_dim));
+    VSMC_CUDA_CHECK_LAUNCH();
+    pf->host_equal = false;
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_pf_get_status(vsmc_cuda_pf *pf, vsmc_cuda_pf_status *out)
+{
+    if (pf == nullptr || out == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
+    PfScalars sc;
+    VSMC_CUDA_TRY(cudaMemcpyAsync(
+        &sc, pf->sc, sizeof(sc), cudaMemcpyDeviceToHost, pf->stream));
+    VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
+    *out = vsmc_cuda_pf_status{};
+    out->ess = sc.ess;
+    out->log_evidence = sc.logz;
+    out->max_log_weight = sc.M;
+    out->sum_weight = sc.S;
+    for (size_t d = 0; d < pf->mon_dim; ++d)
+        out->mean[d] = sc.mean[d];
+    out->step = pf->t;
+    out->resampled = sc.resampled;
+    out->monitor_dim = static_cast<int>(pf->mon_dim);
+    if (sc.err & DEV_ERR_NONFINITE)
+        return VSMC_CUDA_ERR_NONFINITE;
+    if (sc.err)
+        return VSMC_CUDA_ERR_INTERNAL;
     return VSMC_CUDA_OK;
 }
 
@@ -527,12 +808,13 @@ static int pf_next(vsmc_cuda_pf *pf)
     return VSMC_CUDA_OK;
 }
 
+// The FP64 filter records step t's monitor inside step t + 1; its last step
+// needs one more kernel.  The FP32 step records its own.
 static int pf_flush_mean(vsmc_cuda_pf *pf)
 {
-    if (!pf->mean_pending || pf->t == 0)
+    if (pf->precision == 32 || !pf->mean_pending || pf->t == 0)
         return VSMC_CUDA_OK;
-    const int rc =
-        pf->precision == 32 ? final_mean32(pf) : pf64_final_mean(pf);
+    const int rc = pf64_final_mean(pf);
     if (rc == VSMC_CUDA_OK)
         pf->mean_pending = false;
     return rc;
@@ -540,7 +822,7 @@ static int pf_flush_mean(vsmc_cuda_pf *pf)
 
 int vsmc_cuda_pf_initialize(vsmc_cuda_pf *pf, const double *obs_dev)
 {
-    if (pf == nullptr || obs_dev == nullptr)
+    if (pf == nullptr || obs_dev == nullptr || pf->custom)
         return VSMC_CUDA_ERR_ARG;
     VSMC_CUDA_TRY(cudaMemcpyAsync(pf->obs, obs_dev, 2 * sizeof(double),
         cudaMemcpyDeviceToDevice, pf->stream));
@@ -549,7 +831,7 @@ int vsmc_cuda_pf_initialize(vsmc_cuda_pf *pf, const double *obs_dev)
 
 int vsmc_cuda_pf_iterate(vsmc_cuda_pf *pf, const double *obs_dev)
 {
-    if (pf == nullptr || obs_dev == nullptr)
+    if (pf == nullptr || obs_dev == nullptr || pf->custom)
         return VSMC_CUDA_ERR_ARG;
     if (pf->t == 0)
         return VSMC_CUDA_ERR_ARG;
@@ -562,7 +844,7 @@ int vsmc_cuda_pf_iterate(vsmc_cuda_pf *pf, const double *obs_dev)
 
 int vsmc_cuda_pf_run_device(vsmc_cuda_pf *pf, size_t T, const double *obs_dev)
 {
-    if (pf == nullptr || obs_dev == nullptr || T == 0)
+    if (pf == nullptr || obs_dev == nullptr || T == 0 || pf->custom)
         return VSMC_CUDA_ERR_ARG;
     if (T > pf->max_steps)
         return VSMC_CUDA_ERR_SIZE;
@@ -582,15 +864,15 @@ int vsmc_cuda_pf_history(vsmc_cuda_pf *pf, size_t T, double *mean_host,
 {
     if (pf == nullptr)
         return VSMC_CUDA_ERR_ARG;
-    if (T > pf->t)
+    if (T > pf->t || T > pf->max_steps)
         return VSMC_CUDA_ERR_SIZE;
     int rc = pf_flush_mean(pf);
     if (rc != VSMC_CUDA_OK)
         return rc;
     cudaStream_t st = pf->stream;
-    if (mean_host)
+    if (mean_host && pf->mon_dim > 0)
         VSMC_CUDA_TRY(cudaMemcpyAsync(mean_host, pf->h_mean,
-            2 * T * sizeof(double), cudaMemcpyDeviceToHost, st));
+            pf->mon_dim * T * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (ess_host)
         VSMC_CUDA_TRY(cudaMemcpyAsync(ess_host, pf->h_ess, T * sizeof(double),
             cudaMemcpyDeviceToHost, st));
@@ -617,7 +899,7 @@ static void drop_graphs(vsmc_cuda_pf *pf)
 
 int vsmc_cuda_pf_record_genealogy(vsmc_cuda_pf *pf, int on)
 {
-    if (pf == nullptr || pf->precision != 32)
+    if (pf == nullptr || pf->precision != 32 || pf->custom)
         return VSMC_CUDA_ERR_ARG;
     if (on && pf->gen == nullptr) {
         void *p = nullptr;
@@ -632,7 +914,7 @@ int vsmc_cuda_pf_record_genealogy(vsmc_cuda_pf *pf, int on)
 
 int vsmc_cuda_pf_set_mcmc(vsmc_cuda_pf *pf, size_t sweeps, double scale)
 {
-    if (pf == nullptr || pf->precision != 32 || !(scale >= 0) ||
+    if (pf == nullptr || pf->precision != 32 || pf->custom || !(scale >= 0) ||
         !(pf->model.sigma_a > 0) || pf->t != 0)
         return VSMC_CUDA_ERR_ARG;
     if (sweeps > 1024)
@@ -674,7 +956,8 @@ int vsmc_cuda_pf_print(vsmc_cuda_pf *pf, size_t T, char sep, char *buf,
 {
     if (pf == nullptr || len == nullptr || T > pf->max_steps)
         return VSMC_CUDA_ERR_ARG;
-    std::vector<double> mean(2 * T), ess(T), logz(T);
+    const size_t md = pf->mon_dim;
+    std::vector<double> mean(md * T + 1), ess(T), logz(T);
     std::vector<int> res(T);
     if (T > 0) {
         const int rc = vsmc_cuda_pf_history(
@@ -683,7 +966,7 @@ int vsmc_cuda_pf_print(vsmc_cuda_pf *pf, size_t T, char sep, char *buf,
             return rc;
     }
     if (pf->mcmc_sweeps == 0)
-        return vsmc_cuda_sampler_print(T, pf->n, res.data(), ess.data(), 2,
+        return vsmc_cuda_sampler_print(T, pf->n, res.data(), ess.data(), md,
             "pos", mean.data(), 0, nullptr, sep, buf, cap, len);
     // the move accepts every particle; the MCMC column is the accept count
     std::vector<uint32_t> acc(T);
@@ -703,7 +986,7 @@ int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
     double *mean_host, double *ess_host, int *resampled_host,
     double *logz_host)
 {
-    if (pf == nullptr || obs_host == nullptr || T == 0)
+    if (pf == nullptr || obs_host == nullptr || T == 0 || pf->custom)
         return VSMC_CUDA_ERR_ARG;
     if (T > pf->max_steps)
         return VSMC_CUDA_ERR_SIZE;

@@ -27,395 +27,129 @@ namespace vsmc_cuda
 {
 
 // ------------------------------------------------------------ fused step
+//
+// The step kernel itself is the model template k_pf_step of
+// vsmc_cuda_filter.cuh; the library instantiates it with CvModel below.
 
-// Per-particle body of the fused kernel.  First: draw the prior at t = 0.
-// x..vy hold the particle as read (after any resampling gather) on entry and
-// the moved particle on exit.
-template <bool First>
-__device__ __forceinline__ void step_one(const Pf32Args &a, uint32_t i,
-    uint32_t t, float ox, float oy, int resampled, float Mprev, float &x,
-    float &y, float &vx, float &vy, float &lw, float &m, float &s, float &s2,
-    float &sx, float &sy, float &sw)
-{
-    const u32x4 w = particle_block(t, a.seed, i);
-    float lw_old = 0.0f;
-    if (First) {
-        float z1, z2, z3, z4;
-        normal_pair_f(w.x, w.y, z1, z2);
-        normal_pair_f(w.z, w.w, z3, z4);
-        x = a.c.sd_pos0 * z1;
-        y = a.c.sd_pos0 * z2;
-        vx = a.c.sd_vel0 * z3;
-        vy = a.c.sd_vel0 * z4;
-    } else {
-        lw_old = resampled ? 0.0f : lw - Mprev;
-        const float wo = resampled ? 1.0f : __expf(lw_old);
-        sx += wo * x;
-        sy += wo * y;
-        sw += wo;
-        float z1, z2;
-        normal_pair_f(w.x, w.y, z1, z2);
-        cv_move(a.c, a.c.sigma_a * z1, a.c.sigma_a * z2, x, y, vx, vy);
+// The constant-velocity / Student-t model of the benchmark as a step-kernel
+// model: dim 4 (x, y, vx, vy), the weighted mean of (x, y) recorded.
+// Observation t (clamped to the last one past max_steps, for profiling
+// loops that run past the horizon) is read once per thread and step.
+struct CvModel {
+    static constexpr int dim = 4;
+    static constexpr int monitor_dim = 2;
+    struct step_type {
+        float ox, oy;
+    };
+
+    CvConst<float> c;
+    const double *obs; // max_steps x 2 (device)
+    uint32_t max_steps;
+
+    __device__ __forceinline__ step_type step(uint32_t t) const
+    {
+        const uint32_t to = t < max_steps ? t : max_steps - 1;
+        return {static_cast<float>(obs[2 * to + 0]),
+            static_cast<float>(obs[2 * to + 1])};
     }
-    lw = lw_old + cv_loglik(a.c, ox, oy, x, y);
-    lse_push(lw, m, s, s2);
-}
+
+    __device__ __forceinline__ void init(
+        const step_type &, ParticleRng &rng, float (&x)[4]) const
+    {
+        float z1, z2, z3, z4;
+        rng.normal_pair(z1, z2);
+        rng.normal_pair(z3, z4);
+        x[0] = c.sd_pos0 * z1;
+        x[1] = c.sd_pos0 * z2;
+        x[2] = c.sd_vel0 * z3;
+        x[3] = c.sd_vel0 * z4;
+    }
+
+    __device__ __forceinline__ void move(
+        const step_type &, ParticleRng &rng, float (&x)[4]) const
+    {
+        float z1, z2;
+        rng.normal_pair(z1, z2);
+        cv_move(c, c.sigma_a * z1, c.sigma_a * z2, x[0], x[1], x[2], x[3]);
+    }
+
+    __device__ __forceinline__ float log_likelihood(
+        const step_type &s, const float (&x)[4]) const
+    {
+        return cv_loglik(c, s.ox, s.oy, x[0], x[1]);
+    }
+};
 
 __device__ __forceinline__ float4 ld4(const float *p, uint32_t i)
 {
-    return __ldcs(reinterpret_cast<const float4 *>(p + i));
+    return pf_ld4(p + i);
 }
 
-__device__ __forceinline__ void st4(float *p, uint32_t i, float4 v)
+// Monitor of equal-weight particles: block sums of the first mon_dim rows
+// of `rows` (FP32 per thread, FP64 across warps) go to part[block].mon; the
+// last block to finish (sc->done2) writes their mean to sc->mean and, for
+// a recorded step, to h_mean[t].  Called by every thread of the block.
+__device__ __forceinline__ void equal_mean_finish(const float (&acc)[kMaxMonitorDim],
+    uint32_t mon_dim, double inv_n, PfPartial *part, PfScalars *sc,
+    double *h_mean, uint32_t t, uint32_t max_steps)
 {
-    __stcs(reinterpret_cast<float4 *>(p + i), v);
-}
-
-// source slot of slot i after a resample: idx[i] >= 0 is the slot itself
-// (a parent), idx[i] = -(e + 1) is the e-th empty slot, filled from srcs[e]
-__device__ __forceinline__ uint32_t source_of(
-    const int32_t *idx, const uint32_t *srcs, int32_t v)
-{
-    return v >= 0 ? static_cast<uint32_t>(v) : __ldcg(srcs + (-v - 1));
-    (void)idx;
-}
-
-// Reads the state of particles i0..i0+3 (gathered through idx after a
-// resample).
-__device__ __forceinline__ void load_group(const Pf32Args &a, uint32_t i0,
-    bool gather, float4 &X, float4 &Y, float4 &VX, float4 &VY)
-{
-    if (gather) {
-        const int4 I = __ldcs(reinterpret_cast<const int4 *>(a.idx + i0));
-        const int b = static_cast<int>(i0);
-        if (I.x == b && I.y == b + 1 && I.z == b + 2 && I.w == b + 3) {
-            X = ld4(a.ax, i0);
-            Y = ld4(a.ay, i0);
-            VX = ld4(a.avx, i0);
-            VY = ld4(a.avy, i0);
-        } else {
-            uint32_t s0 = source_of(a.idx, a.srcs, I.x);
-            uint32_t s1 = source_of(a.idx, a.srcs, I.y);
-            uint32_t s2 = source_of(a.idx, a.srcs, I.z);
-            uint32_t s3 = source_of(a.idx, a.srcs, I.w);
-            if (max(max(s0, s1), max(s2, s3)) >= a.n) {
-                // an index outside the particles: record it, read slot 0
-                atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
-                s0 = s0 < a.n ? s0 : 0;
-                s1 = s1 < a.n ? s1 : 0;
-                s2 = s2 < a.n ? s2 : 0;
-                s3 = s3 < a.n ? s3 : 0;
-            }
-            X = make_float4(a.ax[s0], a.ax[s1], a.ax[s2], a.ax[s3]);
-            Y = make_float4(a.ay[s0], a.ay[s1], a.ay[s2], a.ay[s3]);
-            VX = make_float4(a.avx[s0], a.avx[s1], a.avx[s2], a.avx[s3]);
-            VY = make_float4(a.avy[s0], a.avy[s1], a.avy[s2], a.avy[s3]);
-        }
-    } else {
-        X = ld4(a.ax, i0);
-        Y = ld4(a.ay, i0);
-        VX = ld4(a.avx, i0);
-        VY = ld4(a.avy, i0);
-    }
-}
-
-template <bool First>
-__global__ void __launch_bounds__(kPfBlock, 4) k_pf32_step(const Pf32Args a)
-{
-    const uint32_t t = a.sc->step;
-    const int resampled = First ? 1 : a.sc->resampled;
-    const bool gather = First ? false : (a.sc->gather != 0);
-    const float Mprev = First ? 0.0f : static_cast<float>(a.sc->M);
-    // steps past the capacity (profiling loops) reuse the last observation
-    // and record nothing
-    const uint32_t to = t < a.max_steps ? t : a.max_steps - 1;
-    const float ox = static_cast<float>(a.obs[2 * to + 0]);
-    const float oy = static_cast<float>(a.obs[2 * to + 1]);
-    const uint32_t n = a.n;
-    float m = -INFINITY, s = 0, s2 = 0, sx = 0, sy = 0, sw = 0;
-
-    const uint32_t ntiles = (n + kPfTile - 1) / kPfTile;
-    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const uint32_t i0 = tile * kPfTile + threadIdx.x * 4;
-        if (i0 + 3 < n) {
-            float4 X, Y, VX, VY, LW;
-            if (!First) {
-                load_group(a, i0, gather, X, Y, VX, VY);
-                LW = resampled ? make_float4(0, 0, 0, 0) : ld4(a.lw, i0);
-            }
-            step_one<First>(a, i0 + 0, t, ox, oy, resampled, Mprev, X.x, Y.x,
-                VX.x, VY.x, LW.x, m, s, s2, sx, sy, sw);
-            step_one<First>(a, i0 + 1, t, ox, oy, resampled, Mprev, X.y, Y.y,
-                VX.y, VY.y, LW.y, m, s, s2, sx, sy, sw);
-            step_one<First>(a, i0 + 2, t, ox, oy, resampled, Mprev, X.z, Y.z,
-                VX.z, VY.z, LW.z, m, s, s2, sx, sy, sw);
-            step_one<First>(a, i0 + 3, t, ox, oy, resampled, Mprev, X.w, Y.w,
-                VX.w, VY.w, LW.w, m, s, s2, sx, sy, sw);
-            st4(a.bx, i0, X);
-            st4(a.by, i0, Y);
-            st4(a.bvx, i0, VX);
-            st4(a.bvy, i0, VY);
-            st4(a.lw, i0, LW);
-        } else {
-            for (uint32_t i = i0; i < n && i < i0 + 4; ++i) {
-                float X = 0, Y = 0, VX = 0, VY = 0, LW = 0;
-                if (!First) {
-                    uint32_t src =
-                        gather ? source_of(a.idx, a.srcs, a.idx[i]) : i;
-                    if (src >= a.n) {
-                        atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
-                        src = 0;
-                    }
-                    X = a.ax[src];
-                    Y = a.ay[src];
-                    VX = a.avx[src];
-                    VY = a.avy[src];
-                    LW = resampled ? 0.0f : a.lw[i];
-                }
-                step_one<First>(a, i, t, ox, oy, resampled, Mprev, X, Y, VX,
-                    VY, LW, m, s, s2, sx, sy, sw);
-                a.bx[i] = X;
-                a.by[i] = Y;
-                a.bvx[i] = VX;
-                a.bvy[i] = VY;
-                a.lw[i] = LW;
-            }
-        }
-    }
-
-    // ---- warp level in FP32
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        const float om = __shfl_xor_sync(0xFFFFFFFFu, m, d);
-        const float os = __shfl_xor_sync(0xFFFFFFFFu, s, d);
-        const float os2 = __shfl_xor_sync(0xFFFFFFFFu, s2, d);
-        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, d);
-        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, d);
-        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, d);
-        lse_merge_f(m, s, s2, om, os, os2);
-    }
-    // ---- block level in FP32 (warp 0 merges the warps' records), then one
-    // FP64 record per block
     constexpr int kW = kPfBlock / 32;
-    __shared__ float shw[6][kW];
-    __shared__ double sh[5][kW];
+    __shared__ double sh[kMaxMonitorDim][kW];
     __shared__ bool is_last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-        shw[0][wid] = m;
-        shw[1][wid] = s;
-        shw[2][wid] = s2;
-        shw[3][wid] = sx;
-        shw[4][wid] = sy;
-        shw[5][wid] = sw;
-    }
-    __syncthreads();
-    if (wid == 0) {
-        const bool in = lane < kW;
-        float wm = in ? shw[0][lane] : -INFINITY;
-        float ws = in ? shw[1][lane] : 0.0f, ws2 = in ? shw[2][lane] : 0.0f;
-        float wx = in ? shw[3][lane] : 0.0f, wy = in ? shw[4][lane] : 0.0f;
-        float ww = in ? shw[5][lane] : 0.0f;
 #pragma unroll
-        for (int d = kW / 2; d > 0; d >>= 1) {
-            const float om = __shfl_xor_sync(0xFFFFFFFFu, wm, d);
-            const float os = __shfl_xor_sync(0xFFFFFFFFu, ws, d);
-            const float os2 = __shfl_xor_sync(0xFFFFFFFFu, ws2, d);
-            wx += __shfl_xor_sync(0xFFFFFFFFu, wx, d);
-            wy += __shfl_xor_sync(0xFFFFFFFFu, wy, d);
-            ww += __shfl_xor_sync(0xFFFFFFFFu, ww, d);
-            lse_merge_f(wm, ws, ws2, om, os, os2);
-        }
-        if (lane == 0) {
-            const MovePartial p = {wx, wy, ww, wm, ws, ws2};
-            a.part[blockIdx.x] = p;
-            __threadfence();
-            is_last = atomicAdd(&a.sc->done, 1u) == gridDim.x - 1;
-        }
-    }
-    __syncthreads();
-    if (!is_last)
-        return;
-
-    // ---- last block: combine every block's record
-    __threadfence();
-    float M = -INFINITY;
-    for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x)
-        M = fmaxf(M, static_cast<float>(a.part[b].m));
-    __shared__ float shmax[kPfBlock / 32 + 1];
-    M = block_reduce(M, OpMax(), -INFINITY, shmax);
-    double S = 0, S2 = 0, SX = 0, SY = 0, SW = 0;
-    for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-        const MovePartial p = a.part[b];
-        SX += p.sx;
-        SY += p.sy;
-        SW += p.sw;
-        if (p.m > -INFINITY) {
-            const double f = __expf(static_cast<float>(p.m) - M);
-            S += p.s * f;
-            S2 += p.s2 * f * f;
-        }
-    }
+    for (int d = 0; d < kMaxMonitorDim; ++d) {
+        double v = acc[d];
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        S += __shfl_xor_sync(0xFFFFFFFFu, S, d);
-        S2 += __shfl_xor_sync(0xFFFFFFFFu, S2, d);
-        SX += __shfl_xor_sync(0xFFFFFFFFu, SX, d);
-        SY += __shfl_xor_sync(0xFFFFFFFFu, SY, d);
-        SW += __shfl_xor_sync(0xFFFFFFFFu, SW, d);
-    }
-    __syncthreads();
-    if (lane == 0) {
-        sh[0][wid] = S;
-        sh[1][wid] = S2;
-        sh[2][wid] = SX;
-        sh[3][wid] = SY;
-        sh[4][wid] = SW;
+        for (int o = 16; o > 0; o >>= 1)
+            v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        if (lane == 0)
+            sh[d][wid] = v;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double S1 = 0, S21 = 0, SX1 = 0, SY1 = 0, SW1 = 0;
-        for (int w = 0; w < kPfBlock / 32; ++w) {
-            S1 += sh[0][w];
-            S21 += sh[1][w];
-            SX1 += sh[2][w];
-            SY1 += sh[3][w];
-            SW1 += sh[4][w];
-        }
-        PfScalars &sc = *a.sc;
-        const double prev_mass = First ? static_cast<double>(n) : SW1;
-        const bool rec = t < a.max_steps;
-        if (!First && rec) {
-            a.h_mean[2 * (t - 1) + 0] = SX1 / SW1;
-            a.h_mean[2 * (t - 1) + 1] = SY1 / SW1;
-        }
-        const double ess = S1 * S1 / S21;
-        const double M1 = static_cast<double>(M);
-        sc.logz += M1 + log(S1) - log(prev_mass);
-        if (!(S1 > 0) || !(ess > 0))
-            sc.err |= DEV_ERR_NONFINITE;
-        const int flag = ess < a.threshold * static_cast<double>(n) ? 1 : 0;
-        if (rec) {
-            a.h_ess[t] = ess;
-            a.h_logz[t] = sc.logz;
-            a.h_res[t] = flag;
-        }
-        sc.M = M1;
-        sc.S = S1;
-        sc.ess = ess;
-        sc.resampled = flag;
-        sc.gather = 0; // every block has read it; a resample sets it again
-        sc.step = t + 1;
-        sc.done = 0;
-    }
-}
-
-// Weighted mean of the current particles (the last step's monitor).
-__global__ void __launch_bounds__(kPfBlock) k_pf32_final_mean(
-    const Pf32Args a, uint32_t t_rec)
-{
-    const int resampled = a.sc->resampled;
-    const bool gather = a.sc->gather != 0;
-    const float M = static_cast<float>(a.sc->M);
-    const uint32_t n = a.n;
-    // FP32 within a thread and a warp, FP64 across warps and blocks, as
-    // the step kernel forms the monitor sums; four particles per thread
-    // step (float4 rows when nothing is gathered)
-    float sx = 0, sy = 0, sw = 0;
-    auto add = [&](uint32_t i, float x, float y) {
-        const float w = resampled ? 1.0f : __expf(a.lw[i] - M);
-        sx += w * x;
-        sy += w * y;
-        sw += w;
-    };
-    const uint32_t ngroups = n / 4;
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups;
-         g += gridDim.x * blockDim.x) {
-        const uint32_t i0 = 4 * g;
-        if (!gather) {
-            const float4 X = ld4(a.ax, i0), Y = ld4(a.ay, i0);
-            add(i0 + 0, X.x, Y.x);
-            add(i0 + 1, X.y, Y.y);
-            add(i0 + 2, X.z, Y.z);
-            add(i0 + 3, X.w, Y.w);
-        } else {
-            for (uint32_t i = i0; i < i0 + 4; ++i) {
-                uint32_t src = source_of(a.idx, a.srcs, a.idx[i]);
-                if (src >= n) {
-                    atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
-                    src = 0;
-                }
-                add(i, a.ax[src], a.ay[src]);
-            }
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x < n - 4 * ngroups) { // the last 1-3
-        const uint32_t i = 4 * ngroups + threadIdx.x;
-        uint32_t src = gather ? source_of(a.idx, a.srcs, a.idx[i]) : i;
-        if (src >= n) {
-            atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
-            src = 0;
-        }
-        add(i, a.ax[src], a.ay[src]);
-    }
-    __shared__ double sh[3][kPfBlock / 32];
-    __shared__ bool is_last;
+        PfPartial p = {};
+        for (int w = 0; w < kW; ++w)
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, d);
-        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, d);
-        sw += __shfl_xor_sync(0xFFFFFFFFu, sw, d);
-    }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-        sh[0][wid] = sx;
-        sh[1][wid] = sy;
-        sh[2][wid] = sw;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        MovePartial p = {0, 0, 0, 0, 0, 0};
-        for (int w = 0; w < kPfBlock / 32; ++w) {
-            p.sx += sh[0][w];
-            p.sy += sh[1][w];
-            p.sw += sh[2][w];
-        }
-        a.part[blockIdx.x] = p;
+            for (int d = 0; d < kMaxMonitorDim; ++d)
+                p.mon[d] += sh[d][w];
+        part[blockIdx.x] = p;
         __threadfence();
-        is_last = atomicAdd(&a.sc->done, 1u) == gridDim.x - 1;
+        is_last = atomicAdd(&sc->done2, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!is_last || threadIdx.x != 0)
         return;
     __threadfence();
-    double SX = 0, SY = 0, SW = 0;
-    for (uint32_t b = 0; b < gridDim.x; ++b) {
-        SX += a.part[b].sx;
-        SY += a.part[b].sy;
-        SW += a.part[b].sw;
+    double tot[kMaxMonitorDim] = {};
+    for (uint32_t b = 0; b < gridDim.x; ++b)
+#pragma unroll
+        for (int d = 0; d < kMaxMonitorDim; ++d)
+            tot[d] += __ldcg(&part[b].mon[d]);
+#pragma unroll
+    for (int d = 0; d < kMaxMonitorDim; ++d) {
+        if (static_cast<uint32_t>(d) >= mon_dim)
+            break;
+        sc->mean[d] = tot[d] * inv_n;
+        if (t < max_steps)
+            h_mean[static_cast<size_t>(t) * mon_dim + d] = tot[d] * inv_n;
     }
-    if (t_rec < a.max_steps) {
-        a.h_mean[2 * t_rec + 0] = SX / SW;
-        a.h_mean[2 * t_rec + 1] = SY / SW;
-    }
-    a.sc->done = 0;
+    sc->done2 = 0;
 }
 
-// B = A gathered through idx (materializes a pending resample)
+// out = in gathered through idx (materializes a pending resample)
 __global__ void __launch_bounds__(kPfBlock) k_pf32_materialize(
-    const Pf32Args a)
+    const PfStepArgs a, uint32_t dim)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
          i += gridDim.x * blockDim.x) {
-        uint32_t src = source_of(a.idx, a.srcs, a.idx[i]);
+        uint32_t src = pf_source(a.srcs, a.idx[i]);
         if (src >= a.n) {
             atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
             src = 0;
         }
-        a.bx[i] = a.ax[src];
-        a.by[i] = a.ay[src];
-        a.bvx[i] = a.avx[src];
-        a.bvy[i] = a.avy[src];
+        for (uint32_t d = 0; d < dim; ++d)
+            a.out[d * a.stride + i] = a.in[d * a.stride + src];
     }
 }
 
@@ -448,8 +182,15 @@ __device__ __forceinline__ uint64_t q_at(
 // flight)
 __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
 {
-    if (!a.sc->resampled)
+    if (!(a.force || a.sc->resampled))
         return;
+    if (a.force && blockIdx.x == 0 && threadIdx.x == 0) {
+        // a host decision: the later passes see the flag set
+        a.sc->resampled = 1;
+        const uint32_t t = a.sc->step - 1;
+        if (a.h_res != nullptr && t < a.max_steps)
+            a.h_res[t] = 1;
+    }
     const float M = static_cast<float>(a.sc->M);
     uint32_t lo, hi;
     chunk_range(a.n, a.chunk, lo, hi);
@@ -671,6 +412,8 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
             engine_advance(sc, jf < a.n ? jf + 1 : a.n);
         }
     }
+    // monitor of the resampled particles: sum_i rep_i x_{d,i}
+    float macc[kMaxMonitorDim] = {};
     // the next tile's counts are loaded while this one is scanned
     int4 nxt = load_rep4(a.rep, lo + threadIdx.x * 4, hi);
     for (uint32_t base = lo; base < hi; base += kPfTile) {
@@ -679,6 +422,22 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         if (base + kPfTile < hi)
             nxt = load_rep4(a.rep, i0 + kPfTile, hi);
         const int32_t r[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+        for (int d = 0; d < kMaxMonitorDim; ++d) {
+            if (static_cast<uint32_t>(d) >= a.mon_dim)
+                break;
+            const float *row = a.mon_state + d * a.stride;
+            if (i0 + 3 < hi) {
+                const float4 X = ld4(row, i0);
+                macc[d] += static_cast<float>(r[0]) * X.x +
+                    static_cast<float>(r[1]) * X.y +
+                    static_cast<float>(r[2]) * X.z +
+                    static_cast<float>(r[3]) * X.w;
+            } else {
+                for (uint32_t k = 0; k < 4 && i0 + k < hi; ++k)
+                    macc[d] += static_cast<float>(r[k]) * row[i0 + k];
+            }
+        }
         uint32_t tr = 0, te = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -725,6 +484,9 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         coff += static_cast<uint32_t>(tot >> 32);
         eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
     }
+    if (a.mon_dim > 0)
+        equal_mean_finish(macc, a.mon_dim, 1.0 / static_cast<double>(a.n),
+            a.mon_part, a.sc, a.h_mean, a.sc->step - 1, a.max_steps);
 }
 
 __device__ __forceinline__ void rank_range(
@@ -837,7 +599,7 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_fill(const Rs32Args a)
 // parent among the step's particles before resampling, or itself when the
 // step did not resample.
 __global__ void __launch_bounds__(kPfBlock) k_pf32_record(
-    const Pf32Args a, int32_t *rows)
+    const PfStepArgs a, int32_t *rows)
 {
     const uint32_t t = a.sc->step - 1;
     if (t >= a.max_steps)
@@ -846,7 +608,7 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_record(
     int32_t *row = rows + static_cast<size_t>(t) * a.n;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
          i += gridDim.x * blockDim.x) {
-        uint32_t src = res ? source_of(a.idx, a.srcs, a.idx[i]) : i;
+        uint32_t src = res ? pf_source(a.srcs, a.idx[i]) : i;
         if (src >= a.n) {
             atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
             src = 0;
@@ -857,47 +619,58 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_record(
 
 // Resample-move: after a step that resampled (t >= 1), `sweeps` random-walk
 // Metropolis steps (cv_mcmc_step) on each particle's acceleration, on the
-// gathered state; the result goes to the other buffer (out).  Steps that
-// did not resample (weights not equal) copy the state through unchanged.
-// acc_hist[t] += the accepted steps.
-__global__ void __launch_bounds__(kPfBlock) k_pf32_mcmc(const Pf32Args a,
-    float *ox_, float *oy_, float *ovx, float *ovy, uint32_t sweeps,
-    float s_rw, float inv_var, uint32_t *acc_hist)
+// gathered state read from a.in (the step's output); the result goes to
+// a.out (the step's input buffer, so the next step reads it with no
+// gather).  Steps that did not resample (weights not equal) copy the state
+// through unchanged.  acc_hist[t] += the accepted steps.  After moving, the
+// monitor (sc->mean, h_mean[t]) is the equal-weight mean of the moved
+// particles, as the reference's monitor sees them after the mcmc queue
+// (core/sampler.hpp:746-754).
+__global__ void __launch_bounds__(kPfBlock) k_pf32_mcmc(const PfStepArgs a,
+    CvConst<float> c, const double *obs, uint32_t sweeps, float s_rw,
+    float inv_var, uint32_t *acc_hist)
 {
     const uint32_t t = a.sc->step - 1;
     const bool gather = a.sc->gather != 0;
     const bool move = a.sc->resampled != 0 && t >= 1;
     const uint32_t to = t < a.max_steps ? t : a.max_steps - 1;
-    const float obx = static_cast<float>(a.obs[2 * to + 0]);
-    const float oby = static_cast<float>(a.obs[2 * to + 1]);
+    const float obx = static_cast<float>(obs[2 * to + 0]);
+    const float oby = static_cast<float>(obs[2 * to + 1]);
+    const size_t ld = a.stride;
     uint32_t acc = 0;
+    float macc[kMaxMonitorDim] = {};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
          i += gridDim.x * blockDim.x) {
-        uint32_t src = gather ? source_of(a.idx, a.srcs, a.idx[i]) : i;
+        uint32_t src = gather ? pf_source(a.srcs, a.idx[i]) : i;
         if (src >= a.n) {
             atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
             src = 0;
         }
-        // the step's output is in the b buffer
-        float x = a.bx[src], y = a.by[src], vx = a.bvx[src], vy = a.bvy[src];
+        float x = a.in[src], y = a.in[ld + src], vx = a.in[2 * ld + src],
+              vy = a.in[3 * ld + src];
         if (move) {
             float ax, ay;
-            cv_innovation(a.c, t, a.seed, src, ax, ay);
+            cv_innovation(c, t, a.seed, src, ax, ay);
             float lt = -0.5f * inv_var * (ax * ax + ay * ay) +
-                cv_loglik(a.c, obx, oby, x, y);
+                cv_loglik(c, obx, oby, x, y);
             for (uint32_t k = 0; k < sweeps; ++k)
-                acc += cv_mcmc_step(a.c, obx, oby, s_rw, inv_var, t, a.seed, i,
+                acc += cv_mcmc_step(c, obx, oby, s_rw, inv_var, t, a.seed, i,
                     k, x, y, vx, vy, ax, ay, lt);
+            macc[0] += x;
+            macc[1] += y;
         }
-        ox_[i] = x;
-        oy_[i] = y;
-        ovx[i] = vx;
-        ovy[i] = vy;
+        a.out[i] = x;
+        a.out[ld + i] = y;
+        a.out[2 * ld + i] = vx;
+        a.out[3 * ld + i] = vy;
     }
     __shared__ uint32_t sh[kPfBlock / 32 + 1];
     acc = block_reduce(acc, OpAdd(), 0u, sh);
     if (threadIdx.x == 0 && acc && t < a.max_steps)
         atomicAdd(acc_hist + t, acc);
+    if (move)
+        equal_mean_finish(macc, 2, 1.0 / static_cast<double>(a.n), a.part,
+            a.sc, a.h_mean, t, a.max_steps);
 }
 
 // parent index of every slot from the encoded idx (reference layout)

@@ -14,6 +14,10 @@ struct Pf64State; // FP64 driver state (pf64.cu)
 struct vsmc_cuda_pf {
     size_t n = 0;
     size_t stride = 0; // SoA row stride (n rounded up to 256 elements)
+    size_t dim = 4;     // state components (rows)
+    size_t mon_dim = 2; // monitored leading components
+    bool custom = false; // precision 32 with the caller's model (no CV model)
+    bool host_equal = false; // custom: weights set equal by the host
     int precision = 32;
     int scheme = VSMC_CUDA_SYSTEMATIC;
     double threshold = 0.5;
@@ -27,21 +31,23 @@ struct vsmc_cuda_pf {
     bool use_graph = true;
 
     // device buffers
-    void *state = nullptr;  // 4 rows of `stride` (float or double)
+    void *state = nullptr;  // dim rows of `stride` (float or double)
     void *state2 = nullptr; // FP32: second buffer; a step reads one, writes the other
     int cur = 0;            // FP32: buffer holding the current state (0: state)
     void *weight = nullptr; // FP32: log-weights (float); FP64: W (double)
     double *obs = nullptr;  // max_steps x 2
-    double *h_mean = nullptr, *h_ess = nullptr, *h_logz = nullptr;
+    double *h_mean = nullptr; // max_steps x mon_dim
+    double *h_ess = nullptr, *h_logz = nullptr;
     int *h_res = nullptr;
     vsmc_cuda::PfScalars *sc = nullptr;
 
     // FP32 fused-step workspace
+    size_t max_grid = 0; // records in `part`
     int grid_step = 0;
     int grid_rs = 0;
     uint32_t chunk_rs = 0;
     uint32_t shift = 0;
-    vsmc_cuda::MovePartial *part = nullptr;
+    vsmc_cuda::PfPartial *part = nullptr;
     uint64_t *qpart = nullptr;
     uint32_t *epart = nullptr, *cpart = nullptr, *mpart = nullptr;
     int32_t *rep = nullptr;

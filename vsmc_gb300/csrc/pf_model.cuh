@@ -58,25 +58,6 @@ __device__ __forceinline__ u32x4 particle_block(
     return philox4x32_10(1u, i, 0u, 0u, t, seed);
 }
 
-// FP32 standard-normal pair: Box-Muller, (0,1] radius uniform, [0,1) angle,
-// on the SFU: the hardware log2 (absolute error ~2^-21 in ln u), the
-// reciprocal square root for the radius, and the hardware sine and cosine
-// of 2 pi u in [0, 2 pi).  A normal differs from the one with the
-// correctly rounded functions by ~1e-6 relative, more only for radius
-// uniforms within ~1e-6 of 1, where the normal itself is below ~1e-3.
-__device__ __forceinline__ void normal_pair_f(uint32_t w0, uint32_t w1,
-    float &z1, float &z2)
-{
-    const float u1 = u01_oc_f(w0);
-    const float u2 = u01_co_f(w1);
-    const float l = -2.0f * __logf(u1);
-    const float r = l > 0.0f ? l * rsqrtf(l) : 0.0f;
-    float sv, cv;
-    __sincosf(6.28318530717958648f * u2, &sv, &cv);
-    z1 = r * cv;
-    z2 = r * sv;
-}
-
 // FP64 standard-normal pair: NormalDistribution<double> (cosine value
 // first, sine value cached), [0,1) uniforms from 32-bit words.
 __device__ __forceinline__ void normal_pair_d(uint32_t w0, uint32_t w1,
