@@ -203,22 +203,79 @@ def cpu_filter_rate(n, T, threads=0, seed=0):
     return n * T / dt, dt, nthreads
 
 
+def ref_filter_rate(n, T, seed=0):
+    """The reference's own filter on host cores: its Sampler<T> with the
+    OpenMP backend (StateOMP / MoveOMP / MonitorEvalOMP) from oracle/_ref,
+    built from the reference's sources where they are present.  Returns
+    (particle-steps/s, seconds, threads), or None without the build."""
+    from oracle import binding
+    if binding.build_ref() is None:
+        return None
+    ref = binding.ref()
+    if ref is None:
+        return None
+    port = binding.port()
+    m = binding.default_model()
+    tr = np.zeros(4 * T)
+    ob = np.zeros(2 * T)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    port.vo_pf_simulate(seed, T, ctypes.byref(m), P(tr), P(ob))
+    mean = np.zeros(2 * T)
+    ess = np.zeros(T)
+    res = np.zeros(T, np.int32)
+    logz = np.zeros(T)
+    # the reference's OpenMP backend takes every host thread (OMP default)
+    nthreads = int(os.environ.get("OMP_NUM_THREADS", "0")) or \
+        (os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    ref.ref_pf_run(32, n, T, 1, SCHEME, THRESHOLD, 0, m.dt, m.sigma_a,
+                   m.obs_scale, m.nu, m.sd_pos0, m.sd_vel0, P(ob), P(mean),
+                   P(ess), P(res), P(logz))
+    dt = time.perf_counter() - t0
+    return n * T / dt, dt, nthreads
+
+
+def run_cpu_compare(args):
+    """The reference itself (oracle/_ref) and the oracle's C restatement on
+    the same sample and the same host threads: one JSON line with both
+    rates and their ratio."""
+    n, T = 1 << 20, 20
+    ref_filter_rate(n, T)  # warm-up (and the build)
+    cpu_filter_rate(n, T)
+    r = ref_filter_rate(n, T)
+    p = cpu_filter_rate(n, T)
+    line = {"cpu_compare": "N=2^20 particles x T=20 steps, FP32 state, "
+                           "systematic, ESS < N/2",
+            "threads": p[2], "port": p[0],
+            "reference": r[0] if r else None,
+            "port_over_reference": (p[0] / r[0]) if r else None}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     n, T = 1 << 20, 50
+    # the reference itself where it can be built here, else its C
+    # restatement (the reference tree is absent on the GPU host)
+    kind = "reference" if ref_filter_rate(1 << 12, 2) is not None else "port"
+    rate = ref_filter_rate if kind == "reference" else cpu_filter_rate
     for _ in range(args.warmup):
-        cpu_filter_rate(n, T)
+        rate(n, T)
     total = 0.0
     rates = []
     for _ in range(args.steps):
-        r, dt, threads = cpu_filter_rate(n, T)
+        r, dt, threads = rate(n, T)
         total += dt
         rates.append(r)
     value = n * T * args.steps / total
     sample = (f"N=2^20 particles x T={T} steps per bench step (the "
-              f"N=2^24, T=200 workload scaled down), FP32 state, systematic")
+              f"N=2^24, T=200 workload scaled down), FP32 state, systematic"
+              + (", the reference's Sampler<T> with its OpenMP backend"
+                 if kind == "reference" else
+                 ", the oracle's C restatement of the reference filter"))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -229,7 +286,8 @@ def run_reference(args):
                    "particles": n, "steps_T": T, "scheme": "systematic",
                    "threshold": THRESHOLD},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
-                         "kind": "port", "sample": sample},
+                         "kind": kind, "sample": sample},
+        "same_config": False,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -892,7 +950,12 @@ def main():
                     help="micro workload: comma-separated item names to run "
                          "(default all; philox4x32_u32 always runs)")
     ap.add_argument("--tune-steps", type=int, default=60)
+    ap.add_argument("--cpu-compare", action="store_true",
+                    help="time the reference (oracle/_ref) beside the "
+                         "oracle's C restatement on the host and exit")
     args = ap.parse_args()
+    if args.cpu_compare:
+        return run_cpu_compare(args)
     if args.impl == "reference":
         return run_reference(args)
     args.warmup = max(args.warmup, 3)

@@ -396,6 +396,11 @@ typedef struct {
     uint32_t seed;
     double threshold;        /* the device's resampling threshold (< 0: never) */
     void *stream;            /* the filter's stream */
+    int record_previous_mean; /* nonzero: the step records the previous
+                                 step's monitor from the particles it reads
+                                 (and not its own), as the filter's own
+                                 runs do; 0: its own (after a resample the
+                                 resampling passes replace it) */
 } vsmc_cuda_pf_step_desc;
 
 /* The first call after creation or vsmc_cuda_pf_reset (step 0) also resets
@@ -571,9 +576,22 @@ int vsmc_cuda_batch_set_shape(vsmc_cuda_batch *batch, int ppt, int block);
 int vsmc_cuda_batch_get_shape(vsmc_cuda_batch *batch, int *ppt, int *block);
 /* Time the first `steps` steps of the batch over obs_dev for each shape and
  * keep the fastest; ms_host (6 floats, may be NULL) receives the times in
- * the order (1,128) (2,128) (4,128) (1,256) (2,256) (4,256).  Synchronizes. */
+ * the order (1,128) (2,128) (4,128) (1,256) (2,256) (4,256).  Then tunes the
+ * scan schedule for that shape (vsmc_cuda_batch_autotune_schedule).
+ * Synchronizes. */
 int vsmc_cuda_batch_autotune(vsmc_cuda_batch *batch, const double *obs_dev,
     int steps, float *ms_host);
+/* Scan schedule of the batched resampling: a filter's particles are
+ * resampled in chunks of min_chunk (4096, 8192, 16384 or 32768), doubled
+ * until the filter has at most 32 chunks; each chunk is one entry of the
+ * step's resampling list.  Results do not depend on it (the counts are
+ * exact integers).  autotune_schedule times the first `steps` steps for each
+ * of the four and keeps the fastest; ms_host (4 floats, may be NULL) gets
+ * the times.  No reference counterpart. */
+int vsmc_cuda_batch_set_schedule(vsmc_cuda_batch *batch, uint32_t min_chunk);
+int vsmc_cuda_batch_get_schedule(vsmc_cuda_batch *batch, uint32_t *min_chunk);
+int vsmc_cuda_batch_autotune_schedule(vsmc_cuda_batch *batch,
+    const double *obs_dev, int steps, float *ms_host);
 
 /* --------------------------------------------- genealogy and summary */
 

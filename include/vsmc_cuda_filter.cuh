@@ -100,6 +100,8 @@ struct PfScalars {
 struct PfPartial {
     double m, s, s2;
     double mon[kMaxMonitorDim];
+    double prev[kMaxMonitorDim]; // previous-step monitor sums (Previous)
+    double prev_w;
 };
 
 // Kernel arguments (from vsmc_cuda_pf_step_desc).
@@ -116,6 +118,7 @@ struct PfStepArgs {
     size_t stride;
     uint32_t n, seed, max_steps;
     double threshold; // resample when ESS < threshold * n (< 0: never)
+    int mon_prev;     // PfMon::Previous (the filter's own runs)
 };
 
 // ------------------------------------------------- weighted accumulation
@@ -281,12 +284,26 @@ __device__ __forceinline__ void pf_load_group(
     }
 }
 
+// The monitor's place in the step.  Current: the step's own weighted mean
+// of the moved particles, reduced with the evidence (a host reading the
+// monitor after every step, as Sampler<T> does).  Previous: the previous
+// step's monitor, from the particles this step reads (weights
+// exp(lw_prev - M_prev), or equal after a resample); the filter's own runs,
+// where it costs one exponential and no pass after a resample.
+enum class PfMon { Current, Previous };
+
+template <int MD>
+struct PrevSums {
+    float x[MD > 0 ? MD : 1];
+    float w;
+};
+
 // One particle: draw or move, weight, accumulate.
-template <class Model, bool First, int MD>
+template <class Model, bool First, PfMon Mon, int MD, int AMD>
 __device__ __forceinline__ void pf_particle(const Model &model,
     const typename Model::step_type &ctx, uint32_t t, uint32_t seed,
     uint32_t i, int resampled, float Mprev, float (&x)[Model::dim], float &lw,
-    LseMon<MD> &acc)
+    LseMon<AMD> &acc, PrevSums<MD> &prev)
 {
     ParticleRng rng(t, seed, i);
     float lw_old = 0.0f;
@@ -294,6 +311,13 @@ __device__ __forceinline__ void pf_particle(const Model &model,
         model.init(ctx, rng, x);
     } else {
         lw_old = resampled ? 0.0f : lw - Mprev;
+        if (Mon == PfMon::Previous) {
+            const float wo = resampled ? 1.0f : __expf(lw_old);
+#pragma unroll
+            for (int d = 0; d < MD; ++d)
+                prev.x[d] = fmaf(wo, x[d], prev.x[d]);
+            prev.w += wo;
+        }
         model.move(ctx, rng, x);
     }
     lw = lw_old + model.log_likelihood(ctx, x);
@@ -302,19 +326,26 @@ __device__ __forceinline__ void pf_particle(const Model &model,
 
 // ------------------------------------------------------------ fused step
 
-template <class Model, bool First>
+template <class Model, bool First, PfMon Mon>
 __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
     const PfStepArgs a, const Model model)
 {
     constexpr int D = Model::dim;
     constexpr int MD = Model::monitor_dim;
+    // the evidence sums carry the monitor only for the current-step mode
+    constexpr int AMD = Mon == PfMon::Current ? MD : 0;
     const uint32_t t = a.sc->step;
     const int resampled = First ? 1 : a.sc->resampled;
     const bool gather = First ? false : (a.sc->gather != 0);
     const float Mprev = First ? 0.0f : static_cast<float>(a.sc->M);
     const typename Model::step_type ctx = model.step(t);
     const uint32_t n = a.n;
-    LseMon<MD> acc = lse_empty<MD>();
+    LseMon<AMD> acc = lse_empty<AMD>();
+    PrevSums<MD> prev;
+#pragma unroll
+    for (int d = 0; d < (MD > 0 ? MD : 1); ++d)
+        prev.x[d] = 0.0f;
+    prev.w = 0.0f;
 
     const uint32_t ntiles = (n + kPfTile - 1) / kPfTile;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -338,8 +369,8 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
                 for (int d = 0; d < D; ++d)
                     x[d] = pf_get(R[d], k);
                 float l = pf_get(LW, k);
-                pf_particle<Model, First, MD>(model, ctx, t, a.seed, i0 + k,
-                    resampled, Mprev, x, l, acc);
+                pf_particle<Model, First, Mon, MD, AMD>(model, ctx, t, a.seed,
+                    i0 + k, resampled, Mprev, x, l, acc, prev);
 #pragma unroll
                 for (int d = 0; d < D; ++d)
                     pf_set(R[d], k, x[d]);
@@ -368,8 +399,9 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
                     for (int d = 0; d < D; ++d)
                         x[d] = 0.0f;
                 }
-                pf_particle<Model, First, MD>(
-                    model, ctx, t, a.seed, i, resampled, Mprev, x, l, acc);
+                pf_particle<Model, First, Mon, MD, AMD>(
+                    model, ctx, t, a.seed, i, resampled, Mprev, x, l, acc,
+                    prev);
 #pragma unroll
                 for (int d = 0; d < D; ++d)
                     a.out[d * a.stride + i] = x[d];
@@ -382,19 +414,37 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1)
         acc.merge(acc.shfl_xor(d));
+    constexpr bool prev_on = !First && Mon == PfMon::Previous;
+    if (prev_on) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int d = 0; d < MD; ++d)
+                prev.x[d] += __shfl_xor_sync(0xFFFFFFFFu, prev.x[d], o);
+            prev.w += __shfl_xor_sync(0xFFFFFFFFu, prev.w, o);
+        }
+    }
     // ---- block level in FP32 (warp 0 merges the warps' records), then one
     // FP64 record per block
     constexpr int kW = kPfBlock / 32;
-    __shared__ LseMon<MD> shw[kW];
-    __shared__ double shd[3 + kMaxMonitorDim][kW];
+    __shared__ LseMon<AMD> shw[kW];
+    __shared__ float shp[kMaxMonitorDim + 1][kW];
+    __shared__ double shd[3 + 2 * kMaxMonitorDim + 1][kW];
     __shared__ float shmax[kW];
     __shared__ bool is_last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
+    if (lane == 0) {
         shw[wid] = acc;
+        if (prev_on) {
+#pragma unroll
+            for (int d = 0; d < MD; ++d)
+                shp[d][wid] = prev.x[d];
+            shp[kMaxMonitorDim][wid] = prev.w;
+        }
+    }
     __syncthreads();
     if (wid == 0) {
-        LseMon<MD> w = lse_empty<MD>();
+        LseMon<AMD> w = lse_empty<AMD>();
         if (lane < kW)
             w = shw[lane];
 #pragma unroll
@@ -406,8 +456,19 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
             p.s = w.s;
             p.s2 = w.s2;
 #pragma unroll
-            for (int d = 0; d < kMaxMonitorDim; ++d)
-                p.mon[d] = d < MD ? w.mon[d < MD ? d : 0] : 0.0;
+            for (int d = 0; d < kMaxMonitorDim; ++d) {
+                p.mon[d] = d < AMD ? w.mon[d < AMD ? d : 0] : 0.0;
+                double pv = 0;
+                if (prev_on && d < MD)
+                    for (int k = 0; k < kW; ++k)
+                        pv += shp[d < MD ? d : 0][k];
+                p.prev[d] = pv;
+            }
+            double pw = 0;
+            if (prev_on)
+                for (int k = 0; k < kW; ++k)
+                    pw += shp[kMaxMonitorDim][k];
+            p.prev_w = pw;
             a.part[blockIdx.x] = p;
             __threadfence();
             is_last = atomicAdd(&a.sc->done, 1u) == gridDim.x - 1;
@@ -432,7 +493,7 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
 #pragma unroll
     for (int w = 1; w < kW; ++w)
         M = fmaxf(M, shmax[w]);
-    double v[3 + kMaxMonitorDim] = {};
+    double v[3 + 2 * kMaxMonitorDim + 1] = {};
     for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
         const double pm = __ldcg(&a.part[b].m);
         if (pm > -INFINITY) {
@@ -440,12 +501,18 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
             v[0] += __ldcg(&a.part[b].s) * f;
             v[1] += __ldcg(&a.part[b].s2) * f * f;
 #pragma unroll
-            for (int d = 0; d < MD; ++d)
+            for (int d = 0; d < AMD; ++d)
                 v[3 + d] += __ldcg(&a.part[b].mon[d]) * f;
+        }
+        if (prev_on) {
+#pragma unroll
+            for (int d = 0; d < MD; ++d)
+                v[3 + kMaxMonitorDim + d] += __ldcg(&a.part[b].prev[d]);
+            v[3 + 2 * kMaxMonitorDim] += __ldcg(&a.part[b].prev_w);
         }
     }
 #pragma unroll
-    for (int k = 0; k < 3 + kMaxMonitorDim; ++k) {
+    for (int k = 0; k < 3 + 2 * kMaxMonitorDim + 1; ++k) {
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1)
             v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], d);
@@ -454,13 +521,22 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double S = 0, S2 = 0, MON[kMaxMonitorDim] = {};
+        double S = 0, S2 = 0, MON[kMaxMonitorDim] = {},
+               PREV[kMaxMonitorDim] = {}, PW = 0;
         for (int w = 0; w < kW; ++w) {
             S += shd[0][w];
             S2 += shd[1][w];
 #pragma unroll
-            for (int d = 0; d < MD; ++d)
+            for (int d = 0; d < MD; ++d) {
                 MON[d] += shd[3 + d][w];
+                PREV[d] += shd[3 + kMaxMonitorDim + d][w];
+            }
+            PW += shd[3 + 2 * kMaxMonitorDim][w];
+        }
+        if (prev_on && t >= 1 && t - 1 < a.max_steps) {
+#pragma unroll
+            for (int d = 0; d < MD; ++d)
+                a.h_mean[static_cast<size_t>(t - 1) * MD + d] = PREV[d] / PW;
         }
         PfScalars &sc = *a.sc;
         const double prev_mass = resampled ? static_cast<double>(n) : sc.S;
@@ -472,11 +548,13 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
             sc.err |= DEV_ERR_NONFINITE;
         const int flag =
             ess < a.threshold * static_cast<double>(n) ? 1 : 0;
+        if (Mon == PfMon::Current) {
 #pragma unroll
-        for (int d = 0; d < MD; ++d) {
-            sc.mean[d] = MON[d] / S;
-            if (rec)
-                a.h_mean[static_cast<size_t>(t) * MD + d] = MON[d] / S;
+            for (int d = 0; d < MD; ++d) {
+                sc.mean[d] = MON[d] / S;
+                if (rec)
+                    a.h_mean[static_cast<size_t>(t) * MD + d] = MON[d] / S;
+            }
         }
         if (rec) {
             a.h_ess[t] = ess;
@@ -496,14 +574,15 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_pf_step(
 
 // ------------------------------------------------------------ host launch
 
-template <class Model, bool First>
+template <class Model, bool First, PfMon Mon>
 inline int pf_step_occupancy()
 {
     static int occ = 0;
     if (occ == 0) {
         int o = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &o, k_pf_step<Model, First>, kPfBlock, 0) != cudaSuccess ||
+                &o, k_pf_step<Model, First, Mon>, kPfBlock, 0) !=
+                cudaSuccess ||
             o < 1)
             o = 1;
         occ = o;
@@ -545,14 +624,19 @@ inline int pf_step_launch(const vsmc_cuda_pf_step_desc &d, const Model &model)
     a.seed = d.seed;
     a.max_steps = static_cast<uint32_t>(d.max_steps);
     a.threshold = d.threshold;
+    a.mon_prev = d.record_previous_mean;
     const bool first = d.step == 0;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
             cudaSuccess)
         return VSMC_CUDA_ERR_CUDA;
-    const int occ = first ? pf_step_occupancy<Model, true>()
-                          : pf_step_occupancy<Model, false>();
+    const bool prevmon = a.mon_prev != 0;
+    const int occ = first
+        ? (prevmon ? pf_step_occupancy<Model, true, PfMon::Previous>()
+                   : pf_step_occupancy<Model, true, PfMon::Current>())
+        : (prevmon ? pf_step_occupancy<Model, false, PfMon::Previous>()
+                   : pf_step_occupancy<Model, false, PfMon::Current>());
     const size_t ntiles = (d.n + kPfTile - 1) / kPfTile;
     size_t grid = static_cast<size_t>(sms) * static_cast<size_t>(occ);
     if (grid > ntiles)
@@ -562,12 +646,19 @@ inline int pf_step_launch(const vsmc_cuda_pf_step_desc &d, const Model &model)
     if (grid < 1)
         return VSMC_CUDA_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(d.stream);
-    if (first)
-        k_pf_step<Model, true>
-            <<<static_cast<unsigned>(grid), kPfBlock, 0, st>>>(a, model);
+    const unsigned g = static_cast<unsigned>(grid);
+    if (first && prevmon)
+        k_pf_step<Model, true, PfMon::Previous><<<g, kPfBlock, 0, st>>>(a,
+            model);
+    else if (first)
+        k_pf_step<Model, true, PfMon::Current><<<g, kPfBlock, 0, st>>>(a,
+            model);
+    else if (prevmon)
+        k_pf_step<Model, false, PfMon::Previous><<<g, kPfBlock, 0, st>>>(a,
+            model);
     else
-        k_pf_step<Model, false>
-            <<<static_cast<unsigned>(grid), kPfBlock, 0, st>>>(a, model);
+        k_pf_step<Model, false, PfMon::Current><<<g, kPfBlock, 0, st>>>(a,
+            model);
     return cudaGetLastError() == cudaSuccess ? VSMC_CUDA_OK
                                              : VSMC_CUDA_ERR_CUDA;
 }

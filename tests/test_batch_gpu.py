@@ -130,3 +130,28 @@ def test_batch_member_tracks_oracle(vc, port):
     assert np.abs(g["mean"] - mean.reshape(T, 2)).max() < 0.2
     assert abs(g["logz"][-1] - logz[-1]) < 1.0
     assert np.abs(g["mean"] - tr.reshape(T, 4)[:, :2]).mean() < 0.5
+
+
+def test_batch_scan_schedules_agree_and_autotune(vc):
+    """The resampling chunk (scan schedule) changes how a filter's particles
+    are split across the list, not the counts: every schedule gives the same
+    histories, bit for bit, and the schedule autotuner keeps one of them."""
+    n, T, seeds, models = _spec(vc, nf=40, seed=11, nmax_log2=16, tmax=60)
+    b = vc.FilterBatch(n, T, seeds, models)
+    obs = _simulate(vc, b)
+    outs = []
+    for c in (4096, 8192, 16384, 32768):
+        b.set_schedule(c)
+        assert b.schedule() == c
+        b.run_device(obs.data_ptr())
+        outs.append(b.history())
+    for o in outs[1:]:
+        for f in range(len(n)):
+            for k in ("mean", "ess", "resampled", "logz"):
+                assert np.array_equal(o[f][k], outs[0][f][k]), (f, k)
+    with pytest.raises(vc.VsmcCudaError):
+        b.set_schedule(5000)
+    ms = b.autotune_schedule(obs.data_ptr(), steps=20)
+    assert (ms > 0).all()
+    assert b.schedule() in (4096, 8192, 16384, 32768)
+    b.close()

@@ -106,11 +106,12 @@ def test_schemes_at_2_to_24(vc, port, weights, scheme):
     assert np.all((np.minimum(a1, a2) <= b) & (b <= np.maximum(a1, a2)))
     dist = _ulps(np.where(np.abs(a1 - b) < np.abs(a2 - b), a1, a2), b) \
         if len(cross) else np.zeros(0)
+    # u = 1 - exp(l): the difference of the two libm's exp results near 1,
+    # in units of 2^-53 (a few), and so in absolute terms, not in ulps of u
+    du = np.abs(u_gpu - u_ref).max() / 2.0**-53
     print(f"{NAMES[scheme]} N=2^24: {len(differ)} of {R} sorted uniforms "
-          f"differ in their last bits (max {_ulps(u_gpu, u_ref).max():.0f} "
-          f"ulp); {len(cross)} cross a CDF boundary (within "
-          f"{dist.max() if len(cross) else 0:.0f} ulp of it); "
-          f"{len(mism)} counts differ")
-    # the uniforms agree to 1e-13 relative (CUDA's and the host's libm)
-    np.testing.assert_allclose(u_gpu, u_ref, rtol=1e-13, atol=0)
+          f"differ (max |du| = {du:.1f} x 2^-53); {len(cross)} cross a CDF "
+          f"boundary (within {dist.max() if len(cross) else 0:.0f} ulp of "
+          f"it); {len(mism)} counts differ")
+    assert du <= 64, du
     assert len(cross) <= 4, len(cross)

@@ -100,7 +100,8 @@ class PfStepDesc(ctypes.Structure):
                 ("dim", ctypes.c_size_t), ("monitor_dim", ctypes.c_size_t),
                 ("max_steps", ctypes.c_size_t), ("max_grid", ctypes.c_size_t),
                 ("step", ctypes.c_size_t), ("seed", ctypes.c_uint32),
-                ("threshold", ctypes.c_double), ("stream", ctypes.c_void_p)]
+                ("threshold", ctypes.c_double), ("stream", ctypes.c_void_p),
+                ("record_previous_mean", ctypes.c_int)]
 
 
 class PfStatus(ctypes.Structure):
@@ -189,6 +190,9 @@ PROTOTYPES = {
     "vsmc_cuda_batch_create_bearings": (
         I32, [ctypes.POINTER(VP), SZ, VP, VP, VP, VP, VP, I32, F64, VP]),
     "vsmc_cuda_batch_destroy": (I32, [VP]),
+    "vsmc_cuda_batch_set_schedule": (I32, [VP, U32]),
+    "vsmc_cuda_batch_get_schedule": (I32, [VP, ctypes.POINTER(U32)]),
+    "vsmc_cuda_batch_autotune_schedule": (I32, [VP, VP, I32, VP]),
     "vsmc_cuda_resample_index_trace": (I32, [SZ, SZ, VP, SZ, VP, VP]),
     "vsmc_cuda_resample_index_matrix": (I32, [SZ, SZ, VP, I32, VP, VP]),
     "vsmc_cuda_sampler_print": (I32, [SZ, SZ, VP, VP, SZ, ctypes.c_char_p,
@@ -439,6 +443,21 @@ class FilterBatch:
         ms = np.zeros(6, dtype=np.float32)
         call("vsmc_cuda_batch_autotune", self.handle, obs_dev_ptr, steps,
              ms.ctypes.data)
+        return ms
+
+    def set_schedule(self, min_chunk):
+        call("vsmc_cuda_batch_set_schedule", self.handle, min_chunk)
+
+    def schedule(self):
+        c = U32()
+        call("vsmc_cuda_batch_get_schedule", self.handle, ctypes.byref(c))
+        return c.value
+
+    def autotune_schedule(self, obs_dev_ptr, steps=50):
+        import numpy as np
+        ms = np.zeros(4, dtype=np.float32)
+        call("vsmc_cuda_batch_autotune_schedule", self.handle, obs_dev_ptr,
+             steps, ms.ctypes.data)
         return ms
 
 

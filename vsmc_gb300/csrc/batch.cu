@@ -1165,6 +1165,20 @@ __global__ void k_batch_simulate_bearings(
 constexpr uint32_t kRsMinChunk = 4 * kPfTile; // resampling chunk: 4096 or more
 constexpr uint32_t kMaxRsChunks = 32;          // chunks of one filter, at most
 constexpr int kRsKernels = 5;
+// the scan schedules the autotuner times: the smallest chunk of a filter
+constexpr uint32_t kRsSchedules[] = {4096, 8192, 16384, 32768};
+constexpr int kNumSchedules = 4;
+
+// A filter's resampling chunk: min_chunk, doubled until the filter has at
+// most kMaxRsChunks chunks.  Larger chunks mean fewer list entries (and
+// fewer partial records to sum) but a longer last wave.
+inline uint32_t rs_chunk_for(uint32_t n, uint32_t min_chunk)
+{
+    uint32_t c = min_chunk;
+    while ((n + c - 1) / c > kMaxRsChunks)
+        c *= 2;
+    return c;
+}
 
 struct Shape {
     int ppt, block;
@@ -1295,10 +1309,14 @@ struct vsmc_cuda_batch {
     double *d_obs = nullptr;
     double *d_mean = nullptr, *d_ess = nullptr, *d_logz = nullptr;
     int *d_res = nullptr;
-    // run graph (for one observation pointer and shape)
+    // run graph (for one observation pointer, shape and schedule)
     cudaGraphExec_t graph = nullptr;
     const double *graph_obs = nullptr;
     Shape graph_shape = {0, 0};
+    uint32_t graph_chunk = 0;
+    // scan schedule: the smallest resampling chunk of a filter (the list and
+    // its buffers are sized for kRsMinChunk, the smallest allowed)
+    uint32_t rs_min_chunk = 0;
 };
 
 namespace vsmc_cuda
@@ -1528,6 +1546,7 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     std::stable_sort(b->order.begin(), b->order.end(),
         [&](uint32_t x, uint32_t y) { return T[x] > T[y]; });
     b->flt.resize(nfilters);
+    b->rs_min_chunk = kRsMinChunk;
     size_t off = 0;
     for (uint32_t k = 0; k < nfilters; ++k) {
         const uint32_t f = b->order[k];
@@ -1544,9 +1563,7 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
         while ((size_t(1) << lg) < n[f])
             ++lg;
         F.shift = static_cast<uint32_t>(63 - lg);
-        F.rs_chunk = kRsMinChunk;
-        while ((F.n + F.rs_chunk - 1) / F.rs_chunk > kMaxRsChunks)
-            F.rs_chunk *= 2;
+        F.rs_chunk = rs_chunk_for(F.n, kRsMinChunk);
         b->rs_cap += (F.n + F.rs_chunk - 1) / F.rs_chunk;
         if (kind == kKindCv)
             F.c = make_cv_const<float>(cv[f]);
@@ -1717,7 +1734,8 @@ int vsmc_cuda_batch_run_device(vsmc_cuda_batch *b, const double *obs_dev)
     const int nsteps = static_cast<int>(b->tmax) + 1;
     if (b->graph == nullptr || b->graph_obs != obs_dev ||
         b->graph_shape.ppt != b->shape.ppt ||
-        b->graph_shape.block != b->shape.block) {
+        b->graph_shape.block != b->shape.block ||
+        b->graph_chunk != b->rs_min_chunk) {
         if (b->graph) {
             cudaGraphExecDestroy(b->graph);
             b->graph = nullptr;
@@ -1739,6 +1757,7 @@ int vsmc_cuda_batch_run_device(vsmc_cuda_batch *b, const double *obs_dev)
         VSMC_CUDA_TRY(ei);
         b->graph_obs = obs_dev;
         b->graph_shape = b->shape;
+        b->graph_chunk = b->rs_min_chunk;
     }
     VSMC_CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
     return VSMC_CUDA_OK;
@@ -1806,6 +1825,90 @@ int vsmc_cuda_batch_get_shape(vsmc_cuda_batch *b, int *ppt, int *block)
     return VSMC_CUDA_OK;
 }
 
+int vsmc_cuda_batch_set_schedule(vsmc_cuda_batch *b, uint32_t min_chunk)
+{
+    if (b == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    bool known = false;
+    for (int k = 0; k < kNumSchedules; ++k)
+        known = known || kRsSchedules[k] == min_chunk;
+    if (!known)
+        return VSMC_CUDA_ERR_ARG;
+    for (uint32_t k = 0; k < b->nf; ++k) {
+        BFilter &F = b->flt[k];
+        F.rs_chunk = rs_chunk_for(F.n, min_chunk);
+    }
+    b->rs_min_chunk = min_chunk;
+    // re-uploads the filter descriptions (their chunks); the list keeps the
+    // capacity of the smallest chunk, which bounds every schedule
+    return batch_layout(b, b->shape);
+}
+
+int vsmc_cuda_batch_get_schedule(vsmc_cuda_batch *b, uint32_t *min_chunk)
+{
+    if (b == nullptr || min_chunk == nullptr)
+        return VSMC_CUDA_ERR_ARG;
+    *min_chunk = b->rs_min_chunk;
+    return VSMC_CUDA_OK;
+}
+
+// time `nsteps` steps of the batch (one warm-up run first)
+static int time_steps(vsmc_cuda_batch *b, const double *obs_dev, int nsteps,
+    cudaEvent_t e0, cudaEvent_t e1, float *ms)
+{
+    const int grid = num_sms() * occupancy(b->kind, b->shape);
+    int rc = enqueue_run(b, obs_dev, nsteps, grid); // warm-up
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    VSMC_CUDA_TRY(cudaEventRecord(e0, b->stream));
+    rc = enqueue_run(b, obs_dev, nsteps, grid);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    VSMC_CUDA_TRY(cudaEventRecord(e1, b->stream));
+    VSMC_CUDA_TRY(cudaEventSynchronize(e1));
+    VSMC_CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_batch_autotune_schedule(vsmc_cuda_batch *b,
+    const double *obs_dev, int steps, float *ms_host)
+{
+    if (b == nullptr || obs_dev == nullptr || steps < 1)
+        return VSMC_CUDA_ERR_ARG;
+    const int nsteps = std::min(steps, static_cast<int>(b->tmax) + 1);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    VSMC_CUDA_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return VSMC_CUDA_ERR_CUDA;
+    }
+    int best = -1;
+    float best_ms = 0;
+    int rc = VSMC_CUDA_OK;
+    for (int k = 0; k < kNumSchedules && rc == VSMC_CUDA_OK; ++k) {
+        rc = vsmc_cuda_batch_set_schedule(b, kRsSchedules[k]);
+        float ms = 0;
+        if (rc == VSMC_CUDA_OK)
+            rc = time_steps(b, obs_dev, nsteps, e0, e1, &ms);
+        if (rc != VSMC_CUDA_OK)
+            break;
+        if (ms_host)
+            ms_host[k] = ms;
+        if (best < 0 || ms < best_ms) {
+            best = k;
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    rc = check_errors(b);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    return vsmc_cuda_batch_set_schedule(b, kRsSchedules[best]);
+}
+
 int vsmc_cuda_batch_autotune(vsmc_cuda_batch *b, const double *obs_dev,
     int steps, float *ms_host)
 {
@@ -1858,7 +1961,11 @@ int vsmc_cuda_batch_autotune(vsmc_cuda_batch *b, const double *obs_dev,
     rc = check_errors(b);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    return batch_layout(b, kShapes[best]);
+    rc = batch_layout(b, kShapes[best]);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    // then the scan schedule (the resampling chunk) for that shape
+    return vsmc_cuda_batch_autotune_schedule(b, obs_dev, steps, nullptr);
 }
 
 } // extern "C"

@@ -88,7 +88,7 @@ static CvModel cv_model(vsmc_cuda_pf *pf)
 // Resampling arguments; mon_state is the state the resample draws from
 // (the last step's output), whose resampled mean becomes the monitor.
 static Rs32Args make_rs_args32(
-    vsmc_cuda_pf *pf, const float *mon_state, int force)
+    vsmc_cuda_pf *pf, const float *mon_state, int force, bool with_mon)
 {
     Rs32Args r = {};
     r.lw = static_cast<const float *>(pf->weight);
@@ -109,7 +109,7 @@ static Rs32Args make_rs_args32(
     r.sc = pf->sc;
     r.mon_state = mon_state;
     r.stride = pf->stride;
-    r.mon_dim = static_cast<uint32_t>(pf->mon_dim);
+    r.mon_dim = with_mon ? static_cast<uint32_t>(pf->mon_dim) : 0u;
     r.max_steps = static_cast<uint32_t>(pf->max_steps);
     r.mon_part = pf->part;
     r.h_mean = pf->h_mean;
@@ -117,14 +117,17 @@ static Rs32Args make_rs_args32(
     return r;
 }
 
+// The resampling passes.  with_mon: the assign pass also records the mean
+// of the resampled particles (for a host that reads the monitor right after
+// resampling); the filter's own runs leave it to the next step's kernel.
 static void launch_resample32(
-    vsmc_cuda_pf *pf, const float *mon_state, int force)
+    vsmc_cuda_pf *pf, const float *mon_state, int force, bool with_mon)
 {
-    const Rs32Args r = make_rs_args32(pf, mon_state, force);
+    const Rs32Args r = make_rs_args32(pf, mon_state, force, with_mon);
     cudaStream_t st = pf->stream;
     k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     launch_rs32_count(pf->grid_rs, st, r);
-    k_rs32_assign<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
+    launch_rs32_assign(pf->grid_rs, st, r);
     k_rs32_markmax<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     k_rs32_fill<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
 }
@@ -136,6 +139,9 @@ static int launch_step_kernel32(vsmc_cuda_pf *pf, bool first)
     vsmc_cuda_pf_step_desc d;
     step_desc(pf, &d);
     d.step = first ? 0 : (pf->t > 0 ? pf->t : 1);
+    // the previous step's post-resample mean from this step's input (a
+    // resample-move sweep records its own)
+    d.record_previous_mean = pf->mcmc_sweeps == 0 ? 1 : 0;
     const int rc = pf_step_launch(d, cv_model(pf));
     if (rc == VSMC_CUDA_ERR_CUDA)
         set_last_cuda_error(cudaGetLastError());
@@ -167,7 +173,10 @@ static int launch_step32(vsmc_cuda_pf *pf, bool first)
     const int rc = launch_step_kernel32(pf, first);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    launch_resample32(pf, buf32(pf, 1 - pf->cur), 0);
+    // the filter's own runs take a resampled step's monitor from the next
+    // step (resample-move sweeps replace it from t = 1; the assign pass
+    // covers a resampled t = 0 then)
+    launch_resample32(pf, buf32(pf, 1 - pf->cur), 0, pf->mcmc_sweeps > 0);
     launch_post32(pf);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
@@ -396,6 +405,8 @@ static void free_all(vsmc_cuda_pf *pf)
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
+    if (pf->sc_host)
+        cudaFreeHost(pf->sc_host);
     if (pf->p64)
         pf64_destroy(pf);
     if (pf->own_stream && pf->stream)
@@ -487,11 +498,17 @@ static int pf_create(vsmc_cuda_pf **out, size_t n, size_t dim,
     PF_TRY(dalloc(&pf->h_logz, max_steps));
     PF_TRY(dalloc(&pf->h_res, max_steps));
     PF_TRY(dalloc(&pf->sc, 1));
+    if (cudaMallocHost(&pf->sc_host, sizeof(PfScalars)) != cudaSuccess) {
+        pf->sc_host = nullptr;
+        PF_TRY(VSMC_CUDA_ERR_ALLOC);
+    }
     if (precision == 32) {
         if (model) {
             // looked up here, outside any stream capture of a step
-            pf_step_occupancy<CvModel, true>();
-            pf_step_occupancy<CvModel, false>();
+            pf_step_occupancy<CvModel, true, PfMon::Previous>();
+            pf_step_occupancy<CvModel, false, PfMon::Previous>();
+            pf_step_occupancy<CvModel, true, PfMon::Current>();
+            pf_step_occupancy<CvModel, false, PfMon::Current>();
         }
         const size_t sms = static_cast<size_t>(num_sms());
         pf->max_grid = sms * 16;
@@ -598,7 +615,7 @@ int vsmc_cuda_pf_step_commit(vsmc_cuda_pf *pf)
         return VSMC_CUDA_ERR_ARG;
     pf->cur = 1 - pf->cur;
     if (pf->threshold >= 0)
-        launch_resample32(pf, buf32(pf, pf->cur), 0);
+        launch_resample32(pf, buf32(pf, pf->cur), 0, true);
     VSMC_CUDA_CHECK_LAUNCH();
     ++pf->t;
     pf->host_equal = false;
@@ -624,7 +641,7 @@ int vsmc_cuda_pf_resample_now(vsmc_cuda_pf *pf)
             pf->stream>>>(static_cast<float *>(pf->weight),
             static_cast<uint32_t>(pf->n), pf->sc);
     }
-    launch_resample32(pf, buf32(pf, pf->cur), 1);
+    launch_resample32(pf, buf32(pf, pf->cur), 1, true);
     VSMC_CUDA_CHECK_LAUNCH();
     pf->host_equal = true;
     return VSMC_CUDA_OK;
@@ -663,10 +680,11 @@ int vsmc_cuda_pf_get_status(vsmc_cuda_pf *pf, vsmc_cuda_pf_status *out)
 {
     if (pf == nullptr || out == nullptr || pf->precision != 32)
         return VSMC_CUDA_ERR_ARG;
-    PfScalars sc;
-    VSMC_CUDA_TRY(cudaMemcpyAsync(
-        &sc, pf->sc, sizeof(sc), cudaMemcpyDeviceToHost, pf->stream));
+    // pinned: the copy goes straight into it, without a staging buffer
+    VSMC_CUDA_TRY(cudaMemcpyAsync(pf->sc_host, pf->sc, sizeof(PfScalars),
+        cudaMemcpyDeviceToHost, pf->stream));
     VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
+    const PfScalars &sc = *pf->sc_host;
     *out = vsmc_cuda_pf_status{};
     out->ess = sc.ess;
     out->log_evidence = sc.logz;
@@ -724,7 +742,7 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
         static_cast<uint32_t>(rng->ctr[3]), rng->index);
     k_rs32_qsum<<<grid, kPfBlock, 0, st>>>(r);
     launch_rs32_count(grid, st, r);
-    k_rs32_assign<<<grid, kPfBlock, 0, st>>>(r);
+    launch_rs32_assign(grid, st, r);
     k_rs32_markmax<<<grid, kPfBlock, 0, st>>>(r);
     k_rs32_fill<<<grid, kPfBlock, 0, st>>>(r);
     VSMC_CUDA_CHECK_LAUNCH();
@@ -808,13 +826,29 @@ static int pf_next(vsmc_cuda_pf *pf)
     return VSMC_CUDA_OK;
 }
 
-// The FP64 filter records step t's monitor inside step t + 1; its last step
-// needs one more kernel.  The FP32 step records its own.
+// Both filters record step t's monitor inside step t + 1 (from the
+// particles that step reads); the last step needs one more kernel.  With
+// resample-move sweeps the FP32 steps record their own (and the sweeps
+// replace a resampled step's).
 static int pf_flush_mean(vsmc_cuda_pf *pf)
 {
-    if (pf->precision == 32 || !pf->mean_pending || pf->t == 0)
+    if (!pf->mean_pending || pf->t == 0)
         return VSMC_CUDA_OK;
-    const int rc = pf64_final_mean(pf);
+    int rc = VSMC_CUDA_OK;
+    if (pf->precision == 32) {
+        if (!pf->custom && pf->mcmc_sweeps == 0) {
+            const PfStepArgs a =
+                step_args(pf, buf32(pf, pf->cur), buf32(pf, 1 - pf->cur));
+            int grid = grid_for(pf->n, kPfBlock, 4, 4);
+            if (static_cast<size_t>(grid) > pf->max_grid)
+                grid = static_cast<int>(pf->max_grid);
+            k_pf32_final_mean<<<grid, kPfBlock, 0, pf->stream>>>(
+                a, static_cast<uint32_t>(pf->mon_dim));
+            VSMC_CUDA_CHECK_LAUNCH();
+        }
+    } else {
+        rc = pf64_final_mean(pf);
+    }
     if (rc == VSMC_CUDA_OK)
         pf->mean_pending = false;
     return rc;
@@ -1130,7 +1164,7 @@ extern "C" int vsmc_cuda_resample_fixed_noalloc(size_t n, const uint64_t *q,
     const int g = static_cast<int>(grid);
     k_rs32_qsum<<<g, kPfBlock, 0, st>>>(r);
     launch_rs32_count(g, st, r);
-    k_rs32_assign<<<g, kPfBlock, 0, st>>>(r);
+    launch_rs32_assign(g, st, r);
     k_rs32_markmax<<<g, kPfBlock, 0, st>>>(r);
     k_rs32_fill<<<g, kPfBlock, 0, st>>>(r);
     VSMC_CUDA_CHECK_LAUNCH();

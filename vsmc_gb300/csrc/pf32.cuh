@@ -85,16 +85,19 @@ __device__ __forceinline__ float4 ld4(const float *p, uint32_t i)
     return pf_ld4(p + i);
 }
 
-// Monitor of equal-weight particles: block sums of the first mon_dim rows
-// of `rows` (FP32 per thread, FP64 across warps) go to part[block].mon; the
-// last block to finish (sc->done2) writes their mean to sc->mean and, for
-// a recorded step, to h_mean[t].  Called by every thread of the block.
-__device__ __forceinline__ void equal_mean_finish(const float (&acc)[kMaxMonitorDim],
-    uint32_t mon_dim, double inv_n, PfPartial *part, PfScalars *sc,
-    double *h_mean, uint32_t t, uint32_t max_steps)
+// Monitor from per-thread sums: block sums of the first mon_dim rows (FP32
+// per thread, FP64 across warps) go to part[block].mon, the block's weight
+// total (weighted) to part[block].prev_w; the last block to finish
+// (sc->done2) writes the mean (sums over the weight total, or times inv_n
+// for equal weights) to sc->mean and, for a recorded step, to h_mean[t].
+// Called by every thread of the block; wblock is the block's weight total.
+__device__ __forceinline__ void mean_finish(const float (&acc)[kMaxMonitorDim],
+    double wblock, bool weighted, double inv_n, uint32_t mon_dim,
+    PfPartial *part, PfScalars *sc, double *h_mean, uint32_t t,
+    uint32_t max_steps)
 {
     constexpr int kW = kPfBlock / 32;
-    __shared__ double sh[kMaxMonitorDim][kW];
+    __shared__ double sh[kMaxMonitorDim + 1][kW];
     __shared__ bool is_last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -113,28 +116,60 @@ __device__ __forceinline__ void equal_mean_finish(const float (&acc)[kMaxMonitor
 #pragma unroll
             for (int d = 0; d < kMaxMonitorDim; ++d)
                 p.mon[d] += sh[d][w];
+        p.prev_w = wblock;
         part[blockIdx.x] = p;
         __threadfence();
         is_last = atomicAdd(&sc->done2, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!is_last || threadIdx.x != 0)
+    if (!is_last)
         return;
+    // the last block: every thread sums a stride of the blocks' records
     __threadfence();
-    double tot[kMaxMonitorDim] = {};
-    for (uint32_t b = 0; b < gridDim.x; ++b)
+    double tot[kMaxMonitorDim + 1] = {};
+    for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
 #pragma unroll
         for (int d = 0; d < kMaxMonitorDim; ++d)
             tot[d] += __ldcg(&part[b].mon[d]);
+        tot[kMaxMonitorDim] += __ldcg(&part[b].prev_w);
+    }
+#pragma unroll
+    for (int d = 0; d <= kMaxMonitorDim; ++d) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            tot[d] += __shfl_xor_sync(0xFFFFFFFFu, tot[d], o);
+        if (lane == 0)
+            sh[d][wid] = tot[d];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    double wsum = 0;
+    for (int w = 0; w < kW; ++w)
+        wsum += sh[kMaxMonitorDim][w];
+    const double scale = weighted ? 1.0 / wsum : inv_n;
 #pragma unroll
     for (int d = 0; d < kMaxMonitorDim; ++d) {
         if (static_cast<uint32_t>(d) >= mon_dim)
             break;
-        sc->mean[d] = tot[d] * inv_n;
+        double v = 0;
+        for (int w = 0; w < kW; ++w)
+            v += sh[d][w];
+        sc->mean[d] = v * scale;
         if (t < max_steps)
-            h_mean[static_cast<size_t>(t) * mon_dim + d] = tot[d] * inv_n;
+            h_mean[static_cast<size_t>(t) * mon_dim + d] = v * scale;
     }
     sc->done2 = 0;
+}
+
+// the mean of equal-weight particles (sums times 1 / n)
+__device__ __forceinline__ void equal_mean_finish(
+    const float (&acc)[kMaxMonitorDim], uint32_t mon_dim, double inv_n,
+    PfPartial *part, PfScalars *sc, double *h_mean, uint32_t t,
+    uint32_t max_steps)
+{
+    mean_finish(acc, 0.0, false, inv_n, mon_dim, part, sc, h_mean, t,
+        max_steps);
 }
 
 // out = in gathered through idx (materializes a pending resample)
@@ -151,6 +186,56 @@ __global__ void __launch_bounds__(kPfBlock) k_pf32_materialize(
         for (uint32_t d = 0; d < dim; ++d)
             a.out[d * a.stride + i] = a.in[d * a.stride + src];
     }
+}
+
+// The last step's monitor, for runs whose steps record the previous step's
+// (the filter's own runs): the weighted mean of the current particles,
+// read through a pending gather; equal weights after a resample,
+// exp(lw - M) otherwise.  FP32 within a thread and a warp, FP64 across
+// warps and blocks, as the step kernel forms it.
+__global__ void __launch_bounds__(kPfBlock) k_pf32_final_mean(
+    const PfStepArgs a, uint32_t mon_dim)
+{
+    const int resampled = a.sc->resampled;
+    const bool gather = a.sc->gather != 0;
+    const float M = static_cast<float>(a.sc->M);
+    float macc[kMaxMonitorDim] = {};
+    float sw = 0.0f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+         i += gridDim.x * blockDim.x) {
+        uint32_t src = gather ? pf_source(a.srcs, a.idx[i]) : i;
+        if (src >= a.n) {
+            atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+            src = 0;
+        }
+        const float w = resampled ? 1.0f : __expf(a.lw[i] - M);
+        sw += w;
+#pragma unroll
+        for (int d = 0; d < kMaxMonitorDim; ++d)
+            if (static_cast<uint32_t>(d) < mon_dim)
+                macc[d] = fmaf(w, a.in[d * a.stride + src], macc[d]);
+    }
+    // the block's weight total (FP64 across warps) for the mean's divisor
+    constexpr int kW = kPfBlock / 32;
+    __shared__ double shw[kW];
+    __shared__ double wtot;
+    double v = sw;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        shw[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int w = 0; w < kW; ++w)
+            s += shw[w];
+        wtot = s;
+    }
+    __syncthreads();
+    mean_finish(macc, wtot, true, 0.0, mon_dim, a.part, a.sc, a.h_mean,
+        a.sc->step - 1, a.max_steps);
 }
 
 __global__ void k_pf32_clear_gather(PfScalars *sc)
@@ -384,6 +469,7 @@ inline void launch_rs32_count(int grid, cudaStream_t st, const Rs32Args &a)
 // idx[i] = -(e + 1) for the e-th empty slot (its source is srcs[e], filled
 // below); marks[first surplus rank of a parent with two or more copies] =
 // parent + 1.
+template <bool Mon>
 __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
 {
     if (!a.sc->resampled)
@@ -412,8 +498,17 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
             engine_advance(sc, jf < a.n ? jf + 1 : a.n);
         }
     }
-    // monitor of the resampled particles: sum_i rep_i x_{d,i}
+    // monitor of the resampled particles, sum_i rep_i x_{d,i}, when the
+    // host asks for it right after resampling (mon_dim > 0); the rows, like
+    // the counts, are loaded one tile ahead
+    const uint32_t md = Mon ? a.mon_dim : 0u;
     float macc[kMaxMonitorDim] = {};
+    float4 mrow[kMaxMonitorDim], mnxt[kMaxMonitorDim];
+#pragma unroll
+    for (int d = 0; d < kMaxMonitorDim; ++d)
+        mnxt[d] = static_cast<uint32_t>(d) < md
+            ? load_row4(a.mon_state + d * a.stride, lo + threadIdx.x * 4, hi)
+            : make_float4(0, 0, 0, 0);
     // the next tile's counts are loaded while this one is scanned
     int4 nxt = load_rep4(a.rep, lo + threadIdx.x * 4, hi);
     for (uint32_t base = lo; base < hi; base += kPfTile) {
@@ -421,23 +516,22 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         const int4 cur = nxt;
         if (base + kPfTile < hi)
             nxt = load_rep4(a.rep, i0 + kPfTile, hi);
-        const int32_t r[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
         for (int d = 0; d < kMaxMonitorDim; ++d) {
-            if (static_cast<uint32_t>(d) >= a.mon_dim)
-                break;
-            const float *row = a.mon_state + d * a.stride;
-            if (i0 + 3 < hi) {
-                const float4 X = ld4(row, i0);
-                macc[d] += static_cast<float>(r[0]) * X.x +
-                    static_cast<float>(r[1]) * X.y +
-                    static_cast<float>(r[2]) * X.z +
-                    static_cast<float>(r[3]) * X.w;
-            } else {
-                for (uint32_t k = 0; k < 4 && i0 + k < hi; ++k)
-                    macc[d] += static_cast<float>(r[k]) * row[i0 + k];
-            }
+            mrow[d] = mnxt[d];
+            if (static_cast<uint32_t>(d) < md && base + kPfTile < hi)
+                mnxt[d] = load_row4(a.mon_state + d * a.stride,
+                    i0 + kPfTile, hi);
         }
+        const int32_t r[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+        for (int d = 0; d < kMaxMonitorDim; ++d)
+            if (static_cast<uint32_t>(d) < md)
+                macc[d] += static_cast<float>(max(r[0], 0)) * mrow[d].x +
+                    static_cast<float>(max(r[1], 0)) * mrow[d].y +
+                    static_cast<float>(max(r[2], 0)) * mrow[d].z +
+                    static_cast<float>(max(r[3], 0)) * mrow[d].w;
+
         uint32_t tr = 0, te = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -484,9 +578,18 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         coff += static_cast<uint32_t>(tot >> 32);
         eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
     }
-    if (a.mon_dim > 0)
-        equal_mean_finish(macc, a.mon_dim, 1.0 / static_cast<double>(a.n),
+    if (Mon && md > 0)
+        equal_mean_finish(macc, md, 1.0 / static_cast<double>(a.n),
             a.mon_part, a.sc, a.h_mean, a.sc->step - 1, a.max_steps);
+}
+
+// the assign pass, with the resampled particles' mean when asked for
+inline void launch_rs32_assign(int grid, cudaStream_t st, const Rs32Args &a)
+{
+    if (a.mon_dim > 0)
+        k_rs32_assign<true><<<grid, kPfBlock, 0, st>>>(a);
+    else
+        k_rs32_assign<false><<<grid, kPfBlock, 0, st>>>(a);
 }
 
 __device__ __forceinline__ void rank_range(

@@ -99,11 +99,10 @@ __device__ __forceinline__ void engine_advance(PfScalars &sc, uint64_t k)
 // are integers.  The counts follow from one exact floor(C N / Q) with its
 // remainder per CDF value.
 struct CountP {
-    uint64_t Q;  // CDF total
-    uint64_t G;  // systematic: ceil(a Q / 2^32) (one word for every j)
+    uint64_t Q;     // CDF total
+    uint64_t G;     // systematic: ceil(a Q / 2^32) (one word for every j)
     uint32_t n;
-    int sh;      // Q >> sh < 2^24
-    float scale; // n / (Q >> sh)
+    double dscale;  // n / Q
 };
 
 __device__ __forceinline__ uint64_t ceil_aq(uint32_t a, uint64_t Q)
@@ -120,10 +119,7 @@ __device__ __forceinline__ CountP make_count_params(
     p.Q = Q;
     p.G = ceil_aq(a_sys, Q);
     p.n = n;
-    const int bits = 64 - __clzll(static_cast<long long>(Q));
-    p.sh = bits > 24 ? bits - 24 : 0;
-    p.scale = static_cast<float>(n) /
-        __uint2float_rz(static_cast<uint32_t>(Q >> p.sh));
+    p.dscale = static_cast<double>(n) / static_cast<double>(Q);
     return p;
 }
 
@@ -139,10 +135,11 @@ __device__ __forceinline__ bool cn_divmod(uint64_t C, uint64_t G,
         --xh;
     }
     xl -= G;
-    // estimate within a few units of the answer
-    const float f =
-        __uint2float_rz(static_cast<uint32_t>(C >> p.sh)) * p.scale;
-    long long jj = static_cast<long long>(__float2int_rz(f)) - 2;
+    // estimate within a unit or two of the answer: C n / Q in FP64 is off
+    // by at most n 2^-51 + 1 (three roundings), below 2 for any n < 2^31
+    // (one FP64 product per call; callers make one per block or fewer)
+    const double f = static_cast<double>(C) * p.dscale;
+    long long jj = static_cast<long long>(f) - 2;
     if (jj < 0)
         jj = 0;
     if (jj > static_cast<long long>(p.n))
@@ -220,32 +217,53 @@ __device__ __forceinline__ QR qr_add(const QR &a, const QR &b, uint64_t Q)
     return c;
 }
 
-// Bring r below Q, adding the quotient to j.  A float estimate held below
-// the true quotient removes most of it; each round cuts r / Q by about 2^18,
-// so a few rounds finish (bounded; error bit if the bound is hit).
+// A quotient estimate of r / Q that never exceeds the true quotient.  The
+// conversion of r (toward zero, then one rounding) is within 1.5 2^-23 of
+// r, invQ = rcp(float(Q)) within 2^-23 of 1 / Q, and the two products add
+// 2^-23: est <= (r / Q)(1 + 3.5 2^-23)(1 - 2^-20) < r / Q.  Its floor is at
+// most the quotient, and at least the quotient minus (r / Q) 1.4e-6 + 1.
+__device__ __forceinline__ uint32_t quot_below(uint64_t r, float invQ)
+{
+    const float est = fmaf(__uint2float_rz(static_cast<uint32_t>(r >> 32)),
+                          4294967296.0f,
+                          __uint2float_rz(static_cast<uint32_t>(r))) *
+        invQ * (1.0f - 0x1p-20f);
+    return __float2uint_rz(est);
+}
+
+// Bring r below Q, adding the quotient to j.  No copy and one copy (r < 2Q)
+// are the common cases.  Otherwise one estimate from below leaves at most
+// (r / Q) 1.4e-6 + 1 (below 2 for fewer than 7e5 copies) and one
+// conditional step usually finishes; a position advanced by q n with q <= Q
+// has r < Q (n + 1), a quotient below 2^31, so a second estimate (below 2
+// left after it) and one more step always do.  No path loops, so a warp
+// whose lanes need different numbers of copies does not iterate.
 __device__ __forceinline__ void qr_reduce(
     uint64_t &r, uint32_t &j, uint64_t Q, float invQ, uint32_t &err)
 {
-    // the common case: r < 2Q (at most one more multiple)
     if (r < Q)
         return;
     r -= Q;
     ++j;
-    int guard = 0;
-    while (r >= Q) {
-        const float est = fmaf(__uint2float_rz(static_cast<uint32_t>(r >> 32)),
-                              4294967296.0f,
-                              __uint2float_rz(static_cast<uint32_t>(r))) *
-            invQ;
-        uint32_t d = 1;
-        if (est > 4.0f)
-            d = __float2uint_rz(est * 0.999998f) - 2;
+    if (r < Q)
+        return;
+    uint32_t d = quot_below(r, invQ);
+    r -= static_cast<uint64_t>(d) * Q;
+    j += d;
+    if (r >= Q) {
+        r -= Q;
+        ++j;
+    }
+    if (r >= Q) { // more than 7e5 copies: a second estimate
+        d = quot_below(r, invQ);
         r -= static_cast<uint64_t>(d) * Q;
         j += d;
-        if (++guard > 16) {
-            err |= DEV_ERR_BOUND;
-            break;
+        if (r >= Q) {
+            r -= Q;
+            ++j;
         }
+        if (r >= Q) // unreachable by the bounds above; recorded if ever
+            err |= DEV_ERR_BOUND;
     }
 }
 
@@ -442,6 +460,20 @@ __device__ __forceinline__ int4 load_rep4(
     v.y = i0 + 1 < hi ? rep[i0 + 1] : -1;
     v.z = i0 + 2 < hi ? rep[i0 + 2] : -1;
     v.w = i0 + 3 < hi ? rep[i0 + 3] : -1;
+    return v;
+}
+
+// row values i0..i0+3 below hi (0 past hi); i0 is a multiple of 4
+__device__ __forceinline__ float4 load_row4(
+    const float *row, uint32_t i0, uint32_t hi)
+{
+    if (i0 + 3 < hi)
+        return __ldcs(reinterpret_cast<const float4 *>(row + i0));
+    float4 v;
+    v.x = i0 + 0 < hi ? row[i0 + 0] : 0.0f;
+    v.y = i0 + 1 < hi ? row[i0 + 1] : 0.0f;
+    v.z = i0 + 2 < hi ? row[i0 + 2] : 0.0f;
+    v.w = i0 + 3 < hi ? row[i0 + 3] : 0.0f;
     return v;
 }
 

@@ -40,6 +40,7 @@ struct vsmc_cuda_pf {
     double *h_ess = nullptr, *h_logz = nullptr;
     int *h_res = nullptr;
     vsmc_cuda::PfScalars *sc = nullptr;
+    vsmc_cuda::PfScalars *sc_host = nullptr; // pinned copy for status reads
 
     // FP32 fused-step workspace
     size_t max_grid = 0; // records in `part`
