@@ -443,8 +443,8 @@ def run_batched(args):
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             # per run: the observation conversion and the reset, then per
-            # global step the step kernel and the five resampling passes
-            "gpu_launches": (2 + 6 * (int(T.max()) + 1)) * args.steps,
+            # global step the step kernel and the three resampling passes
+            "gpu_launches": (2 + 4 * (int(T.max()) + 1)) * args.steps,
         }
         line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
         print(json.dumps(line), flush=True)
@@ -538,6 +538,47 @@ def run_micro(args):
             "particles": n, "seconds": sec, "particles_per_s": n / sec,
             "GB_per_s": 12 * n / sec / 1e9,
             "frac_hbm": 12 * n / sec / 1e9 / peak}
+    # the learned proposal's network on the tensor cores: loss + gradient
+    # of a 65536-row minibatch (weight gradients on tcgen05), and the
+    # forward pass over 2^20 rows in both forms (mma.sync per warp, tcgen05
+    # per 128-row tile)
+    mlp_items = [name for name in ("mlp_loss_grad", "mlp_forward",
+                                   "mlp_forward_tc") if keep(name)]
+    if mlp_items and wanted is not None:
+        nparams = ctypes.c_size_t()
+        npacked = ctypes.c_size_t()
+        vc.call("vsmc_cuda_mlp_sizes", ctypes.byref(nparams),
+                ctypes.byref(npacked))
+        g = np.random.default_rng(5)
+        params = torch.from_numpy(
+            g.normal(0, 0.3, nparams.value).astype(np.float32)).cuda()
+        packed = torch.empty(npacked.value, dtype=torch.int32, device="cuda")
+        vc.call("vsmc_cuda_mlp_pack", params.data_ptr(), packed.data_ptr(),
+                sptr)
+        flops_row = 2.0 * (6 * 64 + 64 * 64 + 64 * 8)  # useful forward MACs
+        for name in mlp_items:
+            B = 1 << 16 if name == "mlp_loss_grad" else 1 << 20
+            feat = torch.from_numpy(
+                g.normal(0, 1, (B, 6)).astype(np.float32)).cuda()
+            if name == "mlp_loss_grad":
+                nu = torch.from_numpy(
+                    g.normal(0, 1, (B, 4)).astype(np.float32)).cuda()
+                loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+                grad = torch.zeros(nparams.value, dtype=torch.float32,
+                                   device="cuda")
+                fn = lambda: vc.call(  # noqa: E731
+                    "vsmc_cuda_mlp_loss_grad", packed.data_ptr(), B,
+                    feat.data_ptr(), nu.data_ptr(), loss.data_ptr(),
+                    grad.data_ptr(), sptr)
+            else:
+                out = torch.empty((B, 8), dtype=torch.float32, device="cuda")
+                entry = "vsmc_cuda_" + name
+                fn = lambda: vc.call(  # noqa: E731
+                    entry, packed.data_ptr(), B, feat.data_ptr(),
+                    out.data_ptr(), sptr)
+            sec = timed(fn)
+            items[name] = {"rows": B, "seconds": sec, "rows_per_s": B / sec,
+                           "forward_TFLOP_per_s": flops_row * B / sec / 1e12}
     clocks.stop()
     # end to end: Philox words into pinned host memory through the C ABI
     host = torch.empty(4 * nw, dtype=torch.uint8, pin_memory=True)
@@ -1051,16 +1092,16 @@ def main():
     e2e_value = aggregate_rate(psteps * e2e_steps, world, e2e_max)
     peak, peak_kind = measured_peaks()
     achieved = BYTES_PER_PARTICLE_STEP * n / (kernel_ms / 1000.0) / 1e9
-    # DRAM bytes per launch from the step kernel's ncu capture (bytes per
-    # particle at N = 2^23, scaled to this launch's particles)
+    # DRAM bytes per launch from the step kernel's ncu capture at the
+    # bench's own size (N = 2^24); scaled by particles for another N
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_pf32_step_N2e23.md")
+    prof = os.path.join(ROOT, "profiles", "k_pf_step_N2e24.md")
     if os.path.exists(prof):
         import re
         with open(prof) as fh:
-            mt = re.search(r"dram bytes per particle:\s*([0-9.]+)", fh.read())
+            mt = re.search(r"dram bytes per launch:\s*([0-9.]+)", fh.read())
         if mt:
-            traffic = float(mt.group(1)) * n
+            traffic = float(mt.group(1)) * n / float(1 << 24)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -1072,10 +1113,10 @@ def main():
                          "resampling as in the reference"}
 
     if rank == 0:
-        # reset, T steps of 6 kernels (the fused step and 5 resampling
-        # kernels, which return at once on steps that do not resample),
+        # reset, T steps of 4 kernels (the fused step and 3 resampling
+        # passes, which return at once on steps that do not resample),
         # final mean
-        launches_per_run = 1 + 6 * T + 1
+        launches_per_run = 1 + 4 * T + 1
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,

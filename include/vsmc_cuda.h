@@ -110,6 +110,21 @@ int vsmc_cuda_rng_normal(vsmc_cuda_rng *rng, size_t n, double *r, double mean,
 int vsmc_cuda_rng_normal_f32(vsmc_cuda_rng *rng, size_t n, float *r,
     float mean, float stddev, void *stream);
 
+/* student_t_distribution: n Student-t(df) variates with the reference's
+ * batch semantics (rng/student_t_distribution.hpp:97-128): per chunk of at
+ * most 1024, chi-squared by the batch gamma (one vectorised attempt, the
+ * accepted values packed first, a scalar GammaDistribution draw for each
+ * rejected slot; rng/gamma_distribution.hpp:230-410), then a batch of
+ * normals divided by sqrt(chi2 / df).  The engine is advanced by exactly the
+ * words the reference consumes.  Values agree within libm accuracy (a value
+ * within an ulp of an accept / reject boundary can take the other branch).
+ * The chunks are sequential in the engine stream, so one block of the GPU
+ * walks them.  Synchronizes the stream; VSMC_CUDA_ERR_TIMEOUT if a rejection
+ * loop reached its bound of 65536 tries (the variate is NaN).
+ * Replaces vsmc_rng_student_t (vsmc.h:162, lib/src/vsmc_rng.cpp:207). */
+int vsmc_cuda_rng_student_t(vsmc_cuda_rng *rng, size_t n, double *r,
+    double df, void *stream);
+
 /* Independent streams with the scalar distribution semantics: stream s is
  * the engine (kind, key) placed at counter {0, s, 0, 0}; it yields
  * per_stream variates into r[s * per_stream + k] exactly as successive
@@ -231,7 +246,7 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
  * allocate device memory while they run (inside an allocator or memory-pool
  * callback, or in a loop that reserved all device memory beforehand).  Same
  * arguments, results and engine advance as vsmc_cuda_resample_fixed; its
- * scratch is one fixed array of about 4 MiB in the library's device image.
+ * scratch is one fixed array of about 3 MiB in the library's device image.
  *   - n must be at most VSMC_CUDA_RESAMPLE_FIXED_NOALLOC_MAX_N, otherwise
  *     VSMC_CUDA_ERR_SIZE is returned before any device work;
  *   - the first call on each device (that device current) looks up the
@@ -476,13 +491,25 @@ int vsmc_cuda_bearings_simulate(uint32_t seed, size_t T,
 int vsmc_cuda_mlp_sizes(size_t *nparams, size_t *npacked);
 int vsmc_cuda_mlp_init(uint32_t seed, float *params, void *stream);
 int vsmc_cuda_mlp_pack(const float *params, uint32_t *packed, void *stream);
-/* out[B][8] = network(feat[B][6]) (BF16 operands, FP32 accumulation). */
+/* out[B][8] = network(feat[B][6]) (BF16 operands, FP32 accumulation):
+ * mma.sync fragments per warp (16 rows at a time, activations kept in
+ * registers). */
 int vsmc_cuda_mlp_forward(const uint32_t *packed, size_t B, const float *feat,
     float *out, void *stream);
+/* The same network on the Blackwell tensor core (tcgen05.mma, accumulators
+ * in tensor memory), 128 rows per tile and one thread per row.  Results
+ * agree with vsmc_cuda_mlp_forward up to FP32 summation order (and the BF16
+ * rounding of an activation that lands on a rounding boundary).  A block
+ * whose tensor-core wait runs out writes NaN for its rows. */
+int vsmc_cuda_mlp_forward_tc(const uint32_t *packed, size_t B,
+    const float *feat, float *out, void *stream);
 /* Mean loss 0.5 sum_d [(nu_d - m_d)^2 exp(-l_d) + l_d] over B rows
  * (loss_dev: 1 double, may be NULL) and its gradient with respect to the
  * parameters (grad_dev: nparams floats); the sum over rows is in a fixed
- * order. */
+ * order.  The weight gradients are contractions over the rows on the
+ * Blackwell tensor core (tcgen05.mma into tensor memory, FP32 deltas split
+ * into BF16 hi + lo parts); a block whose tensor-core wait runs out makes
+ * the result NaN. */
 int vsmc_cuda_mlp_loss_grad(const uint32_t *packed, size_t B,
     const float *feat, const float *nu, double *loss_dev, float *grad_dev,
     void *stream);

@@ -60,6 +60,7 @@ PORT_PROTOTYPES = {
     "vo_normal_f64": (None, [I32, VP, VP, SZ, F64, F64, VP, I32]),
     "vo_normal_f32": (None, [I32, VP, VP, SZ, F32, F32, VP, I32]),
     "vo_student_t_f64": (None, [I32, VP, VP, SZ, F64, VP]),
+    "vo_student_t_batch_f64": (None, [I32, VP, VP, SZ, SZ, F64, VP, VP, VP]),
     "vo_u01_sequence": (None, [I32, SZ, VP, VP, VP, VP]),
     "vo_u01_sorted": (None, [SZ, VP, VP]),
     "vo_u01_stratified": (None, [SZ, VP, VP]),

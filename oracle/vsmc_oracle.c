@@ -718,6 +718,169 @@ void vo_student_t_f64(int eng, const uint64_t key[4], const uint64_t ctr[4],
 }
 
 /* =====================================================================
+ * Student-t, batch form  (rng/student_t_distribution.hpp:97-128, which the
+ * C ABI's vsmc_rng_student_t calls, lib/src/vsmc_rng.cpp:41-64, 207): per
+ * chunk of at most 1024 variates, chi-squared = Gamma(df/2, 2) by the batch
+ * gamma (rng/gamma_distribution.hpp:230-410: one vectorised attempt of the
+ * chunk, the accepted values packed in order, then scalar draws for the
+ * rest), r = sqrt(r * (1/df)), a batch of normals z, r = z / r.
+ * ===================================================================== */
+
+/* one vectorised gamma attempt over n <= 1024 values; returns how many were
+ * accepted (rng/gamma_distribution.hpp:230-355) */
+static size_t vo_gamma_batch_once(
+    const vo_gamma *g, vo_eng *e, size_t n, double *r)
+{
+    static double s[5 * 1024];
+    const double d = g->d, c = g->c, beta = g->beta;
+    size_t m = 0;
+    if (g->alg == VO_GAMMA_T) {
+        double *u = s, *ee = s + n, *x = s + 2 * n;
+        vo_u01_distribution_d(e, 2 * n, s);
+        for (size_t i = 0; i != n; ++i)
+            ee[i] = log(ee[i]);
+        for (size_t i = 0; i != n; ++i)
+            ee[i] = -1.0 * ee[i];
+        for (size_t i = 0; i != n; ++i) {
+            if (u[i] > d) {
+                u[i] = -log(c * (1 - u[i]));
+                ee[i] += u[i];
+                u[i] = d + g->alpha * u[i];
+            }
+        }
+        for (size_t i = 0; i != n; ++i)
+            x[i] = log(u[i]);
+        for (size_t i = 0; i != n; ++i)
+            x[i] = c * x[i];
+        for (size_t i = 0; i != n; ++i)
+            x[i] = exp(x[i]);
+        for (size_t i = 0; i != n; ++i)
+            u[i] = fabs(x[i]);
+        for (size_t i = 0; i != n; ++i)
+            x[i] = beta * x[i];
+        for (size_t i = 0; i != n; ++i)
+            if (u[i] < ee[i])
+                r[m++] = x[i];
+    } else if (g->alg == VO_GAMMA_W) {
+        double *u = s, *ee = s + n, *x = s + 2 * n;
+        vo_u01_distribution_d(e, 2 * n, s);
+        for (size_t i = 0; i != 2 * n; ++i)
+            s[i] = log(s[i]);
+        for (size_t i = 0; i != 2 * n; ++i)
+            s[i] = -1.0 * s[i];
+        for (size_t i = 0; i != n; ++i)
+            x[i] = log(s[i]);
+        for (size_t i = 0; i != n; ++i)
+            x[i] = c * x[i];
+        for (size_t i = 0; i != n; ++i)
+            x[i] = exp(x[i]);
+        for (size_t i = 0; i != n; ++i)
+            u[i] = u[i] + ee[i];
+        for (size_t i = 0; i != n; ++i)
+            ee[i] = d + x[i];
+        for (size_t i = 0; i != n; ++i)
+            x[i] = beta * x[i];
+        for (size_t i = 0; i != n; ++i)
+            if (u[i] > ee[i])
+                r[m++] = x[i];
+    } else if (g->alg == VO_GAMMA_N) {
+        double *u = s, *ee = s + n, *v = s + 2 * n, *w = s + 3 * n,
+               *x = s + 4 * n;
+        vo_u01_distribution_d(e, n, u);
+        vo_normal_impl_d(e, n, w, 0, 1);
+        if (n % 2 != 0) { /* normal_distribution's odd tail */
+            const double a = vo_eng_u01d(e);
+            const double b = vo_eng_u01d(e);
+            w[n - 1] = 0 + 1 * sqrt(-2 * log(a)) * cos(VO_PI_2 * b);
+        }
+        for (size_t i = 0; i != n; ++i)
+            v[i] = c * w[i] + 1;
+        vo_normal_d rnorm = {0, 1, 0, 0};
+        for (size_t i = 0; i != n; ++i) {
+            if (v[i] <= 0) {
+                do {
+                    w[i] = vo_normal_d_draw(&rnorm, e);
+                    v[i] = 1 + c * w[i];
+                } while (v[i] <= 0);
+            }
+        }
+        for (size_t i = 0; i != n; ++i)
+            ee[i] = v[i] * v[i];
+        for (size_t i = 0; i != n; ++i)
+            v[i] = v[i] * ee[i];
+        for (size_t i = 0; i != n; ++i)
+            ee[i] = w[i] * w[i];
+        for (size_t i = 0; i != n; ++i)
+            ee[i] = ee[i] * ee[i];
+        for (size_t i = 0; i != n; ++i)
+            ee[i] = -0.0331 * ee[i] + 1;
+        const double db = d * beta;
+        for (size_t i = 0; i != n; ++i)
+            x[i] = db * v[i];
+        for (size_t i = 0; i != n; ++i) {
+            if (u[i] < ee[i]) {
+                r[m++] = x[i];
+            } else {
+                ee[i] = w[i] * w[i] / 2 + d * (1 - v[i] + log(v[i]));
+                if (log(u[i]) < ee[i])
+                    r[m++] = x[i];
+            }
+        }
+    } else {
+        vo_u01_distribution_d(e, n, r);
+        for (size_t i = 0; i != n; ++i)
+            r[i] = log(r[i]);
+        for (size_t i = 0; i != n; ++i)
+            r[i] = -beta * r[i];
+        m = n;
+    }
+    return m;
+}
+
+/* The engine placed at (key, ctr) with an exhausted buffer, `skip` words
+ * drawn through the scalar path, then student_t_distribution(rng, n, r, df).
+ * The engine's counter and buffer index afterwards go to ctr_out /
+ * index_out (either may be NULL). */
+void vo_student_t_batch_f64(int eng, const uint64_t key[4],
+    const uint64_t ctr[4], size_t skip, size_t n, double df, double *r,
+    uint64_t ctr_out[4], uint32_t *index_out)
+{
+    vo_eng e;
+    vo_eng_init(&e, eng, key, ctr);
+    for (size_t i = 0; i != skip; ++i)
+        (void)vo_eng_u01d(&e);
+    vo_gamma g;
+    vo_gamma_init(&g, df / 2, 2);
+    double z[1024];
+    for (size_t base = 0; base < n; base += 1024) {
+        const size_t k = n - base < 1024 ? n - base : 1024;
+        double *rr = r + base;
+        const size_t m = vo_gamma_batch_once(&g, &e, k, rr);
+        for (size_t i = m; i < k; ++i)
+            rr[i] = vo_gamma_draw(&g, &e);
+        const double inv = 1 / df;
+        for (size_t i = 0; i != k; ++i)
+            rr[i] = inv * rr[i];
+        for (size_t i = 0; i != k; ++i)
+            rr[i] = sqrt(rr[i]);
+        vo_normal_impl_d(&e, k, z, 0, 1);
+        if (k % 2 != 0) {
+            const double a = vo_eng_u01d(&e);
+            const double b = vo_eng_u01d(&e);
+            z[k - 1] = 0 + 1 * sqrt(-2 * log(a)) * cos(VO_PI_2 * b);
+        }
+        for (size_t i = 0; i != k; ++i)
+            rr[i] = z[i] / rr[i];
+    }
+    if (ctr_out) {
+        for (int i = 0; i < 4; ++i)
+            ctr_out[i] = eng == 0 ? e.p.ctr[i] : e.t.ctr[i];
+    }
+    if (index_out)
+        *index_out = eng == 0 ? e.p.index : e.t.index;
+}
+
+/* =====================================================================
  * u01 sequences  (rng/u01_sequence.hpp:53-89 array forms; 131-259 lazy
  * classes: only indices that are read consume engine words)
  * ===================================================================== */

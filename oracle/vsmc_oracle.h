@@ -79,6 +79,11 @@ void vo_normal_f32(int eng, const uint64_t key[4], const uint64_t ctr[4],
 /* scalar StudentTDistribution semantics only */
 void vo_student_t_f64(int eng, const uint64_t key[4], const uint64_t ctr[4],
     size_t n, double df, double *r);
+/* student_t_distribution (batch form; vsmc_rng_student_t) after `skip`
+ * scalar words; the engine state afterwards in ctr_out / index_out */
+void vo_student_t_batch_f64(int eng, const uint64_t key[4],
+    const uint64_t ctr[4], size_t skip, size_t n, double df, double *r,
+    uint64_t ctr_out[4], uint32_t *index_out);
 
 /* ------------------------------------------------------- u01 sequences */
 void vo_u01_sequence(int kind, size_t N, const uint32_t key[2],

@@ -96,6 +96,14 @@ def dists(R):
             a = np.zeros(500)
             R.ref_student_t_f64(eng, P(key), P(ctr), 500, df, P(a), 0)
             out[f"student_t_e{eng}_df{df}"] = a
+            # the batch form (student_t_distribution, as vsmc_rng_student_t
+            # calls it): gamma algorithms T (0.2), W (1.5), E (2), N (3, 10)
+            if df not in (0.2, 1.5, 2.0, 3.0, 10.0):
+                continue
+            for n in (1, 7, 1025, 2049):
+                b = np.zeros(n)
+                R.ref_student_t_f64(eng, P(key), P(ctr), n, df, P(b), 1)
+                out[f"student_t_batch_e{eng}_df{df}_n{n}"] = b
     out.update(key=key, ctr=ctr)
     return out
 

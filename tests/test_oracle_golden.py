@@ -90,6 +90,14 @@ def test_distributions(port):
             a = np.zeros(500)
             port.vo_student_t_f64(eng, P(key), P(ctr), 500, df, P(a))
             assert np.array_equal(a, g[f"student_t_e{eng}_df{df}"])
+            if df not in (0.2, 1.5, 2.0, 3.0, 10.0):
+                continue
+            for n in (1, 7, 1025, 2049):
+                b = np.zeros(n)
+                port.vo_student_t_batch_f64(eng, P(key), P(ctr), 0, n, df,
+                                            P(b), None, None)
+                assert np.array_equal(
+                    b, g[f"student_t_batch_e{eng}_df{df}_n{n}"]), (eng, df, n)
 
 
 def test_sequences(port):

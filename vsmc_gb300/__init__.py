@@ -132,6 +132,7 @@ PROTOTYPES = {
     "vsmc_cuda_rng_u01_f32": (I32, [_RNGP, SZ, VP, VP]),
     "vsmc_cuda_rng_normal": (I32, [_RNGP, SZ, VP, F64, F64, VP]),
     "vsmc_cuda_rng_normal_f32": (I32, [_RNGP, SZ, VP, F32, F32, VP]),
+    "vsmc_cuda_rng_student_t": (I32, [_RNGP, SZ, VP, F64, VP]),
     "vsmc_cuda_normal_streams": (I32, [I32, VP, SZ, SZ, F64, F64, VP, VP]),
     "vsmc_cuda_student_t_streams": (I32, [I32, VP, SZ, SZ, F64, VP, VP]),
     "vsmc_cuda_u01_sorted": (I32, [SZ, VP, VP, VP]),
@@ -211,6 +212,7 @@ PROTOTYPES = {
     "vsmc_cuda_mlp_init": (I32, [U32, VP, VP]),
     "vsmc_cuda_mlp_pack": (I32, [VP, VP, VP]),
     "vsmc_cuda_mlp_forward": (I32, [VP, SZ, VP, VP, VP]),
+    "vsmc_cuda_mlp_forward_tc": (I32, [VP, SZ, VP, VP, VP]),
     "vsmc_cuda_mlp_loss_grad": (I32, [VP, SZ, VP, VP, VP, VP, VP]),
     "vsmc_cuda_mlp_train": (I32, [_BMODELP, U32, SZ, SZ, SZ, SZ, F64, VP,
                                   VP, VP]),

@@ -3,7 +3,7 @@
 // Thousands of independent filters, each with its own particle count,
 // horizon, model constants and seed, advance together: per global step one
 // persistent kernel moves, weights and reduces the particles of every filter
-// still running, and five kernels resample the filters whose ESS fell below
+// still running, and three kernels resample the filters whose ESS fell below
 // the threshold, in equal chunks listed by the step kernel.  A whole run
 // (every step of the longest horizon) is one CUDA graph.
 //
@@ -82,7 +82,7 @@ struct BatchArgs {
     float *bx, *by, *bvx, *bvy;       // state out
     float *lw;
     int32_t *rep, *idx;
-    uint32_t *marks, *srcs;
+    uint32_t *srcs;
     TileRecord *part; // per tile
     const float *obs; // the observations in FP32 (converted once per run)
     const float2 *obs_sc; // bearings kinds: (sin z, cos z) of each bearing
@@ -95,7 +95,7 @@ struct BatchArgs {
     uint32_t *rs_count;
     uint32_t *work; // step kernel's tile counters, by step parity
     uint64_t *rs_q;
-    uint32_t *rs_e, *rs_c, *rs_m;
+    uint32_t *rs_e, *rs_c;
     uint32_t rs_cap, rpar;
     const uint32_t *packed; // proposal network (learned kind)
     uint32_t nfilters, tmax;
@@ -660,14 +660,14 @@ __global__ void __launch_bounds__(kLearnBlock) k_batch_step_learned(
 
 // ---------------------------------------------------------------- resampling
 //
-// The filters that resample at a step are resampled together by five
+// The filters that resample at a step are resampled together by three
 // kernels over the step's list of equal chunks: entry v of the list is chunk
 // k of filter f (its particles [k c, (k + 1) c) with c = F.rs_chunk), and
 // the chunks of a filter are consecutive entries, listed by the block that
-// finished the filter's step (tile_finish).  The five passes are the single
-// filter's k_rs32_qsum / count / assign / markmax / fill: a fixed-point
-// total per chunk, replication counts, slot assignment, the max of the marks
-// per chunk of surplus ranks, and the sources of the empty slots.  A chunk
+// finished the filter's step (tile_finish).  The three passes are the single
+// filter's k_rs32_qsum / count / assign: a fixed-point total per chunk,
+// replication counts, and slot assignment with the sources of the empty
+// slots.  A chunk
 // takes its offsets from the per-chunk totals of the earlier chunks of its
 // filter (at most kMaxRsChunks, summed by every warp on its own).  Blocks
 // walk the list with a grid stride: the grids are fixed when a run is
@@ -896,15 +896,16 @@ __global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
 
 // pass 3: slot assignment.  With c copies and e empty slots before slot i,
 // the first surplus rank of i is c - (i - e); idx[i] = i for a parent,
-// -(e + 1) for the e-th empty slot; marks[first surplus rank of a parent
-// with two or more copies] = parent + 1.  Chunk 0 records the filter's
-// resample: Q, the empty count, the gather flag and the engine words the
-// scheme consumed.
+// -(e + 1) for the e-th empty slot, and the sources of the surplus ranks of
+// a parent with two or more copies are written by its warp
+// (write_surplus_runs).  Chunk 0 records the filter's resample: Q, the
+// empty count, the gather flag and the engine words the scheme consumed.
 __global__ void __launch_bounds__(kPfBlock) k_brs_assign(const BatchArgs a)
 {
     const uint32_t count = __ldcg(a.rs_count + a.rpar);
     const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
     __shared__ uint64_t sh64[kPfBlock / 32 + 1];
+    __shared__ __align__(16) uint32_t shm[kPfBlock / 32][kRunChunk];
     for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
         const RsChunk c = rs_chunk_at(a, v);
         PfScalars &S = a.st[c.f];
@@ -920,7 +921,7 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_assign(const BatchArgs a)
         chunk_totals(a.rs_c, c, OpAdd(), 0u, coff, ctotal);
         const int32_t *rep = a.rep + c.off;
         int32_t *idx = a.idx + c.off;
-        uint32_t *marks = a.marks + c.off;
+        uint32_t *srcs = a.srcs + c.off;
         if (c.k == 0 && threadIdx.x == 0) {
             S.Q = Q;
             S.nempty = etotal;
@@ -960,25 +961,42 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_assign(const BatchArgs a)
             const uint64_t exv = incl - w;
             uint32_t cc = coff + static_cast<uint32_t>(exv >> 32);
             uint32_t e = eoff + static_cast<uint32_t>(exv & 0xFFFFFFFFu);
+            const uint32_t c0 = cc, e0 = e;
             int32_t out[4];
+            uint32_t rs[4], rl[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const uint32_t i = i0 + k;
+                rs[k] = 0;
+                rl[k] = 0;
                 if (r[k] == 0) {
                     out[k] = -static_cast<int32_t>(e) - 1;
                     ++e;
                 } else {
                     out[k] = static_cast<int32_t>(i);
                     if (r[k] >= 2) {
-                        const uint32_t rk = cc - (i - e);
-                        if (rk < c.n)
-                            marks[rk] = i + 1;
-                        else
-                            err |= DEV_ERR_INTERNAL;
+                        rs[k] = cc - (i - e);
+                        rl[k] = static_cast<uint32_t>(r[k]) - 1;
                     }
                 }
                 if (r[k] > 0)
                     cc += static_cast<uint32_t>(r[k]);
+            }
+            // the sources of the warp's surplus ranks
+            {
+                const uint32_t first = c0 - (i0 - e0);
+                const uint32_t W0 = __shfl_sync(0xFFFFFFFFu, first, 0);
+                uint32_t Sw = rl[0] + rl[1] + rl[2] + rl[3];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    Sw += __shfl_xor_sync(0xFFFFFFFFu, Sw, o);
+                if (Sw != 0) {
+                    if (Sw > etotal || W0 > etotal - Sw)
+                        err |= DEV_ERR_INTERNAL;
+                    else
+                        write_surplus_runs(srcs, rs, rl, i0, W0, Sw,
+                            shm[threadIdx.x >> 5], err);
+                }
             }
             if (i0 + 3 < c.hi) {
                 *reinterpret_cast<int4 *>(idx + i0) =
@@ -991,108 +1009,6 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_assign(const BatchArgs a)
             }
             coff += static_cast<uint32_t>(tot >> 32);
             eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
-        }
-        if (err)
-            atomicOr(&S.err, err);
-    }
-}
-
-// pass 4: max of the marks over each chunk's surplus ranks (ranks [lo, hi)
-// below the filter's empty count)
-__global__ void __launch_bounds__(kPfBlock) k_brs_markmax(const BatchArgs a)
-{
-    const uint32_t count = __ldcg(a.rs_count + a.rpar);
-    __shared__ uint32_t sh[kPfBlock / 32 + 1];
-    for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
-        const RsChunk c = rs_chunk_at(a, v);
-        const uint32_t K = min(a.st[c.f].nempty, c.n);
-        const uint32_t lo = min(K, c.lo), hi = min(K, c.hi);
-        const uint32_t *marks = a.marks + c.off;
-        uint32_t mx = 0;
-        constexpr uint32_t kStep = 4 * kPfBlock;
-        for (uint32_t k0 = lo + threadIdx.x * 4; k0 < hi; k0 += 2 * kStep) {
-            const uint4 x = load_marks4(marks, k0, hi);
-            const uint4 y = k0 + kStep < hi ? load_marks4(marks, k0 + kStep, hi)
-                                            : make_uint4(0, 0, 0, 0);
-            mx = max(mx, max(max(x.x, x.y), max(x.z, x.w)));
-            mx = max(mx, max(max(y.x, y.y), max(y.z, y.w)));
-        }
-        mx = block_reduce(mx, OpMax(), 0u, sh);
-        if (threadIdx.x == 0)
-            a.rs_m[v] = mx;
-    }
-}
-
-// pass 5: the running max of the marks is the parent of each surplus rank:
-// srcs[k] = that parent; the marks are cleared for the next resample
-__global__ void __launch_bounds__(kPfBlock) k_brs_fill(const BatchArgs a)
-{
-    const uint32_t count = __ldcg(a.rs_count + a.rpar);
-    __shared__ uint32_t sh[kPfBlock / 32 + 1];
-    __shared__ uint32_t shl[kPfBlock / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    constexpr uint32_t kStep = 4 * kPfBlock;
-    for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
-        const RsChunk c = rs_chunk_at(a, v);
-        PfScalars &S = a.st[c.f];
-        const uint32_t K = min(S.nempty, c.n);
-        const uint32_t lo = min(K, c.lo), hi = min(K, c.hi);
-        if (lo >= hi)
-            continue; // the same for the whole block
-        uint32_t carry, mall;
-        chunk_totals(a.rs_m, c, OpMax(), 0u, carry, mall);
-        uint32_t *marks = a.marks + c.off;
-        uint32_t *srcs = a.srcs + c.off;
-        uint32_t err = 0;
-        uint4 nxt = load_marks4(marks, lo + threadIdx.x * 4, hi);
-        for (uint32_t base = lo; base < hi; base += kStep) {
-            const uint32_t k0 = base + threadIdx.x * 4;
-            const uint4 cur = nxt;
-            if (base + kStep < hi)
-                nxt = load_marks4(marks, k0 + kStep, hi);
-            const uint32_t mk[4] = {cur.x, cur.y, cur.z, cur.w};
-            uint32_t run[4];
-            uint32_t tmax = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                tmax = max(tmax, mk[k]);
-                run[k] = tmax;
-            }
-            uint32_t tot;
-            const uint32_t incl =
-                block_inclusive_scan(tmax, OpMax(), 0u, sh, &tot);
-            // exclusive max: the previous lane's inclusive value, or the
-            // previous warp's total for lane 0
-            uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
-            if (lane == 31)
-                shl[wid] = incl;
-            __syncthreads();
-            if (lane == 0)
-                before = wid > 0 ? shl[wid - 1] : 0u;
-            __syncthreads();
-            before = max(before, carry);
-            uint32_t out[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t rk = max(run[k], before);
-                if (k0 + k < hi && (rk == 0 || rk - 1 >= c.n))
-                    err |= DEV_ERR_INTERNAL;
-                out[k] = rk - 1;
-            }
-            if (k0 + 3 < hi) {
-                *reinterpret_cast<uint4 *>(srcs + k0) =
-                    make_uint4(out[0], out[1], out[2], out[3]);
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (k0 + k < hi)
-                        srcs[k0 + k] = out[k];
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (mk[k] && k0 + k < hi)
-                    marks[k0 + k] = 0;
-            carry = max(carry, tot);
         }
         if (err)
             atomicOr(&S.err, err);
@@ -1164,7 +1080,7 @@ __global__ void k_batch_simulate_bearings(
 
 constexpr uint32_t kRsMinChunk = 4 * kPfTile; // resampling chunk: 4096 or more
 constexpr uint32_t kMaxRsChunks = 32;          // chunks of one filter, at most
-constexpr int kRsKernels = 5;
+constexpr int kRsKernels = 3;
 // the scan schedules the autotuner times: the smallest chunk of a filter
 constexpr uint32_t kRsSchedules[] = {4096, 8192, 16384, 32768};
 constexpr int kNumSchedules = 4;
@@ -1298,11 +1214,11 @@ struct vsmc_cuda_batch {
     uint2 *d_rs_list = nullptr;
     uint32_t *d_rs_count = nullptr;
     uint64_t *d_rs_q = nullptr;
-    uint32_t *d_rs_e = nullptr, *d_rs_c = nullptr, *d_rs_m = nullptr;
+    uint32_t *d_rs_e = nullptr, *d_rs_c = nullptr;
     float *d_state[2] = {nullptr, nullptr};
     float *d_lw = nullptr;
     int32_t *d_rep = nullptr, *d_idx = nullptr;
-    uint32_t *d_marks = nullptr, *d_srcs = nullptr;
+    uint32_t *d_srcs = nullptr;
     TileRecord *d_part = nullptr;
     float *d_obsf = nullptr; // the run's observations in FP32
     float2 *d_obs_sc = nullptr; // bearings kinds: sin, cos of each bearing
@@ -1337,8 +1253,8 @@ static void batch_free(vsmc_cuda_batch *b)
         cudaGraphExecDestroy(b->graph);
     void *ptrs[] = {b->d_flt, b->d_st, b->d_tile_filter, b->d_active,
         b->d_step, b->d_rs_list, b->d_rs_count, b->d_rs_q, b->d_rs_e,
-        b->d_rs_c, b->d_rs_m, b->d_state[0], b->d_state[1], b->d_lw,
-        b->d_rep, b->d_idx, b->d_marks, b->d_srcs, b->d_part, b->d_obs, b->d_obsf, b->d_obs_sc,
+        b->d_rs_c, b->d_state[0], b->d_state[1], b->d_lw,
+        b->d_rep, b->d_idx, b->d_srcs, b->d_part, b->d_obs, b->d_obsf, b->d_obs_sc,
         b->d_mean, b->d_ess, b->d_logz, b->d_res};
     for (void *p : ptrs)
         if (p)
@@ -1404,7 +1320,6 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.lw = b->d_lw;
     a.rep = b->d_rep;
     a.idx = b->d_idx;
-    a.marks = b->d_marks;
     a.srcs = b->d_srcs;
     a.part = b->d_part;
     a.obs = b->d_obsf;
@@ -1420,7 +1335,6 @@ static BatchArgs batch_args(vsmc_cuda_batch *b, const double *obs, int cur)
     a.rs_q = b->d_rs_q;
     a.rs_e = b->d_rs_e;
     a.rs_c = b->d_rs_c;
-    a.rs_m = b->d_rs_m;
     a.rs_cap = b->rs_cap;
     a.rpar = static_cast<uint32_t>(cur); // step parity, as the state buffers
     a.packed = b->packed;
@@ -1453,8 +1367,6 @@ static int enqueue_run(
         k_brs_qsum<<<b->rs_grid[0], blk, 0, st>>>(a);
         k_brs_count<<<b->rs_grid[1], blk, 0, st>>>(a);
         k_brs_assign<<<b->rs_grid[2], blk, 0, st>>>(a);
-        k_brs_markmax<<<b->rs_grid[3], blk, 0, st>>>(a);
-        k_brs_fill<<<b->rs_grid[4], blk, 0, st>>>(a);
         VSMC_CUDA_CHECK_LAUNCH();
     }
     return VSMC_CUDA_OK;
@@ -1576,9 +1488,7 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
         const int sms = num_sms();
         const int occ[kRsKernels] = {occupancy_of(k_brs_qsum, kPfBlock),
             occupancy_of(k_brs_count, kPfBlock),
-            occupancy_of(k_brs_assign, kPfBlock),
-            occupancy_of(k_brs_markmax, kPfBlock),
-            occupancy_of(k_brs_fill, kPfBlock)};
+            occupancy_of(k_brs_assign, kPfBlock)};
         for (int k = 0; k < kRsKernels; ++k)
             b->rs_grid[k] = static_cast<int>(std::min<size_t>(
                 static_cast<size_t>(sms) * occ[k], b->rs_cap));
@@ -1612,14 +1522,12 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     B_TRY(balloc(&b->d_rs_q, b->rs_cap));
     B_TRY(balloc(&b->d_rs_e, b->rs_cap));
     B_TRY(balloc(&b->d_rs_c, b->rs_cap));
-    B_TRY(balloc(&b->d_rs_m, b->rs_cap));
     B_TRY(balloc(&b->d_step, 1));
     B_TRY(balloc(&b->d_state[0], 4 * total));
     B_TRY(balloc(&b->d_state[1], 4 * total));
     B_TRY(balloc(&b->d_lw, total));
     B_TRY(balloc(&b->d_rep, total));
     B_TRY(balloc(&b->d_idx, total));
-    B_TRY(balloc(&b->d_marks, total));
     B_TRY(balloc(&b->d_srcs, total));
     B_TRY(balloc(&b->d_part, tiles));
     B_TRY(balloc(&b->d_obs, 2 * totalT));
@@ -1630,9 +1538,6 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     B_TRY(balloc(&b->d_ess, totalT));
     B_TRY(balloc(&b->d_logz, totalT));
     B_TRY(balloc(&b->d_res, totalT));
-    if (cudaMemsetAsync(b->d_marks, 0, sizeof(uint32_t) * total, b->stream) !=
-        cudaSuccess)
-        B_TRY(VSMC_CUDA_ERR_CUDA);
     if (cudaMemsetAsync(b->d_mean, 0, sizeof(double) * 2 * totalT,
             b->stream) != cudaSuccess)
         B_TRY(VSMC_CUDA_ERR_CUDA);

@@ -101,10 +101,8 @@ static Rs32Args make_rs_args32(
     r.qpart = pf->qpart;
     r.epart = pf->epart;
     r.cpart = pf->cpart;
-    r.mpart = pf->mpart;
     r.rep = pf->rep;
     r.idx = pf->idx;
-    r.marks = pf->marks;
     r.srcs = pf->empties;
     r.sc = pf->sc;
     r.mon_state = mon_state;
@@ -128,8 +126,6 @@ static void launch_resample32(
     k_rs32_qsum<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
     launch_rs32_count(pf->grid_rs, st, r);
     launch_rs32_assign(pf->grid_rs, st, r);
-    k_rs32_markmax<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
-    k_rs32_fill<<<pf->grid_rs, kPfBlock, 0, st>>>(r);
 }
 
 // the fused step kernel of the built-in model (reads buffer cur, writes the
@@ -400,8 +396,7 @@ static void free_all(vsmc_cuda_pf *pf)
         pf->obs,
         pf->h_mean,
         pf->h_ess, pf->h_logz, pf->h_res, pf->sc, pf->part, pf->qpart,
-        pf->epart, pf->cpart, pf->mpart, pf->rep, pf->idx, pf->marks,
-        pf->empties};
+        pf->epart, pf->cpart, pf->rep, pf->idx, pf->empties};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -525,16 +520,11 @@ static int pf_create(vsmc_cuda_pf **out, size_t n, size_t dim,
         PF_TRY(dalloc(&pf->qpart, pf->grid_rs));
         PF_TRY(dalloc(&pf->epart, pf->grid_rs));
         PF_TRY(dalloc(&pf->cpart, pf->grid_rs));
-        PF_TRY(dalloc(&pf->mpart, pf->grid_rs));
         PF_TRY(dalloc(reinterpret_cast<char **>(&pf->state2),
             esz * dim * pf->stride));
         PF_TRY(dalloc(&pf->rep, n + 4));
         PF_TRY(dalloc(&pf->idx, pf->stride));
-        PF_TRY(dalloc(&pf->marks, n));
         PF_TRY(dalloc(&pf->empties, n));
-        if (cudaMemsetAsync(pf->marks, 0, sizeof(uint32_t) * n, pf->stream) !=
-            cudaSuccess)
-            PF_TRY(VSMC_CUDA_ERR_CUDA);
     } else {
         PF_TRY(pf64_create(pf));
     }
@@ -726,16 +716,13 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
     r.qpart = scratch.get<uint64_t>(grid);
     r.epart = scratch.get<uint32_t>(grid);
     r.cpart = scratch.get<uint32_t>(grid);
-    r.mpart = scratch.get<uint32_t>(grid);
     r.rep = scratch.get<int32_t>(n + 4);
     r.idx = scratch.get<int32_t>(n + 4);
-    r.marks = scratch.get<uint32_t>(n);
     r.srcs = scratch.get<uint32_t>(n);
     r.sc = scratch.get<PfScalars>(1);
-    if (!r.qpart || !r.epart || !r.cpart || !r.mpart || !r.rep || !r.idx ||
-        !r.marks || !r.srcs || !r.sc)
+    if (!r.qpart || !r.epart || !r.cpart || !r.rep || !r.idx || !r.srcs ||
+        !r.sc)
         return VSMC_CUDA_ERR_ALLOC;
-    VSMC_CUDA_TRY(cudaMemsetAsync(r.marks, 0, sizeof(uint32_t) * n, st));
     k_rs32_setup<<<1, 1, 0, st>>>(r.sc, static_cast<uint32_t>(rng->key[0]),
         static_cast<uint32_t>(rng->key[1]), static_cast<uint32_t>(rng->ctr[0]),
         static_cast<uint32_t>(rng->ctr[1]), static_cast<uint32_t>(rng->ctr[2]),
@@ -743,8 +730,6 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
     k_rs32_qsum<<<grid, kPfBlock, 0, st>>>(r);
     launch_rs32_count(grid, st, r);
     launch_rs32_assign(grid, st, r);
-    k_rs32_markmax<<<grid, kPfBlock, 0, st>>>(r);
-    k_rs32_fill<<<grid, kPfBlock, 0, st>>>(r);
     VSMC_CUDA_CHECK_LAUNCH();
     if (index)
         k_rs32_decode<<<grid_for(n, kPfBlock, 4, 8), kPfBlock, 0, st>>>(r, index);
@@ -1039,7 +1024,7 @@ int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
 // Integer-CDF resampling that allocates nothing.
 //
 // vsmc_cuda_resample_fixed takes its scratch (partial sums, replication
-// counts, slot marks, empty-slot sources, engine scalars) from
+// counts, slot indices, empty-slot sources, engine scalars) from
 // cudaMallocAsync on every call.  Some callers cannot allocate at call time:
 // code that runs inside a memory-pool or allocator callback (allocating
 // there re-enters the allocator), loops that have reserved all device memory
@@ -1050,7 +1035,7 @@ int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
 // Limits and rules for its users:
 //   * n <= VSMC_CUDA_RESAMPLE_FIXED_NOALLOC_MAX_N (2^18 particles); larger n
 //     is rejected with VSMC_CUDA_ERR_SIZE before any device work.  The array
-//     is about 4 MiB, present on every device the library is loaded on.
+//     is about 3 MiB, present on every device the library is loaded on.
 //   * The first call on each device (with that device current) looks up the
 //     array's address with cudaGetSymbolAddress, which may load the
 //     library's device code; make that first call before any stream capture.
@@ -1062,9 +1047,8 @@ int vsmc_cuda_pf_run(vsmc_cuda_pf *pf, size_t T, const double *obs_host,
 //     stream, since a call queues several launches.
 //   * The address is looked up once per device and kept for the life of the
 //     process; a device reset between calls is not supported.
-//   * The slot marks must be zero when counting starts; each call clears them
-//     with cudaMemsetAsync on its stream (no allocation).  Everything else
-//     in the array is fully written before it is read.
+//   * Nothing in the array needs clearing: every piece a call reads was
+//     written earlier in the same call.
 namespace vsmc_cuda
 {
 
@@ -1081,14 +1065,11 @@ constexpr size_t kNaEpart =
     kNaQpart + na_align(sizeof(uint64_t) * kNoAllocMaxBlocks);
 constexpr size_t kNaCpart =
     kNaEpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
-constexpr size_t kNaMpart =
-    kNaCpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
 constexpr size_t kNaRep =
-    kNaMpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
+    kNaCpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
 constexpr size_t kNaIdx = kNaRep + na_align(sizeof(int32_t) * (kNoAllocMaxN + 4));
-constexpr size_t kNaMarks =
+constexpr size_t kNaSrcs =
     kNaIdx + na_align(sizeof(int32_t) * (kNoAllocMaxN + 4));
-constexpr size_t kNaSrcs = kNaMarks + na_align(sizeof(uint32_t) * kNoAllocMaxN);
 constexpr size_t kNaBytes = kNaSrcs + na_align(sizeof(uint32_t) * kNoAllocMaxN);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
@@ -1151,12 +1132,9 @@ extern "C" int vsmc_cuda_resample_fixed_noalloc(size_t n, const uint64_t *q,
     r.qpart = reinterpret_cast<uint64_t *>(base + kNaQpart);
     r.epart = reinterpret_cast<uint32_t *>(base + kNaEpart);
     r.cpart = reinterpret_cast<uint32_t *>(base + kNaCpart);
-    r.mpart = reinterpret_cast<uint32_t *>(base + kNaMpart);
     r.rep = reinterpret_cast<int32_t *>(base + kNaRep);
     r.idx = reinterpret_cast<int32_t *>(base + kNaIdx);
-    r.marks = reinterpret_cast<uint32_t *>(base + kNaMarks);
     r.srcs = reinterpret_cast<uint32_t *>(base + kNaSrcs);
-    VSMC_CUDA_TRY(cudaMemsetAsync(r.marks, 0, sizeof(uint32_t) * n, st));
     k_rs32_setup<<<1, 1, 0, st>>>(r.sc, static_cast<uint32_t>(rng->key[0]),
         static_cast<uint32_t>(rng->key[1]), static_cast<uint32_t>(rng->ctr[0]),
         static_cast<uint32_t>(rng->ctr[1]), static_cast<uint32_t>(rng->ctr[2]),
@@ -1165,8 +1143,6 @@ extern "C" int vsmc_cuda_resample_fixed_noalloc(size_t n, const uint64_t *q,
     k_rs32_qsum<<<g, kPfBlock, 0, st>>>(r);
     launch_rs32_count(g, st, r);
     launch_rs32_assign(g, st, r);
-    k_rs32_markmax<<<g, kPfBlock, 0, st>>>(r);
-    k_rs32_fill<<<g, kPfBlock, 0, st>>>(r);
     VSMC_CUDA_CHECK_LAUNCH();
     if (index)
         k_rs32_decode<<<grid_for(n, kPfBlock, 4, 8), kPfBlock, 0, st>>>(

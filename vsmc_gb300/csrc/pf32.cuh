@@ -466,9 +466,9 @@ inline void launch_rs32_count(int grid, cudaStream_t st, const Rs32Args &a)
 // Slot assignment.  With c = copies before slot i and e = empty slots before
 // i, the first surplus rank of i is c - (i - e) (every non-empty slot before
 // i keeps one of its copies).  idx[i] = i for a parent (it keeps its slot),
-// idx[i] = -(e + 1) for the e-th empty slot (its source is srcs[e], filled
-// below); marks[first surplus rank of a parent with two or more copies] =
-// parent + 1.
+// idx[i] = -(e + 1) for the e-th empty slot, and srcs[first surplus rank ..
+// + r - 1) = i for a parent with r >= 2 copies: the reference's layout
+// (resample/transform.hpp:116-133) in one pass over the counts.
 template <bool Mon>
 __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
 {
@@ -509,6 +509,8 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         mnxt[d] = static_cast<uint32_t>(d) < md
             ? load_row4(a.mon_state + d * a.stride, lo + threadIdx.x * 4, hi)
             : make_float4(0, 0, 0, 0);
+    uint32_t err = 0;
+    __shared__ __align__(16) uint32_t shm[kPfBlock / 32][kRunChunk];
     // the next tile's counts are loaded while this one is scanned
     int4 nxt = load_rep4(a.rep, lo + threadIdx.x * 4, hi);
     for (uint32_t base = lo; base < hi; base += kPfTile) {
@@ -546,25 +548,43 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         const uint64_t ex = incl - v;
         uint32_t c = coff + static_cast<uint32_t>(ex >> 32);
         uint32_t e = eoff + static_cast<uint32_t>(ex & 0xFFFFFFFFu);
+        const uint32_t c0 = c, e0 = e;
         int32_t out[4];
+        uint32_t rs[4], rl[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const uint32_t i = i0 + k;
+            rs[k] = 0;
+            rl[k] = 0;
             if (r[k] == 0) {
                 out[k] = -static_cast<int32_t>(e) - 1;
                 ++e;
             } else {
                 out[k] = static_cast<int32_t>(i);
                 if (r[k] >= 2) {
-                    const uint32_t rank = c - (i - e);
-                    if (rank < a.n)
-                        a.marks[rank] = i + 1;
-                    else
-                        atomicOr(&a.sc->err, DEV_ERR_INTERNAL);
+                    rs[k] = c - (i - e);
+                    rl[k] = static_cast<uint32_t>(r[k]) - 1;
                 }
             }
             if (r[k] > 0)
                 c += static_cast<uint32_t>(r[k]);
+        }
+        // the warp's surplus ranks: copies minus kept slots before its first
+        // particle, and the sum of its runs
+        {
+            const uint32_t first = c0 - (i0 - e0);
+            const uint32_t W0 = __shfl_sync(0xFFFFFFFFu, first, 0);
+            uint32_t Sw = rl[0] + rl[1] + rl[2] + rl[3];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                Sw += __shfl_xor_sync(0xFFFFFFFFu, Sw, o);
+            if (Sw != 0) {
+                if (Sw > etotal || W0 > etotal - Sw)
+                    err |= DEV_ERR_INTERNAL; // ranks past the empty slots
+                else
+                    write_surplus_runs(a.srcs, rs, rl, i0, W0, Sw,
+                        shm[threadIdx.x >> 5], err);
+            }
         }
         if (i0 + 3 < hi) {
             *reinterpret_cast<int4 *>(a.idx + i0) =
@@ -578,6 +598,8 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         coff += static_cast<uint32_t>(tot >> 32);
         eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
     }
+    if (err)
+        atomicOr(&a.sc->err, err);
     if (Mon && md > 0)
         equal_mean_finish(macc, md, 1.0 / static_cast<double>(a.n),
             a.mon_part, a.sc, a.h_mean, a.sc->step - 1, a.max_steps);
@@ -590,112 +612,6 @@ inline void launch_rs32_assign(int grid, cudaStream_t st, const Rs32Args &a)
         k_rs32_assign<true><<<grid, kPfBlock, 0, st>>>(a);
     else
         k_rs32_assign<false><<<grid, kPfBlock, 0, st>>>(a);
-}
-
-__device__ __forceinline__ void rank_range(
-    uint32_t K, uint32_t &lo, uint32_t &hi)
-{
-    uint32_t per = (K + gridDim.x - 1) / gridDim.x;
-    per = (per + 3) / 4 * 4;
-    lo = blockIdx.x * per;
-    hi = lo + per;
-    if (lo > K)
-        lo = K;
-    if (hi > K)
-        hi = K;
-}
-
-// per-block max of the marks over the block's share of the surplus ranks
-__global__ void __launch_bounds__(kPfBlock) k_rs32_markmax(const Rs32Args a)
-{
-    if (!a.sc->resampled)
-        return;
-    uint32_t lo, hi;
-    rank_range(min(a.sc->nempty, a.n), lo, hi);
-    uint32_t mx = 0;
-    const uint32_t step = 4 * blockDim.x;
-    for (uint32_t k0 = lo + threadIdx.x * 4; k0 < hi; k0 += 2 * step) {
-        const uint4 v = load_marks4(a.marks, k0, hi);
-        const uint4 w = k0 + step < hi ? load_marks4(a.marks, k0 + step, hi)
-                                       : make_uint4(0, 0, 0, 0);
-        mx = max(mx, max(max(v.x, v.y), max(v.z, v.w)));
-        mx = max(mx, max(max(w.x, w.y), max(w.z, w.w)));
-    }
-    __shared__ uint32_t sh[kPfBlock / 32 + 1];
-    mx = block_reduce(mx, OpMax(), 0u, sh);
-    if (threadIdx.x == 0)
-        a.mpart[blockIdx.x] = mx;
-}
-
-// Running max of the marks gives the parent of each surplus rank:
-// srcs[k] = that parent; the marks are cleared for the next resample.
-__global__ void __launch_bounds__(kPfBlock) k_rs32_fill(const Rs32Args a)
-{
-    if (!a.sc->resampled)
-        return;
-    uint32_t lo, hi;
-    rank_range(min(a.sc->nempty, a.n), lo, hi);
-    __shared__ uint32_t sh[kPfBlock / 32 + 1];
-    __shared__ uint32_t shl[kPfBlock / 32];
-    uint32_t carry = 0;
-    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x)
-        carry = max(carry, a.mpart[b]);
-    carry = block_reduce(carry, OpMax(), 0u, sh);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint32_t step = 4 * blockDim.x;
-    // the next group's marks are loaded while this one is scanned
-    uint4 nxt = load_marks4(a.marks, lo + threadIdx.x * 4, hi);
-    uint32_t err = 0;
-    for (uint32_t base = lo; base < hi; base += step) {
-        const uint32_t k0 = base + threadIdx.x * 4;
-        const uint4 cur = nxt;
-        if (base + step < hi)
-            nxt = load_marks4(a.marks, k0 + step, hi);
-        const uint32_t mk[4] = {cur.x, cur.y, cur.z, cur.w};
-        uint32_t run[4];
-        uint32_t tmax = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            tmax = max(tmax, mk[k]);
-            run[k] = tmax;
-        }
-        uint32_t tot;
-        const uint32_t incl = block_inclusive_scan(tmax, OpMax(), 0u, sh, &tot);
-        // exclusive max: the previous lane's inclusive value, or the
-        // previous warp's total for lane 0
-        uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
-        if (lane == 31)
-            shl[wid] = incl;
-        __syncthreads();
-        if (lane == 0)
-            before = wid > 0 ? shl[wid - 1] : 0u;
-        __syncthreads();
-        before = max(before, carry);
-        uint32_t out[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t rk = max(run[k], before);
-            if (k0 + k < hi && (rk == 0 || rk - 1 >= a.n))
-                err |= DEV_ERR_INTERNAL;
-            out[k] = rk - 1;
-        }
-        if (k0 + 3 < hi) {
-            *reinterpret_cast<uint4 *>(a.srcs + k0) =
-                make_uint4(out[0], out[1], out[2], out[3]);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (k0 + k < hi)
-                    a.srcs[k0 + k] = out[k];
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (mk[k] && k0 + k < hi)
-                a.marks[k0 + k] = 0;
-        carry = max(carry, tot);
-    }
-    if (err)
-        atomicOr(&a.sc->err, err);
 }
 
 // Genealogy row of the step just finished (t = step - 1): each particle's

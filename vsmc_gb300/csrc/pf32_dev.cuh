@@ -477,18 +477,95 @@ __device__ __forceinline__ float4 load_row4(
     return v;
 }
 
-// marks k0..k0+3 below hi (0 past hi); k0 is a multiple of 4
-__device__ __forceinline__ uint4 load_marks4(
-    const uint32_t *marks, uint32_t k0, uint32_t hi)
+// Surplus runs of one warp's 128 particles.  A parent with r >= 2 copies
+// keeps one in its own slot and its other r - 1 fill the next r - 1 empty
+// slots in order, so the warp's parents own consecutive runs that together
+// cover the warp's surplus ranks [W0, W0 + S) exactly.  The sources
+// srcs[W0 .. W0 + S) are written in order from position p:
+//   * when the run holding p goes on for at least a chunk (kRunChunk ranks),
+//     the warp stores its parent up to the run's end directly (32
+//     consecutive ranks per store), so a parent with a huge copy count costs
+//     its ranks' stores and nothing more;
+//   * otherwise each parent marks the first rank of its run inside the
+//     chunk [p, p + kRunChunk) in the warp's shared-memory row, a warp
+//     max-scan over the chunk gives every rank its parent, and the warp
+//     stores the chunk (coalesced).
+// Warp-synchronous: called by every lane with warp-uniform W0 and S; rs / rl:
+// the lane's runs (start rank, length; 0 for none).
+constexpr uint32_t kRunChunk = 128;
+
+__device__ __forceinline__ void write_surplus_runs(uint32_t *srcs,
+    const uint32_t (&rs)[4], const uint32_t (&rl)[4], uint32_t i0,
+    uint32_t W0, uint32_t S, uint32_t *shm, uint32_t &err)
 {
-    if (k0 + 3 < hi)
-        return __ldcg(reinterpret_cast<const uint4 *>(marks + k0));
-    uint4 v;
-    v.x = k0 + 0 < hi ? __ldcg(marks + k0 + 0) : 0u;
-    v.y = k0 + 1 < hi ? __ldcg(marks + k0 + 1) : 0u;
-    v.z = k0 + 2 < hi ? __ldcg(marks + k0 + 2) : 0u;
-    v.w = k0 + 3 < hi ? __ldcg(marks + k0 + 3) : 0u;
-    return v;
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t p0 = 0;
+    while (p0 < S) {
+        // the run holding p0 (exactly one lane has it)
+        uint32_t own_end = 0, own_par = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t b0 = rs[k] - W0;
+            if (rl[k] != 0 && b0 <= p0 && p0 < b0 + rl[k]) {
+                own_end = b0 + rl[k];
+                own_par = i0 + k;
+            }
+        }
+        const unsigned who = __ballot_sync(0xFFFFFFFFu, own_end != 0);
+        if (who == 0) {
+            err |= DEV_ERR_INTERNAL; // a rank no run covers
+            return;
+        }
+        const int src = __ffs(who) - 1;
+        const uint32_t end = __shfl_sync(0xFFFFFFFFu, own_end, src);
+        const uint32_t par = __shfl_sync(0xFFFFFFFFu, own_par, src);
+        const uint32_t stop = end < S ? end : S;
+        if (stop - p0 >= kRunChunk) {
+            for (uint32_t q = p0 + lane; q < stop; q += 32)
+                srcs[W0 + q] = par;
+            p0 = stop;
+            continue;
+        }
+        reinterpret_cast<uint4 *>(shm)[lane] = make_uint4(0, 0, 0, 0);
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (rl[k] == 0)
+                continue;
+            const uint32_t b0 = rs[k] - W0, b1 = b0 + rl[k];
+            if (b1 > p0 && b0 < p0 + kRunChunk)
+                shm[(b0 > p0 ? b0 : p0) - p0] = i0 + k + 1;
+        }
+        __syncwarp();
+        const uint4 m = reinterpret_cast<const uint4 *>(shm)[lane];
+        uint32_t run[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+        for (int j = 1; j < 4; ++j)
+            run[j] = max(run[j], run[j - 1]);
+        uint32_t incl = run[3];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<uint32_t>(o))
+                incl = max(incl, y);
+        }
+        uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+        if (lane == 0)
+            before = 0;
+        const uint32_t lim = S - p0 < kRunChunk ? S - p0 : kRunChunk;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t pos = 4 * lane + j;
+            if (pos < lim) {
+                const uint32_t o = max(run[j], before);
+                if (o == 0)
+                    err |= DEV_ERR_INTERNAL; // a rank no run covers
+                srcs[W0 + p0 + pos] = o - 1;
+            }
+        }
+        __syncwarp(); // the row is reused by the next chunk
+        p0 += kRunChunk;
+    }
 }
 
 } // namespace vsmc_cuda

@@ -19,10 +19,8 @@ struct Rs32Args {
     uint64_t *qpart; // per-block sum of q
     uint32_t *epart; // per-block empty count
     uint32_t *cpart; // per-block copy count (sum of rep)
-    uint32_t *mpart; // per-block max of marks
     int32_t *rep;
     int32_t *idx;      // per slot: itself (>= 0) or -(empty rank + 1)
-    uint32_t *marks;   // N entries, zero between resamples
     uint32_t *srcs;    // N entries: source of the k-th empty slot
     PfScalars *sc;
     // monitor of the resampled particles: sum_i rep_i x_{d,i} / n over the

@@ -50,10 +50,10 @@ struct vsmc_cuda_pf {
     uint32_t shift = 0;
     vsmc_cuda::PfPartial *part = nullptr;
     uint64_t *qpart = nullptr;
-    uint32_t *epart = nullptr, *cpart = nullptr, *mpart = nullptr;
+    uint32_t *epart = nullptr, *cpart = nullptr;
     int32_t *rep = nullptr;
     int32_t *idx = nullptr;
-    uint32_t *marks = nullptr, *empties = nullptr;
+    uint32_t *empties = nullptr;
     uint32_t mcmc_sweeps = 0; // FP32 resample-move: sweeps after resampling
     float mcmc_scale = 0;
     uint32_t *h_acc = nullptr; // accepted MCMC steps per step (max_steps)

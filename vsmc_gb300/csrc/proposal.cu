@@ -13,6 +13,7 @@
 // No reference counterpart (the reference has no learned proposal).
 #include "bearings.cuh"
 #include "mlp.cuh"
+#include "tc05.cuh"
 #include "rng_device.cuh"
 
 #include <cmath>
@@ -225,91 +226,161 @@ __global__ void __launch_bounds__(128) k_mlp_forward(
 }
 
 // ------------------------------------------------------------ gradient
+//
+// Loss and gradient partials of one block over its samples.  The forward
+// pass and the backward data path (deltas through W3 and W2) run per warp
+// on 16 rows with mma.sync, as in the filters.  The weight gradients are
+// contractions over the samples, dW = delta^T a, and run on the Blackwell
+// tensor core: every round of 64 samples the block writes its activations
+// and deltas into shared memory as K-major BF16 operands (K = the samples)
+// and one thread issues tcgen05.mma into FP32 accumulators in tensor memory
+// that live for the whole kernel.  Two products cover every weight:
+//
+//   D1 (128 x 80) = [a1 | a2]^T [dp2 | dout | 0]:
+//       D1[k][j] = dW2[j][k] (k, j < 64), D1[64 + k][64 + d] = dW3[d][k]
+//   D2 (128 x 16) = [dp1 | dp2]^T [a0 | 1 | 0]:
+//       D2[j][c] = dW1[j][c] (c < 6), D2[j][6] = db1[j], D2[64 + j][6] = db2[j]
+//
+// The activations are BF16 already (the forward's operands); each FP32
+// delta is split into BF16 hi + lo parts (v = hi + lo to about 2^-17
+// relative) and both are multiplied, so the sums keep the deltas' FP32
+// precision.  Stage buffers alternate, and an mbarrier per buffer
+// (tcgen05.commit) says when the tensor core has finished reading one, so
+// a round's contraction overlaps the next round's forward and backward
+// passes.  db3 and the loss are register sums.  part: [grid][kNumParams + 1]
+// (the last entry is the block's loss sum); a block whose tensor-core wait
+// ran out writes NaN there and in its gradient entries.
 
 constexpr int kGradWarps = 4;
-constexpr int kGradRows = 16 * kGradWarps; // samples per block round
-constexpr int kLd = 68;                    // staging row stride (floats)
+constexpr int kGradRows = 16 * kGradWarps; // samples per round (the K tile)
 
-// staging: a0 [rows][8], a1 / a2 / dp1 / dp2 [rows][kLd], dout [rows][8]
-constexpr int kStA0 = 0;
-constexpr int kStA1 = kStA0 + kGradRows * 8;
-constexpr int kStA2 = kStA1 + kGradRows * kLd;
-constexpr int kStD1 = kStA2 + kGradRows * kLd;
-constexpr int kStD2 = kStD1 + kGradRows * kLd;
-constexpr int kStDo = kStD2 + kGradRows * kLd;
-constexpr int kStTotal = kStDo + kGradRows * 8;
-constexpr size_t kGradSmem =
-    sizeof(uint32_t) * kPackedWords + sizeof(float) * kStTotal;
+// operands inside one stage buffer: K-major, no swizzle, rows of 64 samples
+// (8 core matrices of 128 B along K, 8-row groups 1024 B apart)
+constexpr uint32_t kTcLbo = 128;
+constexpr uint32_t kTcSbo = 1024;
+constexpr uint32_t kOpA1 = 0;                   // 128 rows: a1, a2
+constexpr uint32_t kOpB1h = kOpA1 + 128 * 128;  // 80 rows: dp2, dout, 0 (hi)
+constexpr uint32_t kOpB1l = kOpB1h + 80 * 128;  // (lo)
+constexpr uint32_t kOpA2h = kOpB1l + 80 * 128;  // 128 rows: dp1, dp2 (hi)
+constexpr uint32_t kOpA2l = kOpA2h + 128 * 128; // (lo)
+constexpr uint32_t kOpB2 = kOpA2l + 128 * 128;  // 16 rows: a0, 1, 0
+constexpr uint32_t kStageBytes = kOpB2 + 16 * 128;
+constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kD1Col = 0, kD2Col = 96;
+constexpr uint32_t kPackedBytes = (sizeof(uint32_t) * kPackedWords + 1023) / 1024 * 1024;
+constexpr size_t kGradSmem = 1024 /* alignment slack */ + kPackedBytes +
+    2 * kStageBytes + 64 /* mbarriers, TMEM address */;
+constexpr uint64_t kTcWaitNs = 1000000000ull; // 1 s
 
-// accumulator fragment (rows g, g + 8 of 16) -> staging rows
-__device__ __forceinline__ void stage_c(
-    float *st, int ld, int row0, int col0, const float (&c)[4])
+// byte offset of (operand row, sample s) in a K-major no-swizzle operand
+__device__ __forceinline__ uint32_t op_off(uint32_t row, uint32_t s)
 {
-    const int lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    st[(row0 + g) * ld + col0 + 2 * t] = c[0];
-    st[(row0 + g) * ld + col0 + 2 * t + 1] = c[1];
-    st[(row0 + g + 8) * ld + col0 + 2 * t] = c[2];
-    st[(row0 + g + 8) * ld + col0 + 2 * t + 1] = c[3];
+    return (row >> 3) * kTcSbo + (s >> 3) * kTcLbo + (row & 7) * 16u +
+        (s & 7) * 2u;
 }
 
-__device__ __forceinline__ float2 unpack_bf16(uint32_t w)
+__device__ __forceinline__ void st16(unsigned char *buf, uint32_t off,
+    uint32_t v)
 {
-    return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xFFFF0000u));
+    *reinterpret_cast<uint16_t *>(buf + off) = static_cast<uint16_t>(v);
 }
 
-// operand fragment (16 x 16 bf16) -> staging rows, columns col0..col0+15
-__device__ __forceinline__ void stage_a(
-    float *st, int ld, int row0, int col0, const uint32_t (&a)[4])
+// the two BF16 halves of a packed operand word at rows r, r + 1
+__device__ __forceinline__ void st_pair(unsigned char *buf, uint32_t op,
+    uint32_t row, uint32_t s, uint32_t w)
 {
-    const int lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const float2 v0 = unpack_bf16(a[0]), v1 = unpack_bf16(a[1]);
-    const float2 v2 = unpack_bf16(a[2]), v3 = unpack_bf16(a[3]);
-    st[(row0 + g) * ld + col0 + 2 * t] = v0.x;
-    st[(row0 + g) * ld + col0 + 2 * t + 1] = v0.y;
-    st[(row0 + g + 8) * ld + col0 + 2 * t] = v1.x;
-    st[(row0 + g + 8) * ld + col0 + 2 * t + 1] = v1.y;
-    st[(row0 + g) * ld + col0 + 2 * t + 8] = v2.x;
-    st[(row0 + g) * ld + col0 + 2 * t + 9] = v2.y;
-    st[(row0 + g + 8) * ld + col0 + 2 * t + 8] = v3.x;
-    st[(row0 + g + 8) * ld + col0 + 2 * t + 9] = v3.y;
+    st16(buf, op + op_off(row, s), w & 0xFFFFu);
+    st16(buf, op + op_off(row + 1, s), w >> 16);
 }
 
-// Loss and gradient partials of one block over its samples.  Forward and
-// the backward data path on the tensor cores; the weight gradients as
-// register-blocked FP32 sums over staged rows.  part: [grid][kNumParams + 1]
-// (the last entry is the block's loss sum).
-__global__ void __launch_bounds__(128) k_mlp_grad(const uint32_t *packed,
+// an FP32 delta as BF16 hi and lo parts into two operands
+__device__ __forceinline__ void st_split(unsigned char *buf, uint32_t oph,
+    uint32_t opl, uint32_t row, uint32_t s, float v)
+{
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+    const uint32_t o = op_off(row, s);
+    *reinterpret_cast<__nv_bfloat16 *>(buf + oph + o) = h;
+    *reinterpret_cast<__nv_bfloat16 *>(buf + opl + o) = l;
+}
+
+// the round's contraction, issued by one thread on stage buffer `sb`
+__device__ __forceinline__ void grad_mma_round(
+    uint32_t sb, uint32_t tmem, bool accumulate)
+{
+    constexpr uint32_t id1 = tc05::idesc_bf16(128, 80);
+    constexpr uint32_t id2 = tc05::idesc_bf16(128, 16);
+#pragma unroll
+    for (uint32_t kk = 0; kk < kGradRows / 16; ++kk) {
+        const uint32_t ko = kk * 2 * kTcLbo; // 16 samples = 2 core matrices
+        const uint32_t acc = (accumulate || kk > 0) ? 1u : 0u;
+        const uint64_t a1 = tc05::desc_kmajor(sb + kOpA1 + ko, kTcLbo, kTcSbo);
+        tc05::mma_bf16(tmem + kD1Col, a1,
+            tc05::desc_kmajor(sb + kOpB1h + ko, kTcLbo, kTcSbo), id1, acc);
+        tc05::mma_bf16(tmem + kD1Col, a1,
+            tc05::desc_kmajor(sb + kOpB1l + ko, kTcLbo, kTcSbo), id1, 1u);
+        const uint64_t b2 = tc05::desc_kmajor(sb + kOpB2 + ko, kTcLbo, kTcSbo);
+        tc05::mma_bf16(tmem + kD2Col,
+            tc05::desc_kmajor(sb + kOpA2h + ko, kTcLbo, kTcSbo), b2, id2, acc);
+        tc05::mma_bf16(tmem + kD2Col,
+            tc05::desc_kmajor(sb + kOpA2l + ko, kTcLbo, kTcSbo), b2, id2, 1u);
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_grad(const uint32_t *packed,
     uint32_t B, const float *feat, const float *nu_in, float inv_b,
     double *part)
 {
-    extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t *sp = smem;
-    float *st = reinterpret_cast<float *>(smem + kPackedWords);
-    load_packed(sp, packed);
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned carve-up (the descriptors need 16)
+    const uint32_t raw = tc05::smem_addr(smem_raw);
+    unsigned char *smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+    uint32_t *sp = reinterpret_cast<uint32_t *>(smem);
+    unsigned char *stage[2] = {smem + kPackedBytes,
+        smem + kPackedBytes + kStageBytes};
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(
+        smem + kPackedBytes + 2 * kStageBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
+    __shared__ double shl[128 / 32 + 1];
+    __shared__ float shb3[kGradWarps][kOut];
+
     const int tid = threadIdx.x;
     const int lane = tid & 31, wid = tid >> 5;
     const int g = lane >> 2, q = lane & 3;
-    // weight-gradient accumulators
-    const int j2 = (tid >> 3) * 4, k2 = (tid & 7) * 8; // dW2 block 4 x 8
-    const int d3 = tid >> 4, k3 = (tid & 15) * 4;       // dW3 1 x 4
-    const int j1 = tid >> 1, k1 = (tid & 1) * 3;        // dW1 1 x 3
-    float gw2[4][8], gw3[4], gw1[3], gb = 0, gb3 = 0;
+
+    // constant operand rows: dout padding (B1 rows 72..79), the ones row
+    // and padding of B2 (rows 6..15), in both buffers
+    for (int b = 0; b < 2; ++b) {
+        for (uint32_t w = tid; w < 8 * 64; w += 128) {
+            const uint32_t row = 72 + w / 64, s = w % 64;
+            st16(stage[b], kOpB1h + op_off(row, s), 0);
+            st16(stage[b], kOpB1l + op_off(row, s), 0);
+        }
+        for (uint32_t w = tid; w < 10 * 64; w += 128) {
+            const uint32_t row = 6 + w / 64, s = w % 64;
+            st16(stage[b], kOpB2 + op_off(row, s), row == 6 ? 0x3F80u : 0u);
+        }
+    }
+    if (tid == 0) {
+        tc05::mbar_init(&mbar[0], 1);
+        tc05::mbar_init(&mbar[1], 1);
+    }
+    if (wid == 0)
+        tc05::tmem_alloc(tmem_slot, kTmemCols);
+    tc05::fence_before_sync();
+    load_packed(sp, packed); // ends with __syncthreads
+    tc05::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    float gb3[kOut];
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int s = 0; s < 8; ++s)
-            gw2[r][s] = 0;
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-        gw3[s] = 0;
-#pragma unroll
-    for (int s = 0; s < 3; ++s)
-        gw1[s] = 0;
-    double loss = 0;
+    for (int d = 0; d < kOut; ++d)
+        gb3[d] = 0;
+    float loss = 0;
+    bool timed_out = false;
     const uint32_t rounds = (B + kGradRows - 1) / kGradRows;
-    for (uint32_t rd = blockIdx.x; rd < rounds; rd += gridDim.x) {
+    uint32_t it = 0;
+    for (uint32_t rd = blockIdx.x; rd < rounds; rd += gridDim.x, ++it) {
         const uint32_t p0 = rd * kGradRows + 16 * wid;
         const uint32_t i = p0 + g + (q == 1 ? 8u : 0u);
         const bool mine = q < 2 && i < B;
@@ -335,8 +406,11 @@ __global__ void __launch_bounds__(128) k_mlp_grad(const uint32_t *packed,
             dv[d] = mine ? -r * el * inv_b : 0.0f;
             dv[4 + d] = mine ? 0.5f * (1.0f - r * r * el) * inv_b : 0.0f;
             if (mine)
-                loss += 0.5 * (static_cast<double>(r) * r * el + v[4 + d]);
+                loss += 0.5f * (r * r * el + v[4 + d]);
         }
+#pragma unroll
+        for (int d = 0; d < kOut; ++d)
+            gb3[d] += dv[d];
         // dh2 = dout W3 (8 n-tiles), dpre2 = dh2 * gelu'(pre2)
         uint32_t ad[4];
         owner8_to_a(dv, ad);
@@ -371,92 +445,341 @@ __global__ void __launch_bounds__(128) k_mlp_grad(const uint32_t *packed,
             for (int r = 0; r < 4; ++r)
                 dp1[nt][r] *= gelu_grad_f(pre1[nt][r]);
         }
-        // ---- stage this warp's 16 rows
-        const int row0 = 16 * wid;
-        {
-            // input rows: columns 0..7 only (inputs 0..5, 6..7 zero)
-            const float2 v0 = unpack_bf16(a0[0]), v1 = unpack_bf16(a0[1]);
-            float *s0 = st + kStA0 + (row0 + g) * 8 + 2 * q;
-            float *s1 = st + kStA0 + (row0 + g + 8) * 8 + 2 * q;
-            s0[0] = v0.x;
-            s0[1] = v0.y;
-            s1[0] = v1.x;
-            s1[1] = v1.y;
+        // ---- the stage buffer is free once the contraction that last
+        // read it (two rounds ago) has finished
+        const int sbi = static_cast<int>(it & 1);
+        bool ok = true;
+        if (it >= 2)
+            ok = tc05::mbar_wait(&mbar[sbi], ((it >> 1) - 1) & 1, kTcWaitNs);
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
         }
+        unsigned char *buf = stage[sbi];
+        const uint32_t s0 = 16 * wid + g, s1 = s0 + 8;
 #pragma unroll
         for (int kt = 0; kt < 4; ++kt) {
-            stage_a(st + kStA1, kLd, row0, 16 * kt, act1[kt]);
-            stage_a(st + kStA2, kLd, row0, 16 * kt, act2[kt]);
+            const uint32_t c = 16 * kt + 2 * q;
+            st_pair(buf, kOpA1, c, s0, act1[kt][0]);
+            st_pair(buf, kOpA1, c, s1, act1[kt][1]);
+            st_pair(buf, kOpA1, c + 8, s0, act1[kt][2]);
+            st_pair(buf, kOpA1, c + 8, s1, act1[kt][3]);
+            st_pair(buf, kOpA1, 64 + c, s0, act2[kt][0]);
+            st_pair(buf, kOpA1, 64 + c, s1, act2[kt][1]);
+            st_pair(buf, kOpA1, 64 + c + 8, s0, act2[kt][2]);
+            st_pair(buf, kOpA1, 64 + c + 8, s1, act2[kt][3]);
         }
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
-            stage_c(st + kStD1, kLd, row0, 8 * nt, dp1[nt]);
-            stage_c(st + kStD2, kLd, row0, 8 * nt, dp2[nt]);
+            const uint32_t c = 8 * nt + 2 * q;
+            st_split(buf, kOpB1h, kOpB1l, c, s0, dp2[nt][0]);
+            st_split(buf, kOpB1h, kOpB1l, c + 1, s0, dp2[nt][1]);
+            st_split(buf, kOpB1h, kOpB1l, c, s1, dp2[nt][2]);
+            st_split(buf, kOpB1h, kOpB1l, c + 1, s1, dp2[nt][3]);
+            st_split(buf, kOpA2h, kOpA2l, 64 + c, s0, dp2[nt][0]);
+            st_split(buf, kOpA2h, kOpA2l, 64 + c + 1, s0, dp2[nt][1]);
+            st_split(buf, kOpA2h, kOpA2l, 64 + c, s1, dp2[nt][2]);
+            st_split(buf, kOpA2h, kOpA2l, 64 + c + 1, s1, dp2[nt][3]);
+            st_split(buf, kOpA2h, kOpA2l, c, s0, dp1[nt][0]);
+            st_split(buf, kOpA2h, kOpA2l, c + 1, s0, dp1[nt][1]);
+            st_split(buf, kOpA2h, kOpA2l, c, s1, dp1[nt][2]);
+            st_split(buf, kOpA2h, kOpA2l, c + 1, s1, dp1[nt][3]);
         }
         if (q < 2) {
-            const int row = row0 + g + (q == 1 ? 8 : 0);
+            const uint32_t s = q == 0 ? s0 : s1;
 #pragma unroll
-            for (int d = 0; d < 8; ++d)
-                st[kStDo + row * 8 + d] = dv[d];
+            for (int d = 0; d < kOut; ++d)
+                st_split(buf, kOpB1h, kOpB1l, 64 + d, s, dv[d]);
         }
-        __syncthreads();
-        // ---- weight gradients over the block's rows
-        for (int s = 0; s < kGradRows; ++s) {
-            const float *a1r = st + kStA1 + s * kLd;
-            const float *d2r = st + kStD2 + s * kLd;
-            float av[8], dvv[4];
-#pragma unroll
-            for (int c8 = 0; c8 < 8; ++c8)
-                av[c8] = a1r[k2 + c8];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-                dvv[r] = d2r[j2 + r];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int c8 = 0; c8 < 8; ++c8)
-                    gw2[r][c8] = fmaf(dvv[r], av[c8], gw2[r][c8]);
-            const float *a2r = st + kStA2 + s * kLd;
-            const float dd = st[kStDo + s * 8 + d3];
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4)
-                gw3[c4] = fmaf(dd, a2r[k3 + c4], gw3[c4]);
-            const float d1 = st[kStD1 + s * kLd + j1];
-#pragma unroll
-            for (int c3 = 0; c3 < 3; ++c3)
-                gw1[c3] = fmaf(d1, st[kStA0 + s * 8 + k1 + c3], gw1[c3]);
-            // biases: b1 (threads 0..63), b2 (64..127), b3 (0..7)
-            gb += tid < kHid ? st[kStD1 + s * kLd + tid]
-                             : st[kStD2 + s * kLd + tid - kHid];
-            if (tid < kOut)
-                gb3 += st[kStDo + s * 8 + tid];
+        if (q < 3) { // inputs 2q, 2q + 1 of rows s0 (a0[0]) and s1 (a0[1])
+            st_pair(buf, kOpB2, 2 * q, s0, a0[0]);
+            st_pair(buf, kOpB2, 2 * q, s1, a0[1]);
         }
+        tc05::fence_async_shared();
         __syncthreads();
+        if (tid == 0) {
+            tc05::fence_after_sync();
+            grad_mma_round(tc05::smem_addr(buf), tmem, it > 0);
+            tc05::commit(&mbar[sbi]);
+        }
     }
-    // ---- block partials
+    // ---- every contraction finished: the last commit covers the earlier
+    if (it > 0) {
+        const uint32_t last = it - 1;
+        const bool ok = tc05::mbar_wait(
+            &mbar[last & 1], (last >> 1) & 1, kTcWaitNs);
+        if (__syncthreads_or(!ok))
+            timed_out = true;
+    }
+    tc05::fence_after_sync();
     double *out = part + static_cast<size_t>(blockIdx.x) * (kNumParams + 1);
+    if (timed_out) {
+        // record it; give the tensor core one more bounded wait before the
+        // accumulators are released
+        if (it > 0)
+            tc05::mbar_wait(&mbar[(it - 1) & 1], ((it - 1) >> 1) & 1,
+                kTcWaitNs);
+        for (int k = tid; k <= kNumParams; k += 128)
+            out[k] = __longlong_as_double(0x7FF8000000000000ll);
+    } else if (it == 0) {
+        for (int k = tid; k <= kNumParams; k += 128)
+            out[k] = 0.0;
+    } else {
+        // ---- accumulators -> block partials (warp w reads TMEM lanes
+        // 32w .. 32w + 31: row m = 32w + lane)
+        const uint32_t m = 32 * wid + lane;
+        const uint32_t tw = tmem + ((32u * wid) << 16);
+        float vv[16];
+        if (wid < 2) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
+            for (int c0 = 0; c0 < 64; c0 += 16) {
+                tc05::ld16(tw + kD1Col + c0, vv);
 #pragma unroll
-        for (int c8 = 0; c8 < 8; ++c8)
-            out[kW2 + (j2 + r) * kHid + k2 + c8] = gw2[r][c8];
+                for (int c = 0; c < 16; ++c) // dW2[j = c0 + c][k = m]
+                    out[kW2 + (c0 + c) * kHid + m] = vv[c];
+            }
+            tc05::ld16(tw + kD2Col, vv);
 #pragma unroll
-    for (int c4 = 0; c4 < 4; ++c4)
-        out[kW3 + d3 * kHid + k3 + c4] = gw3[c4];
+            for (int c = 0; c < kIn; ++c)
+                out[kW1 + m * kIn + c] = vv[c];
+            out[kB1 + m] = vv[kIn];
+        } else {
+            const uint32_t k = m - 64;
+            tc05::ld16(tw + kD1Col + 64, vv);
 #pragma unroll
-    for (int c3 = 0; c3 < 3; ++c3)
-        out[kW1 + j1 * kIn + k1 + c3] = gw1[c3];
-    if (tid < kHid)
-        out[kB1 + tid] = gb;
-    else
-        out[kB2 + tid - kHid] = gb;
-    if (tid < kOut)
-        out[kB3 + tid] = gb3;
-    // loss: owners' sums over the block
-    __shared__ double shl[128 / 32 + 1];
-    loss = block_reduce(loss, OpAdd(), 0.0, shl);
+            for (int d = 0; d < kOut; ++d) // dW3[d][k]
+                out[kW3 + d * kHid + k] = vv[d];
+            tc05::ld16(tw + kD2Col, vv);
+            out[kB2 + k] = vv[kIn];
+        }
+        // db3 and the loss: register sums over the block
+#pragma unroll
+        for (int d = 0; d < kOut; ++d) {
+            float s = gb3[d];
+#pragma unroll
+            for (int o2 = 16; o2 > 0; o2 >>= 1)
+                s += __shfl_xor_sync(0xFFFFFFFFu, s, o2);
+            if (lane == 0)
+                shb3[wid][d] = s;
+        }
+        __syncthreads();
+        if (tid < kOut) {
+            float s = 0;
+            for (int w = 0; w < kGradWarps; ++w)
+                s += shb3[w][tid];
+            out[kB3 + tid] = s;
+        }
+        const double lb = block_reduce(static_cast<double>(loss), OpAdd(),
+            0.0, shl);
+        if (tid == 0)
+            out[kNumParams] = lb;
+    }
+    // ---- release the tensor memory (after every warp's reads)
+    tc05::fence_before_sync();
+    __syncthreads();
+    if (wid == 0) {
+        tc05::fence_after_sync();
+        tc05::tmem_free(tmem, kTmemCols);
+    }
+}
+
+// ------------------------------------------- forward on tcgen05 (128 rows)
+//
+// The same network on the Blackwell tensor core, 128 rows per tile: one
+// thread per row.  Each layer is one tcgen05.mma chain (M = 128; N = 64,
+// 64, 16) from K-major BF16 operands in shared memory into FP32 tensor
+// memory; the row's thread reads its accumulators back (tcgen05.ld), adds
+// the bias, applies GELU and writes the row of the next layer's operand.
+// The weights come from the packed mma.sync fragments, decoded once per
+// block into K-major operands.  A block whose tensor-core wait runs out
+// writes NaN outputs for its rows and stops.
+
+constexpr uint32_t kFwK16Sbo = 256;   // K = 16 operands: 2 core matrices per group
+constexpr uint32_t kFwK64Sbo = 1024;  // K = 64 operands: 8 per group
+constexpr uint32_t kFwW1 = 0;                         // 64 x 16
+constexpr uint32_t kFwW2 = kFwW1 + 64 * 32;           // 64 x 64
+constexpr uint32_t kFwW3 = kFwW2 + 64 * 128;          // 16 x 64 (rows 8..15 zero)
+constexpr uint32_t kFwX = kFwW3 + 16 * 128;           // 128 x 16
+constexpr uint32_t kFwH1 = kFwX + 128 * 32;           // 128 x 64
+constexpr uint32_t kFwH2 = kFwH1 + 128 * 128;         // 128 x 64
+constexpr uint32_t kFwBias = kFwH2 + 128 * 128;       // b1, b2, b3 (FP32)
+constexpr uint32_t kFwBar = kFwBias + 4 * (kHid + kHid + kOut);
+constexpr size_t kFwSmem = 1024 + kFwBar + 16;
+constexpr uint32_t kFwTmemCols = 128; // D1 / D3 at column 0, D2 at 64
+
+__device__ __forceinline__ uint32_t kmaj_off(uint32_t row, uint32_t k,
+    uint32_t sbo)
+{
+    return (row >> 3) * sbo + (k >> 3) * 128u + (row & 7) * 16u + (k & 7) * 2u;
+}
+
+// packed fragment word -> its two BF16 elements (k, n), (k + 1, n) of the
+// B operand it belongs to: tile `tile` of a region with `ntn` n-tiles
+__device__ __forceinline__ void frag_word_kn(uint32_t w, uint32_t ntn,
+    uint32_t &k, uint32_t &n)
+{
+    const uint32_t tile = w / 64, within = w % 64;
+    const uint32_t ln = within / 2, hi = within % 2;
+    const uint32_t kt = tile / ntn, nt = tile % ntn;
+    k = 16 * kt + 2 * (ln & 3) + 8 * hi;
+    n = 8 * nt + (ln >> 2);
+}
+
+__global__ void __launch_bounds__(128, 4) k_mlp_forward_tc(
+    const uint32_t *packed, uint32_t B, const float *feat, float *out)
+{
+    extern __shared__ __align__(1024) unsigned char fsm_raw[];
+    const uint32_t raw = tc05::smem_addr(fsm_raw);
+    unsigned char *sm = fsm_raw + ((1024u - (raw & 1023u)) & 1023u);
+    float *bias = reinterpret_cast<float *>(sm + kFwBias);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + kFwBar);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kFwBar + 8);
+    const int tid = threadIdx.x, wid = tid >> 5;
+
+    // weights: W1^T fragments (1 k-tile x 8 n-tiles), W2^T (4 x 8), W3^T
+    // (4 x 1) -> K-major operands with rows = output units
+    for (uint32_t w = tid; w < 8 * 64; w += 128) {
+        uint32_t k, n;
+        frag_word_kn(w, 8, k, n);
+        const uint32_t v = packed[kF1 + w];
+        st16(sm, kFwW1 + kmaj_off(n, k, kFwK16Sbo), v & 0xFFFFu);
+        st16(sm, kFwW1 + kmaj_off(n, k + 1, kFwK16Sbo), v >> 16);
+    }
+    for (uint32_t w = tid; w < 32 * 64; w += 128) {
+        uint32_t k, n;
+        frag_word_kn(w, 8, k, n);
+        const uint32_t v = packed[kF2 + w];
+        st16(sm, kFwW2 + kmaj_off(n, k, kFwK64Sbo), v & 0xFFFFu);
+        st16(sm, kFwW2 + kmaj_off(n, k + 1, kFwK64Sbo), v >> 16);
+    }
+    for (uint32_t w = tid; w < 4 * 64; w += 128) {
+        uint32_t k, n;
+        frag_word_kn(w, 1, k, n);
+        const uint32_t v = packed[kF3 + w];
+        st16(sm, kFwW3 + kmaj_off(n, k, kFwK64Sbo), v & 0xFFFFu);
+        st16(sm, kFwW3 + kmaj_off(n, k + 1, kFwK64Sbo), v >> 16);
+        st16(sm, kFwW3 + kmaj_off(n + 8, k, kFwK64Sbo), 0);
+        st16(sm, kFwW3 + kmaj_off(n + 8, k + 1, kFwK64Sbo), 0);
+    }
+    for (int i = tid; i < kHid + kHid + kOut; i += 128)
+        bias[i] = __uint_as_float(packed[kPackedBias + i]);
     if (tid == 0)
-        out[kNumParams] = loss;
+        tc05::mbar_init(mbar, 1);
+    if (wid == 0)
+        tc05::tmem_alloc(tmem_slot, kFwTmemCols);
+    tc05::fence_before_sync();
+    __syncthreads();
+    tc05::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tw = tmem + ((32u * wid) << 16); // this warp's lanes
+    const uint32_t sbase = tc05::smem_addr(sm);
+    const uint32_t r = tid; // the thread's row of the tile
+    uint32_t phase = 0;
+    bool bad = false;
+    const uint32_t ntiles = (B + 127) / 128;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t i = tile * 128 + r;
+        const bool mine = i < B;
+        // ---- input row: 6 features (BF16), zeros to 16
+        {
+            float f[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                f[k] = mine ? feat[6 * i + k] : 0.0f;
+            uint4 lo;
+            lo.x = pack_bf16(f[0], f[1]);
+            lo.y = pack_bf16(f[2], f[3]);
+            lo.z = pack_bf16(f[4], f[5]);
+            lo.w = 0;
+            *reinterpret_cast<uint4 *>(sm + kFwX + kmaj_off(r, 0, kFwK16Sbo)) = lo;
+            *reinterpret_cast<uint4 *>(sm + kFwX + kmaj_off(r, 8, kFwK16Sbo)) =
+                make_uint4(0, 0, 0, 0);
+        }
+        // three layers: MMA chain, then the rows' epilogue
+#pragma unroll 1
+        for (int layer = 0; layer < 3; ++layer) {
+            tc05::fence_async_shared();
+            tc05::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc05::fence_after_sync();
+                if (layer == 0) {
+                    tc05::mma_bf16(tmem,
+                        tc05::desc_kmajor(sbase + kFwX, 128, kFwK16Sbo),
+                        tc05::desc_kmajor(sbase + kFwW1, 128, kFwK16Sbo),
+                        tc05::idesc_bf16(128, 64), 0u);
+                } else {
+                    const uint32_t a = sbase + (layer == 1 ? kFwH1 : kFwH2);
+                    const uint32_t b = sbase + (layer == 1 ? kFwW2 : kFwW3);
+                    const uint32_t d = tmem + (layer == 1 ? 64u : 0u);
+                    const uint32_t id = layer == 1 ? tc05::idesc_bf16(128, 64)
+                                                   : tc05::idesc_bf16(128, 16);
+#pragma unroll
+                    for (uint32_t kk = 0; kk < 4; ++kk)
+                        tc05::mma_bf16(d,
+                            tc05::desc_kmajor(a + kk * 256, 128, kFwK64Sbo),
+                            tc05::desc_kmajor(b + kk * 256, 128, kFwK64Sbo),
+                            id, kk > 0 ? 1u : 0u);
+                }
+                tc05::commit(mbar);
+            }
+            const bool ok = tc05::mbar_wait(mbar, phase & 1, kTcWaitNs);
+            ++phase;
+            if (__syncthreads_or(!ok)) {
+                bad = true;
+                break;
+            }
+            tc05::fence_after_sync();
+            if (layer < 2) {
+                const uint32_t col = layer == 0 ? 0u : 64u;
+                const float *bl = bias + (layer == 0 ? 0 : kHid);
+                unsigned char *h = sm + (layer == 0 ? kFwH1 : kFwH2);
+#pragma unroll
+                for (int c0 = 0; c0 < 64; c0 += 16) {
+                    float v[16];
+                    tc05::ld16(tw + col + c0, v);
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int c = 0; c < 16; c += 2)
+                        pk[c / 2] = pack_bf16(gelu_f(v[c] + bl[c0 + c]),
+                            gelu_f(v[c + 1] + bl[c0 + c + 1]));
+                    *reinterpret_cast<uint4 *>(
+                        h + kmaj_off(r, c0, kFwK64Sbo)) =
+                        make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    *reinterpret_cast<uint4 *>(
+                        h + kmaj_off(r, c0 + 8, kFwK64Sbo)) =
+                        make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                }
+            } else {
+                float v[16];
+                tc05::ld16(tw, v);
+                if (mine) {
+                    const float *b3 = bias + 2 * kHid;
+#pragma unroll
+                    for (int k = 0; k < kOut; ++k)
+                        out[8 * i + k] = v[k] + b3[k];
+                }
+            }
+        }
+        if (bad)
+            break;
+    }
+    if (bad) {
+        // one more bounded wait for the tensor core, then mark the rows
+        tc05::mbar_wait(mbar, (phase - 1) & 1, kTcWaitNs);
+        for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            const uint32_t i = tile * 128 + r;
+            if (i < B)
+                for (int k = 0; k < 8; ++k)
+                    out[8 * i + k] = __int_as_float(0x7FC00000);
+        }
+    }
+    tc05::fence_before_sync();
+    __syncthreads();
+    if (wid == 0) {
+        tc05::fence_after_sync();
+        tc05::tmem_free(tmem, kFwTmemCols);
+    }
 }
 
 // sum of the block partials (fixed order); grad = mean gradient
@@ -705,7 +1028,7 @@ __global__ void k_minibatch(uint64_t total, uint64_t nx, uint32_t batch,
 static int grad_blocks(uint32_t B)
 {
     const int rounds = static_cast<int>((B + kGradRows - 1) / kGradRows);
-    const int cap = num_sms() * 2;
+    const int cap = num_sms(); // one block per SM (shared memory)
     return rounds < cap ? rounds : cap;
 }
 
@@ -783,6 +1106,29 @@ int vsmc_cuda_mlp_forward(const uint32_t *packed, size_t B, const float *feat,
         return VSMC_CUDA_OK;
     const int grid = grid_for((B + 31) / 32 * 32, 128, 1, 8);
     k_mlp_forward<<<grid, 128, 0, as_stream(stream)>>>(
+        packed, static_cast<uint32_t>(B), feat, out);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
+int vsmc_cuda_mlp_forward_tc(const uint32_t *packed, size_t B,
+    const float *feat, float *out, void *stream)
+{
+    if (packed == nullptr || (B && (feat == nullptr || out == nullptr)))
+        return VSMC_CUDA_ERR_ARG;
+    if (B >= (size_t(1) << 31))
+        return VSMC_CUDA_ERR_SIZE;
+    if (B == 0)
+        return VSMC_CUDA_OK;
+    static const bool ready = cudaFuncSetAttribute(k_mlp_forward_tc,
+        cudaFuncAttributeMaxDynamicSharedMemorySize,
+        static_cast<int>(kFwSmem)) == cudaSuccess;
+    if (!ready)
+        return VSMC_CUDA_ERR_CUDA;
+    const size_t tiles = (B + 127) / 128;
+    const size_t cap = static_cast<size_t>(num_sms()) * 4;
+    const int grid = static_cast<int>(tiles < cap ? tiles : cap);
+    k_mlp_forward_tc<<<grid, 128, kFwSmem, as_stream(stream)>>>(
         packed, static_cast<uint32_t>(B), feat, out);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
