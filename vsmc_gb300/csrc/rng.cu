@@ -6,6 +6,7 @@
 #include "common.cuh"
 #include "rng_device.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -123,35 +124,75 @@ __global__ void __launch_bounds__(256) k_plan_stream(Gen gen, StreamPlan plan,
     }
 }
 
-// In-place Box-Muller over the reference's batch layout: per 1024-element
-// chunk of k values, nu = k / 2 radii then nu angles; out[i] = s sin,
-// out[nu + i] = s cos (normal_distribution.hpp:222-239).
-template <typename R>
-__global__ void __launch_bounds__(256) k_normal_layout(
+// Box-Muller over the reference's batch layout (normal_distribution.hpp:
+// 222-239: per 1024-value chunk of k values, nu = k / 2 radii then nu
+// angles; out[i] = s sin, out[nu + i] = s cos) in one pass: per chunk, the
+// block generates the chunk's Philox / Threefry blocks once into shared
+// memory (one per thread, the chunk's words in stream order), then turns
+// each (radius, angle) pair into its sine and cosine values, so every value
+// is written once and no word goes through memory.
+template <typename Gen, typename R>
+__global__ void __launch_bounds__(256) k_normal_fused(Gen gen, StreamPlan plan,
     size_t n, R *r, R mean, R sd)
 {
-    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
-    const size_t npairs_full = (n / 1024) * 512;
-    const size_t l = n % 1024;
-    const size_t npairs = npairs_full + l / 2;
-    for (size_t q = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-         q < npairs; q += stride) {
-        size_t base, nu, i;
-        if (q < npairs_full) {
-            base = (q / 512) * 1024;
-            nu = 512;
-            i = q % 512;
-        } else {
-            base = (n / 1024) * 1024;
-            nu = l / 2;
-            i = q - npairs_full;
+    using W = typename Gen::word_t;
+    __shared__ W words[1024];
+    const size_t nchunks = (n + 1023) / 1024;
+    for (size_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint64_t base = static_cast<uint64_t>(c) * 1024;
+        const uint32_t k = static_cast<uint32_t>(
+            n - base < 1024 ? n - base : 1024);
+        const uint32_t nu = k / 2;
+        const uint32_t used = 2 * nu; // the odd value comes from the tail
+        // words of positions [base, base + used)
+        if (base < plan.head && threadIdx.x == 0) {
+            const typename Gen::block_t blk = gen.block_at_start(plan);
+            for (uint64_t p = base; p < plan.head && p < base + used; ++p)
+                words[p - base] =
+                    Gen::word(blk, plan.x + static_cast<uint32_t>(p));
         }
-        R *u1 = r + base;
-        R *u2 = r + base + nu;
-        R s, sv, cv;
-        box_muller_batch(u1[i], u2[i], sd, s, sv, cv);
-        u1[i] = fma_free_add(fma_free_mul(s, sv), mean);
-        u2[i] = fma_free_add(fma_free_mul(s, cv), mean);
+        const uint64_t plo = base > plan.head ? base : plan.head;
+        const uint64_t phi = base + used;
+        if (phi > plo) {
+            const uint64_t j0 = (plo - plan.head) / 4;
+            const uint64_t j1 = (phi - plan.head + 3) / 4;
+            for (uint64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+                const typename Gen::block_t blk = gen.block(plan, j);
+                const uint64_t p0 = plan.head + 4 * j;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const uint64_t p = p0 + i;
+                    if (p >= base && p < phi)
+                        words[p - base] = Gen::word(blk, i);
+                }
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < nu; i += blockDim.x) {
+            R u1, u2;
+            if constexpr (sizeof(R) == 8) {
+                if constexpr (sizeof(W) == 4) {
+                    u1 = u01_co_d(words[i]);
+                    u2 = u01_co_d(words[nu + i]);
+                } else {
+                    u1 = u01_co_d64(words[i]);
+                    u2 = u01_co_d64(words[nu + i]);
+                }
+            } else {
+                if constexpr (sizeof(W) == 4) {
+                    u1 = u01_co_f(words[i]);
+                    u2 = u01_co_f(words[nu + i]);
+                } else {
+                    u1 = u01_co_f64(words[i]);
+                    u2 = u01_co_f64(words[nu + i]);
+                }
+            }
+            R s, sv, cv;
+            box_muller_batch(u1, u2, sd, s, sv, cv);
+            __stcs(r + base + i, fma_free_add(fma_free_mul(s, sv), mean));
+            __stcs(r + base + nu + i, fma_free_add(fma_free_mul(s, cv), mean));
+        }
+        __syncthreads(); // words[] is reused by the next chunk
     }
 }
 
@@ -255,26 +296,30 @@ static int rng_normal_impl(
         if (extra == nullptr)
             return VSMC_CUDA_ERR_ALLOC;
     }
-    int rc;
+    int rc = VSMC_CUDA_OK;
+    // the pairs of every chunk in one pass; the odd value's two words
+    // (positions n, n + 1) through the stream kernel
+    const size_t nchunks = (n + 1023) / 1024;
+    const int grid = static_cast<int>(
+        std::min<size_t>(nchunks, static_cast<size_t>(num_sms()) * 8));
     if (rng->kind == VSMC_CUDA_PHILOX4X32) {
         PhiloxGen gen(*rng);
-        rc = launch_plan<PhiloxGen, E>(gen, plan, 0, n, r, st);
-        if (rc == VSMC_CUDA_OK && odd)
+        if (n >= 2)
+            k_normal_fused<PhiloxGen, R><<<grid, 256, 0, st>>>(
+                gen, plan, n, r, mean, sd);
+        if (odd)
             rc = launch_plan<PhiloxGen, E>(gen, plan, n, n + 2, extra, st);
     } else {
         ThreefryGen gen(*rng);
-        rc = launch_plan<ThreefryGen, E>(gen, plan, 0, n, r, st);
-        if (rc == VSMC_CUDA_OK && odd)
+        if (n >= 2)
+            k_normal_fused<ThreefryGen, R><<<grid, 256, 0, st>>>(
+                gen, plan, n, r, mean, sd);
+        if (odd)
             rc = launch_plan<ThreefryGen, E>(gen, plan, n, n + 2, extra, st);
     }
+    VSMC_CUDA_CHECK_LAUNCH();
     if (rc != VSMC_CUDA_OK)
         return rc;
-    const size_t npairs = (n / 1024) * 512 + (n % 1024) / 2;
-    if (npairs) {
-        k_normal_layout<R><<<grid_for(npairs, 256, 1, 8), 256, 0, st>>>(
-            n, r, mean, sd);
-        VSMC_CUDA_CHECK_LAUNCH();
-    }
     if (odd) {
         k_normal_odd_tail<R><<<1, 32, 0, st>>>(n, r, extra, mean, sd);
         VSMC_CUDA_CHECK_LAUNCH();
