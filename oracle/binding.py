@@ -77,6 +77,7 @@ PORT_PROTOTYPES = {
     "vo_weight_add_log": (F64, [SZ, VP, VP, VP]),
     "vo_weight_set": (F64, [SZ, VP, VP]),
     "vo_pf_simulate": (None, [U32, SZ, _MP, VP, VP]),
+    "vo_pf_run_replay": (I32, [I32, SZ, SZ, U32, _MP, VP, VP, VP, VP, VP, VP]),
     "vo_pf_run": (I32, [I32, SZ, SZ, U32, I32, F64, _MP, VP, I32, VP, VP, VP,
                         VP]),
     "vo_pf_move_f64": (None, [SZ, SZ, U32, _MP, VP, VP, VP]),
@@ -90,7 +91,7 @@ PORT_PROTOTYPES = {
     "vo_mlp_loss_grad": (None, [VP, SZ, VP, VP, VP, VP]),
     "vo_mlp_set_rounding": (None, [I32]),
     "vo_resample_index_trace": (None, [SZ, SZ, VP, SZ, VP]),
-    "vo_cv_mcmc_f32": (None, [SZ, SZ, SZ, U32, _MP, VP, F64, VP, VP, VP]),
+    "vo_cv_mcmc_f32": (None, [SZ, SZ, SZ, U32, _MP, VP, F64, VP, VP, VP, VP]),
     "vo_resample_index_matrix": (None, [SZ, SZ, VP, I32, VP]),
     "vo_bearings_pf_run": (I32, [I32, SZ, SZ, U32, I32, F64, _BMP, VP, VP,
                                  I32, VP, VP, VP, VP]),

@@ -1391,6 +1391,85 @@ static void vo_pf_mean(size_t N, const void *state, int precision,
     }
 }
 
+/* The filter of vo_pf_run with its resampling replayed from a record
+ * instead of drawn (core/sampler.hpp:772-778 with the op's indices given):
+ * at step t with resampled[t] set, particle i takes the state of particle
+ * parents[t * N + i] and the weights become equal (core/particle.hpp:
+ * 186-193).  With a device run's recorded decisions and genealogy rows this
+ * isolates the move, weight, evidence and monitor arithmetic from the
+ * resampler, step by step. */
+int vo_pf_run_replay(int precision, size_t N, size_t T, uint32_t seed,
+    const vo_model *m, const double *obs, const int *resampled,
+    const int *parents, double *mean_out, double *ess_out, double *logz_out)
+{
+    const size_t esz = precision == 32 ? sizeof(float) : sizeof(double);
+    void *state = malloc(esz * 4 * N);
+    void *tmp = malloc(esz * 4 * N);
+    double *W = (double *)malloc(sizeof(double) * N);
+    double *ll = (double *)malloc(sizeof(double) * N);
+    float *llf = (float *)malloc(sizeof(float) * N);
+    double ess = vo_weight_set_equal(N, W);
+    double logz = 0;
+    for (size_t t = 0; t != T; ++t) {
+        if (precision == 32) {
+            if (t == 0)
+                vo_pf_init_f32(N, seed, m, obs, (float *)state, llf);
+            else
+                vo_pf_move_f32(N, t, seed, m, obs + 2 * t, (float *)state, llf);
+            for (size_t i = 0; i != N; ++i)
+                ll[i] = (double)llf[i];
+        } else {
+            if (t == 0)
+                vo_pf_init_f64(N, seed, m, obs, (double *)state, ll);
+            else
+                vo_pf_move_f64(N, t, seed, m, obs + 2 * t, (double *)state, ll);
+        }
+        double mx = -INFINITY;
+        for (size_t i = 0; i != N; ++i)
+            if (mx < ll[i])
+                mx = ll[i];
+        double s = 0;
+        if (t == 0) {
+            for (size_t i = 0; i != N; ++i)
+                s += exp(ll[i] - mx);
+            logz += mx + log(s / (double)N);
+            ess = vo_weight_set_log(N, ll, W);
+        } else {
+            for (size_t i = 0; i != N; ++i)
+                s += W[i] * exp(ll[i] - mx);
+            logz += mx + log(s);
+            for (size_t i = 0; i != N; ++i)
+                W[i] = log(W[i]) + ll[i];
+            ess = vo_weight_post_set_log(N, W);
+        }
+        logz_out[t] = logz;
+        ess_out[t] = ess;
+        if (resampled[t]) {
+            const int *par = parents + t * N;
+            memcpy(tmp, state, esz * 4 * N);
+            for (size_t i = 0; i != N; ++i) {
+                const size_t p = (size_t)par[i];
+                for (size_t d = 0; d != 4; ++d) {
+                    if (precision == 32)
+                        ((float *)state)[d * N + i] =
+                            ((const float *)tmp)[d * N + p];
+                    else
+                        ((double *)state)[d * N + i] =
+                            ((const double *)tmp)[d * N + p];
+                }
+            }
+            vo_weight_set_equal(N, W);
+        }
+        vo_pf_mean(N, state, precision, W, mean_out + 2 * t);
+    }
+    free(state);
+    free(tmp);
+    free(W);
+    free(ll);
+    free(llf);
+    return 0;
+}
+
 int vo_pf_run(int precision, size_t N, size_t T, uint32_t seed, int scheme,
     double threshold, const vo_model *m, const double *obs, int threads,
     double *mean_out, double *ess_out, int *resampled_out, double *logz_out)
@@ -2019,7 +2098,7 @@ void vo_resample_index_matrix(
  * ===================================================================== */
 void vo_cv_mcmc_f32(size_t N, size_t t, size_t sweeps, uint32_t seed,
     const vo_model *m, const double obs[2], double scale, const int *parent,
-    float *state, uint32_t *accepted)
+    float *state, uint32_t *accepted, float *margin)
 {
     const float dt = (float)m->dt, h = (float)(0.5 * m->dt * m->dt);
     const float sa = (float)m->sigma_a;
@@ -2035,6 +2114,7 @@ void vo_cv_mcmc_f32(size_t N, size_t t, size_t sweeps, uint32_t seed,
         float vx = state[2 * N + i], vy = state[3 * N + i];
         float lt = -0.5f * inv_var * (ax * ax + ay * ay) +
             vo_ll_f32(m, obs, x, y);
+        float closest = INFINITY; /* min |log u - (lt2 - lt)| over sweeps */
         for (size_t k = 0; k < sweeps; ++k) {
             const uint32_t ctr[4] = {(uint32_t)(2 + k), (uint32_t)i, 0, 0};
             const uint32_t key[2] = {(uint32_t)t, seed};
@@ -2051,7 +2131,10 @@ void vo_cv_mcmc_f32(size_t N, size_t t, size_t sweeps, uint32_t seed,
             const float nvx = vx + dt * dx, nvy = vy + dt * dy;
             const float lt2 = -0.5f * inv_var * (bx * bx + by * by) +
                 vo_ll_f32(m, obs, nx, ny);
-            if (logf(vo_u01_u32_f32(1, w[2])) < lt2 - lt) {
+            const float lu = logf(vo_u01_u32_f32(1, w[2]));
+            if (fabsf(lu - (lt2 - lt)) < closest)
+                closest = fabsf(lu - (lt2 - lt));
+            if (lu < lt2 - lt) {
                 x = nx;
                 y = ny;
                 vx = nvx;
@@ -2066,6 +2149,8 @@ void vo_cv_mcmc_f32(size_t N, size_t t, size_t sweeps, uint32_t seed,
         state[N + i] = y;
         state[2 * N + i] = vx;
         state[3 * N + i] = vy;
+        if (margin)
+            margin[i] = closest;
     }
     *accepted += acc;
 }

@@ -126,6 +126,11 @@ void vo_pf_simulate(uint32_t seed, size_t T, const vo_model *m, double *truth,
 /* precision 64 or 32; threads <= 0 means all OpenMP threads.  Uses the
  * (key = {step, seed}, counter = {0, particle, 0, 0}) particle streams and a
  * resampling engine keyed {0, seed} starting at counter {0, 0, 1, 0}. */
+/* vo_pf_run with the resampling replayed from a record: at step t with
+ * resampled[t] set, particle i takes particle parents[t * N + i]'s state */
+int vo_pf_run_replay(int precision, size_t N, size_t T, uint32_t seed,
+    const vo_model *m, const double *obs, const int *resampled,
+    const int *parents, double *mean_out, double *ess_out, double *logz_out);
 int vo_pf_run(int precision, size_t N, size_t T, uint32_t seed, int scheme,
     double threshold, const vo_model *m, const double *obs, int threads,
     double *mean_out, double *ess_out, int *resampled_out, double *logz_out);
@@ -173,7 +178,7 @@ int vo_bearings_pf_run(int precision, size_t N, size_t T, uint32_t seed,
  * acceleration innovation (parent: NULL = identity); *accepted += accepts */
 void vo_cv_mcmc_f32(size_t N, size_t t, size_t sweeps, uint32_t seed,
     const vo_model *m, const double obs[2], double scale, const int *parent,
-    float *state, uint32_t *accepted);
+    float *state, uint32_t *accepted, float *margin);
 
 /* ResampleIndex::index for every id at `iter`, and index_matrix (layout 0
  * row-major [N][iters], 1 column-major [iters][N]); rows: [iters][N] */

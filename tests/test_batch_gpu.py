@@ -51,12 +51,39 @@ def test_batch_simulate_matches_single_simulator(vc):
     b.close()
 
 
+def _spec_config4(vc, nf, seed):
+    """Filters drawn like the benchmark's batch: particles log-uniform in
+    [2^8, 2^16], horizons uniform in [50, 500], sigma_a U(0.5, 2), obs
+    scale U(0.2, 1)."""
+    rng = np.random.default_rng(100 + seed)
+    n = np.exp(rng.uniform(np.log(2 ** 8), np.log(2 ** 16), nf)).astype(
+        np.uint32)
+    n[0] = 1 << 16
+    T = rng.integers(50, 501, nf).astype(np.uint32)
+    T[0] = 500
+    seeds = (5000 + np.arange(nf)).astype(np.uint32)
+    models = []
+    for f in range(nf):
+        m = vc.default_model()
+        m.sigma_a = float(rng.uniform(0.5, 2.0))
+        m.obs_scale = float(rng.uniform(0.2, 1.0))
+        models.append(m)
+    return n, T, seeds, models
+
+
+@pytest.mark.parametrize("size", ["small", "config4"])
 @pytest.mark.parametrize("scheme", [1, 2])
-def test_batch_members_match_single_filters(vc, scheme):
+def test_batch_members_match_single_filters(vc, scheme, size):
     """Filter f of the batch against vsmc_cuda_pf with seed f and model f:
     identical particles and counts, so identical resampling decisions; the
-    FP64 sums differ only in their order."""
-    n, T, seeds, models = _spec(vc, nf=24, seed=scheme)
+    FP64 sums differ only in their order.  The single filter is checked
+    step by step against the oracle (test_pf32_gpu.py), so this carries the
+    oracle's parity to every member, at the benchmark batch's sizes too
+    (up to 2^16 particles and 500 steps)."""
+    if size == "small":
+        n, T, seeds, models = _spec(vc, nf=24, seed=scheme)
+    else:
+        n, T, seeds, models = _spec_config4(vc, nf=48, seed=scheme)
     b = vc.FilterBatch(n, T, seeds, models, scheme=scheme)
     obs = host(_simulate(vc, b)).reshape(-1, 2)
     got = b.run(obs)

@@ -31,13 +31,20 @@ def test_cv_mcmc_matches_oracle(vc, port, parent):
             ds.data_ptr(), acc.data_ptr(), None)
     ref = state.copy()
     racc = ctypes.c_uint32(0)
+    margin = np.zeros(n, np.float32)
     port.vo_cv_mcmc_f32(n, t, sweeps, 21, ctypes.byref(_omodel()), P(obs),
                         scale, P(par) if parent else None, P(ref),
-                        ctypes.byref(racc))
+                        ctypes.byref(racc), P(margin))
     got = host(ds)
-    # an accept decision sitting on the threshold can go the other way
-    # under FP32 differences in the normal generator: allow 0.5% of particles
+    # An accept decision whose log-uniform lies within FP32 rounding of the
+    # log acceptance ratio can go the other way (the device's normal pair
+    # and log-density use the SFU).  Every particle that differs must have
+    # had such a decision on the oracle's path: its closest |log u - log
+    # ratio| over the sweeps is below 1e-4 (typical values are O(1)).
     bad = ~np.isclose(got, ref, rtol=1e-4, atol=1e-4).all(axis=0)
+    unexplained = bad & (margin >= 1e-4)
+    assert not unexplained.any(), (np.flatnonzero(unexplained)[:10],
+                                   margin[unexplained][:10])
     assert bad.mean() < 5e-3, bad.mean()
     a = int(host(acc)[0])
     assert abs(a - racc.value) <= max(5, 0.005 * racc.value)

@@ -183,6 +183,60 @@ def test_pf32_filter_tracks_oracle(vc, port, scheme, graph):
     assert g["resampled"].sum() > 5
 
 
+def _download_i32(dev_ptr, count):
+    """count int32 values from a raw device address (through torch)."""
+    import torch
+    out = torch.empty(count, dtype=torch.int32, device="cuda")
+    cudart = None
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            cudart = ctypes.CDLL(name)
+            break
+        except OSError:
+            continue
+    assert cudart is not None
+    torch.cuda.synchronize()
+    rc = cudart.cudaMemcpy(ctypes.c_void_p(out.data_ptr()),
+                           ctypes.c_void_p(dev_ptr), ctypes.c_size_t(4 * count),
+                           ctypes.c_int(3))  # device to device
+    assert rc == 0, rc
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+def test_pf32_filter_every_step_against_oracle_replay(vc, port, scheme):
+    """The whole run, step by step: the oracle's FP32 filter replays the
+    device's own resampling (its decisions and genealogy rows), so the two
+    runs hold the same particles at every step and differ only by FP32
+    rounding in the move, the weights and the reductions.  Every step's ESS,
+    log-evidence and filtering mean must agree tightly, and every device
+    decision must match the oracle's ESS against the threshold unless the
+    ESS sits within 1e-4 of it."""
+    T, n = 100, 1 << 14
+    obs, _ = _obs(port, T)
+    pf = vc.ParticleFilter(n, 32, scheme, 0.5, seed=3, max_steps=T)
+    pf.record_genealogy(True)
+    g = pf.run(obs)
+    rows = _download_i32(pf.genealogy_ptr(), T * n)
+    pf.close()
+    mean = np.zeros(2 * T)
+    ess = np.zeros(T)
+    logz = np.zeros(T)
+    res = np.ascontiguousarray(g["resampled"], np.int32)
+    port.vo_pf_run_replay(32, n, T, 3, ctypes.byref(_omodel()),
+                          P(np.ascontiguousarray(obs)), P(res), P(rows),
+                          P(mean), P(ess), P(logz))
+    mean = mean.reshape(T, 2)
+    assert res.sum() > 5
+    rel_ess = np.abs(g["ess"] - ess) / ess
+    assert rel_ess.max() < 1e-4, (rel_ess.argmax(), rel_ess.max())
+    assert np.abs(g["logz"] - logz).max() < 1e-3, np.abs(g["logz"] - logz).max()
+    assert np.abs(g["mean"] - mean).max() < 1e-3, np.abs(g["mean"] - mean).max()
+    near = np.abs(ess / n - 0.5) < 1e-4
+    decided = (ess < 0.5 * n).astype(np.int32)
+    assert np.array_equal(res[~near], decided[~near])
+
+
 def test_pf32_reproducible_and_graph_equal(vc, port):
     T, n = 60, 50000
     obs, _ = _obs(port, T, seed=4)
