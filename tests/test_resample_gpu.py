@@ -189,8 +189,10 @@ def test_residual_split(vc, port, m, n):
     assert np.array_equal(host(resid), resid_ref)
 
 
-SCHEME_SIZES = [(1, 5), (5, 0), (2, 3), (100, 100), (1000, 1000), (1000, 700),
-                (50000, 50000), (1 << 18, 1 << 18)]
+# n a power of two (1, 4096, 2^18) takes the integer path of the
+# stratified / systematic uniforms; the others the FP64 one
+SCHEME_SIZES = [(1, 5), (5, 0), (2, 3), (64, 1), (100, 100), (1000, 1000),
+                (1000, 700), (4096, 4096), (50000, 50000), (1 << 18, 1 << 18)]
 EXACT = {1, 2, 4, 5}  # stratified, systematic and their residual forms
 
 

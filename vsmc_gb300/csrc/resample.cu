@@ -261,10 +261,45 @@ __device__ __forceinline__ uint32_t stream_word(const EngineState &e, size_t k)
     return i == 0 ? b.x : (i == 1 ? b.y : (i == 2 ? b.z : b.w));
 }
 
+// x * 2^-e rounded to the nearest double, ties to even, for 0 <= x < 2^63
+// and a result in the normal range: the rounding of an exact value to 53
+// significant bits done on the integer (IEEE 754 round-to-nearest-even),
+// and the double assembled from its bits, so no FP64 instruction runs.
+__device__ __forceinline__ double rne_scaled(uint64_t x, int e)
+{
+    if (x == 0)
+        return 0.0;
+    int b = 64 - __clzll(static_cast<long long>(x)); // significant bits
+    uint64_t m = x;
+    int sh = 0;
+    if (b > 53) {
+        sh = b - 53;
+        const uint64_t rest = x & ((1ull << sh) - 1);
+        const uint64_t half = 1ull << (sh - 1);
+        m = x >> sh;
+        if (rest > half || (rest == half && (m & 1)))
+            ++m;
+        if (m >> 53) { // rounded up to 2^53
+            m >>= 1;
+            ++sh;
+        }
+        b = 53;
+    }
+    // value = m * 2^(sh - e), m < 2^53 with b significant bits
+    const int exp2 = b - 1 + sh - e; // unbiased exponent of the result
+    const uint64_t frac = (m << (53 - b)) & ((1ull << 52) - 1);
+    const uint64_t bits =
+        (static_cast<uint64_t>(exp2 + 1023) << 52) | frac;
+    return __longlong_as_double(static_cast<long long>(bits));
+}
+
 // U01SequenceStratified: u_j = U_j * delta + j * delta.  Word j is at
 // stream position index + j; one Philox block gives the four words of
-// positions 4b .. 4b + 3.
-__global__ void k_stratified_seq(EngineState e, size_t n, double *u)
+// positions 4b .. 4b + 3.  For n = 2^k (log2n = k, else -1) delta is exact,
+// both products are exact scalings of U_j = w 2^-32 and j, and the one
+// rounding is that of the sum: u_j = RNE(j 2^32 + w) 2^-(32 + k), formed in
+// integers (rne_scaled).  Otherwise the FP64 arithmetic of the reference.
+__global__ void k_stratified_seq(EngineState e, size_t n, int log2n, double *u)
 {
     const double delta = 1.0 / static_cast<double>(n);
     const uint64_t first = e.index;
@@ -281,18 +316,30 @@ __global__ void k_stratified_seq(EngineState e, size_t n, double *u)
             if (pos < first || pos - first >= n)
                 continue;
             const size_t j = static_cast<size_t>(pos - first);
-            const double U = u01_co_d(ws[k]);
-            u[j] = __dadd_rn(__dmul_rn(U, delta),
-                __dmul_rn(static_cast<double>(j), delta));
+            if (log2n >= 0) {
+                u[j] = rne_scaled((static_cast<uint64_t>(j) << 32) | ws[k],
+                    32 + log2n);
+            } else {
+                const double U = u01_co_d(ws[k]);
+                u[j] = __dadd_rn(__dmul_rn(U, delta),
+                    __dmul_rn(static_cast<double>(j), delta));
+            }
         }
     }
 }
 
-// U01SequenceSystematic: u0 = U * delta, u_j = u0 + j * delta
-__global__ void k_systematic_seq(EngineState e, size_t n, double *u)
+// U01SequenceSystematic: u0 = U * delta, u_j = u0 + j * delta (for n = 2^k
+// the same integer rounding with one word for every j)
+__global__ void k_systematic_seq(EngineState e, size_t n, int log2n, double *u)
 {
+    const uint32_t w0 = stream_word(e, 0);
+    if (log2n >= 0) {
+        GRID_LOOP(j, n)
+        u[j] = rne_scaled((static_cast<uint64_t>(j) << 32) | w0, 32 + log2n);
+        return;
+    }
     const double delta = 1.0 / static_cast<double>(n);
-    const double u0 = __dmul_rn(u01_co_d(stream_word(e, 0)), delta);
+    const double u0 = __dmul_rn(u01_co_d(w0), delta);
     GRID_LOOP(j, n)
     u[j] = __dadd_rn(u0, __dmul_rn(static_cast<double>(j), delta));
 }
@@ -831,10 +878,17 @@ int scheme_device(size_t m, size_t n, vsmc_cuda_rng *rng, const double *w,
     if (u == nullptr)
         return VSMC_CUDA_ERR_ALLOC;
     if (N > 0) {
+        // N = 2^k: the uniforms are formed in integers (exact, no FP64)
+        int log2n = -1;
+        if ((N & (N - 1)) == 0 && N <= (size_t(1) << 31)) {
+            log2n = 0;
+            while ((size_t(1) << log2n) < N)
+                ++log2n;
+        }
         if (base == VSMC_CUDA_STRATIFIED) {
-            k_stratified_seq<<<grid1(N), kB, 0, st>>>(es, N, u);
+            k_stratified_seq<<<grid1(N), kB, 0, st>>>(es, N, log2n, u);
         } else if (base == VSMC_CUDA_SYSTEMATIC) {
-            k_systematic_seq<<<grid1(N), kB, 0, st>>>(es, N, u);
+            k_systematic_seq<<<grid1(N), kB, 0, st>>>(es, N, log2n, u);
         } else {
             double *t = scratch.get<double>(N);
             if (t == nullptr)
