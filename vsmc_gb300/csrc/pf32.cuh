@@ -263,8 +263,26 @@ __device__ __forceinline__ uint64_t q_at(
     return a.q ? a.q[i] : fixed_q(a.lw[i], M, a.shift);
 }
 
-// block sum of q over the block's chunk (four groups of four per thread in
-// flight)
+// Each block's chunk is split into kRsWarps equal warp ranges (the chunk
+// is a multiple of kPfTile, so a range is a multiple of 128 particles); the
+// passes address a range by (block, warp).
+constexpr uint32_t kRsWarps = kPfBlock / 32;
+
+__device__ __forceinline__ void warp_range(
+    uint32_t lo, uint32_t hi, uint32_t chunk, uint32_t w, uint32_t &wlo,
+    uint32_t &whi)
+{
+    const uint32_t span = chunk / kRsWarps;
+    wlo = lo + w * span;
+    whi = wlo + span;
+    if (wlo > hi)
+        wlo = hi;
+    if (whi > hi)
+        whi = hi;
+}
+
+// Sum of q over each warp range (four groups of four per lane in flight):
+// qpart[block * kRsWarps + warp].
 __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
 {
     if (!(a.force || a.sc->resampled))
@@ -279,15 +297,18 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
     const float M = static_cast<float>(a.sc->M);
     uint32_t lo, hi;
     chunk_range(a.n, a.chunk, lo, hi);
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t wlo, whi;
+    warp_range(lo, hi, a.chunk, w, wlo, whi);
     uint64_t acc = 0;
     constexpr int kG = 4;
-    for (uint32_t base = lo; base < hi; base += kG * kPfTile) {
-        if (a.q == nullptr && base + kG * kPfTile <= hi) {
+    for (uint32_t base = wlo; base < whi; base += kG * 128) {
+        if (a.q == nullptr && base + kG * 128 <= whi) {
             float4 v[kG];
 #pragma unroll
             for (int h = 0; h < kG; ++h)
                 v[h] = __ldcg(reinterpret_cast<const float4 *>(
-                    a.lw + base + h * kPfTile + threadIdx.x * 4));
+                    a.lw + base + h * 128 + lane * 4));
 #pragma unroll
             for (int h = 0; h < kG; ++h)
                 acc += fixed_q(v[h].x, M, a.shift) +
@@ -295,16 +316,17 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
                     fixed_q(v[h].z, M, a.shift) + fixed_q(v[h].w, M, a.shift);
         } else {
             for (int h = 0; h < kG; ++h) {
-                const uint32_t i0 = base + h * kPfTile + threadIdx.x * 4;
-                for (uint32_t i = i0; i < hi && i < i0 + 4; ++i)
+                const uint32_t i0 = base + h * 128 + lane * 4;
+                for (uint32_t i = i0; i < whi && i < i0 + 4; ++i)
                     acc += q_at(a, i, M);
             }
         }
     }
-    __shared__ uint64_t sh[kPfBlock / 32 + 1];
-    acc = block_reduce(acc, OpAdd(), uint64_t(0), sh);
-    if (threadIdx.x == 0)
-        a.qpart[blockIdx.x] = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+    if (lane == 0)
+        a.qpart[blockIdx.x * kRsWarps + w] = acc;
 }
 
 // sum of part[0..upto) and of part[0..total) over the block
@@ -340,7 +362,8 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
     __shared__ uint4 wbuf[2 * kPfBlock];        // stratified words of a tile
     __shared__ uint32_t wsh[2 * (kPfBlock / 32)];
     uint64_t offset, Q;
-    block_prefix_of_parts(a.qpart, blockIdx.x, gridDim.x, offset, Q, shq);
+    block_prefix_of_parts(a.qpart, blockIdx.x * kRsWarps,
+        gridDim.x * kRsWarps, offset, Q, shq);
     if (blockIdx.x == 0 && threadIdx.x == 0)
         a.sc->Q = Q;
     const PfScalars sc = *a.sc;
@@ -454,11 +477,162 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
     }
 }
 
+// Warp-wide exclusive scan of positions; *total gets the warp's sum.
+__device__ __forceinline__ QR warp_exclusive_qr(QR v, uint64_t Q, QR *total)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    QR x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        QR o;
+        o.j = __shfl_up_sync(0xFFFFFFFFu, x.j, d);
+        o.r = __shfl_up_sync(0xFFFFFFFFu, x.r, d);
+        if (lane >= static_cast<uint32_t>(d))
+            x = qr_add(o, x, Q);
+    }
+    total->j = __shfl_sync(0xFFFFFFFFu, x.j, 31);
+    total->r = __shfl_sync(0xFFFFFFFFu, x.r, 31);
+    QR ex;
+    ex.j = __shfl_up_sync(0xFFFFFFFFu, x.j, 1);
+    ex.r = __shfl_up_sync(0xFFFFFFFFu, x.r, 1);
+    if (lane == 0)
+        ex = QR{0, 0};
+    return ex;
+}
+
+// Systematic counts, one warp per warp range: the range's first CDF
+// position comes from the per-range q sums (one 128-bit division by the
+// range's lane 0), then the warp walks its range 128 particles at a time
+// with warp scans of the positions and no block barrier.  The counts are
+// the same integers as k_rs32_count<true> gives.
+__global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count_sys(const Rs32Args a)
+{
+    if (!a.sc->resampled)
+        return;
+    const float M = static_cast<float>(a.sc->M);
+    uint32_t lo, hi;
+    chunk_range(a.n, a.chunk, lo, hi);
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __shared__ uint64_t shq[kPfBlock / 32 + 1];
+    __shared__ uint32_t she[kPfBlock / 32 + 1];
+    // offset of the block (every earlier range) and of this warp's range
+    uint64_t boff, Q;
+    block_prefix_of_parts(a.qpart, blockIdx.x * kRsWarps,
+        gridDim.x * kRsWarps, boff, Q, shq);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        a.sc->Q = Q;
+    uint64_t woff =
+        lane < w ? a.qpart[blockIdx.x * kRsWarps + lane] : uint64_t(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        woff += __shfl_xor_sync(0xFFFFFFFFu, woff, o);
+    woff += boff;
+    uint32_t wlo, whi;
+    warp_range(lo, hi, a.chunk, w, wlo, whi);
+    const bool checked = a.q != nullptr;
+    const uint32_t n = a.n;
+    const CountP cp = make_count_params(Q, n, engine_word(*a.sc, 0));
+    const float invQ = __frcp_rn(__ull2float_rn(Q));
+    uint32_t err = 0;
+    // the range's first CDF position (lane 0), broadcast
+    QR carry = {0, 0};
+    if (lane == 0 && wlo < whi) {
+        long long j;
+        uint64_t r;
+        if (cn_divmod(woff, cp.G, cp, j, r, err)) {
+            carry.j = static_cast<uint32_t>(j + 1);
+            carry.r = r;
+        } else { // woff n < G < Q: X = -(G - woff n)
+            carry.j = 0;
+            carry.r = Q - (cp.G - woff * static_cast<uint64_t>(n));
+        }
+    }
+    carry.j = __shfl_sync(0xFFFFFFFFu, carry.j, 0);
+    carry.r = __shfl_sync(0xFFFFFFFFu, carry.r, 0);
+    uint32_t empties = 0, copies = 0;
+    float4 nxt = make_float4(0, 0, 0, 0);
+    if (!checked && wlo + lane * 4 + 3 < whi)
+        nxt = __ldcg(reinterpret_cast<const float4 *>(a.lw + wlo + lane * 4));
+    for (uint32_t base = wlo; base < whi; base += 128) {
+        const uint32_t i0 = base + lane * 4;
+        const float4 v = nxt;
+        if (!checked && i0 + 128 + 3 < whi)
+            nxt = __ldcg(reinterpret_cast<const float4 *>(a.lw + i0 + 128));
+        uint64_t q[4];
+        if (i0 + 3 < whi && !checked) {
+            q[0] = fixed_q(v.x, M, a.shift);
+            q[1] = fixed_q(v.y, M, a.shift);
+            q[2] = fixed_q(v.z, M, a.shift);
+            q[3] = fixed_q(v.w, M, a.shift);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                q[k] = (i0 + k < whi) ? q_at(a, i0 + k, M) : 0;
+        }
+        QR loc[4];
+        QR acc = {0, 0};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            qr_push(acc, q[k], n, checked, Q, invQ, cp, err);
+            loc[k] = acc;
+        }
+        QR total;
+        const QR ex = warp_exclusive_qr(acc, Q, &total);
+        const QR st = qr_add(carry, ex, Q);
+        uint32_t F[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = i0 + k;
+            if (i + 1 >= n) {
+                F[k] = n; // the last particle takes the rest
+            } else if (i < whi) {
+                const QR x = qr_add(st, loc[k], Q);
+                F[k] = x.j < n ? x.j : n;
+            } else {
+                F[k] = 0;
+            }
+        }
+        uint32_t Fprev = i0 == 0 ? 0u : (st.j < n ? st.j : n);
+        int32_t r[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            r[k] = static_cast<int32_t>(F[k] - Fprev);
+            Fprev = F[k];
+        }
+        if (i0 + 3 < whi) {
+            *reinterpret_cast<int4 *>(a.rep + i0) =
+                make_int4(r[0], r[1], r[2], r[3]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                empties += r[k] == 0 ? 1u : 0u;
+                copies += static_cast<uint32_t>(r[k]);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (i0 + k < whi) {
+                    a.rep[i0 + k] = r[k];
+                    empties += r[k] == 0 ? 1u : 0u;
+                    copies += static_cast<uint32_t>(r[k]);
+                }
+        }
+        carry = qr_add(carry, total, Q);
+    }
+    if (err)
+        atomicOr(&a.sc->err, err);
+    empties = block_reduce(empties, OpAdd(), 0u, she);
+    copies = block_reduce(copies, OpAdd(), 0u, she);
+    if (threadIdx.x == 0) {
+        a.epart[blockIdx.x] = empties;
+        a.cpart[blockIdx.x] = copies;
+    }
+}
+
 // the counting kernel of the scheme (systematic or stratified)
 inline void launch_rs32_count(int grid, cudaStream_t st, const Rs32Args &a)
 {
     if (a.scheme == VSMC_CUDA_SYSTEMATIC)
-        k_rs32_count<true><<<grid, kPfBlock, 0, st>>>(a);
+        k_rs32_count_sys<<<grid, kPfBlock, 0, st>>>(a);
     else
         k_rs32_count<false><<<grid, kPfBlock, 0, st>>>(a);
 }

@@ -231,33 +231,35 @@ __device__ __forceinline__ uint32_t quot_below(uint64_t r, float invQ)
     return __float2uint_rz(est);
 }
 
-// Bring r below Q, adding the quotient to j.  No copy and one copy (r < 2Q)
-// are the common cases.  Otherwise one estimate from below leaves at most
-// (r / Q) 1.4e-6 + 1 (below 2 for fewer than 7e5 copies) and one
-// conditional step usually finishes; a position advanced by q n with q <= Q
-// has r < Q (n + 1), a quotient below 2^31, so a second estimate (below 2
-// left after it) and one more step always do.  No path loops, so a warp
-// whose lanes need different numbers of copies does not iterate.
+// Bring r below Q, adding the quotient to j.  Every lane takes the same
+// path: one estimate from below (quot_below; 0 when r < Q), which leaves at
+// most (r / Q) 1.4e-6 + 1 (below 2 for fewer than 7e5 copies), then two
+// conditional steps, so the warp does not split on how many copies its
+// lanes' particles take.  Only a position advanced by 7e5 or more copies
+// needs the second estimate (a quotient below 2^31 always leaves less than
+// 2 after it), and one more step.
 __device__ __forceinline__ void qr_reduce(
     uint64_t &r, uint32_t &j, uint64_t Q, float invQ, uint32_t &err)
 {
-    if (r < Q)
-        return;
-    r -= Q;
-    ++j;
-    if (r < Q)
-        return;
     uint32_t d = quot_below(r, invQ);
-    r -= static_cast<uint64_t>(d) * Q;
+    r -= static_cast<uint64_t>(d) * Q; // d Q <= r: no wrap
     j += d;
     if (r >= Q) {
         r -= Q;
         ++j;
     }
-    if (r >= Q) { // more than 7e5 copies: a second estimate
+    if (r >= Q) {
+        r -= Q;
+        ++j;
+    }
+    if (r >= Q) { // 7e5 or more copies: a second estimate
         d = quot_below(r, invQ);
         r -= static_cast<uint64_t>(d) * Q;
         j += d;
+        if (r >= Q) {
+            r -= Q;
+            ++j;
+        }
         if (r >= Q) {
             r -= Q;
             ++j;

@@ -16,7 +16,7 @@ struct Rs32Args {
     uint32_t chunk;  // particles per block (multiple of kPfTile)
     int scheme;      // VSMC_CUDA_STRATIFIED or VSMC_CUDA_SYSTEMATIC
     int force;       // resample whatever the step decided (host decision)
-    uint64_t *qpart; // per-block sum of q
+    uint64_t *qpart; // per-(block, warp range) sum of q
     uint32_t *epart; // per-block empty count
     uint32_t *cpart; // per-block copy count (sum of rep)
     int32_t *rep;
