@@ -941,6 +941,7 @@ def run_sampler(args):
             "device_threshold": "the Sampler's (resampling queued right "
                                 "after each step)",
             "timing": "host clock around initialize + iterate per run",
+            "graph": "steps from t = 2 replayed as CUDA graphs",
             "resampled_steps_last_run": resampled,
             "ms_per_run_each": timed,
         },

@@ -428,6 +428,14 @@ int vsmc_cuda_pf_reset(vsmc_cuda_pf *pf);
  * resampling passes (threshold >= 0; they return at once unless the step
  * flagged a resample), then the buffers swap and the step index advances. */
 int vsmc_cuda_pf_step_commit(vsmc_cuda_pf *pf);
+/* The host-side part of vsmc_cuda_pf_step_commit (the buffers swap, the
+ * step index advances) without its launches: for a caller that replays a
+ * step it captured in a CUDA graph from one step_desc_get ->
+ * pf_step_launch -> step_commit sequence on the filter's stream (the graph
+ * holds the step kernel and the resampling passes; a graph per buffer
+ * parity, since the descriptor's buffers alternate).  No reference
+ * counterpart. */
+int vsmc_cuda_pf_step_advance(vsmc_cuda_pf *pf);
 /* Resample the current particles now (precision 32): the host decided
  * ESS < threshold * N.  Particle::resample -> StateCUDA::copy(N, nullptr)
  * (core/particle.hpp:186-192); the weights become equal, and the monitor

@@ -42,6 +42,12 @@
 // covers the step, the resample and the monitor.  Without it, the passes run
 // when Particle::resample calls copy(N, nullptr).  A device decision the
 // host did not take (the two thresholds differ) throws at the next step.
+//
+// From the third step on, a step (the fused kernel and, with a device
+// threshold, the three resampling passes) is replayed as a CUDA graph: one
+// graph per buffer parity, captured the first time that parity comes up
+// and captured again when the model's bytes change.  use_graph(false) on
+// the state launches every step on its own.
 #ifndef VSMC_CUDA_SAMPLER_CUH
 #define VSMC_CUDA_SAMPLER_CUH
 
@@ -52,6 +58,7 @@
 #include <vsmc/rng/rng_set.hpp>
 
 #include <cmath>
+#include <cstring>
 #include <memory>
 
 namespace vsmc
@@ -70,6 +77,7 @@ class FilterCore
     FilterCore &operator=(const FilterCore &) = delete;
     ~FilterCore()
     {
+        drop_graphs();
         if (pf_ != nullptr)
             vsmc_cuda_pf_destroy(pf_);
     }
@@ -92,6 +100,11 @@ class FilterCore
     {
         history_ = T > 0 ? T : 1;
         drop();
+    }
+    void use_graph(bool on)
+    {
+        use_graph_ = on;
+        drop_graphs();
     }
 
     // a filter at step 0 for a model with monitor_dim monitored components
@@ -127,8 +140,12 @@ class FilterCore
         vsmc_cuda_pf_step_desc d;
         check(vsmc_cuda_pf_step_desc_get(pf_, &d),
             "vsmc_cuda_pf_step_desc_get");
-        check(::vsmc_cuda::pf_step_launch(d, model), "pf_step_launch");
-        check(vsmc_cuda_pf_step_commit(pf_), "vsmc_cuda_pf_step_commit");
+        if (use_graph_ && d.step >= 2) {
+            replay(d, model);
+        } else {
+            check(::vsmc_cuda::pf_step_launch(d, model), "pf_step_launch");
+            check(vsmc_cuda_pf_step_commit(pf_), "vsmc_cuda_pf_step_commit");
+        }
         ++version_;
         equal_ = false;
         fresh_ = true;
@@ -198,10 +215,78 @@ class FilterCore
 
     void drop()
     {
+        drop_graphs();
         if (pf_ != nullptr)
             vsmc_cuda_pf_destroy(pf_);
         pf_ = nullptr;
         ++version_;
+    }
+
+    template <typename Model>
+    static const void *model_tag()
+    {
+        static const char tag = 0;
+        return &tag;
+    }
+
+    void drop_graphs()
+    {
+        for (int k = 0; k != 2; ++k) {
+            if (graph_[k] != nullptr)
+                cudaGraphExecDestroy(graph_[k]);
+            graph_[k] = nullptr;
+            graph_in_[k] = nullptr;
+        }
+        graph_tag_ = nullptr;
+        graph_model_.clear();
+    }
+
+    // the step of d as a graph launch; the host's half of step_commit
+    // follows a replay, and runs inside the capture the first time
+    template <typename Model>
+    void replay(const vsmc_cuda_pf_step_desc &d, const Model &model)
+    {
+        const unsigned char *mb = reinterpret_cast<const unsigned char *>(&model);
+        if (graph_tag_ != model_tag<Model>() ||
+            graph_model_.size() != sizeof(Model) ||
+            std::memcmp(graph_model_.data(), mb, sizeof(Model)) != 0) {
+            drop_graphs();
+            graph_tag_ = model_tag<Model>();
+            graph_model_.assign(mb, mb + sizeof(Model));
+        }
+        cudaStream_t st = static_cast<cudaStream_t>(d.stream);
+        for (int k = 0; k != 2; ++k) {
+            if (graph_[k] != nullptr && graph_in_[k] == d.state_in) {
+                check_cuda(cudaGraphLaunch(graph_[k], st), "cudaGraphLaunch");
+                check(vsmc_cuda_pf_step_advance(pf_),
+                    "vsmc_cuda_pf_step_advance");
+                return;
+            }
+        }
+        const int k = graph_[0] == nullptr ? 0 : 1;
+        if (graph_[k] != nullptr)
+            throw Error(VSMC_CUDA_ERR_ARG,
+                "StateCUDA: a third state buffer for the step graphs");
+        check_cuda(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal),
+            "cudaStreamBeginCapture");
+        int rc = ::vsmc_cuda::pf_step_launch(d, model);
+        if (rc == VSMC_CUDA_OK)
+            rc = vsmc_cuda_pf_step_commit(pf_);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc != VSMC_CUDA_OK || e != cudaSuccess) {
+            if (g != nullptr)
+                cudaGraphDestroy(g);
+            check(rc, "captured step");
+            check_cuda(e, "cudaStreamEndCapture");
+        }
+        cudaGraphExec_t x = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+        cudaGraphDestroy(g);
+        check_cuda(ei, "cudaGraphInstantiate");
+        graph_[k] = x;
+        graph_in_[k] = d.state_in;
+        check_cuda(cudaGraphLaunch(x, st), "cudaGraphLaunch");
     }
 
     std::size_t N_, dim_;
@@ -216,6 +301,11 @@ class FilterCore
     bool equal_ = false;   // the host made the weights equal
     bool fresh_ = false;   // nothing changed the weights since the last step
     bool pending_ = false; // a device resample the host has not taken yet
+    bool use_graph_ = true;
+    cudaGraphExec_t graph_[2] = {nullptr, nullptr}; // by input buffer
+    const float *graph_in_[2] = {nullptr, nullptr};
+    const void *graph_tag_ = nullptr;               // the captured model
+    std::vector<unsigned char> graph_model_;
 };
 
 // weight_type of StateCUDA<Dim, float>: the Weight interface
@@ -371,6 +461,9 @@ class StateCUDA<Dim, float>
 
     // steps of device history kept (ESS, log-evidence, monitor)
     void reserve_history(std::size_t T) { core_->history(T); }
+
+    // replay steps as CUDA graphs (default) or launch each on its own
+    void use_graph(bool on) { core_->use_graph(on); }
 
     FilterCore &core() { return *core_; }
     const std::shared_ptr<FilterCore> &core_ptr() { return core_; }

@@ -108,7 +108,8 @@ int main(int argc, char **argv)
 {
     if (argc < 9) {
         std::fprintf(stderr, "usage: %s N T seed scheme threshold "
-                             "device_threshold obs.bin out.bin [runs]\n",
+                             "device_threshold obs.bin out.bin [runs] "
+                             "[graph]\n",
             argv[0]);
         return 2;
     }
@@ -119,6 +120,7 @@ int main(int argc, char **argv)
     const double threshold = std::stod(argv[5]);
     const bool dev_thr = std::stoi(argv[6]) != 0;
     const int runs = argc > 9 ? std::stoi(argv[9]) : 1;
+    const bool graph = argc > 10 ? std::stoi(argv[10]) != 0 : true;
 
     std::vector<double> obs(2 * T);
     {
@@ -144,6 +146,7 @@ int main(int argc, char **argv)
     sampler.particle().value().resample_scheme(sch, seed);
     if (dev_thr)
         sampler.particle().value().resample_threshold(threshold);
+    sampler.particle().value().use_graph(graph);
     sampler.init(vsmc::cuda::InitializeCUDA<PfModel>(model));
     sampler.move(vsmc::cuda::MoveCUDA<PfModel>(model), false);
     sampler.monitor("pos", 2, vsmc::cuda::MonitorMeanCUDA<4, float>(), true);

@@ -57,15 +57,16 @@ def build_sampler_program(out_path):
 
 
 def run_sampler_program(exe, tmpdir, n, T, seed, scheme, threshold, dev_thr,
-                        obs, runs=1):
-    """Runs the program; returns (histories, its JSON timing line)."""
+                        obs, runs=1, graph=True):
+    """Runs the program; returns (histories, its JSON timing line).  graph:
+    steps replayed as CUDA graphs (StateCUDA::use_graph)."""
     import json
     obs_path = os.path.join(str(tmpdir), "obs.bin")
     out_path = os.path.join(str(tmpdir), "out.bin")
     np.ascontiguousarray(obs, dtype=np.float64).tofile(obs_path)
     r = subprocess.run([exe, str(n), str(T), str(seed), str(scheme),
                         repr(threshold), "1" if dev_thr else "0", obs_path,
-                        out_path, str(runs)],
+                        out_path, str(runs), "1" if graph else "0"],
                        capture_output=True, text=True, timeout=600)
     if r.returncode != 0:
         raise RuntimeError(r.stderr[-3000:])
@@ -131,3 +132,20 @@ def test_sampler_tracks_oracle_fp32_filter(vc, port, exe, tmp_path):
     assert abs(got["logz"][0] - logz[0]) < 1e-5 * max(1, abs(logz[0]))
     assert np.abs(got["mean"] - mean.reshape(T, 2)).max() < 0.5
     assert abs(got["logz"][-1] - logz[-1]) < 2.0
+
+
+@pytest.mark.parametrize("dev_thr", [False, True])
+def test_sampler_graph_replay_equals_launches(vc, port, exe, tmp_path,
+                                              dev_thr):
+    """Steps replayed from the captured graphs (one per buffer parity, kept
+    across Sampler::initialize) give the histories of steps launched one by
+    one, bit for bit, over two runs of the same sampler."""
+    n, T, seed, thr = 100003, 40, 11, 0.6
+    obs = _obs(port, T)
+    a, _ = run_sampler_program(exe, tmp_path, n, T, seed, 2, thr, dev_thr,
+                               obs, runs=2, graph=True)
+    b, _ = run_sampler_program(exe, tmp_path, n, T, seed, 2, thr, dev_thr,
+                               obs, runs=2, graph=False)
+    assert a["resampled"].sum() > 3
+    for k in ("mean", "ess", "resampled", "logz"):
+        assert np.array_equal(a[k], b[k]), k

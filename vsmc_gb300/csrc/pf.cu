@@ -612,6 +612,16 @@ int vsmc_cuda_pf_step_commit(vsmc_cuda_pf *pf)
     return VSMC_CUDA_OK;
 }
 
+int vsmc_cuda_pf_step_advance(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr || pf->precision != 32 || pf->t == 0)
+        return VSMC_CUDA_ERR_ARG;
+    pf->cur = 1 - pf->cur;
+    ++pf->t;
+    pf->host_equal = false;
+    return VSMC_CUDA_OK;
+}
+
 int vsmc_cuda_pf_reset(vsmc_cuda_pf *pf)
 {
     if (pf == nullptr || pf->precision != 32 || !pf->custom)
