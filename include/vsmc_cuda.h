@@ -462,6 +462,13 @@ typedef struct {
 } vsmc_cuda_pf_status;
 
 int vsmc_cuda_pf_get_status(vsmc_cuda_pf *pf, vsmc_cuda_pf_status *out);
+/* vsmc_cuda_pf_get_status in two halves.  status_enqueue queues the copy of
+ * the device scalars into the filter's pinned host copy on its stream (no
+ * wait; it may be captured into a graph with the step).  status_read waits
+ * for the stream and reads that copy, with no copy of its own: it returns
+ * what the last queued copy saw.  No reference counterpart. */
+int vsmc_cuda_pf_status_enqueue(vsmc_cuda_pf *pf);
+int vsmc_cuda_pf_status_read(vsmc_cuda_pf *pf, vsmc_cuda_pf_status *out);
 
 /* ------------------------------------- bearings-only model, proposal */
 

@@ -43,8 +43,11 @@
 // when Particle::resample calls copy(N, nullptr).  A device decision the
 // host did not take (the two thresholds differ) throws at the next step.
 //
-// From the third step on, a step (the fused kernel and, with a device
-// threshold, the three resampling passes) is replayed as a CUDA graph: one
+// Each step queues the copy of the filter's scalars (ESS, log-evidence,
+// monitor, decision) behind its kernels, and the host's first read after it
+// waits for that copy alone.  From the third step on, a step (the fused
+// kernel, with a device threshold the three resampling passes, and the
+// scalars' copy) is replayed as a CUDA graph: one
 // graph per buffer parity, captured the first time that parity comes up
 // and captured again when the model's bytes change.  use_graph(false) on
 // the state launches every step on its own.
@@ -145,8 +148,11 @@ class FilterCore
         } else {
             check(::vsmc_cuda::pf_step_launch(d, model), "pf_step_launch");
             check(vsmc_cuda_pf_step_commit(pf_), "vsmc_cuda_pf_step_commit");
+            check(vsmc_cuda_pf_status_enqueue(pf_),
+                "vsmc_cuda_pf_status_enqueue");
         }
         ++version_;
+        queued_version_ = version_;
         equal_ = false;
         fresh_ = true;
     }
@@ -192,8 +198,13 @@ class FilterCore
     {
         require_open();
         if (status_version_ != version_) {
-            check(vsmc_cuda_pf_get_status(pf_, &status_),
-                "vsmc_cuda_pf_get_status");
+            // the step queued the copy of the scalars after its work
+            if (queued_version_ == version_)
+                check(vsmc_cuda_pf_status_read(pf_, &status_),
+                    "vsmc_cuda_pf_status_read");
+            else
+                check(vsmc_cuda_pf_get_status(pf_, &status_),
+                    "vsmc_cuda_pf_get_status");
             status_version_ = version_;
             if (fresh_ && threshold_ >= 0 && status_.resampled)
                 pending_ = true; // until Particle::resample agrees
@@ -272,6 +283,8 @@ class FilterCore
         int rc = ::vsmc_cuda::pf_step_launch(d, model);
         if (rc == VSMC_CUDA_OK)
             rc = vsmc_cuda_pf_step_commit(pf_);
+        if (rc == VSMC_CUDA_OK)
+            rc = vsmc_cuda_pf_status_enqueue(pf_);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(st, &g);
         if (rc != VSMC_CUDA_OK || e != cudaSuccess) {
@@ -298,6 +311,7 @@ class FilterCore
     vsmc_cuda_pf *pf_ = nullptr;
     vsmc_cuda_pf_status status_ = {};
     unsigned long long version_ = 1, status_version_ = 0;
+    unsigned long long queued_version_ = 0; // a step queued its status copy
     bool equal_ = false;   // the host made the weights equal
     bool fresh_ = false;   // nothing changed the weights since the last step
     bool pending_ = false; // a device resample the host has not taken yet

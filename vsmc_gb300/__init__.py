@@ -180,6 +180,8 @@ PROTOTYPES = {
     "vsmc_cuda_pf_create_model": (
         I32, [ctypes.POINTER(VP), SZ, SZ, SZ, I32, F64, U32, SZ, VP]),
     "vsmc_cuda_pf_step_desc_get": (I32, [VP, ctypes.POINTER(PfStepDesc)]),
+    "vsmc_cuda_pf_status_enqueue": (I32, [VP]),
+    "vsmc_cuda_pf_status_read": (I32, [VP, ctypes.POINTER(PfStatus)]),
     "vsmc_cuda_pf_step_advance": (I32, [VP]),
     "vsmc_cuda_pf_step_commit": (I32, [VP]),
     "vsmc_cuda_pf_reset": (I32, [VP]),

@@ -263,6 +263,18 @@ static int reset_scalars(vsmc_cuda_pf *pf)
     return VSMC_CUDA_OK;
 }
 
+// The scalars copied into the pinned host copy by the GPU itself (32-bit
+// words; the host copy is mapped): a kernel node behind the step's kernels
+// instead of a copy-engine transfer.
+__global__ void k_pf32_status_out(const PfScalars *sc, PfScalars *host)
+{
+    static_assert(sizeof(PfScalars) % 4 == 0, "whole words");
+    const uint32_t *s = reinterpret_cast<const uint32_t *>(sc);
+    uint32_t *d = reinterpret_cast<uint32_t *>(host);
+    for (uint32_t i = threadIdx.x; i < sizeof(PfScalars) / 4; i += blockDim.x)
+        d[i] = s[i];
+}
+
 // Weight::set_equal: every weight equal, the stored log-weights stale
 __global__ void k_pf32_set_equal(PfScalars *sc, uint32_t n)
 {
@@ -493,10 +505,14 @@ static int pf_create(vsmc_cuda_pf **out, size_t n, size_t dim,
     PF_TRY(dalloc(&pf->h_logz, max_steps));
     PF_TRY(dalloc(&pf->h_res, max_steps));
     PF_TRY(dalloc(&pf->sc, 1));
-    if (cudaMallocHost(&pf->sc_host, sizeof(PfScalars)) != cudaSuccess) {
+    if (cudaHostAlloc(reinterpret_cast<void **>(&pf->sc_host),
+            sizeof(PfScalars), cudaHostAllocMapped) != cudaSuccess) {
         pf->sc_host = nullptr;
         PF_TRY(VSMC_CUDA_ERR_ALLOC);
     }
+    if (cudaHostGetDevicePointer(reinterpret_cast<void **>(&pf->sc_host_dev),
+            pf->sc_host, 0) != cudaSuccess)
+        PF_TRY(VSMC_CUDA_ERR_CUDA);
     if (precision == 32) {
         if (model) {
             // looked up here, outside any stream capture of a step
@@ -676,13 +692,29 @@ int vsmc_cuda_pf_weight_log(vsmc_cuda_pf *pf, const double *lw_dev, int add)
     return VSMC_CUDA_OK;
 }
 
+int vsmc_cuda_pf_status_enqueue(vsmc_cuda_pf *pf)
+{
+    if (pf == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
+    k_pf32_status_out<<<1, 32, 0, pf->stream>>>(pf->sc, pf->sc_host_dev);
+    VSMC_CUDA_CHECK_LAUNCH();
+    return VSMC_CUDA_OK;
+}
+
 int vsmc_cuda_pf_get_status(vsmc_cuda_pf *pf, vsmc_cuda_pf_status *out)
 {
     if (pf == nullptr || out == nullptr || pf->precision != 32)
         return VSMC_CUDA_ERR_ARG;
-    // pinned: the copy goes straight into it, without a staging buffer
-    VSMC_CUDA_TRY(cudaMemcpyAsync(pf->sc_host, pf->sc, sizeof(PfScalars),
-        cudaMemcpyDeviceToHost, pf->stream));
+    const int rc = vsmc_cuda_pf_status_enqueue(pf);
+    if (rc != VSMC_CUDA_OK)
+        return rc;
+    return vsmc_cuda_pf_status_read(pf, out);
+}
+
+int vsmc_cuda_pf_status_read(vsmc_cuda_pf *pf, vsmc_cuda_pf_status *out)
+{
+    if (pf == nullptr || out == nullptr || pf->precision != 32)
+        return VSMC_CUDA_ERR_ARG;
     VSMC_CUDA_TRY(cudaStreamSynchronize(pf->stream));
     const PfScalars &sc = *pf->sc_host;
     *out = vsmc_cuda_pf_status{};

@@ -41,6 +41,7 @@ struct vsmc_cuda_pf {
     int *h_res = nullptr;
     vsmc_cuda::PfScalars *sc = nullptr;
     vsmc_cuda::PfScalars *sc_host = nullptr; // pinned copy for status reads
+    vsmc_cuda::PfScalars *sc_host_dev = nullptr; // its mapped device address
 
     // FP32 fused-step workspace
     size_t max_grid = 0; // records in `part`
