@@ -238,7 +238,8 @@ int vsmc_cuda_resample_residual_systematic(size_t m, size_t n,
  * device outputs (either may be NULL); the engine consumes the words the
  * reference's U01SequenceStratified / U01SequenceSystematic would
  * (rng/u01_sequence.hpp:177-259).  Synchronizes the stream.  No reference
- * counterpart for the integer CDF itself (the reference sums doubles). */
+ * counterpart for the integer CDF itself (the reference sums doubles).
+ * A total of 0 or of 2^63 and more returns VSMC_CUDA_ERR_NONFINITE. */
 int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
     vsmc_cuda_rng *rng, int *replication, int *index, void *stream);
 

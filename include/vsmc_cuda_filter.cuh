@@ -81,6 +81,14 @@ struct PfScalars {
     double ess;
     double mean[kMaxMonitorDim]; // monitor: weighted mean after the step
     uint64_t Q;          // fixed-point CDF total of the pending resample
+    uint64_t qrcp;       // floor((2^128 - 1) / (Q << qz)) - 2^64
+    uint64_t qG;         // systematic: ceil(a Q / 2^32) for the shared word a
+    uint64_t qgam;       // systematic: floor(2^64 qG / Q)
+    uint64_t qm;         // floor(2^(64 + qs) n / Q) (when qs > 0)
+    uint64_t qgs;        // floor(2^qs qG / Q)
+    uint32_t qz;         // leading zero bits of Q
+    uint32_t qs;         // fraction bits of the n / Q reciprocal (0: unused)
+    uint32_t done3;      // completion counter of the resampling passes
     uint32_t step;       // next step index t
     int32_t resampled;   // last step resampled: weights equal, lw stale
     int32_t gather;      // state must be read through idx (after a resample)

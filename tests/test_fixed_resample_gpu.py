@@ -117,3 +117,73 @@ def test_fixed_point_resampler_exact(vc, port, scheme, n, kind):
     ctr[1] += carry
     assert [int(v) for v in r.ctr] == ctr
     assert r.index == total % 4 + 1
+
+
+def _integer_weights(kind, n, rng):
+    """Integer CDFs that put many CDF values on or next to a uniform: small
+    totals (every C n / Q a fraction of small denominator), equal and
+    power-of-two weights (C n / Q an integer or a fixed fraction), totals
+    near 2^63, single weights of 2^62 among tiny ones, and long zero runs."""
+    if kind == "tiny":
+        return rng.integers(0, 3, n).astype(np.uint64)
+    if kind == "equal1":
+        return np.ones(n, np.uint64)
+    if kind == "pow2":
+        return np.full(n, 1 << 20, np.uint64)
+    if kind == "near_max":
+        top = (1 << 63) // n - 1
+        return rng.integers(top - 1000, top, n, dtype=np.uint64)
+    if kind == "huge_spike":
+        q = rng.integers(0, 1 << 10, n).astype(np.uint64)
+        q[n // 2] = np.uint64(1 << 62)
+        return q
+    if kind == "sparse":
+        q = np.zeros(n, np.uint64)
+        pos = rng.choice(n, max(1, n // 50), replace=False)
+        q[pos] = rng.integers(1, 1 << 40, len(pos), dtype=np.uint64)
+        return q
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("kind", ["tiny", "equal1", "pow2", "near_max",
+                                  "huge_spike", "sparse"])
+@pytest.mark.parametrize("n", [3, 130, 5000, 70001])
+def test_fixed_point_resampler_boundaries(vc, port, scheme, kind, n):
+    """CDF values on and next to the uniforms' grid: counts still bit-exact
+    against the big-integer definition, and the engine advance unchanged."""
+    import torch
+    rng = np.random.default_rng(7 * n + scheme)
+    q = _integer_weights(kind, n, rng)
+    if int(q.sum()) == 0:
+        q[0] = 1
+    qi = [int(v) for v in q]
+    assert sum(qi) < 1 << 63
+    words = engine_words(port, n)
+    ref = reference_counts(qi, scheme, words)
+    r = vc.rng(vc.PHILOX4X32, key=list(KEY), ctr=list(CTR))
+    rep = torch.zeros(n, dtype=torch.int32, device="cuda")
+    idx = torch.zeros(n, dtype=torch.int32, device="cuda")
+    vc.call("vsmc_cuda_resample_fixed", n, dev(q).data_ptr(), scheme,
+            ctypes.byref(r), rep.data_ptr(), idx.data_ptr(), None)
+    got = host(rep)
+    assert np.array_equal(got, ref), int((got != ref).sum())
+    want_idx = np.zeros(n, np.int32)
+    port.vo_resample_trans_rep_index(n, n, P(ref), P(want_idx))
+    assert np.array_equal(host(idx), want_idx)
+    k = consumed(ref, scheme)
+    total = 4 + k - 1
+    assert r.index == total % 4 + 1
+
+
+def test_fixed_point_resampler_rejects_zero_total(vc):
+    """All-zero integer weights have no CDF: the call reports invalid
+    weights instead of counting."""
+    import torch
+    n = 1000
+    q = torch.zeros(n, dtype=torch.int64, device="cuda")
+    r = vc.rng(vc.PHILOX4X32, key=list(KEY), ctr=list(CTR))
+    rep = torch.zeros(n, dtype=torch.int32, device="cuda")
+    rc = vc.lib().vsmc_cuda_resample_fixed(
+        n, q.data_ptr(), 2, ctypes.byref(r), rep.data_ptr(), None, None)
+    assert rc == vc.ERR_NONFINITE

@@ -752,22 +752,48 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_qsum(const BatchArgs a)
             }
         }
         acc = block_reduce(acc, OpAdd(), uint64_t(0), sh);
-        if (threadIdx.x == 0)
+        // the filter's last chunk to finish (a thread-fenced ticket on
+        // done3; nothing waits) sets the filter's counting constants
+        __shared__ bool last;
+        if (threadIdx.x == 0) {
             a.rs_q[v] = acc;
+            __threadfence();
+            PfScalars &S = a.st[c.f];
+            last = atomicAdd(&S.done3, 1u) == c.nc - 1;
+            if (last) {
+                S.done3 = 0;
+                __threadfence();
+                uint64_t Q = 0;
+                for (uint32_t k = 0; k < c.nc; ++k)
+                    Q += __ldcg(a.rs_q + c.base + k);
+                uint32_t err = 0;
+                cdf_constants(S, Q, c.n, a.scheme == VSMC_CUDA_SYSTEMATIC, err);
+                if (err & ~DEV_ERR_NONFINITE) // a zero total: pass 2 says so
+                    atomicOr(&S.err, err & ~DEV_ERR_NONFINITE);
+            }
+        }
+        __syncthreads(); // sh and last are reused by the next chunk
     }
 }
 
 // pass 2: replication counts from the fixed-point CDF; empty and copy
-// counts per chunk
+// counts per chunk.  Each particle's CDF value is its exact 64-bit prefix
+// sum (the chunk's offset, a block scan per tile) and F(C) comes from the
+// filter's fixed-point reciprocal (cdf_floor), set by the filter's last
+// chunk in pass 1.  A thread's first count needs F just before its first
+// particle: lanes 1..31 take it from the lane before, lane 0 evaluates it.
+// Stratified words come from the tile's block of engine words in shared
+// memory.
+template <bool Sys>
 __global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
 {
     const uint32_t count = __ldcg(a.rs_count + a.rpar);
-    const bool sys = a.scheme == VSMC_CUDA_SYSTEMATIC;
-    __shared__ QR shqr[kPfBlock / 32];
+    constexpr bool sys = Sys; // the scheme (a.scheme) picked the instance
+    __shared__ uint64_t shs[kPfBlock / 32 + 1];
     __shared__ uint32_t she[kPfBlock / 32 + 1];
-    __shared__ QR start0;
     __shared__ uint4 wbuf[2 * kPfBlock];        // stratified words of a tile
     __shared__ uint32_t wsh[2 * (kPfBlock / 32)];
+    const uint32_t lane = threadIdx.x & 31;
     for (uint32_t v = blockIdx.x; v < count; v += gridDim.x) {
         const RsChunk c = rs_chunk_at(a, v);
         PfScalars &S = a.st[c.f];
@@ -778,31 +804,14 @@ __global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
                 atomicOr(&S.err, DEV_ERR_NONFINITE);
             continue;
         }
-        const PfScalars sc = S; // the engine before this resample
+        // the engine before this resample (pass 3 advances it)
+        const PfScalars &sc = S;
         const float M = sc.Mf;
         const uint32_t n = c.n;
         const float *lw = a.lw + c.off;
         int32_t *rep = a.rep + c.off;
-        const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
-        const float invQ = __frcp_rn(__ull2float_rn(Q));
-        uint32_t err = 0;
-        if (threadIdx.x == 0) {
-            // the chunk's first CDF value, offset, by one 128-bit division
-            const uint64_t G = sys ? cp.G : 0;
-            long long j;
-            uint64_t r;
-            QR s;
-            if (cn_divmod(offset, G, cp, j, r, err)) {
-                s.j = static_cast<uint32_t>(j + 1);
-                s.r = r;
-            } else { // offset n < G < Q: X = -(G - offset n)
-                s.j = 0;
-                s.r = Q - (G - offset * static_cast<uint64_t>(n));
-            }
-            start0 = s;
-        }
-        __syncthreads();
-        QR carry = start0;
+        const CdfRcp p = load_cdf_rcp(sc, n);
+        uint64_t carry = offset;
         uint32_t empties = 0, copies = 0;
         // the next tile's log-weights are loaded while this one is counted
         float4 nxt = make_float4(0, 0, 0, 0);
@@ -826,38 +835,60 @@ __global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
                 for (int k = 0; k < 4; ++k)
                     q[k] = i0 + k < c.hi ? fixed_q(lw[i0 + k], M, c.shift) : 0;
             }
-            // positions after each of this thread's particles, from its start
-            QR loc[4];
-            QR acc = {0, 0};
+            uint64_t s[4];
+            s[0] = q[0];
+            s[1] = s[0] + q[1];
+            s[2] = s[1] + q[2];
+            s[3] = s[2] + q[3];
+            uint64_t tile_total;
+            const uint64_t incl =
+                block_inclusive_scan(s[3], OpAdd(), uint64_t(0), shs, &tile_total);
+            const uint64_t cb = carry + (incl - s[3]);
+            uint32_t Fv[4], Fl = 0;
+            if (sys) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                qr_push(acc, q[k], n, false, Q, invQ, cp, err);
-                loc[k] = acc;
-            }
-            QR tile_total;
-            const QR ex = block_exclusive_qr(acc, Q, shqr, &tile_total);
-            const QR st = qr_add(carry, ex, Q);
-            WordBuf wv = {wbuf, 0, 0};
-            if (!sys) {
-                uint32_t wlo, whi;
-                words_span(st, qr_add(st, loc[3], Q), n, sc, wlo, whi);
-                wv = fill_words<kPfBlock>(
-                    sc, wlo, whi, wbuf, 2 * kPfBlock, wsh);
-            }
-            uint32_t Fv[4];
+                for (int k = 0; k < 4; ++k)
+                    Fv[k] = i0 + k + 1 >= n ? n : sys_F(cb + s[k], p);
+                if (lane == 0 && i0 != 0)
+                    Fl = sys_F(cb, p);
+            } else {
+                uint32_t j[4];
+                uint64_t r[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t i = i0 + k;
-                if (i + 1 >= n)
-                    Fv[k] = n; // the last particle takes the rest
-                else if (i < c.hi)
-                    Fv[k] = f_of_buf(qr_add(st, loc[k], Q), sys, n, Q, sc, wv);
-                else
-                    Fv[k] = 0;
+                for (int k = 0; k < 4; ++k)
+                    j[k] = strat_j(cb + s[k], p, r[k]);
+                uint32_t jv = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (j[k] < n)
+                        jv = j[k];
+                const uint32_t wlo = j[0] < n ? sc.rindex + j[0] : 0xFFFFFFFFu;
+                const uint32_t whi = j[0] < n ? sc.rindex + jv : 0u;
+                const WordBuf wv =
+                    fill_words<kPfBlock>(sc, wlo, whi, wbuf, 2 * kPfBlock, wsh);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    Fv[k] = i0 + k + 1 >= n ? n
+                        : (j[k] >= n ? n
+                                     : j[k] + (ceil_aq(buf_word(sc,
+                                                   sc.rindex + j[k], wv), Q) <=
+                                                       r[k]
+                                                   ? 1u
+                                                   : 0u));
+                if (lane == 0 && i0 != 0) {
+                    uint64_t r0;
+                    const uint32_t j0 = strat_j(cb, p, r0);
+                    Fl = j0 >= n ? n
+                        : j0 + (ceil_aq(buf_word(sc, sc.rindex + j0, wv), Q) <=
+                                       r0
+                                   ? 1u
+                                   : 0u);
+                }
             }
-            // F before this thread's first particle is F at its start
-            // position (particle 0 has nothing before it)
-            uint32_t Fprev = i0 == 0 ? 0u : f_of_buf(st, sys, n, Q, sc, wv);
+            // F before this thread's first particle (particle 0 has
+            // nothing before it)
+            const uint32_t Fup = __shfl_up_sync(0xFFFFFFFFu, Fv[3], 1);
+            uint32_t Fprev = lane == 0 ? Fl : Fup;
             int32_t r[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -881,10 +912,8 @@ __global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
                         copies += static_cast<uint32_t>(r[k]);
                     }
             }
-            carry = qr_add(carry, tile_total, Q);
+            carry += tile_total;
         }
-        if (err)
-            atomicOr(&S.err, err);
         empties = block_reduce(empties, OpAdd(), 0u, she);
         copies = block_reduce(copies, OpAdd(), 0u, she);
         if (threadIdx.x == 0) {
@@ -893,6 +922,7 @@ __global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
         }
     }
 }
+
 
 // pass 3: slot assignment.  With c copies and e empty slots before slot i,
 // the first surplus rank of i is c - (i - e); idx[i] = i for a parent,
@@ -1365,7 +1395,10 @@ static int enqueue_run(
         // the filters that resample, in the chunks the step listed
         const dim3 blk(kPfBlock);
         k_brs_qsum<<<b->rs_grid[0], blk, 0, st>>>(a);
-        k_brs_count<<<b->rs_grid[1], blk, 0, st>>>(a);
+        if (a.scheme == VSMC_CUDA_SYSTEMATIC)
+            k_brs_count<true><<<b->rs_grid[1], blk, 0, st>>>(a);
+        else
+            k_brs_count<false><<<b->rs_grid[1], blk, 0, st>>>(a);
         k_brs_assign<<<b->rs_grid[2], blk, 0, st>>>(a);
         VSMC_CUDA_CHECK_LAUNCH();
     }
@@ -1487,7 +1520,8 @@ static int batch_create(vsmc_cuda_batch **out, int kind, size_t nfilters,
     {
         const int sms = num_sms();
         const int occ[kRsKernels] = {occupancy_of(k_brs_qsum, kPfBlock),
-            occupancy_of(k_brs_count, kPfBlock),
+            std::min(occupancy_of(k_brs_count<true>, kPfBlock),
+                occupancy_of(k_brs_count<false>, kPfBlock)),
             occupancy_of(k_brs_assign, kPfBlock)};
         for (int k = 0; k < kRsKernels; ++k)
             b->rs_grid[k] = static_cast<int>(std::min<size_t>(

@@ -533,9 +533,9 @@ static int pf_create(vsmc_cuda_pf **out, size_t n, size_t dim,
             ++lg;
         pf->shift = static_cast<uint32_t>(63 - lg);
         PF_TRY(dalloc(&pf->part, pf->max_grid));
-        PF_TRY(dalloc(&pf->qpart, pf->grid_rs * kRsWarps));
-        PF_TRY(dalloc(&pf->epart, pf->grid_rs));
-        PF_TRY(dalloc(&pf->cpart, pf->grid_rs));
+        PF_TRY(dalloc(&pf->qpart, pf->grid_rs * (kRsWarps + 1)));
+        PF_TRY(dalloc(&pf->epart, pf->grid_rs * (kRsWarps + 1)));
+        PF_TRY(dalloc(&pf->cpart, pf->grid_rs * (kRsWarps + 1)));
         PF_TRY(dalloc(reinterpret_cast<char **>(&pf->state2),
             esz * dim * pf->stride));
         PF_TRY(dalloc(&pf->rep, n + 4));
@@ -755,9 +755,9 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
     r.n = static_cast<uint32_t>(n);
     r.chunk = static_cast<uint32_t>(chunk);
     r.scheme = scheme;
-    r.qpart = scratch.get<uint64_t>(static_cast<size_t>(grid) * kRsWarps);
-    r.epart = scratch.get<uint32_t>(grid);
-    r.cpart = scratch.get<uint32_t>(grid);
+    r.qpart = scratch.get<uint64_t>(static_cast<size_t>(grid) * (kRsWarps + 1));
+    r.epart = scratch.get<uint32_t>(static_cast<size_t>(grid) * (kRsWarps + 1));
+    r.cpart = scratch.get<uint32_t>(static_cast<size_t>(grid) * (kRsWarps + 1));
     r.rep = scratch.get<int32_t>(n + 4);
     r.idx = scratch.get<int32_t>(n + 4);
     r.srcs = scratch.get<uint32_t>(n);
@@ -1104,11 +1104,11 @@ constexpr size_t na_align(size_t b) { return (b + 255) / 256 * 256; }
 constexpr size_t kNaSc = 0;
 constexpr size_t kNaQpart = kNaSc + na_align(sizeof(PfScalars));
 constexpr size_t kNaEpart =
-    kNaQpart + na_align(sizeof(uint64_t) * kNoAllocMaxBlocks * kRsWarps);
+    kNaQpart + na_align(sizeof(uint64_t) * kNoAllocMaxBlocks * (kRsWarps + 1));
 constexpr size_t kNaCpart =
-    kNaEpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
+    kNaEpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks * (kRsWarps + 1));
 constexpr size_t kNaRep =
-    kNaCpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks);
+    kNaCpart + na_align(sizeof(uint32_t) * kNoAllocMaxBlocks * (kRsWarps + 1));
 constexpr size_t kNaIdx = kNaRep + na_align(sizeof(int32_t) * (kNoAllocMaxN + 4));
 constexpr size_t kNaSrcs =
     kNaIdx + na_align(sizeof(int32_t) * (kNoAllocMaxN + 4));

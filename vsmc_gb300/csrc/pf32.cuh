@@ -281,8 +281,114 @@ __device__ __forceinline__ void warp_range(
         whi = hi;
 }
 
-// Sum of q over each warp range (four groups of four per lane in flight):
-// qpart[block * kRsWarps + warp].
+// The block that finishes a resampling pass last (a thread-fenced ticket on
+// sc->done3; nothing waits), in every thread of that block.  Its thread 0
+// resets the ticket for the next pass.
+__device__ __forceinline__ bool rs_last_block(PfScalars *sc)
+{
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        last = atomicAdd(&sc->done3, 1u) == gridDim.x - 1;
+        if (last)
+            sc->done3 = 0;
+    }
+    __syncthreads();
+    if (last)
+        __threadfence();
+    return last;
+}
+
+// Partials of a resampling pass: entry block * kRsWarps + warp for each
+// warp range, then one entry per block from gridDim.x * kRsWarps on.  The
+// last block of the pass turns the block entries into exclusive prefix
+// sums; a range's offset is its block's prefix plus the ranges before it in
+// its block.
+template <typename T>
+__device__ __forceinline__ T *blk_parts(T *v)
+{
+    return v + gridDim.x * kRsWarps;
+}
+
+// Records each warp's value x (the same in every lane) and the block's
+// total.  Called by the whole block; sh holds kRsWarps entries.
+template <typename T>
+__device__ __forceinline__ void put_parts(T *v, T x, T *sh)
+{
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        v[blockIdx.x * kRsWarps + w] = x;
+        sh[w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T t = 0;
+#pragma unroll
+        for (int k = 0; k < kRsWarps; ++k)
+            t += sh[k];
+        blk_parts(v)[blockIdx.x] = t;
+    }
+}
+
+// The offset of the calling warp's range (every lane gets it), once the
+// block entries hold their prefix sums.
+template <typename T>
+__device__ __forceinline__ T range_offset(const T *v)
+{
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    T x = lane < w ? __ldcg(v + blockIdx.x * kRsWarps + lane) : T(0);
+    if (lane == 31)
+        x = __ldcg(v + gridDim.x * kRsWarps + blockIdx.x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
+    return x;
+}
+
+// v[0..m) replaced by its exclusive prefix sums by one block (each thread a
+// contiguous stretch, its loads issued together); returns the total.
+// sh: kPfBlock / 32 + 1 entries.
+template <typename T>
+__device__ __forceinline__ T scan_blocks_in_place(T *v, uint32_t m, T *sh)
+{
+    constexpr uint32_t kK = 4;
+    const uint32_t per = (m + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = min(m, threadIdx.x * per);
+    const uint32_t b1 = min(m, b0 + per);
+    T s = 0;
+    T x[kK];
+    for (uint32_t i = b0; i < b1; i += kK) {
+#pragma unroll
+        for (uint32_t k = 0; k < kK; ++k)
+            x[k] = i + k < b1 ? __ldcg(v + i + k) : T(0);
+#pragma unroll
+        for (uint32_t k = 0; k < kK; ++k)
+            s += x[k];
+    }
+    T tot;
+    T run = block_inclusive_scan(s, OpAdd(), T(0), sh, &tot) - s;
+    if (per <= kK) {
+#pragma unroll
+        for (uint32_t k = 0; k < kK; ++k)
+            if (b0 + k < b1) {
+                v[b0 + k] = run;
+                run += x[k];
+            }
+    } else {
+        for (uint32_t i = b0; i < b1; ++i) {
+            const T y = __ldcg(v + i);
+            v[i] = run;
+            run += y;
+        }
+    }
+    return tot;
+}
+
+// Sum of q over each warp range (four groups of four per lane in flight)
+// and over each block, into qpart.  The last block to finish turns the
+// block sums into prefix sums and sets the event's CDF constants: the total
+// Q and the reciprocal terms.
 __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
 {
     if (!(a.force || a.sc->resampled))
@@ -302,18 +408,35 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
     warp_range(lo, hi, a.chunk, w, wlo, whi);
     uint64_t acc = 0;
     constexpr int kG = 4;
-    for (uint32_t base = wlo; base < whi; base += kG * 128) {
-        if (a.q == nullptr && base + kG * 128 <= whi) {
-            float4 v[kG];
+    constexpr uint32_t kSpan = kG * 128;
+    // the next group's loads are issued before this group's weights
+    const bool direct = a.q == nullptr;
+    float4 v[kG], nv[kG];
+    if (direct && wlo + kSpan <= whi) {
 #pragma unroll
-            for (int h = 0; h < kG; ++h)
-                v[h] = __ldcg(reinterpret_cast<const float4 *>(
-                    a.lw + base + h * 128 + lane * 4));
+        for (int h = 0; h < kG; ++h)
+            v[h] = __ldcg(reinterpret_cast<const float4 *>(
+                a.lw + wlo + h * 128 + lane * 4));
+    }
+    for (uint32_t base = wlo; base < whi; base += kSpan) {
+        if (direct && base + kSpan <= whi) {
+            const bool more = base + 2 * kSpan <= whi;
+            if (more) {
+#pragma unroll
+                for (int h = 0; h < kG; ++h)
+                    nv[h] = __ldcg(reinterpret_cast<const float4 *>(
+                        a.lw + base + kSpan + h * 128 + lane * 4));
+            }
 #pragma unroll
             for (int h = 0; h < kG; ++h)
                 acc += fixed_q(v[h].x, M, a.shift) +
                     fixed_q(v[h].y, M, a.shift) +
                     fixed_q(v[h].z, M, a.shift) + fixed_q(v[h].w, M, a.shift);
+            if (more) {
+#pragma unroll
+                for (int h = 0; h < kG; ++h)
+                    v[h] = nv[h];
+            }
         } else {
             for (int h = 0; h < kG; ++h) {
                 const uint32_t i0 = base + h * 128 + lane * 4;
@@ -325,28 +448,54 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
         acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-    if (lane == 0)
-        a.qpart[blockIdx.x * kRsWarps + w] = acc;
-}
-
-// sum of part[0..upto) and of part[0..total) over the block
-template <typename T>
-__device__ __forceinline__ void block_prefix_of_parts(
-    const T *part, uint32_t upto, uint32_t total, T &prefix, T &all, T *sh)
-{
-    T p = 0, q = 0;
-    for (uint32_t b = threadIdx.x; b < total; b += blockDim.x) {
-        const T v = part[b];
-        q += v;
-        if (b < upto)
-            p += v;
+    __shared__ uint64_t shs[kPfBlock / 32 + 1];
+    put_parts(a.qpart, acc, shs);
+    if (!rs_last_block(a.sc))
+        return;
+    const uint64_t Q = scan_blocks_in_place(blk_parts(a.qpart), gridDim.x, shs);
+    if (threadIdx.x == 0) {
+        uint32_t err = 0;
+        cdf_constants(*a.sc, Q, a.n, a.scheme == VSMC_CUDA_SYSTEMATIC, err);
+        if (err)
+            a.sc->err |= err;
     }
-    prefix = block_reduce(p, OpAdd(), T(0), sh);
-    all = block_reduce(q, OpAdd(), T(0), sh);
 }
 
-// Replication counts from the fixed-point CDF; per-block empty and copy
-// counts.
+// End of a counting pass: each warp's empty and copy counts (the same in
+// every lane) go to epart / cpart with the block totals; the last block
+// turns the block totals into prefix sums (with the ranges' own entries,
+// the offsets the assign pass starts each range from) and records the
+// totals.
+__device__ __forceinline__ void count_finish(
+    const Rs32Args &a, uint32_t empties, uint32_t copies)
+{
+    __shared__ uint32_t sh[kPfBlock / 32 + 1];
+    __shared__ uint32_t sh2[kRsWarps];
+    put_parts(a.epart, empties, sh);
+    put_parts(a.cpart, copies, sh2);
+    if (!rs_last_block(a.sc))
+        return;
+    const uint32_t et = scan_blocks_in_place(blk_parts(a.epart), gridDim.x, sh);
+    const uint32_t ct = scan_blocks_in_place(blk_parts(a.cpart), gridDim.x, sh);
+    if (threadIdx.x == 0) {
+        a.sc->nempty = et;
+        if (ct != a.n)
+            a.sc->err |= DEV_ERR_INTERNAL;
+    }
+}
+
+// Replication counts, one warp per warp range, no block barrier.  Particle
+// i's count is F(C_i) - F(C_{i-1}) for the CDF C_i: exact 64-bit prefix sums
+// (the range's offset from qsum, a warp scan per group of 128 particles).
+// F(C), the uniforms at or below C / Q, comes from the fixed-point
+// reciprocal of Q (cdf_floor): no division and no position carried from
+// particle to particle.  Stratified also reads each particle's word a_{j*}:
+// a group's j* are nondecreasing, so the warp generates the Philox blocks
+// holding them once into its shared-memory row (a word past the row is
+// generated where it is needed).  Per-range empty and copy counts go to
+// epart / cpart.
+constexpr uint32_t kStratRow = 64; // Philox blocks per warp row (256 words)
+
 template <bool Sys>
 __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
 {
@@ -355,200 +504,28 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
     const float M = static_cast<float>(a.sc->M);
     uint32_t lo, hi;
     chunk_range(a.n, a.chunk, lo, hi);
-    __shared__ uint64_t shq[kPfBlock / 32 + 1];
-    __shared__ QR shqr[kPfBlock / 32];
-    __shared__ uint32_t she[kPfBlock / 32 + 1];
-    __shared__ QR start0;
-    __shared__ uint4 wbuf[2 * kPfBlock];        // stratified words of a tile
-    __shared__ uint32_t wsh[2 * (kPfBlock / 32)];
-    uint64_t offset, Q;
-    block_prefix_of_parts(a.qpart, blockIdx.x * kRsWarps,
-        gridDim.x * kRsWarps, offset, Q, shq);
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        a.sc->Q = Q;
-    const PfScalars sc = *a.sc;
-    constexpr bool sys = Sys; // the scheme (a.scheme) picked the instance
-    const bool checked = a.q != nullptr;
-    const uint32_t n = a.n;
-    const CountP cp = make_count_params(Q, n, engine_word(sc, 0));
-    const float invQ = __frcp_rn(__ull2float_rn(Q));
-    uint32_t err = 0;
-    if (threadIdx.x == 0) {
-        // the block's first CDF value, offset, by one 128-bit division
-        const uint64_t G = sys ? cp.G : 0;
-        long long j;
-        uint64_t r;
-        QR s;
-        if (cn_divmod(offset, G, cp, j, r, err)) {
-            s.j = static_cast<uint32_t>(j + 1);
-            s.r = r;
-        } else { // offset n < G < Q: X = -(G - offset n)
-            s.j = 0;
-            s.r = Q - (G - offset * static_cast<uint64_t>(n));
-        }
-        start0 = s;
-    }
-    __syncthreads();
-    QR carry = start0;
-    uint32_t empties = 0, copies = 0;
-    // the next tile's log-weights are loaded while this one is counted
-    float4 nxt = make_float4(0, 0, 0, 0);
-    if (!checked && lo + threadIdx.x * 4 + 3 < hi)
-        nxt = __ldcg(reinterpret_cast<const float4 *>(
-            a.lw + lo + threadIdx.x * 4));
-    for (uint32_t base = lo; base < hi; base += kPfTile) {
-        const uint32_t i0 = base + threadIdx.x * 4;
-        const float4 v = nxt;
-        if (!checked && i0 + kPfTile + 3 < hi)
-            nxt = __ldcg(reinterpret_cast<const float4 *>(a.lw + i0 + kPfTile));
-        uint64_t q[4];
-        if (i0 + 3 < hi && !checked) {
-            q[0] = fixed_q(v.x, M, a.shift);
-            q[1] = fixed_q(v.y, M, a.shift);
-            q[2] = fixed_q(v.z, M, a.shift);
-            q[3] = fixed_q(v.w, M, a.shift);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                q[k] = (i0 + k < hi) ? q_at(a, i0 + k, M) : 0;
-        }
-        // positions after each of this thread's particles, from its start
-        QR loc[4];
-        QR acc = {0, 0};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            qr_push(acc, q[k], n, checked, Q, invQ, cp, err);
-            loc[k] = acc;
-        }
-        QR tile_total;
-        const QR ex = block_exclusive_qr(acc, Q, shqr, &tile_total);
-        const QR st = qr_add(carry, ex, Q);
-        WordBuf wv = {wbuf, 0, 0};
-        if (!sys) {
-            uint32_t wlo, whi;
-            words_span(st, qr_add(st, loc[3], Q), n, sc, wlo, whi);
-            wv = fill_words<kPfBlock>(sc, wlo, whi, wbuf, 2 * kPfBlock, wsh);
-        }
-        uint32_t F[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = i0 + k;
-            if (i + 1 >= n)
-                F[k] = n; // the last particle takes the rest
-            else if (i < hi)
-                F[k] = f_of_buf(qr_add(st, loc[k], Q), sys, n, Q, sc, wv);
-            else
-                F[k] = 0;
-        }
-        // F before this thread's first particle is F at the thread's start
-        // position (particle 0 has nothing before it)
-        uint32_t Fprev = i0 == 0 ? 0u : f_of_buf(st, sys, n, Q, sc, wv);
-        int32_t r[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            r[k] = static_cast<int32_t>(F[k] - Fprev);
-            Fprev = F[k];
-        }
-        if (i0 + 3 < hi) {
-            *reinterpret_cast<int4 *>(a.rep + i0) = make_int4(r[0], r[1], r[2], r[3]);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                empties += r[k] == 0 ? 1u : 0u;
-                copies += static_cast<uint32_t>(r[k]);
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (i0 + k < hi) {
-                    a.rep[i0 + k] = r[k];
-                    empties += r[k] == 0 ? 1u : 0u;
-                    copies += static_cast<uint32_t>(r[k]);
-                }
-        }
-        carry = qr_add(carry, tile_total, Q);
-    }
-    if (err)
-        atomicOr(&a.sc->err, err);
-    empties = block_reduce(empties, OpAdd(), 0u, she);
-    copies = block_reduce(copies, OpAdd(), 0u, she);
-    if (threadIdx.x == 0) {
-        a.epart[blockIdx.x] = empties;
-        a.cpart[blockIdx.x] = copies;
-    }
-}
-
-// Warp-wide exclusive scan of positions; *total gets the warp's sum.
-__device__ __forceinline__ QR warp_exclusive_qr(QR v, uint64_t Q, QR *total)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    QR x = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        QR o;
-        o.j = __shfl_up_sync(0xFFFFFFFFu, x.j, d);
-        o.r = __shfl_up_sync(0xFFFFFFFFu, x.r, d);
-        if (lane >= static_cast<uint32_t>(d))
-            x = qr_add(o, x, Q);
-    }
-    total->j = __shfl_sync(0xFFFFFFFFu, x.j, 31);
-    total->r = __shfl_sync(0xFFFFFFFFu, x.r, 31);
-    QR ex;
-    ex.j = __shfl_up_sync(0xFFFFFFFFu, x.j, 1);
-    ex.r = __shfl_up_sync(0xFFFFFFFFu, x.r, 1);
-    if (lane == 0)
-        ex = QR{0, 0};
-    return ex;
-}
-
-// Systematic counts, one warp per warp range: the range's first CDF
-// position comes from the per-range q sums (one 128-bit division by the
-// range's lane 0), then the warp walks its range 128 particles at a time
-// with warp scans of the positions and no block barrier.  The counts are
-// the same integers as k_rs32_count<true> gives.
-__global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count_sys(const Rs32Args a)
-{
-    if (!a.sc->resampled)
-        return;
-    const float M = static_cast<float>(a.sc->M);
-    uint32_t lo, hi;
-    chunk_range(a.n, a.chunk, lo, hi);
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __shared__ uint64_t shq[kPfBlock / 32 + 1];
-    __shared__ uint32_t she[kPfBlock / 32 + 1];
-    // offset of the block (every earlier range) and of this warp's range
-    uint64_t boff, Q;
-    block_prefix_of_parts(a.qpart, blockIdx.x * kRsWarps,
-        gridDim.x * kRsWarps, boff, Q, shq);
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        a.sc->Q = Q;
-    uint64_t woff =
-        lane < w ? a.qpart[blockIdx.x * kRsWarps + lane] : uint64_t(0);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        woff += __shfl_xor_sync(0xFFFFFFFFu, woff, o);
-    woff += boff;
+    const CdfRcp p = load_cdf_rcp(*a.sc, a.n);
+    EnginePos e = {};
+    if (!Sys)
+        e = engine_pos(*a.sc);
+    __shared__ uint4 rows[Sys ? 1 : kRsWarps][Sys ? 1 : kStratRow];
+    uint4 *row = rows[Sys ? 0 : w];
     uint32_t wlo, whi;
     warp_range(lo, hi, a.chunk, w, wlo, whi);
     const bool checked = a.q != nullptr;
     const uint32_t n = a.n;
-    const CountP cp = make_count_params(Q, n, engine_word(*a.sc, 0));
-    const float invQ = __frcp_rn(__ull2float_rn(Q));
-    uint32_t err = 0;
-    // the range's first CDF position (lane 0), broadcast
-    QR carry = {0, 0};
-    if (lane == 0 && wlo < whi) {
-        long long j;
-        uint64_t r;
-        if (cn_divmod(woff, cp.G, cp, j, r, err)) {
-            carry.j = static_cast<uint32_t>(j + 1);
-            carry.r = r;
-        } else { // woff n < G < Q: X = -(G - woff n)
-            carry.j = 0;
-            carry.r = Q - (cp.G - woff * static_cast<uint64_t>(n));
+    uint64_t carry = range_offset(a.qpart); // the CDF before the range
+    uint32_t Fprev = 0;
+    if (wlo != 0 && wlo < whi) {
+        if (Sys) {
+            Fprev = sys_F(carry, p);
+        } else {
+            uint64_t r;
+            const uint32_t j = strat_j(carry, p, r);
+            Fprev = strat_F(j, r, p, e, row, 0, 0);
         }
     }
-    carry.j = __shfl_sync(0xFFFFFFFFu, carry.j, 0);
-    carry.r = __shfl_sync(0xFFFFFFFFu, carry.r, 0);
     uint32_t empties = 0, copies = 0;
     float4 nxt = make_float4(0, 0, 0, 0);
     if (!checked && wlo + lane * 4 + 3 < whi)
@@ -569,35 +546,59 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count_sys(const Rs32Args a
             for (int k = 0; k < 4; ++k)
                 q[k] = (i0 + k < whi) ? q_at(a, i0 + k, M) : 0;
         }
-        QR loc[4];
-        QR acc = {0, 0};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            qr_push(acc, q[k], n, checked, Q, invQ, cp, err);
-            loc[k] = acc;
-        }
-        QR total;
-        const QR ex = warp_exclusive_qr(acc, Q, &total);
-        const QR st = qr_add(carry, ex, Q);
+        uint64_t s[4];
+        s[0] = q[0];
+        s[1] = s[0] + q[1];
+        s[2] = s[1] + q[2];
+        s[3] = s[2] + q[3];
+        const uint64_t incl = warp_inclusive_scan(s[3], OpAdd());
+        const uint64_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const uint64_t cb = carry + (incl - s[3]);
         uint32_t F[4];
+        if (Sys) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = i0 + k;
-            if (i + 1 >= n) {
-                F[k] = n; // the last particle takes the rest
-            } else if (i < whi) {
-                const QR x = qr_add(st, loc[k], Q);
-                F[k] = x.j < n ? x.j : n;
-            } else {
-                F[k] = 0;
+            for (int k = 0; k < 4; ++k)
+                F[k] = i0 + k + 1 >= n ? n : sys_F(cb + s[k], p);
+        } else {
+            uint32_t j[4];
+            uint64_t r[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                j[k] = strat_j(cb + s[k], p, r[k]);
+            // the group's words: j[0] of lane 0 .. j[3] of lane 31 (j = n
+            // needs none)
+            uint32_t jv = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (j[k] < n)
+                    jv = j[k];
+            const uint32_t jl = __reduce_min_sync(0xFFFFFFFFu, j[0]);
+            const uint32_t jh = __reduce_max_sync(0xFFFFFFFFu, jv);
+            uint32_t b0 = 0, nb = 0;
+            if (jl < n) {
+                b0 = (e.index + jl) >> 2;
+                const uint32_t bl = (e.index + (jh > jl ? jh : jl)) >> 2;
+                nb = bl - b0 + 1;
+                if (nb > kStratRow)
+                    nb = kStratRow;
             }
+            __syncwarp();
+            for (uint32_t d = lane; d < nb; d += 32)
+                row[d] = engine_block(e, b0 + d);
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                F[k] = i0 + k + 1 >= n ? n
+                                       : strat_F(j[k], r[k], p, e, row, b0, nb);
         }
-        uint32_t Fprev = i0 == 0 ? 0u : (st.j < n ? st.j : n);
+        uint32_t Fl = __shfl_up_sync(0xFFFFFFFFu, F[3], 1);
+        if (lane == 0)
+            Fl = Fprev;
         int32_t r[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            r[k] = static_cast<int32_t>(F[k] - Fprev);
-            Fprev = F[k];
+            r[k] = static_cast<int32_t>(F[k] - Fl);
+            Fl = F[k];
         }
         if (i0 + 3 < whi) {
             *reinterpret_cast<int4 *>(a.rep + i0) =
@@ -616,33 +617,36 @@ __global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count_sys(const Rs32Args a
                     copies += static_cast<uint32_t>(r[k]);
                 }
         }
-        carry = qr_add(carry, total, Q);
+        carry += tot;
+        Fprev = __shfl_sync(0xFFFFFFFFu, F[3], 31);
     }
-    if (err)
-        atomicOr(&a.sc->err, err);
-    empties = block_reduce(empties, OpAdd(), 0u, she);
-    copies = block_reduce(copies, OpAdd(), 0u, she);
-    if (threadIdx.x == 0) {
-        a.epart[blockIdx.x] = empties;
-        a.cpart[blockIdx.x] = copies;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        empties += __shfl_xor_sync(0xFFFFFFFFu, empties, o);
+        copies += __shfl_xor_sync(0xFFFFFFFFu, copies, o);
     }
+    count_finish(a, empties, copies);
 }
 
 // the counting kernel of the scheme (systematic or stratified)
 inline void launch_rs32_count(int grid, cudaStream_t st, const Rs32Args &a)
 {
     if (a.scheme == VSMC_CUDA_SYSTEMATIC)
-        k_rs32_count_sys<<<grid, kPfBlock, 0, st>>>(a);
+        k_rs32_count<true><<<grid, kPfBlock, 0, st>>>(a);
     else
         k_rs32_count<false><<<grid, kPfBlock, 0, st>>>(a);
 }
 
-// Slot assignment.  With c = copies before slot i and e = empty slots before
-// i, the first surplus rank of i is c - (i - e) (every non-empty slot before
-// i keeps one of its copies).  idx[i] = i for a parent (it keeps its slot),
-// idx[i] = -(e + 1) for the e-th empty slot, and srcs[first surplus rank ..
-// + r - 1) = i for a parent with r >= 2 copies: the reference's layout
-// (resample/transform.hpp:116-133) in one pass over the counts.
+// Slot assignment, one warp per warp range (no block barrier).  With
+// c = copies before slot i and e = empty slots before i, the first surplus
+// rank of i is c - (i - e) (every non-empty slot before i keeps one of its
+// copies).  idx[i] = i for a parent (it keeps its slot), idx[i] = -(e + 1)
+// for the e-th empty slot, and srcs[first surplus rank .. + r - 1) = i for a
+// parent with r >= 2 copies: the reference's layout
+// (resample/transform.hpp:116-133) in one pass over the counts.  Each range
+// starts from its offsets (c, e) that the counting pass left in cpart /
+// epart, and a warp scan of (copies, empties) carries them through its
+// 128-particle groups.
 template <bool Mon>
 __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
 {
@@ -650,17 +654,11 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
         return;
     uint32_t lo, hi;
     chunk_range(a.n, a.chunk, lo, hi);
-    __shared__ uint32_t sh32[kPfBlock / 32 + 1];
-    __shared__ uint64_t sh64[kPfBlock / 32 + 1];
-    uint32_t eoff, etotal, coff, ctotal;
-    block_prefix_of_parts(a.epart, blockIdx.x, gridDim.x, eoff, etotal, sh32);
-    block_prefix_of_parts(a.cpart, blockIdx.x, gridDim.x, coff, ctotal, sh32);
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t etotal = a.sc->nempty;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         PfScalars &sc = *a.sc;
-        sc.nempty = etotal;
         sc.gather = 1;
-        if (ctotal != a.n)
-            sc.err |= DEV_ERR_INTERNAL;
         // words the scheme consumed: U01SequenceSystematic draws once in its
         // constructor; U01SequenceStratified draws lazily up to the first
         // uniform above the second-to-last cumulative weight
@@ -672,32 +670,33 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
             engine_advance(sc, jf < a.n ? jf + 1 : a.n);
         }
     }
+    uint32_t wlo, whi;
+    warp_range(lo, hi, a.chunk, w, wlo, whi);
+    uint32_t coff = range_offset(a.cpart), eoff = range_offset(a.epart);
     // monitor of the resampled particles, sum_i rep_i x_{d,i}, when the
     // host asks for it right after resampling (mon_dim > 0); the rows, like
-    // the counts, are loaded one tile ahead
+    // the counts, are loaded one group ahead
     const uint32_t md = Mon ? a.mon_dim : 0u;
     float macc[kMaxMonitorDim] = {};
     float4 mrow[kMaxMonitorDim], mnxt[kMaxMonitorDim];
 #pragma unroll
     for (int d = 0; d < kMaxMonitorDim; ++d)
         mnxt[d] = static_cast<uint32_t>(d) < md
-            ? load_row4(a.mon_state + d * a.stride, lo + threadIdx.x * 4, hi)
+            ? load_row4(a.mon_state + d * a.stride, wlo + lane * 4, whi)
             : make_float4(0, 0, 0, 0);
     uint32_t err = 0;
     __shared__ __align__(16) uint32_t shm[kPfBlock / 32][kRunChunk];
-    // the next tile's counts are loaded while this one is scanned
-    int4 nxt = load_rep4(a.rep, lo + threadIdx.x * 4, hi);
-    for (uint32_t base = lo; base < hi; base += kPfTile) {
-        const uint32_t i0 = base + threadIdx.x * 4;
+    int4 nxt = load_rep4(a.rep, wlo + lane * 4, whi);
+    for (uint32_t base = wlo; base < whi; base += 128) {
+        const uint32_t i0 = base + lane * 4;
         const int4 cur = nxt;
-        if (base + kPfTile < hi)
-            nxt = load_rep4(a.rep, i0 + kPfTile, hi);
+        if (base + 128 < whi)
+            nxt = load_rep4(a.rep, i0 + 128, whi);
 #pragma unroll
         for (int d = 0; d < kMaxMonitorDim; ++d) {
             mrow[d] = mnxt[d];
-            if (static_cast<uint32_t>(d) < md && base + kPfTile < hi)
-                mnxt[d] = load_row4(a.mon_state + d * a.stride,
-                    i0 + kPfTile, hi);
+            if (static_cast<uint32_t>(d) < md && base + 128 < whi)
+                mnxt[d] = load_row4(a.mon_state + d * a.stride, i0 + 128, whi);
         }
         const int32_t r[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
@@ -715,13 +714,29 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
                 tr += static_cast<uint32_t>(r[k]);
                 te += r[k] == 0 ? 1u : 0u;
             }
-        const uint64_t v = (static_cast<uint64_t>(tr) << 32) | te;
-        uint64_t tot;
-        const uint64_t incl =
-            block_inclusive_scan(v, OpAdd(), uint64_t(0), sh64, &tot);
-        const uint64_t ex = incl - v;
-        uint32_t c = coff + static_cast<uint32_t>(ex >> 32);
-        uint32_t e = eoff + static_cast<uint32_t>(ex & 0xFFFFFFFFu);
+        // (copies, empties) before each lane: one 32-bit scan of
+        // copies * 256 + empties (a group has at most 128 empties) unless a
+        // lane has 2^16 or more copies
+        uint32_t c, e, tc, tn;
+        if (__any_sync(0xFFFFFFFFu, tr >= (1u << 16))) {
+            const uint64_t v = (static_cast<uint64_t>(tr) << 32) | te;
+            const uint64_t incl = warp_inclusive_scan(v, OpAdd());
+            const uint64_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            const uint64_t ex = incl - v;
+            c = coff + static_cast<uint32_t>(ex >> 32);
+            e = eoff + static_cast<uint32_t>(ex & 0xFFFFFFFFu);
+            tc = static_cast<uint32_t>(tot >> 32);
+            tn = static_cast<uint32_t>(tot & 0xFFFFFFFFu);
+        } else {
+            const uint32_t v = (tr << 8) | te;
+            const uint32_t incl = warp_inclusive_scan(v, OpAdd());
+            const uint32_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            const uint32_t ex = incl - v;
+            c = coff + (ex >> 8);
+            e = eoff + (ex & 0xFFu);
+            tc = tot >> 8;
+            tn = tot & 0xFFu;
+        }
         const uint32_t c0 = c, e0 = e;
         int32_t out[4];
         uint32_t rs[4], rl[4];
@@ -743,24 +758,22 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
             if (r[k] > 0)
                 c += static_cast<uint32_t>(r[k]);
         }
-        // the warp's surplus ranks: copies minus kept slots before its first
-        // particle, and the sum of its runs
+        // the group's surplus ranks: copies minus kept slots before its
+        // first particle, and the sum of its runs
         {
             const uint32_t first = c0 - (i0 - e0);
             const uint32_t W0 = __shfl_sync(0xFFFFFFFFu, first, 0);
-            uint32_t Sw = rl[0] + rl[1] + rl[2] + rl[3];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                Sw += __shfl_xor_sync(0xFFFFFFFFu, Sw, o);
+            const uint32_t Sw =
+                __reduce_add_sync(0xFFFFFFFFu, rl[0] + rl[1] + rl[2] + rl[3]);
             if (Sw != 0) {
-                if (Sw > etotal || W0 > etotal - Sw)
+                if (Sw > etotal || W0 > etotal - Sw) {
                     err |= DEV_ERR_INTERNAL; // ranks past the empty slots
-                else
-                    write_surplus_runs(a.srcs, rs, rl, i0, W0, Sw,
-                        shm[threadIdx.x >> 5], err);
+                } else {
+                    write_surplus_runs(a.srcs, rs, rl, i0, W0, Sw, shm[w], err);
+                }
             }
         }
-        if (i0 + 3 < hi) {
+        if (i0 + 3 < whi) {
             *reinterpret_cast<int4 *>(a.idx + i0) =
                 make_int4(out[0], out[1], out[2], out[3]);
         } else {
@@ -769,8 +782,8 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
                 if (r[k] >= 0)
                     a.idx[i0 + k] = out[k];
         }
-        coff += static_cast<uint32_t>(tot >> 32);
-        eoff += static_cast<uint32_t>(tot & 0xFFFFFFFFu);
+        coff += tc;
+        eoff += tn;
     }
     if (err)
         atomicOr(&a.sc->err, err);

@@ -16,9 +16,12 @@ struct Rs32Args {
     uint32_t chunk;  // particles per block (multiple of kPfTile)
     int scheme;      // VSMC_CUDA_STRATIFIED or VSMC_CUDA_SYSTEMATIC
     int force;       // resample whatever the step decided (host decision)
-    uint64_t *qpart; // per-(block, warp range) sum of q
-    uint32_t *epart; // per-block empty count
-    uint32_t *cpart; // per-block copy count (sum of rep)
+    // per warp range (block * kRsWarps + warp): the range's sum of q, its
+    // empty slots and its copies (sum of rep), each turned into exclusive
+    // prefix sums by the last block of the pass that wrote it
+    uint64_t *qpart;
+    uint32_t *epart;
+    uint32_t *cpart;
     int32_t *rep;
     int32_t *idx;      // per slot: itself (>= 0) or -(empty rank + 1)
     uint32_t *srcs;    // N entries: source of the k-th empty slot
