@@ -523,7 +523,7 @@ static int pf_create(vsmc_cuda_pf **out, size_t n, size_t dim,
         }
         const size_t sms = static_cast<size_t>(num_sms());
         pf->max_grid = sms * 16;
-        size_t grs = sms * 4;
+        size_t grs = sms * kRsBlocksPerSm;
         size_t chunk = (n + grs - 1) / grs;
         chunk = (chunk + kPfTile - 1) / kPfTile * kPfTile;
         pf->chunk_rs = static_cast<uint32_t>(chunk);
@@ -746,7 +746,7 @@ int vsmc_cuda_resample_fixed(size_t n, const uint64_t *q, int scheme,
         return VSMC_CUDA_ERR_SIZE;
     cudaStream_t st = as_stream(stream);
     Scratch scratch(st);
-    const size_t grs0 = static_cast<size_t>(num_sms()) * 4;
+    const size_t grs0 = static_cast<size_t>(num_sms()) * kRsBlocksPerSm;
     size_t chunk = (n + grs0 - 1) / grs0;
     chunk = (chunk + kPfTile - 1) / kPfTile * kPfTile;
     const int grid = static_cast<int>((n + chunk - 1) / chunk);
@@ -1159,7 +1159,7 @@ extern "C" int vsmc_cuda_resample_fixed_noalloc(size_t n, const uint64_t *q,
     if (rc != VSMC_CUDA_OK)
         return rc;
     cudaStream_t st = as_stream(stream);
-    const size_t grs0 = static_cast<size_t>(num_sms()) * 4;
+    const size_t grs0 = static_cast<size_t>(num_sms()) * kRsBlocksPerSm;
     size_t chunk = (n + grs0 - 1) / grs0;
     chunk = (chunk + kPfTile - 1) / kPfTile * kPfTile;
     const size_t grid = (n + chunk - 1) / chunk;

@@ -263,6 +263,10 @@ __device__ __forceinline__ uint64_t q_at(
     return a.q ? a.q[i] : fixed_q(a.lw[i], M, a.shift);
 }
 
+// Resident blocks per SM of the resampling passes (their grid is SMs times
+// this; 64 registers a thread).
+constexpr int kRsBlocksPerSm = 4;
+
 // Each block's chunk is split into kRsWarps equal warp ranges (the chunk
 // is a multiple of kPfTile, so a range is a multiple of 128 particles); the
 // passes address a range by (block, warp).
@@ -385,11 +389,28 @@ __device__ __forceinline__ T scan_blocks_in_place(T *v, uint32_t m, T *sh)
     return tot;
 }
 
+// log-weights i..i+3 (i a multiple of 4) below hi, -inf past it
+__device__ __forceinline__ float4 load_lw4(
+    const float *lw, uint32_t i, uint32_t hi)
+{
+    if (i + 3 < hi)
+        return __ldcg(reinterpret_cast<const float4 *>(lw + i));
+    float4 v = make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY);
+    if (i < hi)
+        v.x = lw[i];
+    if (i + 1 < hi)
+        v.y = lw[i + 1];
+    if (i + 2 < hi)
+        v.z = lw[i + 2];
+    return v;
+}
+
 // Sum of q over each warp range (four groups of four per lane in flight)
 // and over each block, into qpart.  The last block to finish turns the
 // block sums into prefix sums and sets the event's CDF constants: the total
 // Q and the reciprocal terms.
-__global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
+__global__ void __launch_bounds__(kPfBlock, kRsBlocksPerSm) k_rs32_qsum(
+    const Rs32Args a)
 {
     if (!(a.force || a.sc->resampled))
         return;
@@ -409,41 +430,34 @@ __global__ void __launch_bounds__(kPfBlock) k_rs32_qsum(const Rs32Args a)
     uint64_t acc = 0;
     constexpr int kG = 4;
     constexpr uint32_t kSpan = kG * 128;
-    // the next group's loads are issued before this group's weights
-    const bool direct = a.q == nullptr;
-    float4 v[kG], nv[kG];
-    if (direct && wlo + kSpan <= whi) {
+    if (a.q == nullptr) {
+        // groups of kG float4 per lane; the next group's loads are issued
+        // before this group's weights, and a float4 past the range reads as
+        // -inf (weight 0), so the range's last group needs no other path
+        float4 v[kG], nv[kG];
 #pragma unroll
         for (int h = 0; h < kG; ++h)
-            v[h] = __ldcg(reinterpret_cast<const float4 *>(
-                a.lw + wlo + h * 128 + lane * 4));
-    }
-    for (uint32_t base = wlo; base < whi; base += kSpan) {
-        if (direct && base + kSpan <= whi) {
-            const bool more = base + 2 * kSpan <= whi;
-            if (more) {
+            v[h] = load_lw4(a.lw, wlo + h * 128 + lane * 4, whi);
+        for (uint32_t base = wlo; base < whi; base += kSpan) {
 #pragma unroll
-                for (int h = 0; h < kG; ++h)
-                    nv[h] = __ldcg(reinterpret_cast<const float4 *>(
-                        a.lw + base + kSpan + h * 128 + lane * 4));
-            }
+            for (int h = 0; h < kG; ++h)
+                nv[h] = load_lw4(a.lw, base + kSpan + h * 128 + lane * 4, whi);
 #pragma unroll
             for (int h = 0; h < kG; ++h)
                 acc += fixed_q(v[h].x, M, a.shift) +
                     fixed_q(v[h].y, M, a.shift) +
                     fixed_q(v[h].z, M, a.shift) + fixed_q(v[h].w, M, a.shift);
-            if (more) {
 #pragma unroll
-                for (int h = 0; h < kG; ++h)
-                    v[h] = nv[h];
-            }
-        } else {
+            for (int h = 0; h < kG; ++h)
+                v[h] = nv[h];
+        }
+    } else {
+        for (uint32_t base = wlo; base < whi; base += kSpan)
             for (int h = 0; h < kG; ++h) {
                 const uint32_t i0 = base + h * 128 + lane * 4;
                 for (uint32_t i = i0; i < whi && i < i0 + 4; ++i)
-                    acc += q_at(a, i, M);
+                    acc += a.q[i];
             }
-        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
@@ -497,7 +511,8 @@ __device__ __forceinline__ void count_finish(
 constexpr uint32_t kStratRow = 64; // Philox blocks per warp row (256 words)
 
 template <bool Sys>
-__global__ void __launch_bounds__(kPfBlock, 4) k_rs32_count(const Rs32Args a)
+__global__ void __launch_bounds__(kPfBlock, kRsBlocksPerSm) k_rs32_count(
+    const Rs32Args a)
 {
     if (!a.sc->resampled)
         return;
@@ -648,7 +663,8 @@ inline void launch_rs32_count(int grid, cudaStream_t st, const Rs32Args &a)
 // epart, and a warp scan of (copies, empties) carries them through its
 // 128-particle groups.
 template <bool Mon>
-__global__ void __launch_bounds__(kPfBlock) k_rs32_assign(const Rs32Args a)
+__global__ void __launch_bounds__(kPfBlock, kRsBlocksPerSm) k_rs32_assign(
+    const Rs32Args a)
 {
     if (!a.sc->resampled)
         return;

@@ -95,32 +95,14 @@ __device__ __forceinline__ void engine_advance(PfScalars &sc, uint64_t k)
 //
 // Uniform j is u_j = (j + a_j 2^-32) / N with a 32-bit word a_j.  With the
 // integer CDF C_i and total Q, u_j <= C / Q  <=>  (j 2^32 + a_j) Q <= C N 2^32
-// <=>  j Q + G_j <= C N  with G_j = ceil(a_j Q / 2^32) < Q, since both sides
-// are integers.  The counts follow from one exact floor(C N / Q) with its
-// remainder per CDF value.
-struct CountP {
-    uint64_t Q;     // CDF total
-    uint64_t G;     // systematic: ceil(a Q / 2^32) (one word for every j)
-    uint32_t n;
-    double dscale;  // n / Q
-};
-
+// <=>  j Q + G_j <= C N  with G_j = ceil(a_j Q / 2^32) <= Q, since both sides
+// are integers.  The counts follow from one exact floor((C N - G) / Q) per
+// CDF value (below).
 __device__ __forceinline__ uint64_t ceil_aq(uint32_t a, uint64_t Q)
 {
     const uint64_t hi = __umul64hi(static_cast<uint64_t>(a), Q); // < 2^32
     const uint64_t lo = static_cast<uint64_t>(a) * Q;
     return ((hi << 32) | (lo >> 32)) + ((lo & 0xFFFFFFFFull) != 0 ? 1 : 0);
-}
-
-__device__ __forceinline__ CountP make_count_params(
-    uint64_t Q, uint32_t n, uint32_t a_sys)
-{
-    CountP p;
-    p.Q = Q;
-    p.G = ceil_aq(a_sys, Q);
-    p.n = n;
-    p.dscale = static_cast<double>(n) / static_cast<double>(Q);
-    return p;
 }
 
 __device__ __forceinline__ U128 sub_u128(const U128 &a, const U128 &b)
@@ -363,58 +345,6 @@ __device__ __forceinline__ void cdf_constants(
     sc.qgam = G >= Q ? ~0ull : div_u128_u64(G, 0, Q, err);
 }
 
-// j = floor((C n - G) / Q) and r = (C n - G) - j Q; false if C n < G
-__device__ __forceinline__ bool cn_divmod(uint64_t C, uint64_t G,
-    const CountP &p, long long &j, uint64_t &r, uint32_t &err)
-{
-    uint64_t xh = __umul64hi(C, static_cast<uint64_t>(p.n));
-    uint64_t xl = C * static_cast<uint64_t>(p.n);
-    if (xl < G) {
-        if (xh == 0)
-            return false;
-        --xh;
-    }
-    xl -= G;
-    // estimate within a unit or two of the answer: C n / Q in FP64 is off
-    // by at most n 2^-51 + 1 (three roundings), below 2 for any n < 2^31
-    // (one FP64 product per call; callers make one per block or fewer)
-    const double f = static_cast<double>(C) * p.dscale;
-    long long jj = static_cast<long long>(f) - 2;
-    if (jj < 0)
-        jj = 0;
-    if (jj > static_cast<long long>(p.n))
-        jj = static_cast<long long>(p.n);
-    // R = X - jj Q, 128-bit; walk down while negative, up while >= Q
-    const uint64_t ph = __umul64hi(static_cast<uint64_t>(jj), p.Q);
-    const uint64_t pl = static_cast<uint64_t>(jj) * p.Q;
-    uint64_t rl = xl - pl;
-    uint64_t rh = xh - ph - (xl < pl ? 1 : 0);
-    int guard = 0;
-    while (static_cast<long long>(rh) < 0) { // X < jj Q
-        --jj;
-        const uint64_t t = rl + p.Q;
-        rh += (t < rl ? 1 : 0);
-        rl = t;
-        if (++guard > 64) {
-            err |= DEV_ERR_BOUND;
-            break;
-        }
-    }
-    guard = 0;
-    while (rh != 0 || rl >= p.Q) {
-        ++jj;
-        rh -= (rl < p.Q ? 1 : 0);
-        rl -= p.Q;
-        if (++guard > 64) {
-            err |= DEV_ERR_BOUND;
-            break;
-        }
-    }
-    j = jj;
-    r = rl;
-    return true;
-}
-
 // floor(w * 2^shift) for w = exp(lw - M) in [0, 1] and shift <= 63, in two
 // 32-bit halves by float operations that are all exact: x = w 2^shift is
 // w with its exponent moved; h = trunc(x 2^-32) is the high half; and
@@ -432,112 +362,11 @@ __device__ __forceinline__ uint64_t fixed_q(float lw, float M, uint32_t shift)
     return lw > -INFINITY ? q : 0ull;
 }
 
-// A CDF value's position against the uniforms, X = C n - G (G = 0 for
-// stratified), kept as X = (j - 1) Q + r with 0 <= r < Q.  Then F(C) = j
-// (systematic, clamped to n), or j - 1 plus one if uniform j - 1 lies at or
-// below C / Q (stratified).  A step of the CDF adds q n to X, so positions
-// follow from one 128-bit division per block, then only additions.
-struct QR {
-    uint32_t j;
-    uint64_t r;
-};
-
-__device__ __forceinline__ QR qr_add(const QR &a, const QR &b, uint64_t Q)
-{
-    QR c;
-    c.j = a.j + b.j;
-    c.r = a.r + b.r; // both below Q < 2^63: no wrap
-    if (c.r >= Q) {
-        c.r -= Q;
-        ++c.j;
-    }
-    return c;
-}
-
-// A quotient estimate of r / Q that never exceeds the true quotient.  The
-// conversion of r (toward zero, then one rounding) is within 1.5 2^-23 of
-// r, invQ = rcp(float(Q)) within 2^-23 of 1 / Q, and the two products add
-// 2^-23: est <= (r / Q)(1 + 3.5 2^-23)(1 - 2^-20) < r / Q.  Its floor is at
-// most the quotient, and at least the quotient minus (r / Q) 1.4e-6 + 1.
-__device__ __forceinline__ uint32_t quot_below(uint64_t r, float invQ)
-{
-    const float est = fmaf(__uint2float_rz(static_cast<uint32_t>(r >> 32)),
-                          4294967296.0f,
-                          __uint2float_rz(static_cast<uint32_t>(r))) *
-        invQ * (1.0f - 0x1p-20f);
-    return __float2uint_rz(est);
-}
-
-// Bring r below Q, adding the quotient to j.  Every lane takes the same
-// path: one estimate from below (quot_below; 0 when r < Q), which leaves at
-// most (r / Q) 1.4e-6 + 1 (below 2 for fewer than 7e5 copies), then two
-// conditional steps, so the warp does not split on how many copies its
-// lanes' particles take.  Only a position advanced by 7e5 or more copies
-// needs the second estimate (a quotient below 2^31 always leaves less than
-// 2 after it), and one more step.
-__device__ __forceinline__ void qr_reduce(
-    uint64_t &r, uint32_t &j, uint64_t Q, float invQ, uint32_t &err)
-{
-    uint32_t d = quot_below(r, invQ);
-    r -= static_cast<uint64_t>(d) * Q; // d Q <= r: no wrap
-    j += d;
-    if (r >= Q) {
-        r -= Q;
-        ++j;
-    }
-    if (r >= Q) {
-        r -= Q;
-        ++j;
-    }
-    if (r >= Q) { // 7e5 or more copies: a second estimate
-        d = quot_below(r, invQ);
-        r -= static_cast<uint64_t>(d) * Q;
-        j += d;
-        if (r >= Q) {
-            r -= Q;
-            ++j;
-        }
-        if (r >= Q) {
-            r -= Q;
-            ++j;
-        }
-        if (r >= Q) // unreachable by the bounds above; recorded if ever
-            err |= DEV_ERR_BOUND;
-    }
-}
-
-// q n added to a position.  Filter weights satisfy q <= 2^K and
-// n <= 2^(63 - K), so q n <= 2^63 and r + q n < 2^64; integer weights given
-// by a caller are checked and take the 128-bit division when they do not.
-__device__ __forceinline__ void qr_push(QR &acc, uint64_t q, uint32_t n,
-    bool checked, uint64_t Q, float invQ, const CountP &cp, uint32_t &err)
-{
-    if (checked) {
-        const uint64_t plo = static_cast<uint64_t>(static_cast<uint32_t>(q)) * n;
-        const uint64_t phi = (q >> 32) * n;
-        const uint64_t lo = plo + (phi << 32);
-        const uint64_t hi = (phi >> 32) + (lo < plo ? 1 : 0);
-        const uint64_t s = acc.r + lo;
-        if (hi != 0 || s < lo) {
-            long long jj;
-            uint64_t rr;
-            cn_divmod(q, 0, cp, jj, rr, err);
-            acc = qr_add(acc, QR{static_cast<uint32_t>(jj), rr}, Q);
-            return;
-        }
-        acc.r = s;
-    } else {
-        acc.r += q * n;
-    }
-    qr_reduce(acc.r, acc.j, Q, invQ, err);
-}
-
-// Stratified counting needs, for each CDF position X = (j - 1) Q + r, the
-// engine word of uniform j - 1.  A tile's positions are nondecreasing, so
-// the words it needs lie in one range of the engine stream; the block
-// generates that range's Philox blocks once into shared memory (one or two
-// per thread) instead of each thread generating the blocks its own
-// positions fall in.  Block b of the stream is at wb[b - b0] for
+// Stratified counting needs, for each CDF value, the engine word of its
+// uniform j* (strat_j).  A tile's CDF values are nondecreasing, so the words
+// it needs lie in one range of the engine stream; the block generates that
+// range's Philox blocks once into shared memory (one or two per thread)
+// instead of each thread generating the blocks its own words fall in.  Block b of the stream is at wb[b - b0] for
 // b0 <= b < b0 + nb; a block beyond the buffer (a tile whose positions
 // span more than it) is generated where it is needed.
 struct WordBuf {
@@ -566,38 +395,6 @@ __device__ __forceinline__ uint32_t buf_word(
     const uint4 v = d < w.nb ? w.wb[d] : engine_block_at(sc, b);
     const uint32_t r = pos & 3u;
     return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w));
-}
-
-// F from a position (see QR), the stratified words from the tile's buffer
-__device__ __forceinline__ uint32_t f_of_buf(const QR &x, bool sys,
-    uint32_t n, uint64_t Q, const PfScalars &sc, const WordBuf &w)
-{
-    if (sys)
-        return x.j < n ? x.j : n;
-    if (x.j == 0)
-        return 0;
-    const uint32_t j0 = x.j - 1;
-    if (j0 >= n)
-        return n;
-    return j0 + (ceil_aq(buf_word(sc, sc.rindex + j0, w), Q) <= x.r ? 1u
-                                                                     : 0u);
-}
-
-// The engine words [wlo, whi] (empty when wlo > whi) a thread may need:
-// from its start position st to the position after its last particle,
-// last = st + loc (a superset of what f_of_buf reads).
-__device__ __forceinline__ void words_span(const QR &st, const QR &last,
-    uint32_t n, const PfScalars &sc, uint32_t &wlo, uint32_t &whi)
-{
-    const uint32_t jl = st.j >= 1 ? st.j - 1 : 0;
-    const uint32_t jh = (last.j < n ? last.j : n);
-    if (jh == 0 || jl > jh - 1) {
-        wlo = 0xFFFFFFFFu;
-        whi = 0;
-    } else {
-        wlo = sc.rindex + jl;
-        whi = sc.rindex + (jh - 1);
-    }
 }
 
 // Generates the Philox blocks covering every thread's [wlo, whi] into wb
@@ -640,52 +437,6 @@ __device__ __forceinline__ WordBuf fill_words(const PfScalars &sc,
     }
     __syncthreads();
     return w;
-}
-
-// Block-wide exclusive scan of positions over kBlock threads; *total gets
-// the block's sum; sh holds kBlock / 32 entries.
-template <int kBlock = kPfBlock>
-__device__ __forceinline__ QR block_exclusive_qr(
-    QR v, uint64_t Q, QR *sh, QR *total)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    constexpr int nw = kBlock / 32;
-    QR x = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        QR o;
-        o.j = __shfl_up_sync(0xFFFFFFFFu, x.j, d);
-        o.r = __shfl_up_sync(0xFFFFFFFFu, x.r, d);
-        if (lane >= d)
-            x = qr_add(o, x, Q);
-    }
-    if (lane == 31)
-        sh[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-        QR w = lane < nw ? sh[lane] : QR{0, 0};
-#pragma unroll
-        for (int d = 1; d < nw; d <<= 1) {
-            QR o;
-            o.j = __shfl_up_sync(0xFFFFFFFFu, w.j, d);
-            o.r = __shfl_up_sync(0xFFFFFFFFu, w.r, d);
-            if (lane >= d)
-                w = qr_add(o, w, Q);
-        }
-        if (lane < nw)
-            sh[lane] = w;
-    }
-    __syncthreads();
-    QR ex;
-    ex.j = __shfl_up_sync(0xFFFFFFFFu, x.j, 1);
-    ex.r = __shfl_up_sync(0xFFFFFFFFu, x.r, 1);
-    if (lane == 0)
-        ex = QR{0, 0};
-    if (wid > 0)
-        ex = qr_add(sh[wid - 1], ex, Q);
-    *total = sh[nw - 1];
-    __syncthreads();
-    return ex;
 }
 
 // counts of slots i0..i0+3 below hi (-1 past hi)

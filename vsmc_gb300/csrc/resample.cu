@@ -135,10 +135,30 @@ struct OpMaxK {
     }
 };
 
+// Keys of the uniforms for counting: the running maximum's keys (KeysMax),
+// or, for uniforms known to be non-decreasing, each uniform's own key
+// (KeysOwn; the running maximum is then the sequence itself).
+struct KeysMax {
+    const long long *pmk;
+    __device__ __forceinline__ long long operator[](size_t j) const
+    {
+        return pmk[j];
+    }
+};
+
+struct KeysOwn {
+    const double *u;
+    __device__ __forceinline__ long long operator[](size_t j) const
+    {
+        return okey(u[j]);
+    }
+};
+
 // The first index j >= lo with pmk_j > x (hi if none), given that every
 // j < lo has pmk_j <= x and pmk_hi > x or hi == n.
+template <class Keys>
 __device__ __forceinline__ size_t first_above(
-    const long long *pmk, size_t lo, size_t hi, long long x)
+    const Keys &pmk, size_t lo, size_t hi, long long x)
 {
     while (lo < hi) {
         const size_t mid = lo + (hi - lo) / 2;
@@ -151,8 +171,9 @@ __device__ __forceinline__ size_t first_above(
 }
 
 // #{j < n : pmk_j <= x} by exponential search from a guess g <= n.
+template <class Keys>
 __device__ __forceinline__ size_t count_from(
-    const long long *pmk, size_t n, long long x, size_t g)
+    const Keys &pmk, size_t n, long long x, size_t g)
 {
     size_t lo, hi;
     size_t step = 1;
@@ -211,8 +232,9 @@ __device__ __forceinline__ size_t guess_cn(double c, size_t n)
 // answer is near n cdf_i: an exponential search from that guess needs a few
 // loads, and consecutive lanes touch neighbouring addresses.  A weight that
 // takes many copies costs a logarithmic number of loads.
+template <class Keys>
 __global__ void __launch_bounds__(kB) k_counts(size_t m, size_t n,
-    const double *cdf, const long long *pmk, uint32_t *F)
+    const double *cdf, const Keys pmk, uint32_t *F)
 {
     GRID_LOOP(i, m - 1)
     {
@@ -685,10 +707,13 @@ bool size_ok(size_t n) { return n < (size_t(1) << 31); }
 
 // ------------------------------------------------------- internal entries
 
-// rep for m weights against n uniforms u (device); integ added if non-null
+// rep for m weights against n uniforms u (device); integ added if non-null.
+// sorted: the caller knows u is non-decreasing with no NaN (the integer
+// stratified / systematic sequences for N = 2^k), so its running maximum
+// is u itself and is not formed.
 int u01_rep_device(size_t m, size_t n, const double *w, const double *u,
     int *rep, const int *integ, uint32_t *err, Scratch &scratch,
-    cudaStream_t st)
+    cudaStream_t st, bool sorted)
 {
     if (m == 0)
         return VSMC_CUDA_OK;
@@ -713,18 +738,25 @@ int u01_rep_device(size_t m, size_t n, const double *w, const double *u,
         return VSMC_CUDA_OK;
     }
     double *cdf = scratch.get<double>(m - 1);
-    long long *pmk = scratch.get<long long>(n);
-    long long *pp = scratch.get<long long>(scan_parts(n));
     uint32_t *F = scratch.get<uint32_t>(m);
-    if (!cdf || !pmk || !pp || !F)
+    if (!cdf || !F)
         return VSMC_CUDA_ERR_ALLOC;
     int rc = seqsum_device(m - 1, w, cdf, nullptr, err, scratch, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    rc = device_scan(n, LoadOKey{u}, StoreK{pmk}, OpMaxK(), LLONG_MIN, pp, st);
-    if (rc != VSMC_CUDA_OK)
-        return rc;
-    k_counts<<<grid1(m), kB, 0, st>>>(m, n, cdf, pmk, F);
+    if (sorted) {
+        k_counts<<<grid1(m), kB, 0, st>>>(m, n, cdf, KeysOwn{u}, F);
+    } else {
+        long long *pmk = scratch.get<long long>(n);
+        long long *pp = scratch.get<long long>(scan_parts(n));
+        if (!pmk || !pp)
+            return VSMC_CUDA_ERR_ALLOC;
+        rc = device_scan(
+            n, LoadOKey{u}, StoreK{pmk}, OpMaxK(), LLONG_MIN, pp, st);
+        if (rc != VSMC_CUDA_OK)
+            return rc;
+        k_counts<<<grid1(m), kB, 0, st>>>(m, n, cdf, KeysMax{pmk}, F);
+    }
     k_rep_from_counts<<<grid1(m), kB, 0, st>>>(m, n, F, rep, integ);
     VSMC_CUDA_CHECK_LAUNCH();
     return VSMC_CUDA_OK;
@@ -877,14 +909,14 @@ int scheme_device(size_t m, size_t n, vsmc_cuda_rng *rng, const double *w,
     double *u = scratch.get<double>(N);
     if (u == nullptr)
         return VSMC_CUDA_ERR_ALLOC;
+    // N = 2^k: the uniforms are formed in integers (exact, no FP64)
+    int log2n = -1;
+    if (N > 0 && (N & (N - 1)) == 0 && N <= (size_t(1) << 31)) {
+        log2n = 0;
+        while ((size_t(1) << log2n) < N)
+            ++log2n;
+    }
     if (N > 0) {
-        // N = 2^k: the uniforms are formed in integers (exact, no FP64)
-        int log2n = -1;
-        if ((N & (N - 1)) == 0 && N <= (size_t(1) << 31)) {
-            log2n = 0;
-            while ((size_t(1) << log2n) < N)
-                ++log2n;
-        }
         if (base == VSMC_CUDA_STRATIFIED) {
             k_stratified_seq<<<grid1(N), kB, 0, st>>>(es, N, log2n, u);
         } else if (base == VSMC_CUDA_SYSTEMATIC) {
@@ -902,7 +934,11 @@ int scheme_device(size_t m, size_t n, vsmc_cuda_rng *rng, const double *w,
         }
         VSMC_CUDA_CHECK_LAUNCH();
     }
-    rc = u01_rep_device(m, N, wt, u, rep, integ, err, scratch, st);
+    // the integer sequences (N = 2^k) round a non-decreasing sequence of
+    // integers to nearest, so they are non-decreasing themselves
+    const bool sorted = log2n >= 0 &&
+        (base == VSMC_CUDA_STRATIFIED || base == VSMC_CUDA_SYSTEMATIC);
+    rc = u01_rep_device(m, N, wt, u, rep, integ, err, scratch, st, sorted);
     if (rc != VSMC_CUDA_OK)
         return rc;
     uint64_t words = 0;

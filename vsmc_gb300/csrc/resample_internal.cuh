@@ -9,7 +9,7 @@ namespace vsmc_cuda
 
 int u01_rep_device(size_t m, size_t n, const double *w, const double *u,
     int *rep, const int *integ, uint32_t *err, Scratch &scratch,
-    cudaStream_t st);
+    cudaStream_t st, bool sorted = false);
 int rep_index_device(size_t m, size_t n, const int *rep, int *idx,
     uint32_t *err, Scratch &scratch, cudaStream_t st);
 int scheme_device(size_t m, size_t n, vsmc_cuda_rng *rng, const double *w,

@@ -91,20 +91,27 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_reduce(
         part[blockIdx.x] = tot;
 }
 
-// exclusive scan of part[0..nb) in place (one block)
+// exclusive scan of part[0..nb) in place (one block): each thread takes a
+// contiguous stretch (its loads issued together), one block scan of the
+// stretches' totals, then each thread writes its stretch's prefixes
 template <typename T, typename Op>
 __global__ void __launch_bounds__(kScanBlock) k_scan_parts(
     size_t nb, T *part, Op op, T id)
 {
-    T carry = id;
-    for (size_t base = 0; base < nb; base += kScanBlock) {
-        const size_t i = base + threadIdx.x;
-        const T v = i < nb ? part[i] : id;
-        T tot;
-        const T ex = block_excl_any(v, op, id, &tot);
-        if (i < nb)
-            part[i] = op(carry, ex);
-        carry = op(carry, tot);
+    const size_t per = (nb + kScanBlock - 1) / kScanBlock;
+    const size_t b0 = min(nb, threadIdx.x * per);
+    const size_t b1 = min(nb, b0 + per);
+    T acc = id;
+#pragma unroll 8
+    for (size_t i = b0; i < b1; ++i)
+        acc = op(acc, part[i]);
+    T tot;
+    T run = block_excl_any(acc, op, id, &tot);
+#pragma unroll 8
+    for (size_t i = b0; i < b1; ++i) {
+        const T v = part[i];
+        part[i] = run;
+        run = op(run, v);
     }
 }
 
