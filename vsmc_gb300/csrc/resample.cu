@@ -136,8 +136,9 @@ struct OpMaxK {
 };
 
 // Keys of the uniforms for counting: the running maximum's keys (KeysMax),
-// or, for uniforms known to be non-decreasing, each uniform's own key
-// (KeysOwn; the running maximum is then the sequence itself).
+// or, for uniforms known to be non-decreasing, non-negative and free of NaN,
+// each uniform's own key (KeysOwn; the running maximum is then the sequence
+// itself).
 struct KeysMax {
     const long long *pmk;
     __device__ __forceinline__ long long operator[](size_t j) const
@@ -150,7 +151,8 @@ struct KeysOwn {
     const double *u;
     __device__ __forceinline__ long long operator[](size_t j) const
     {
-        return okey(u[j]);
+        // okey of a non-negative, non-NaN double is its bit pattern
+        return __double_as_longlong(u[j]);
     }
 };
 
@@ -708,9 +710,9 @@ bool size_ok(size_t n) { return n < (size_t(1) << 31); }
 // ------------------------------------------------------- internal entries
 
 // rep for m weights against n uniforms u (device); integ added if non-null.
-// sorted: the caller knows u is non-decreasing with no NaN (the integer
-// stratified / systematic sequences for N = 2^k), so its running maximum
-// is u itself and is not formed.
+// sorted: the caller knows u is non-decreasing, non-negative and free of
+// NaN (the integer stratified / systematic sequences for N = 2^k), so its
+// running maximum is u itself and is not formed.
 int u01_rep_device(size_t m, size_t n, const double *w, const double *u,
     int *rep, const int *integ, uint32_t *err, Scratch &scratch,
     cudaStream_t st, bool sorted)

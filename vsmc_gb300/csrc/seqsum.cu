@@ -37,15 +37,17 @@ namespace
 {
 
 struct RF {
-    uint64_t r; // integer increment in units of the element's binade ulp
-    uint32_t f; // 1 = breakpoint
-    uint32_t pad;
+    uint64_t r;   // integer increment in units of the element's binade ulp
+    uint32_t f;   // 1 = breakpoint
+    uint32_t own; // the right operand's own flag (the element's, in a scan)
 };
 
+// Sums (r, f); `own` takes the right operand's, which is associative, so
+// an inclusive scan leaves each element's own breakpoint flag in it.
 struct OpRF {
     __device__ __forceinline__ RF operator()(const RF &a, const RF &b) const
     {
-        return {a.r + b.r, a.f + b.f, 0};
+        return {a.r + b.r, a.f + b.f, b.own};
     }
 };
 
@@ -76,8 +78,11 @@ struct Class {
 __device__ __forceinline__ Class classify(size_t i, const double *x,
     const double *P, uint32_t *err, bool allow_inf)
 {
-    Class c = {false, 0, 0};
+    // every load up front and every test as a flag (no early return), so
+    // the loads of a thread's elements can all be in flight together
     const uint64_t xb = dbits(x[i]);
+    const uint64_t pa = dbits(P[i > 0 ? i - 1 : 0]);
+    const uint64_t pb = dbits(P[i]);
     const uint32_t xe = static_cast<uint32_t>(xb >> 52) & 0x7FFu;
     const uint64_t xf = xb & kFracMask;
     // x >= 0 fails for NaN and for negatives other than -0
@@ -86,39 +91,30 @@ __device__ __forceinline__ Class classify(size_t i, const double *x,
     if (bad || (inf && !allow_inf)) {
         if (err)
             atomicOr(err, DEV_ERR_NONFINITE);
-        return c;
     }
-    if (inf || i == 0)
-        return c;
-    const uint64_t pa = dbits(P[i - 1]);
-    const uint64_t pb = dbits(P[i]);
     const uint32_t ea = static_cast<uint32_t>(pa >> 52); // sign bit included
-    if (ea < kExpMin || ea > 2046u || (pa & kFracMask) < kFracLo)
-        return c;
-    if (static_cast<uint32_t>(pb >> 52) != ea || (pb & kFracMask) >= kFracHi)
-        return c;
+    bool ok = !bad & !inf & (i != 0);
+    ok &= (ea >= kExpMin) & (ea <= 2046u) & ((pa & kFracMask) >= kFracLo);
+    ok &= (static_cast<uint32_t>(pb >> 52) == ea) & ((pb & kFracMask) < kFracHi);
     const int e = static_cast<int>(ea) - 1023;
-    // x = mant 2^q; x / 2^(e-52) = mant / 2^k with k = e - 52 - q
+    // x = mant 2^q; x / 2^(e-52) = mant / 2^k with k = e - 52 - q; k < 0
+    // (x above the running sum's binade) is left to the fix-up
     const uint64_t mant = xe ? (xf | (1ull << 52)) : xf;
     const int q = (xe ? static_cast<int>(xe) : 1) - 1075;
     const int k = e - 52 - q;
-    uint64_t r;
-    if (k < 0) {
-        return c; // x above the running sum's binade: left to the fix-up
-    } else if (k == 0) {
-        r = mant;
-    } else if (k >= 64) {
-        r = 0; // mant < 2^53 <= 2^(k-1): below half a unit, no tie
-    } else {
-        const uint64_t rem = mant & ((1ull << k) - 1);
-        const uint64_t half = 1ull << (k - 1);
-        if (rem == half) // tie: rounding depends on the running sum's parity
-            return c;
-        r = (mant >> k) + (rem > half ? 1u : 0u);
-    }
-    c.regular = true;
+    ok &= k >= 0;
+    // k >= 64: mant < 2^53 <= 2^(k-1), below half a unit and no tie
+    const int kk = k < 1 ? 1 : (k > 63 ? 63 : k);
+    const uint64_t rem = mant & ((1ull << kk) - 1);
+    const uint64_t half = 1ull << (kk - 1);
+    const bool mid = k >= 1 && k <= 63;
+    ok &= !(mid && rem == half); // a tie: rounding depends on the sum's parity
+    const uint64_t r = k == 0 ? mant
+        : (k > 63 ? 0ull : (mant >> kk) + (rem > half ? 1ull : 0ull));
+    Class c;
+    c.regular = ok;
     c.e = e;
-    c.r = r;
+    c.r = ok ? r : 0ull;
     return c;
 }
 
@@ -140,31 +136,27 @@ struct LoadRF {
     __device__ RF operator()(size_t i) const
     {
         const Class c = classify(i, x, P, err, allow_inf);
-        return {c.regular ? c.r : 0ull, c.regular ? 0u : 1u, 0u};
+        const uint32_t f = c.regular ? 0u : 1u;
+        return {c.regular ? c.r : 0ull, f, f};
     }
 };
 
+// The scan's output, and the breakpoint records in order: breakpoint k
+// (the element whose inclusive count f steps to k + 1) is at bidx[k], with
+// the increments through it (its own r is 0) in bcr[k].
 struct StoreRF {
     RF *p;
-    __device__ void operator()(size_t i, RF v) const { p[i] = v; }
-};
-
-// breakpoint records, in order: element i is a breakpoint when the scan's
-// breakpoint count steps at i
-__global__ void __launch_bounds__(256) k_breakpoints(
-    size_t n, const RF *C, uint32_t *bidx, uint64_t *bcr)
-{
-    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-         i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const RF ci = C[i];
-        const uint32_t fprev = i ? C[i - 1].f : 0u;
-        if (ci.f != fprev) {
-            const uint32_t k = ci.f - 1;
-            bidx[k] = static_cast<uint32_t>(i);
-            bcr[k] = ci.r; // r_i = 0, so also the count through i - 1
+    uint32_t *bidx;
+    uint64_t *bcr;
+    __device__ void operator()(size_t i, RF v) const
+    {
+        p[i] = v;
+        if (v.own) {
+            bidx[v.f - 1] = static_cast<uint32_t>(i);
+            bcr[v.f - 1] = v.r;
         }
     }
-}
+};
 
 // One block walks the breakpoints in order with real additions.
 __global__ void __launch_bounds__(256) k_fixup(size_t n, const double *x,
@@ -239,10 +231,9 @@ __global__ void __launch_bounds__(256) k_prefix_out(size_t n, const RF *C,
     for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
          i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const RF ci = C[i];
-        const uint32_t fprev = i ? C[i - 1].f : 0u;
         const uint32_t k = ci.f - 1;
         double s;
-        if (ci.f != fprev) {
+        if (ci.own) {
             s = sb[k];
         } else {
             const uint64_t b = dbits(sb[k]);
@@ -281,12 +272,11 @@ int seqsum_device(size_t n, const double *x, double *prefix, double *total,
     int rc = device_scan(n, LoadX{x}, StoreD{P}, OpAdd(), 0.0, pd, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
-    rc = device_scan(n, LoadRF{x, P, err, allow_inf}, StoreRF{C}, OpRF(),
-        RF{0, 0, 0}, pr, st);
+    rc = device_scan(n, LoadRF{x, P, err, allow_inf}, StoreRF{C, bidx, bcr},
+        OpRF(), RF{0, 0, 0}, pr, st);
     if (rc != VSMC_CUDA_OK)
         return rc;
     const int grid = grid_for(n, 256, 4, 8);
-    k_breakpoints<<<grid, 256, 0, st>>>(n, C, bidx, bcr);
     k_fixup<<<1, 256, 0, st>>>(
         n, x, P, C, bidx, bcr, sb, total, err, allow_inf);
     if (prefix)
