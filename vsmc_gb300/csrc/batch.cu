@@ -33,6 +33,7 @@
 #include "pf_model.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -811,109 +812,117 @@ __global__ void __launch_bounds__(kPfBlock, 3) k_brs_count(const BatchArgs a)
         const float *lw = a.lw + c.off;
         int32_t *rep = a.rep + c.off;
         const CdfRcp p = load_cdf_rcp(sc, n);
-        uint64_t carry = offset;
         uint32_t empties = 0, copies = 0;
-        // the next tile's log-weights are loaded while this one is counted
-        float4 nxt = make_float4(0, 0, 0, 0);
-        if (c.lo + threadIdx.x * 4 + 3 < c.hi)
-            nxt = __ldcg(reinterpret_cast<const float4 *>(
-                lw + c.lo + threadIdx.x * 4));
-        for (uint32_t base = c.lo; base < c.hi; base += kPfTile) {
-            const uint32_t i0 = base + threadIdx.x * 4;
-            const float4 x = nxt;
-            if (i0 + kPfTile + 3 < c.hi)
-                nxt = __ldcg(
-                    reinterpret_cast<const float4 *>(lw + i0 + kPfTile));
-            uint64_t q[4];
-            if (i0 + 3 < c.hi) {
-                q[0] = fixed_q(x.x, M, c.shift);
-                q[1] = fixed_q(x.y, M, c.shift);
-                q[2] = fixed_q(x.z, M, c.shift);
-                q[3] = fixed_q(x.w, M, c.shift);
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    q[k] = i0 + k < c.hi ? fixed_q(lw[i0 + k], M, c.shift) : 0;
-            }
-            uint64_t s[4];
-            s[0] = q[0];
-            s[1] = s[0] + q[1];
-            s[2] = s[1] + q[2];
-            s[3] = s[2] + q[3];
-            uint64_t tile_total;
-            const uint64_t incl =
-                block_inclusive_scan(s[3], OpAdd(), uint64_t(0), shs, &tile_total);
-            const uint64_t cb = carry + (incl - s[3]);
-            uint32_t Fv[4], Fl = 0;
-            if (sys) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    Fv[k] = i0 + k + 1 >= n ? n : sys_F(cb + s[k], p);
-                if (lane == 0 && i0 != 0)
-                    Fl = sys_F(cb, p);
-            } else {
-                uint32_t j[4];
-                uint64_t r[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    j[k] = strat_j(cb + s[k], p, r[k]);
-                uint32_t jv = 0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (j[k] < n)
-                        jv = j[k];
-                const uint32_t wlo = j[0] < n ? sc.rindex + j[0] : 0xFFFFFFFFu;
-                const uint32_t whi = j[0] < n ? sc.rindex + jv : 0u;
-                const WordBuf wv =
-                    fill_words<kPfBlock>(sc, wlo, whi, wbuf, 2 * kPfBlock, wsh);
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    Fv[k] = i0 + k + 1 >= n ? n
-                        : (j[k] >= n ? n
-                                     : j[k] + (ceil_aq(buf_word(sc,
-                                                   sc.rindex + j[k], wv), Q) <=
-                                                       r[k]
-                                                   ? 1u
-                                                   : 0u));
-                if (lane == 0 && i0 != 0) {
-                    uint64_t r0;
-                    const uint32_t j0 = strat_j(cb, p, r0);
-                    Fl = j0 >= n ? n
-                        : j0 + (ceil_aq(buf_word(sc, sc.rindex + j0, wv), Q) <=
-                                       r0
-                                   ? 1u
-                                   : 0u);
+        // one reciprocal case per chunk (Usual: p.s > 0), chosen once
+        auto run = [&](auto usual) {
+            constexpr bool Usual = decltype(usual)::value;
+            uint64_t carry = offset;
+            // the next tile's log-weights are loaded while this one is counted
+            float4 nxt = make_float4(0, 0, 0, 0);
+            if (c.lo + threadIdx.x * 4 + 3 < c.hi)
+                nxt = __ldcg(reinterpret_cast<const float4 *>(
+                    lw + c.lo + threadIdx.x * 4));
+            for (uint32_t base = c.lo; base < c.hi; base += kPfTile) {
+                const uint32_t i0 = base + threadIdx.x * 4;
+                const float4 x = nxt;
+                if (i0 + kPfTile + 3 < c.hi)
+                    nxt = __ldcg(
+                        reinterpret_cast<const float4 *>(lw + i0 + kPfTile));
+                uint64_t q[4];
+                if (i0 + 3 < c.hi) {
+                    q[0] = fixed_q(x.x, M, c.shift);
+                    q[1] = fixed_q(x.y, M, c.shift);
+                    q[2] = fixed_q(x.z, M, c.shift);
+                    q[3] = fixed_q(x.w, M, c.shift);
+                } else {
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        q[k] = i0 + k < c.hi ? fixed_q(lw[i0 + k], M, c.shift) : 0;
                 }
-            }
-            // F before this thread's first particle (particle 0 has
-            // nothing before it)
-            const uint32_t Fup = __shfl_up_sync(0xFFFFFFFFu, Fv[3], 1);
-            uint32_t Fprev = lane == 0 ? Fl : Fup;
-            int32_t r[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                r[k] = static_cast<int32_t>(Fv[k] - Fprev);
-                Fprev = Fv[k];
-            }
-            if (i0 + 3 < c.hi) {
-                *reinterpret_cast<int4 *>(rep + i0) =
-                    make_int4(r[0], r[1], r[2], r[3]);
-#pragma unroll
+                uint64_t s[4];
+                s[0] = q[0];
+                s[1] = s[0] + q[1];
+                s[2] = s[1] + q[2];
+                s[3] = s[2] + q[3];
+                uint64_t tile_total;
+                const uint64_t incl =
+                    block_inclusive_scan(s[3], OpAdd(), uint64_t(0), shs, &tile_total);
+                const uint64_t cb = carry + (incl - s[3]);
+                uint32_t Fv[4], Fl = 0;
+                if (sys) {
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        Fv[k] = i0 + k + 1 >= n ? n : sys_F<Usual>(cb + s[k], p);
+                    if (lane == 0 && i0 != 0)
+                        Fl = sys_F<Usual>(cb, p);
+                } else {
+                    uint32_t j[4];
+                    uint64_t r[4];
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        j[k] = strat_j<Usual>(cb + s[k], p, r[k]);
+                    uint32_t jv = 0;
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (j[k] < n)
+                            jv = j[k];
+                    const uint32_t wlo = j[0] < n ? sc.rindex + j[0] : 0xFFFFFFFFu;
+                    const uint32_t whi = j[0] < n ? sc.rindex + jv : 0u;
+                    const WordBuf wv =
+                        fill_words<kPfBlock>(sc, wlo, whi, wbuf, 2 * kPfBlock, wsh);
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        Fv[k] = i0 + k + 1 >= n ? n
+                            : (j[k] >= n ? n
+                                         : j[k] + (ceil_aq(buf_word(sc,
+                                                       sc.rindex + j[k], wv), Q) <=
+                                                           r[k]
+                                                       ? 1u
+                                                       : 0u));
+                    if (lane == 0 && i0 != 0) {
+                        uint64_t r0;
+                        const uint32_t j0 = strat_j<Usual>(cb, p, r0);
+                        Fl = j0 >= n ? n
+                            : j0 + (ceil_aq(buf_word(sc, sc.rindex + j0, wv), Q) <=
+                                           r0
+                                       ? 1u
+                                       : 0u);
+                    }
+                }
+                // F before this thread's first particle (particle 0 has
+                // nothing before it)
+                const uint32_t Fup = __shfl_up_sync(0xFFFFFFFFu, Fv[3], 1);
+                uint32_t Fprev = lane == 0 ? Fl : Fup;
+                int32_t r[4];
+    #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    empties += r[k] == 0 ? 1u : 0u;
-                    copies += static_cast<uint32_t>(r[k]);
+                    r[k] = static_cast<int32_t>(Fv[k] - Fprev);
+                    Fprev = Fv[k];
                 }
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (i0 + k < c.hi) {
-                        rep[i0 + k] = r[k];
+                if (i0 + 3 < c.hi) {
+                    *reinterpret_cast<int4 *>(rep + i0) =
+                        make_int4(r[0], r[1], r[2], r[3]);
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k) {
                         empties += r[k] == 0 ? 1u : 0u;
                         copies += static_cast<uint32_t>(r[k]);
                     }
+                } else {
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (i0 + k < c.hi) {
+                            rep[i0 + k] = r[k];
+                            empties += r[k] == 0 ? 1u : 0u;
+                            copies += static_cast<uint32_t>(r[k]);
+                        }
+                }
+                carry += tile_total;
             }
-            carry += tile_total;
-        }
+        };
+        if (p.s != 0)
+            run(std::true_type{});
+        else
+            run(std::false_type{});
         empties = block_reduce(empties, OpAdd(), 0u, she);
         copies = block_reduce(copies, OpAdd(), 0u, she);
         if (threadIdx.x == 0) {

@@ -510,38 +510,27 @@ __device__ __forceinline__ void count_finish(
 // epart / cpart.
 constexpr uint32_t kStratRow = 64; // Philox blocks per warp row (256 words)
 
-template <bool Sys>
-__global__ void __launch_bounds__(kPfBlock, kRsBlocksPerSm) k_rs32_count(
-    const Rs32Args a)
+// One warp's range; Usual picks the reciprocal's case for the whole pass.
+template <bool Sys, bool Usual>
+__device__ __forceinline__ void count_range(const Rs32Args &a,
+    const CdfRcp &p, const EnginePos &e, uint4 *row, uint32_t wlo,
+    uint32_t whi, uint32_t &empties, uint32_t &copies)
 {
-    if (!a.sc->resampled)
-        return;
+    const uint32_t lane = threadIdx.x & 31;
     const float M = static_cast<float>(a.sc->M);
-    uint32_t lo, hi;
-    chunk_range(a.n, a.chunk, lo, hi);
-    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const CdfRcp p = load_cdf_rcp(*a.sc, a.n);
-    EnginePos e = {};
-    if (!Sys)
-        e = engine_pos(*a.sc);
-    __shared__ uint4 rows[Sys ? 1 : kRsWarps][Sys ? 1 : kStratRow];
-    uint4 *row = rows[Sys ? 0 : w];
-    uint32_t wlo, whi;
-    warp_range(lo, hi, a.chunk, w, wlo, whi);
     const bool checked = a.q != nullptr;
     const uint32_t n = a.n;
     uint64_t carry = range_offset(a.qpart); // the CDF before the range
     uint32_t Fprev = 0;
     if (wlo != 0 && wlo < whi) {
         if (Sys) {
-            Fprev = sys_F(carry, p);
+            Fprev = sys_F<Usual>(carry, p);
         } else {
             uint64_t r;
-            const uint32_t j = strat_j(carry, p, r);
+            const uint32_t j = strat_j<Usual>(carry, p, r);
             Fprev = strat_F(j, r, p, e, row, 0, 0);
         }
     }
-    uint32_t empties = 0, copies = 0;
     float4 nxt = make_float4(0, 0, 0, 0);
     if (!checked && wlo + lane * 4 + 3 < whi)
         nxt = __ldcg(reinterpret_cast<const float4 *>(a.lw + wlo + lane * 4));
@@ -573,13 +562,13 @@ __global__ void __launch_bounds__(kPfBlock, kRsBlocksPerSm) k_rs32_count(
         if (Sys) {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                F[k] = i0 + k + 1 >= n ? n : sys_F(cb + s[k], p);
+                F[k] = i0 + k + 1 >= n ? n : sys_F<Usual>(cb + s[k], p);
         } else {
             uint32_t j[4];
             uint64_t r[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                j[k] = strat_j(cb + s[k], p, r[k]);
+                j[k] = strat_j<Usual>(cb + s[k], p, r[k]);
             // the group's words: j[0] of lane 0 .. j[3] of lane 31 (j = n
             // needs none)
             uint32_t jv = 0;
@@ -635,6 +624,30 @@ __global__ void __launch_bounds__(kPfBlock, kRsBlocksPerSm) k_rs32_count(
         carry += tot;
         Fprev = __shfl_sync(0xFFFFFFFFu, F[3], 31);
     }
+}
+
+template <bool Sys>
+__global__ void __launch_bounds__(kPfBlock, kRsBlocksPerSm) k_rs32_count(
+    const Rs32Args a)
+{
+    if (!a.sc->resampled)
+        return;
+    uint32_t lo, hi;
+    chunk_range(a.n, a.chunk, lo, hi);
+    const uint32_t w = threadIdx.x >> 5;
+    const CdfRcp p = load_cdf_rcp(*a.sc, a.n);
+    EnginePos e = {};
+    if (!Sys)
+        e = engine_pos(*a.sc);
+    __shared__ uint4 rows[Sys ? 1 : kRsWarps][Sys ? 1 : kStratRow];
+    uint4 *row = rows[Sys ? 0 : w];
+    uint32_t wlo, whi;
+    warp_range(lo, hi, a.chunk, w, wlo, whi);
+    uint32_t empties = 0, copies = 0;
+    if (p.s != 0)
+        count_range<Sys, true>(a, p, e, row, wlo, whi, empties, copies);
+    else
+        count_range<Sys, false>(a, p, e, row, wlo, whi, empties, copies);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         empties += __shfl_xor_sync(0xFFFFFFFFu, empties, o);

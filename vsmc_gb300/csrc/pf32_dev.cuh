@@ -205,10 +205,13 @@ static __device__ __noinline__ int64_t cdf_floor_near(
     return ok ? k + 1 : k;
 }
 
-// floor((C n - G) / Q) for C < Q (at least -1, below n)
+// floor((C n - G) / Q) for C < Q (at least -1, below n).  Usual: the
+// usual case's reciprocal (p.s > 0) is known to apply, so the loop that
+// calls this holds one path only (the choice is made once per pass).
+template <bool Usual>
 __device__ __forceinline__ int64_t cdf_floor(uint64_t C, const CdfRcp &p)
 {
-    if (p.s != 0) {
+    if (Usual) {
         const uint32_t c1 = static_cast<uint32_t>(C >> 32);
         const uint32_t c0 = static_cast<uint32_t>(C);
         const uint32_t m1 = static_cast<uint32_t>(p.m >> 32);
@@ -236,11 +239,12 @@ __device__ __forceinline__ int64_t cdf_floor(uint64_t C, const CdfRcp &p)
 }
 
 // F(C): the systematic uniforms at or below C / Q, clamped to n
+template <bool Usual>
 __device__ __forceinline__ uint32_t sys_F(uint64_t C, const CdfRcp &p)
 {
     if (C >= p.Q)
         return p.n;
-    const int64_t F = cdf_floor(C, p) + 1;
+    const int64_t F = cdf_floor<Usual>(C, p) + 1;
     return F < static_cast<int64_t>(p.n) ? static_cast<uint32_t>(F) : p.n;
 }
 
@@ -278,6 +282,7 @@ static __device__ __noinline__ uint4 engine_block_far(
 // word passes, G_{j*} = ceil(a_{j*} Q / 2^32) <= r = C n - j* Q.  r < Q, so
 // 64-bit wrapping arithmetic gives it exactly.  j and r for one CDF value
 // (j = n when C >= Q).
+template <bool Usual>
 __device__ __forceinline__ uint32_t strat_j(
     uint64_t C, const CdfRcp &p, uint64_t &r)
 {
@@ -285,7 +290,7 @@ __device__ __forceinline__ uint32_t strat_j(
         r = 0;
         return p.n;
     }
-    const uint32_t j = static_cast<uint32_t>(cdf_floor(C, p));
+    const uint32_t j = static_cast<uint32_t>(cdf_floor<Usual>(C, p));
     r = C * static_cast<uint64_t>(p.n) - static_cast<uint64_t>(j) * p.Q;
     return j;
 }
