@@ -11,11 +11,15 @@
 // Resampling, when the decision says so, runs on an exact 64-bit fixed-point
 // CDF: q_i = floor(exp(lw_i - max) * 2^K) with K = 63 - ceil(log2 N), so the
 // integer prefix sums cannot overflow and do not depend on summation order.
-// Systematic / stratified uniforms u_j = (j + a_j 2^-32) / N are compared with
-// C_i / Q exactly in 128-bit integers.  Replication counts then go to parent
-// indices with the reference's slot layout (resample/transform.hpp:116-133):
-// parents keep their slot, empty slots take surplus copies in order.  Only
-// empty slots are written by the gather.
+// Systematic / stratified uniforms u_j = (j + a_j 2^-32) / N are counted
+// against C_i / Q exactly: a fixed-point reciprocal of Q gives
+// floor((C_i N - G) / Q) per particle, and an exact 128-bit comparison
+// settles the rare value next to a uniform (pf32_dev.cuh).  Three passes
+// (sum, count, assign), one warp per range of particles.  Replication counts
+// then go to parent indices with the reference's slot layout
+// (resample/transform.hpp:116-133): parents keep their slot, empty slots
+// take surplus copies in order.  Only empty slots are written by the
+// gather.
 #pragma once
 
 #include "common.cuh"

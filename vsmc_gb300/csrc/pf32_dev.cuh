@@ -367,13 +367,14 @@ __device__ __forceinline__ uint64_t fixed_q(float lw, float M, uint32_t shift)
     return lw > -INFINITY ? q : 0ull;
 }
 
-// Stratified counting needs, for each CDF value, the engine word of its
-// uniform j* (strat_j).  A tile's CDF values are nondecreasing, so the words
-// it needs lie in one range of the engine stream; the block generates that
-// range's Philox blocks once into shared memory (one or two per thread)
-// instead of each thread generating the blocks its own words fall in.  Block b of the stream is at wb[b - b0] for
-// b0 <= b < b0 + nb; a block beyond the buffer (a tile whose positions
-// span more than it) is generated where it is needed.
+// Stratified counting in the batched filters' block-wide tiles needs, for
+// each CDF value, the engine word of its uniform j* (strat_j).  A tile's CDF
+// values are nondecreasing, so the words it needs lie in one range of the
+// engine stream; the block generates that range's Philox blocks once into
+// shared memory (one or two per thread) instead of each thread generating
+// the blocks its own words fall in.  Block b of the stream is at
+// wb[b - b0] for b0 <= b < b0 + nb; a block beyond the buffer (a tile whose
+// words span more than it) is generated where it is needed.
 struct WordBuf {
     const uint4 *wb;
     uint32_t b0, nb;
