@@ -755,13 +755,11 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_qsum(const BatchArgs a)
         acc = block_reduce(acc, OpAdd(), uint64_t(0), sh);
         // the filter's last chunk to finish (a thread-fenced ticket on
         // done3; nothing waits) sets the filter's counting constants
-        __shared__ bool last;
         if (threadIdx.x == 0) {
             a.rs_q[v] = acc;
             __threadfence();
             PfScalars &S = a.st[c.f];
-            last = atomicAdd(&S.done3, 1u) == c.nc - 1;
-            if (last) {
+            if (atomicAdd(&S.done3, 1u) == c.nc - 1) {
                 S.done3 = 0;
                 __threadfence();
                 uint64_t Q = 0;
@@ -773,7 +771,7 @@ __global__ void __launch_bounds__(kPfBlock) k_brs_qsum(const BatchArgs a)
                     atomicOr(&S.err, err & ~DEV_ERR_NONFINITE);
             }
         }
-        __syncthreads(); // sh and last are reused by the next chunk
+        __syncthreads(); // thread 0 done before the next chunk
     }
 }
 
